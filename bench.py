@@ -1,0 +1,469 @@
+"""Throughput benchmark of the GPU ptychography path (position updates/s).
+
+Workload (default): single-slice gradient-descent ptychography at a 128^2
+detector: 128x128 raster scan (J = 16384 positions, 0.75 A step), 512^2 object
+at 0.25 A, 300 kV / 20 mrad / 100 A defocus probe, 1e5 e-/pattern, batch 1024.
+Data are seeded synthetic patterns from py4dstem_gb300.synthetic (no public
+dataset exists for this benchmark).
+
+One step = one full reconstruction iteration over all J positions (16 batches
+of 1024, per-iteration constraints and the error read-back the reference does
+each iteration).
+
+  value  device-resident amplitudes (1 GiB f32, larger than L2), K iterations
+         timed with CUDA events between barriers;
+  e2e    the public API: K calls of reconstruct(num_iter=1) on a
+         SingleslicePtychography whose amplitudes live in pinned host memory;
+         each call uploads the step's inputs and reads object, probe and error
+         back.
+
+`--impl reference` times the reference algorithm (the float32 NumPy restatement
+in oracle/, which reproduces the reference CPU path bit for bit) on the host
+cores, one worker process per core, each step a bounded sample of batches.
+
+Multi-GPU (torchrun): replicas only — each rank reconstructs its own scan;
+value = positions of all ranks / max-over-ranks time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "position updates/s (128^2 det)"
+UNIT = "positions/s"
+WORKLOAD = "single-slice GD, 128x128 scan (J=16384), 128^2 detector, 512^2 object, batch 1024"
+
+
+def parse_args(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--scan", type=int, default=128, help="scan side (positions = scan^2)")
+    ap.add_argument("--batch", type=int, default=1024)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
+    return ap.parse_args(argv)
+
+
+# ------------------------------------------------------------------ distributed
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def timed_region(step, steps, barrier, sync, now_ms, reduce_max):
+    """Barrier + sync on both sides of `steps` calls of step(); returns the
+    max-over-ranks elapsed milliseconds. The callables make the harness testable
+    on CPU (gloo) without a GPU."""
+    barrier()
+    sync()
+    t0 = now_ms()
+    for _ in range(steps):
+        step()
+    sync()
+    t1 = now_ms()
+    barrier()
+    return reduce_max(t1 - t0)
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu_index = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu_index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ workload
+def roofline_constants(n_pixels):
+    """Algorithmic work per single-slice GD position update (5 N log2 N flops per
+    complex 2D FFT, 3 FFTs, ~50 real flops of elementwise work per pixel; bytes:
+    amplitude read 4N + object patch 8N + object-term scatter 8N + |P|^2 scatter 4N)."""
+    flops = 3 * 5 * n_pixels * math.log2(n_pixels) + 50 * n_pixels
+    bytes_ = 24 * n_pixels
+    return flops, bytes_
+
+
+def read_profile_traffic():
+    """DRAM bytes per launch of the position kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "position_kernel_128_gd.md")
+    try:
+        text = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_launch_scaled:\s*([0-9.eE+]+)", text)
+    return float(m.group(1)) if m else None
+
+
+def build_case(scan, seed, device):
+    from py4dstem_gb300 import synthetic
+
+    case = synthetic.make_scan(
+        "bench", seed, (scan, scan), 0.75, 0.05, 128, 512 if scan >= 128 else
+        int(2 ** math.ceil(math.log2(scan * 3 + 128))), dose=1e5, backend="torch",
+        device=device)
+    return case
+
+
+def preprocess(case, storage):
+    from py4dstem_gb300 import SingleslicePtychography
+
+    kw = dict(case.ctor_kwargs)
+    p = SingleslicePtychography(datacube=case.datacube, verbose=False, device="gpu",
+                                storage=storage, **kw)
+    p.preprocess(max_batch_size=1024, **case.preprocess_kwargs)
+    return p
+
+
+def fp32_peak_tflops(torch, lib):
+    """Measured FP32 FMA throughput of this GPU (TFLOP/s)."""
+    import ctypes
+
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    blocks = props.multi_processor_count * 8
+    iters = 1 << 15
+    sink = torch.empty(blocks * 256, dtype=torch.float32, device="cuda")
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for _ in range(2):
+        lib.ptycho_fp32_fma_probe(blocks, iters, ctypes.c_void_p(sink.data_ptr()), stream)
+    best = 0.0
+    for _ in range(5):
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record()
+        lib.ptycho_fp32_fma_probe(blocks, iters, ctypes.c_void_p(sink.data_ptr()), stream)
+        e.record()
+        e.synchronize()
+        ms = s.elapsed_time(e)
+        best = max(best, 16.0 * blocks * 256 * iters / (ms * 1e-3) / 1e12)
+    return best
+
+
+def cpu_baseline_sample(p, seconds):
+    """Oracle (reference algorithm, float32 NumPy) on one core: whole batches of the
+    same workload until ~`seconds` of CPU work; positions/s."""
+    from oracle.ptycho_np import Oracle, State
+
+    st = State(amplitudes=p._amplitudes, positions_px=p._positions_px.copy(),
+               probe=np.array(p._probe), object=np.array(p._object),
+               mean_intensity=p._mean_diffraction_intensity,
+               fov_mask_inverse=p._object_fov_mask_inverse)
+    o = Oracle(st)
+    J = p._num_diffraction_patterns
+    B = min(1024, J)
+    order = np.random.default_rng(0).permutation(J)
+    done = 0
+    t0 = time.perf_counter()
+    sub = 128  # positions per sub-step, the timing granule
+    while time.perf_counter() - t0 < seconds:
+        idx = order[(done % J):(done % J) + sub]
+        _run_oracle_batch(o, idx)
+        done += len(idx)
+    dt = time.perf_counter() - t0
+    return done / dt, done, B
+
+
+def _run_oracle_batch(o, idx):
+    pos = o.positions_px[idx]
+    frac = pos - np.round(pos)
+    rows, cols = o.patch_indices(pos)
+    shifted = o.fft_shift(o.probe, frac)
+    shifted, patches, ov = o.overlap(rows, cols, shifted)
+    ew, _ = o.gd_projection(o.amplitudes[idx], ov, None)
+    o.adjoint(patches, shifted, pos, ew, 0.5, 1.0, False, False)
+
+
+# ------------------------------------------------------------------ reference arm
+def _ref_worker(args):
+    scan, seed, seconds = args
+    import numpy as _np
+
+    from py4dstem_gb300 import synthetic
+    from oracle.ptycho_np import Oracle
+
+    case = synthetic.make_scan("ref", seed, (scan, scan), 0.75, 0.05, 128, 512 if scan >= 128
+                               else int(2 ** math.ceil(math.log2(scan * 3 + 128))), dose=1e5,
+                               backend="numpy")
+    p = preprocess(case, storage="cpu")
+    from oracle.ptycho_np import State
+
+    st = State(amplitudes=p._amplitudes, positions_px=p._positions_px.copy(),
+               probe=_np.array(p._probe), object=_np.array(p._object),
+               mean_intensity=p._mean_diffraction_intensity,
+               fov_mask_inverse=p._object_fov_mask_inverse)
+    o = Oracle(st)
+    J = p._num_diffraction_patterns
+    order = _np.random.default_rng(seed).permutation(J)
+    done = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        idx = order[(done % J):(done % J) + 64]
+        _run_oracle_batch(o, idx)
+        done += len(idx)
+    return done, time.perf_counter() - t0
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import multiprocessing as mp
+
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    # small scans per worker keep the per-process setup short; the per-position
+    # work (128^2 detector) is the workload's
+    per_step = max(2.0, min(20.0, 60.0 / max(1, args.steps + args.warmup)))
+    ctx = mp.get_context("spawn")
+    values = []
+    with ctx.Pool(cores) as pool:
+        for i in range(args.warmup + args.steps):
+            res = pool.map(_ref_worker, [(16, 100 + w + 1000 * i, per_step) for w in range(cores)])
+            tot = sum(r[0] for r in res)
+            wall = max(r[1] for r in res)
+            if i >= args.warmup:
+                values.append(tot / wall)
+    v = float(statistics.median(values))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * 16384 / v,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample": "per-position GD updates at 128^2 detector"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{cores} processes x ~{per_step:.0f} s of 64-position "
+                                   "batches of the 128^2-detector GD update"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ our arm
+def run_ours(args):
+    rank, world, local = dist_env()
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        barrier = dist.barrier
+
+        def reduce_max(x):
+            t = torch.tensor([x], dtype=torch.float64, device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            return float(t.item())
+    else:
+        def barrier():
+            return None
+
+        def reduce_max(x):
+            return x
+
+    from py4dstem_gb300 import _native, engine
+
+    lib = _native.lib()
+    seed = 1234 + rank
+    t_setup = time.time()
+    case = build_case(args.scan, seed, f"cuda:{local}")
+    p = preprocess(case, storage="gpu")
+    setup_s = time.time() - t_setup
+
+    # CPU baseline on rank 0 at N=1 only, before any timing (single core)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, done, _ = cpu_baseline_sample(p, args.cpu_sample_seconds)
+        cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{done} positions of the same 128^2-detector GD workload "
+                         "(float32 NumPy restatement of the reference, 1 core)"}
+
+    J = p._num_diffraction_patterns
+    B = min(args.batch, J)
+    st = engine.create_state(
+        roi_shape=tuple(p._region_of_interest_shape), object_array=np.asarray(p._object),
+        probe_array=p._probe, amplitudes=p._amplitudes, positions_px=p._positions_px,
+        num_slices=1, num_probes=1, potential=False, max_batch=B, storage="gpu",
+        fov_mask_inverse=p._object_fov_mask_inverse)
+    drv = engine.IterationDriver(
+        st, max_batch=B, step_size=0.5, normalization_min=1.0,
+        use_mask=bool(p._object_fov_mask_inverse.sum() > 0),
+        mean_intensity=p._mean_diffraction_intensity)
+    np.random.seed(seed)
+    order = np.arange(J)
+    errors = []
+
+    def step():
+        np.random.shuffle(order)
+        drv.iterate(order)
+        errors.append(float(drv.error()))  # per-iteration read-back, as the reference
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    lib.ptycho_enable_kernel_timing(1)
+    import ctypes
+
+    ms_dummy = ctypes.c_float()
+    n_dummy = ctypes.c_int32()
+    lib.ptycho_kernel_timing(ctypes.byref(ms_dummy), ctypes.byref(n_dummy))  # clear
+    launches0 = st.launches
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+
+    def now_ms():
+        return time.perf_counter() * 1e3
+
+    with ClockSampler(local) as clocks:
+        ev0.record()
+        wall_ms = timed_region(step, args.steps, barrier, torch.cuda.synchronize, now_ms,
+                               lambda x: x)
+        ev1.record()
+        torch.cuda.synchronize()
+    dev_ms = ev0.elapsed_time(ev1)
+    ms = reduce_max(dev_ms)
+    launches = st.launches - launches0
+    lib.ptycho_enable_kernel_timing(0)
+    kms = ctypes.c_float()
+    kn = ctypes.c_int32()
+    _native.check(lib.ptycho_kernel_timing(ctypes.byref(kms), ctypes.byref(kn)))
+
+    value = world * J * args.steps / (ms * 1e-3)
+    flops_pos, bytes_pos = roofline_constants(128 * 128)
+    kernel_avg_ms = kms.value / max(1, kn.value)
+    nb = len(list(engine.generate_batches(J, B)))
+    pos_per_launch = J / nb
+    achieved = flops_pos * pos_per_launch / (kernel_avg_ms * 1e-3) / 1e12
+    peak = fp32_peak_tflops(torch, lib) if rank == 0 else None
+    traffic = read_profile_traffic()
+
+    # e2e through the public API with host-resident inputs
+    e2e = None
+    if not args.no_e2e:
+        pe = p  # preprocessed above; the engine run did not modify its host state
+        pe._amplitudes = torch.from_numpy(np.ascontiguousarray(pe._amplitudes)).pin_memory().numpy()
+        rec = dict(max_batch_size=B, seed_random=seed, progress_bar=False)
+        for _ in range(max(1, args.warmup)):
+            pe.reconstruct(num_iter=1, **rec)
+        torch.cuda.synchronize()
+        e_ms = timed_region(lambda: pe.reconstruct(num_iter=1, **rec), args.steps, barrier,
+                            torch.cuda.synchronize, now_ms, reduce_max)
+        h2d = int(pe._amplitudes.nbytes + np.asarray(pe._object).nbytes +
+                  np.asarray(pe._probe).nbytes + pe._positions_px.nbytes)
+        d2h = int(np.asarray(pe._object).nbytes + np.asarray(pe._probe).nbytes + 4)
+        e2e = {"value": world * J * args.steps / (e_ms * 1e-3), "unit": UNIT,
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "positions": J, "batch": B, "detector": 128,
+                       "object": list(np.shape(p._object)), "iterations_per_step": 1,
+                       "l2": "inputs larger than L2 (1 GiB amplitudes)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "iterations_per_s": args.steps / (ms * 1e-3),
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak,
+                         "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+                         "traffic": traffic, "kernel": "position_kernel<128,128,512>",
+                         "kernel_avg_ms": kernel_avg_ms, "kernel_launches": kn.value,
+                         "peak_source": "measured FP32 FMA probe (ptycho_fp32_fma_probe)",
+                         "flops_per_position": flops_pos, "bytes_per_position": bytes_pos,
+                         "positions_per_launch": pos_per_launch},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clocks.summary(),
+            "final_error": errors[-1] if errors else None,
+            "setup_s": setup_s,
+            "wall_ms_timed": wall_ms,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+def main(argv=None):
+    args = parse_args(argv)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,178 @@
+/*
+ * ptycho_gb300.h — C ABI of the GB300 (sm_103a) iterative-ptychography kernels.
+ *
+ * One shared library (libptycho_gb300.so) exports these entry points. They
+ * replace the array operations the py4DSTEM 0.14.18 reconstruction classes run
+ * per position batch and per iteration on their CuPy path (the reference has no
+ * native code for this path: every operator is NumPy/CuPy array code, so each
+ * entry point cites the reference Python function whose work it performs).
+ *
+ * Conventions
+ *  - All array arguments are DEVICE pointers, row-major, densely packed.
+ *    Complex arrays are interleaved complex64 (float re, float im).
+ *  - Shapes: probe/detector ROI (Sx, Sy); object (T, Px, Py); probe (M, Sx, Sy);
+ *    amplitudes (J, Sx, Sy) float32, corner-centred; positions (J, 2) float32
+ *    in object pixels.
+ *  - "rows" arrays (int32, length batch) select, for batch position b, the
+ *    pattern / position / exit wave row used; NULL means row b.
+ *  - Every call is asynchronous on `stream` (a cudaStream_t, NULL = legacy
+ *    default stream) and allocates nothing: scratch space is the caller's
+ *    `workspace` of at least ptycho_workspace_bytes() bytes, 256-byte aligned.
+ *  - Return value: PTYCHO_OK (0) or an error code; ptycho_last_error() gives a
+ *    message (per host thread). No C++ exception crosses this boundary.
+ *  - Results are deterministic for a given geometry and batch size: gradient
+ *    sums over positions use fixed-order, position-tiled reductions, no float
+ *    atomics.
+ */
+#ifndef PTYCHO_GB300_H
+#define PTYCHO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PTYCHO_ABI_VERSION 1
+
+enum ptycho_status {
+  PTYCHO_OK = 0,
+  PTYCHO_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad size or flag          */
+  PTYCHO_ERR_UNSUPPORTED = 2,      /* ROI size or geometry without a kernel   */
+  PTYCHO_ERR_WORKSPACE = 3,        /* workspace too small or misaligned       */
+  PTYCHO_ERR_CUDA = 4,             /* a CUDA launch or runtime call failed    */
+  PTYCHO_ERR_NONFINITE = 5         /* a reduction produced NaN or Inf         */
+};
+
+/* Geometry shared by every call of one reconstruction. */
+typedef struct ptycho_geometry {
+  int32_t roi_x;               /* Sx: probe / detector pixels along x         */
+  int32_t roi_y;               /* Sy                                          */
+  int32_t object_x;            /* Px (>= Sx)                                  */
+  int32_t object_y;            /* Py (>= Sy)                                  */
+  int32_t num_slices;          /* T: 1 = single slice                         */
+  int32_t num_probes;          /* M: 1 = single probe                         */
+  int32_t object_is_potential; /* 0: complex64 object, 1: float32 potential   */
+  int32_t flags;               /* PTYCHO_FLAG_* bits; unknown bits must be 0  */
+} ptycho_geometry;
+
+/* Use the mixed-state Fourier projection (shared ratio A/sqrt(sum_m |F_m|^2),
+ * mixedstate class) even when num_probes == 1. Implied when num_probes > 1. */
+#define PTYCHO_FLAG_MIXED_STATE 1
+
+/* Library identity and capability queries. */
+int ptycho_abi_version(void);
+const char* ptycho_last_error(void);
+/* 1 if a fused kernel exists for this ROI (Sx, Sy), else 0. */
+int ptycho_roi_supported(int32_t roi_x, int32_t roi_y);
+
+/* Scratch bytes one batch call needs for up to max_batch positions. */
+size_t ptycho_workspace_bytes(const ptycho_geometry* geometry, int32_t max_batch);
+
+/*
+ * One gradient-descent batch: forward model, Fourier amplitude projection,
+ * adjoint and the object/probe update, for `batch` positions.
+ *
+ * Replaces, per batch of reconstruct() (singleslice_ptychography.py:859-929,
+ * multislice_ptychography.py:975-1047, mixedstate_ptychography.py:889-957):
+ *   fft_shift / _return_shifted_probes  (utils.py:508-533, ptychographic_methods.py:1482-1487)
+ *   _overlap_projection                 (ptychographic_methods.py:1489-1527, 2300-2351, 2696-2734)
+ *   _gradient_descent_fourier_projection (ptychographic_methods.py:1576-1635, 2742-2804)
+ *   _gradient_descent_adjoint           (ptychographic_methods.py:1818-1908, 2353-2458, 2906-3000)
+ *   _sum_overlapping_patches_bincounts  (phase_base_class.py:1905-1968)
+ * object: (T,Px,Py) complex64, or float32 if object_is_potential.
+ * probe: (M,Sx,Sy) complex64, updated unless fix_probe.
+ * detector_mask: (Sx,Sy) float32 corner-centred Fourier mask or NULL.
+ * propagators: (T-1,Sx,Sy) complex64 Fresnel propagators (NULL when T == 1).
+ * error_accum: one float32 on the device; the batch error sum is added to it.
+ */
+int ptycho_gd_batch(const ptycho_geometry* geometry, void* object, void* probe,
+                    const float* amplitudes, const int32_t* amplitude_rows,
+                    const float* positions_px, const int32_t* position_rows,
+                    int32_t batch, float step_size, float normalization_min,
+                    int32_t fix_probe, const float* detector_mask,
+                    const void* propagators, float* error_accum, void* workspace,
+                    size_t workspace_bytes, void* stream);
+
+/*
+ * One projection-set batch (DM_AP, RAAR, RRR, SUPERFLIP, generalized (a,b,c)):
+ * exit-wave update and the ASSIGNED (not accumulated) object/probe estimates.
+ * Replaces _projection_sets_fourier_projection (ptychographic_methods.py:1637-1734,
+ * 2806-2904) and _projection_sets_adjoint (1910-1998, 2460-2565, 3002-3093).
+ * exit_waves: (J,M,Sx,Sy) complex64 persistent state indexed by position_rows;
+ * exit_waves_valid = 0 on the first iteration (the overlap seeds them).
+ */
+int ptycho_projection_batch(const ptycho_geometry* geometry, void* object, void* probe,
+                            const float* amplitudes, const int32_t* amplitude_rows,
+                            const float* positions_px, const int32_t* position_rows,
+                            int32_t batch, float projection_a, float projection_b,
+                            float projection_c, float normalization_min,
+                            int32_t fix_probe, void* exit_waves,
+                            int32_t exit_waves_valid, const void* propagators,
+                            float* error_accum, void* workspace,
+                            size_t workspace_bytes, void* stream);
+
+/*
+ * Per-iteration object constraints, default-on subset: shrinkage by
+ * shrinkage_rad plus the mean phase (or potential) over `mask` (Px,Py uint8,
+ * NULL = no mask term), then amplitude threshold |O| <= 1 (pure_phase: |O| = 1)
+ * for complex objects or positivity for potentials.
+ * Replaces _object_shrinkage_constraint / _object_threshold_constraint /
+ * _object_positivity_constraint (ptychographic_constraints.py:29-117, 411-464).
+ */
+int ptycho_object_constraints(const ptycho_geometry* geometry, void* object,
+                              const uint8_t* mask, float shrinkage_rad,
+                              int32_t apply_shrinkage, int32_t pure_phase,
+                              int32_t positivity, void* workspace,
+                              size_t workspace_bytes, void* stream);
+
+/*
+ * Probe centre-of-mass constraint: Fourier-shift every mode so that the
+ * intensity centre of mass of mode 0 sits at the corner origin.
+ * Replaces _probe_center_of_mass_constraint (ptychographic_constraints.py:894-918,
+ * 1156-1179).
+ */
+int ptycho_probe_com_constraint(const ptycho_geometry* geometry, void* probe,
+                                void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * Mixed-state orthogonalisation, step 1: the M x M Gram matrix
+ * gram[i*M+j] = sum conj(P_i) P_j (complex64, full matrix).
+ * Replaces the pairwise products of _probe_orthogonalization_constraint
+ * (ptychographic_constraints.py:1181-1216).
+ */
+int ptycho_probe_gram(const ptycho_geometry* geometry, const void* probe, void* gram,
+                      void* stream);
+
+/*
+ * Mixed-state orthogonalisation, step 2: probe_out[i] = sum_j coeffs[i*M+j] * probe_in[j]
+ * (complex64 coefficients; the eigenvector transform and the intensity sort are
+ * folded into `coeffs` by the caller). probe_out must not alias probe_in.
+ */
+int ptycho_probe_mix(const ptycho_geometry* geometry, const void* probe_in,
+                     const void* coeffs, void* probe_out, void* stream);
+
+/*
+ * Instrumentation. When enabled, every launch of the fused per-position kernel
+ * is bracketed by CUDA events recorded on its stream; ptycho_kernel_timing()
+ * waits for the last one and returns the summed kernel time (ms) and the number
+ * of launches since the previous query, then clears the record. No reference
+ * counterpart (the reference has no kernels of its own on this path).
+ */
+int ptycho_enable_kernel_timing(int32_t enable);
+int ptycho_kernel_timing(float* total_ms, int32_t* launches);
+
+/*
+ * FP32 throughput probe: `blocks` blocks of 256 threads each run `iters`
+ * iterations of 8 independent FMA chains and write one float per thread to
+ * `sink` (device, blocks*256 floats). 16 * blocks * 256 * iters flops. Used to
+ * measure the FP32 (non-tensor) peak the FFT kernels are judged against.
+ */
+int ptycho_fp32_fma_probe(int32_t blocks, int32_t iters, float* sink, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PTYCHO_GB300_H */

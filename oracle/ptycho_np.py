@@ -1,0 +1,412 @@
+"""NumPy restatement of the py4DSTEM 0.14.18 ptychographic reconstruction loop.
+
+TEST INFRASTRUCTURE ONLY (the parity oracle). The product package never imports
+this module; only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
+do, and only to check or to time the CPU reference algorithm.
+
+Input is the preprocessed state (corner-centred amplitudes, pixel positions,
+initial object and probe, mean intensity, FOV mask); output is the object,
+probe and error history after `num_iter` iterations. With dtype="float32" every
+array operation follows the reference's own NumPy expressions in complex64 /
+float32, so on the same inputs it reproduces the reference's CPU path; with
+dtype="float64" the same model runs in complex128 / float64 (the FP64 evaluation
+each GPU result is compared against).
+
+Parity of this module is pinned by tests/golden/*.npz, which hold outputs of the
+unmodified reference (tests/golden/make_golden.py) and are checked in
+tests/test_oracle_golden.py.
+
+Reference citations are py4DSTEM/process/phase/<file>:<line>.
+"""
+
+from __future__ import annotations
+
+import dataclasses
+from typing import Optional
+
+import numpy as np
+
+
+@dataclasses.dataclass
+class State:
+    """Preprocessed inputs of a reconstruction (what preprocess() leaves behind)."""
+
+    amplitudes: np.ndarray          # (J, Sx, Sy) float32, corner-centred
+    positions_px: np.ndarray        # (J, 2) float32
+    probe: np.ndarray               # (Sx,Sy) or (M,Sx,Sy) complex64
+    object: np.ndarray              # (Px,Py) / (T,Px,Py) complex64 or float32
+    mean_intensity: float
+    fov_mask_inverse: np.ndarray    # (Px,Py) bool
+    object_type: str = "complex"
+    num_slices: int = 1             # >1: multislice
+    num_probes: int = 1             # >1 or mixed=True: mixed state
+    mixed: bool = False
+    propagators: Optional[np.ndarray] = None  # (T-1,Sx,Sy) complex64
+
+    def copy(self):
+        return dataclasses.replace(
+            self, positions_px=self.positions_px.copy(), probe=self.probe.copy(),
+            object=self.object.copy())
+
+
+class Oracle:
+    """Reference reconstruction loop over a :class:`State`."""
+
+    def __init__(self, state: State, dtype: str = "float32", fft_round_trip: bool = False):
+        """fft_round_trip=True evaluates every FFT in complex128 and rounds the
+        result to the working precision: the same model with a different (more
+        accurate) float32 FFT, used to measure how far the reference moves under
+        FFT rounding alone."""
+        if dtype not in ("float32", "float64"):
+            raise ValueError("dtype must be 'float32' or 'float64'")
+        self.fft_round_trip = fft_round_trip
+        self.f = np.float32 if dtype == "float32" else np.float64
+        self.c = np.complex64 if dtype == "float32" else np.complex128
+        s = state
+        self.amplitudes = np.asarray(s.amplitudes, dtype=self.f)
+        self.positions_px = np.asarray(s.positions_px, dtype=np.float32).copy()
+        self.object_type = s.object_type
+        otype = self.f if s.object_type == "potential" else self.c
+        self.object = np.asarray(s.object, dtype=otype).copy()
+        self.probe = np.asarray(s.probe, dtype=self.c).copy()
+        self.mean_intensity = s.mean_intensity
+        self.fov_mask_inverse = np.asarray(s.fov_mask_inverse, dtype=bool)
+        self.num_slices = s.num_slices
+        self.mixed = s.mixed or s.num_probes > 1
+        self.num_probes = s.num_probes
+        self.propagators = (None if s.propagators is None
+                            else np.asarray(s.propagators, dtype=self.c))
+        self.roi = np.array(self.amplitudes.shape[-2:])
+        self.object_shape = self.object.shape[-2:]
+        self.J = self.amplitudes.shape[0]
+        self.exit_waves = None
+        self.error_iterations = []
+
+    def fft2(self, a):
+        if self.fft_round_trip:
+            return np.fft.fft2(a.astype(np.complex128)).astype(self.c)
+        return np.fft.fft2(a)
+
+    def ifft2(self, a):
+        if self.fft_round_trip:
+            return np.fft.ifft2(a.astype(np.complex128)).astype(self.c)
+        return np.fft.ifft2(a)
+
+    # ------------------------------------------------------------ A4, A5, A6, A15
+    @staticmethod
+    def batches(num_items, max_batch):
+        """utils.py:539-589."""
+        nb = (num_items + (-num_items % max_batch)) // max_batch
+        if num_items % nb == 0:
+            sizes = [num_items // nb] * nb
+        else:
+            zp = nb - (num_items % nb)
+            pp = num_items // nb
+            sizes = []
+            for i in range(nb):
+                sizes = ([pp + 1] if i >= zp else [pp]) + sizes
+        start = 0
+        for n in sizes:
+            yield start, start + n
+            start += n
+
+    def patch_indices(self, positions_px):
+        """phase_base_class.py:1970-2003."""
+        x0 = np.round(positions_px[:, 0]).astype("int")
+        y0 = np.round(positions_px[:, 1]).astype("int")
+        xi = np.fft.fftfreq(self.roi[0], d=1 / self.roi[0]).astype("int")
+        yi = np.fft.fftfreq(self.roi[1], d=1 / self.roi[1]).astype("int")
+        rows = (x0[:, None, None] + xi[None, :, None]) % self.object_shape[0]
+        cols = (y0[:, None, None] + yi[None, None, :]) % self.object_shape[1]
+        return rows, cols
+
+    def fft_shift(self, array, positions):
+        """utils.py:468-533."""
+        f = self.f
+        kx = np.fft.fftfreq(array.shape[-2], 1.0).astype(f)
+        ky = np.fft.fftfreq(array.shape[-1], 1.0).astype(f)
+        pos = np.asarray(positions, dtype=f)
+        single = pos.ndim == 1
+        if single:
+            pos = pos[None]
+        x = pos[:, 0].ravel()[:, None, None]
+        y = pos[:, 1].ravel()[:, None, None]
+        op = np.exp(-2.0j * np.pi * kx[None, :, None] * x) * np.exp(
+            -2.0j * np.pi * ky[None, None, :] * y)
+        if single:
+            op = op[0]
+        fa = self.fft2(array)
+        if op.ndim == 3 and fa.ndim == 3:
+            shifted = fa[None] * op[:, None]
+        else:
+            shifted = fa * op
+        return self.ifft2(shifted)
+
+    def scatter(self, patches, positions_px):
+        """phase_base_class.py:1905-1968 (float64 bincount, then float32/64)."""
+        if np.iscomplexobj(patches):
+            return self._scatter_real(patches.real, positions_px) + 1.0j * self._scatter_real(
+                patches.imag, positions_px)
+        return self._scatter_real(patches, positions_px)
+
+    def _scatter_real(self, patches, positions_px):
+        x0 = np.round(positions_px[:, 0]).astype("int")
+        y0 = np.round(positions_px[:, 1]).astype("int")
+        xi = np.fft.fftfreq(self.roi[0], d=1 / self.roi[0]).astype("int")
+        yi = np.fft.fftfreq(self.roi[1], d=1 / self.roi[1]).astype("int")
+        shape = self.object_shape
+        idx = ((y0[:, None, None] + yi[None, None, :]) % shape[1]) + (
+            (x0[:, None, None] + xi[None, :, None]) % shape[0]) * shape[1]
+        counts = np.bincount(idx.ravel(), weights=patches.ravel(), minlength=int(np.prod(shape)))
+        return np.reshape(counts, shape).astype(self.f)
+
+    # ------------------------------------------------------------- forward A7-A12
+    def overlap(self, rows, cols, shifted):
+        """ptychographic_methods.py:1489-1527 (2D), 2300-2351 (2.5D), 2696-2734 (mixed)."""
+        if self.num_slices > 1:
+            patches = self.object[:, rows, cols]
+            if self.object_type == "potential":
+                patches = np.exp(1j * patches)
+            probes = np.empty_like(patches)
+            probes[0] = shifted
+            for s in range(self.num_slices):
+                ov = patches[s] * probes[s]
+                if s + 1 < self.num_slices:
+                    probes[s + 1] = self.ifft2(self.fft2(ov) * self.propagators[s])
+            return probes, patches, ov
+        patches = self.object[rows, cols]
+        if self.object_type == "potential":
+            patches = np.exp(1j * patches)
+        if self.mixed:
+            return shifted, patches, shifted * np.expand_dims(patches, axis=1)
+        return shifted, patches, shifted * patches
+
+    def farfield(self, fo):
+        if self.mixed:
+            return np.sqrt(np.sum(np.abs(fo) ** 2, axis=1))
+        return np.abs(fo)
+
+    def gd_projection(self, amplitudes, overlap, mask):
+        """ptychographic_methods.py:1576-1635 and 2742-2804."""
+        fo = self.fft2(overlap)
+        if mask is not None:
+            fo *= mask
+        ff = self.farfield(fo)
+        error = np.sum(np.abs(amplitudes - ff) ** 2)
+        if self.mixed:
+            ff[ff == 0.0] = np.inf
+            mod = (amplitudes / ff)[:, None] * fo - fo
+        else:
+            mod = amplitudes * np.exp(1j * np.angle(fo)) - fo
+        if mask is not None:
+            mod *= mask
+        return self.ifft2(mod), error
+
+    def ps_projection(self, amplitudes, overlap, exit_waves, a, b, c):
+        """ptychographic_methods.py:1637-1734 and 2806-2904."""
+        x = 1 - a - b
+        y = 1 - c
+        if exit_waves is None:
+            exit_waves = overlap.copy()
+        factor = c * overlap + y * exit_waves
+        fp = self.fft2(factor)
+        ff = self.farfield(fp)
+        error = np.sum(np.abs(amplitudes - ff) ** 2)
+        if self.mixed:
+            ff[ff == 0.0] = np.inf
+            fp *= (amplitudes / ff)[:, None]
+        else:
+            fp = amplitudes * np.exp(1j * np.angle(fp))
+        projected = self.ifft2(fp)
+        return x * exit_waves + a * overlap + b * projected, error
+
+    # --------------------------------------------------------------- adjoint A13-A14
+    def _normaliser(self, s, m):
+        return 1 / np.sqrt(1e-16 + ((1 - m) * s) ** 2 + (m * np.max(s)) ** 2)
+
+    def _obj_term(self, patch, probe, chi):
+        if self.object_type == "potential":
+            return np.real(-1j * np.conj(patch) * np.conj(probe) * chi)
+        return np.conj(probe) * chi
+
+    def adjoint(self, patches, shifted, positions_px, ew, step, m, fix_probe, projection):
+        """ptychographic_methods.py:1818-2069 (2D), 2353-2565 (2.5D), 2906-3093 (mixed)."""
+        obj, probe = self.object, self.probe
+        if self.num_slices > 1:
+            ew = ew.copy() if projection else ew
+            for s in reversed(range(self.num_slices)):
+                pr = shifted[s]
+                op = patches[s]
+                nrm = self._normaliser(self.scatter(np.abs(pr) ** 2, positions_px), m)
+                upd = self.scatter(self._obj_term(op, pr, ew), positions_px) * nrm
+                if projection:
+                    obj[s] = upd
+                else:
+                    obj[s] += step * upd
+                ew *= np.conj(op)
+                if s > 0:
+                    ew = self.ifft2(self.fft2(ew) * np.conj(self.propagators[s - 1]))
+                elif not fix_probe:
+                    on = self._normaliser(np.sum(np.abs(op) ** 2, axis=0), m)
+                    if projection:
+                        probe = np.sum(ew, axis=0) * on
+                    else:
+                        probe += step * np.sum(ew, axis=0) * on
+            self.object, self.probe = obj, probe
+            return
+        if self.mixed:
+            pn = np.zeros_like(obj)
+            upd = np.zeros_like(obj)
+            for i in range(self.num_probes):
+                pn += self.scatter(np.abs(shifted[:, i]) ** 2, positions_px)
+                term = self.scatter(self._obj_term(patches, shifted[:, i], ew[:, i]), positions_px)
+                upd += term if projection else step * term
+            pn = self._normaliser(pn, m)
+            if projection:
+                obj = upd * pn
+            else:
+                obj += upd * pn
+            if not fix_probe:
+                on = self._normaliser(np.sum(np.abs(patches) ** 2, axis=0), m)
+                g = np.sum(np.expand_dims(np.conj(patches), axis=1) * ew, axis=0) * on[None]
+                probe = g if projection else probe + step * g
+            self.object, self.probe = obj, probe
+            return
+        pn = self._normaliser(self.scatter(np.abs(shifted) ** 2, positions_px), m)
+        upd = self.scatter(self._obj_term(patches, shifted, ew), positions_px) * pn
+        if projection:
+            obj = upd
+        else:
+            obj += step * upd
+        if not fix_probe:
+            on = self._normaliser(np.sum(np.abs(patches) ** 2, axis=0), m)
+            g = np.sum(np.conj(patches) * ew, axis=0) * on
+            probe = g if projection else probe + step * g
+        self.object, self.probe = obj, probe
+
+    # ------------------------------------------------------------ constraints A17
+    def object_constraints(self, shrinkage_rad, mask, pure_phase, positivity):
+        """ptychographic_constraints.py:29-117, 411-464, 649-726 (default-on subset)."""
+        o = self.object
+        if shrinkage_rad > 0.0 or mask is not None:
+            if self.object_type == "complex":
+                phase = np.angle(o)
+                amp = np.abs(o)
+                if mask is not None:
+                    shrinkage_rad += phase[..., mask].mean()
+                phase -= shrinkage_rad
+                o = amp * np.exp(1.0j * phase)
+            else:
+                if mask is not None:
+                    shrinkage_rad += o[..., mask].mean()
+                o -= shrinkage_rad
+        if self.object_type == "complex":
+            phase = np.angle(o)
+            amp = 1.0 if pure_phase else np.minimum(np.abs(o), 1.0)
+            o = amp * np.exp(1.0j * phase)
+        elif positivity:
+            o = o.clip(0.0)
+        self.object = o
+
+    def center_of_mass(self, ar):
+        """process/utils/utils.py:166-187 (corner-centred)."""
+        nx, ny = ar.shape
+        ry, rx = np.meshgrid(np.fft.fftfreq(ny, 1 / ny), np.fft.fftfreq(nx, 1 / nx))
+        tot = np.sum(ar)
+        return np.sum(rx * ar) / tot, np.sum(ry * ar) / tot
+
+    def probe_com_constraint(self):
+        """ptychographic_constraints.py:894-918, 1156-1179."""
+        inten = np.abs(self.probe[0] if self.mixed else self.probe) ** 2
+        x0, y0 = self.center_of_mass(inten)
+        self.probe = self.fft_shift(self.probe, -np.array([x0, y0]))
+
+    def probe_orthogonalization(self):
+        """ptychographic_constraints.py:1181-1216."""
+        n = self.num_probes
+        p = self.probe
+        gram = np.empty((n, n), dtype=p.dtype)
+        for i in range(n):
+            for j in range(i, n):
+                gram[i, j] = np.sum(p[i].conj() * p[j])
+        _, evecs = np.linalg.eigh(gram, UPLO="U")
+        p = np.tensordot(evecs.T, p, axes=1)
+        inten = np.sum(np.abs(p) ** 2, axis=(-2, -1))
+        self.probe = p[np.argsort(inten, axis=None)[::-1]]
+
+    # ---------------------------------------------------------------- loop A1-A3
+    def reconstruct(self, num_iter=8, method="GD", a=None, b=None, c=None, max_batch_size=None,
+                    seed_random=None, step_size=0.5, normalization_min=1.0, fix_probe=False,
+                    fix_probe_com=True, orthogonalize_probe=True, shrinkage_rad=0.0,
+                    fix_potential_baseline=True, pure_phase_object=False,
+                    object_positivity=True, detector_fourier_mask=None):
+        """singleslice_ptychography.py:606-996 (and the multislice / mixed-state twins)."""
+        projection = method != "GD"
+        J = self.J
+        order = np.arange(J)
+        if max_batch_size is not None:
+            np.random.seed(seed_random)
+        else:
+            max_batch_size = J
+        mask = (self.fov_mask_inverse
+                if fix_potential_baseline and self.fov_mask_inverse.sum() > 0 else None)
+        error = None
+        for _ in range(num_iter):
+            error = 0.0
+            if not projection:
+                np.random.shuffle(order)
+            for start, end in self.batches(J, max_batch_size):
+                idx = order[start:end]
+                pos = self.positions_px[idx]
+                frac = pos - np.round(pos)
+                rows, cols = self.patch_indices(pos)
+                amps = self.amplitudes[idx]
+                shifted = self.fft_shift(self.probe, frac)
+                shifted, patches, ov = self.overlap(rows, cols, shifted)
+                if projection:
+                    self.exit_waves, be = self.ps_projection(amps, ov, self.exit_waves, a, b, c)
+                    ew = self.exit_waves
+                else:
+                    ew, be = self.gd_projection(amps, ov, detector_fourier_mask)
+                self.adjoint(patches, shifted, pos, ew, step_size, normalization_min, fix_probe,
+                             projection)
+                error += be
+            error /= self.mean_intensity * J
+            self.object_constraints(shrinkage_rad, mask,
+                                    pure_phase_object and self.object_type == "complex",
+                                    object_positivity)
+            if fix_probe_com and not fix_probe:
+                self.probe_com_constraint()
+            if self.mixed and orthogonalize_probe:
+                self.probe_orthogonalization()
+            self.error_iterations.append(float(error))
+        return self
+
+    # ---------------------------------------------------- single-batch primitives
+    def forward_batch(self, idx):
+        """Forward model of one batch (no update): returns (shifted probes, patches,
+        exit waves, chi, error) for kernel-level parity tests."""
+        pos = self.positions_px[idx]
+        frac = pos - np.round(pos)
+        rows, cols = self.patch_indices(pos)
+        shifted = self.fft_shift(self.probe, frac)
+        shifted, patches, ov = self.overlap(rows, cols, shifted)
+        chi, err = self.gd_projection(self.amplitudes[idx], ov, None)
+        return shifted, patches, ov, chi, err
+
+
+def method_abc(method, parameter=1.0, a=None, b=None, c=None):
+    """phase_base_class.py:2005-2108: projection parameters of a named method."""
+    if method in ("GD", "gradient-descent"):
+        return "GD", None, None, None
+    if method in ("DM_AP", "difference-map_alternating-projections"):
+        return "PS", -parameter, 1, 1 + parameter
+    if method in ("RAAR", "relaxed-averaged-alternating-reflections"):
+        return "PS", 1 - 2 * parameter, parameter, 2
+    if method in ("RRR", "relax-reflect-reflect"):
+        return "PS", -parameter, parameter, 2
+    if method in ("SUPERFLIP", "charge-flipping"):
+        return "PS", 0, 1, 2
+    if method == "generalized-projections":
+        return "PS", a, b, c
+    raise ValueError(method)

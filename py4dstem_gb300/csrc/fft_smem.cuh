@@ -1,0 +1,260 @@
+// In-shared-memory 2D FFT building blocks for one thread block.
+//
+// A wave of SX x SY complex64 samples lives in shared memory, row-major, with a
+// row pitch of SY + 1 float2 so that both row and column passes are free of bank
+// conflicts (see line_pass below). The 1D transforms are Stockham auto-sort
+// passes: each pass reads R samples of a line with stride L/R, applies the
+// inter-pass twiddles, runs a radix-R DFT in registers and writes the results
+// back in natural order. The pass is in place: every thread keeps its samples in
+// registers across a block barrier between the read and the write phase.
+//
+// Radix-R DFTs (R in {2,4,8,16}) are radix-2 decimation-in-frequency networks
+// fully unrolled in registers; R = 3 uses the standard 3-point butterfly. Their
+// internal twiddles are exact 16th roots of unity. Inter-pass twiddles come from
+// a per-block table exp(-2 pi i m / L), m < L, filled with sincospif().
+//
+// Conventions match numpy.fft: forward = exp(-2 pi i n k / L) unnormalised,
+// inverse = exp(+2 pi i n k / L); the caller applies the 1/(SX*SY) factor.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace pty {
+
+// ---------------------------------------------------------------- complex ops
+__device__ __forceinline__ float2 c_add(float2 a, float2 b) {
+  return make_float2(a.x + b.x, a.y + b.y);
+}
+__device__ __forceinline__ float2 c_sub(float2 a, float2 b) {
+  return make_float2(a.x - b.x, a.y - b.y);
+}
+__device__ __forceinline__ float2 c_mul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// conj(a) * b
+__device__ __forceinline__ float2 c_conj_mul(float2 a, float2 b) {
+  return make_float2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float2 c_scale(float2 a, float s) {
+  return make_float2(a.x * s, a.y * s);
+}
+__device__ __forceinline__ float c_abs2(float2 a) { return a.x * a.x + a.y * a.y; }
+
+// cos(2 pi m / 16) and sin(2 pi m / 16) for compile-time m after unrolling.
+__device__ __forceinline__ float cos16(int m) {
+  switch (m & 15) {
+    case 0: return 1.0f;
+    case 1: return 0.92387953251128674f;
+    case 2: return 0.70710678118654752f;
+    case 3: return 0.38268343236508977f;
+    case 4: return 0.0f;
+    case 5: return -0.38268343236508977f;
+    case 6: return -0.70710678118654752f;
+    case 7: return -0.92387953251128674f;
+    case 8: return -1.0f;
+    case 9: return -0.92387953251128674f;
+    case 10: return -0.70710678118654752f;
+    case 11: return -0.38268343236508977f;
+    case 12: return 0.0f;
+    case 13: return 0.38268343236508977f;
+    case 14: return 0.70710678118654752f;
+    default: return 0.92387953251128674f;
+  }
+}
+__device__ __forceinline__ float sin16(int m) { return cos16(m - 4); }
+
+// d * exp(DIR * 2 pi i m / 16), specialised for the trivial roots.
+template <int DIR>
+__device__ __forceinline__ float2 rot16(float2 d, int m) {
+  m &= 15;
+  if (m == 0) return d;
+  if (m == 4) return DIR < 0 ? make_float2(d.y, -d.x) : make_float2(-d.y, d.x);
+  if (m == 8) return make_float2(-d.x, -d.y);
+  if (m == 12) return DIR < 0 ? make_float2(-d.y, d.x) : make_float2(d.y, -d.x);
+  const float c = cos16(m);
+  const float s = DIR < 0 ? -sin16(m) : sin16(m);
+  return make_float2(d.x * c - d.y * s, d.x * s + d.y * c);
+}
+
+template <int R>
+__device__ __forceinline__ constexpr int bitrev(int k) {
+  int r = 0;
+  for (int b = 1; b < R; b <<= 1) {
+    r = (r << 1) | (k & 1);
+    k >>= 1;
+  }
+  return r;
+}
+
+// In-register DFT of length R (power of two, R <= 16), natural order in/out.
+template <int R, int DIR>
+__device__ __forceinline__ void dft_pow2(float2 (&a)[R]) {
+#pragma unroll
+  for (int half = R / 2; half >= 1; half >>= 1) {
+#pragma unroll
+    for (int base = 0; base < R; base += 2 * half) {
+#pragma unroll
+      for (int i = 0; i < half; ++i) {
+        const float2 u = a[base + i];
+        const float2 v = a[base + i + half];
+        a[base + i] = c_add(u, v);
+        a[base + i + half] = rot16<DIR>(c_sub(u, v), i * (16 / (2 * half)));
+      }
+    }
+  }
+  float2 t[R];
+#pragma unroll
+  for (int k = 0; k < R; ++k) t[k] = a[bitrev<R>(k)];
+#pragma unroll
+  for (int k = 0; k < R; ++k) a[k] = t[k];
+}
+
+template <int DIR>
+__device__ __forceinline__ void dft3(float2 (&a)[3]) {
+  const float h = 0.86602540378443865f;  // sqrt(3)/2
+  const float2 t = c_add(a[1], a[2]);
+  const float2 m = make_float2(a[0].x - 0.5f * t.x, a[0].y - 0.5f * t.y);
+  const float2 d = c_sub(a[1], a[2]);
+  // s = d * (DIR * i * sqrt(3)/2)
+  const float2 s = DIR < 0 ? make_float2(h * d.y, -h * d.x) : make_float2(-h * d.y, h * d.x);
+  a[0] = c_add(a[0], t);
+  a[1] = c_add(m, s);
+  a[2] = c_sub(m, s);
+}
+
+template <int R, int DIR>
+__device__ __forceinline__ void dft(float2 (&a)[R]) {
+  if constexpr (R == 3) {
+    dft3<DIR>(a);
+  } else {
+    static_assert((R & (R - 1)) == 0 && R <= 16, "radix must be 3 or a power of two <= 16");
+    dft_pow2<R, DIR>(a);
+  }
+}
+
+// Fill tw[m] = exp(-2 pi i m / L) for m < L (block-cooperative, no barrier).
+template <int L, int NT>
+__device__ __forceinline__ void fill_twiddles(float2* tw) {
+  for (int m = threadIdx.x; m < L; m += NT) {
+    float s, c;
+    sincospif(2.0f * (float)m / (float)L, &s, &c);
+    tw[m] = make_float2(c, -s);
+  }
+}
+
+// One Stockham pass over NLINES lines of length L with radix R; NS is the length
+// of the sub-transforms already completed. Lanes of a warp take consecutive
+// lines, so with a pitch of SY+1 rows (row pass) or unit-stride columns (column
+// pass) the 32 lanes touch 32 distinct banks pairs.
+template <int L, int R, int NS, int NLINES, int NT, int DIR>
+__device__ __forceinline__ void line_pass(float2* buf, int line_stride, int elem_stride,
+                                          const float2* __restrict__ tw) {
+  constexpr int BF = L / R;            // butterflies per line
+  constexpr int WORK = NLINES * BF;    // butterflies per pass
+  constexpr int ITEMS = (WORK + NT - 1) / NT;
+  static_assert(L % (NS * R) == 0, "invalid Stockham schedule");
+  float2 v[ITEMS][R];
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int it = 0; it < ITEMS; ++it) {
+    const int w = tid + it * NT;
+    if (WORK % NT == 0 || w < WORK) {
+      const int line = w % NLINES;
+      const int j = w / NLINES;
+      const float2* p = buf + line * line_stride;
+#pragma unroll
+      for (int k = 0; k < R; ++k) v[it][k] = p[(j + k * BF) * elem_stride];
+      if constexpr (NS > 1) {
+        const int jm = j % NS;
+#pragma unroll
+        for (int k = 1; k < R; ++k) {
+          float2 t = tw[(jm * k * (L / (NS * R))) % L];
+          if (DIR > 0) t.y = -t.y;
+          v[it][k] = c_mul(v[it][k], t);
+        }
+      }
+      float2 (&row)[R] = v[it];
+      dft<R, DIR>(row);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int it = 0; it < ITEMS; ++it) {
+    const int w = tid + it * NT;
+    if (WORK % NT == 0 || w < WORK) {
+      const int line = w % NLINES;
+      const int j = w / NLINES;
+      const int jm = j % NS;
+      const int base = (j / NS) * NS * R + jm;
+      float2* p = buf + line * line_stride;
+#pragma unroll
+      for (int k = 0; k < R; ++k) p[(base + k * NS) * elem_stride] = v[it][k];
+    }
+  }
+  __syncthreads();
+}
+
+// Radix schedule per transform length: a compile-time list of passes.
+template <int L>
+struct Schedule;
+template <>
+struct Schedule<16> {
+  template <int NLINES, int NT, int DIR>
+  __device__ static void run(float2* b, int ls, int es, const float2* tw) {
+    line_pass<16, 16, 1, NLINES, NT, DIR>(b, ls, es, tw);
+  }
+};
+template <>
+struct Schedule<32> {
+  template <int NLINES, int NT, int DIR>
+  __device__ static void run(float2* b, int ls, int es, const float2* tw) {
+    line_pass<32, 8, 1, NLINES, NT, DIR>(b, ls, es, tw);
+    line_pass<32, 4, 8, NLINES, NT, DIR>(b, ls, es, tw);
+  }
+};
+template <>
+struct Schedule<48> {
+  template <int NLINES, int NT, int DIR>
+  __device__ static void run(float2* b, int ls, int es, const float2* tw) {
+    line_pass<48, 16, 1, NLINES, NT, DIR>(b, ls, es, tw);
+    line_pass<48, 3, 16, NLINES, NT, DIR>(b, ls, es, tw);
+  }
+};
+template <>
+struct Schedule<64> {
+  template <int NLINES, int NT, int DIR>
+  __device__ static void run(float2* b, int ls, int es, const float2* tw) {
+    line_pass<64, 8, 1, NLINES, NT, DIR>(b, ls, es, tw);
+    line_pass<64, 8, 8, NLINES, NT, DIR>(b, ls, es, tw);
+  }
+};
+template <>
+struct Schedule<96> {
+  template <int NLINES, int NT, int DIR>
+  __device__ static void run(float2* b, int ls, int es, const float2* tw) {
+    line_pass<96, 8, 1, NLINES, NT, DIR>(b, ls, es, tw);
+    line_pass<96, 4, 8, NLINES, NT, DIR>(b, ls, es, tw);
+    line_pass<96, 3, 32, NLINES, NT, DIR>(b, ls, es, tw);
+  }
+};
+template <>
+struct Schedule<128> {
+  template <int NLINES, int NT, int DIR>
+  __device__ static void run(float2* b, int ls, int es, const float2* tw) {
+    line_pass<128, 16, 1, NLINES, NT, DIR>(b, ls, es, tw);
+    line_pass<128, 8, 16, NLINES, NT, DIR>(b, ls, es, tw);
+  }
+};
+
+// Full 2D transform of the SX x SY block in shared memory (pitch SY + 1).
+// twx: table for length SX, twy: table for length SY.
+template <int SX, int SY, int NT, int DIR>
+__device__ __forceinline__ void fft2d(float2* buf, const float2* twx, const float2* twy) {
+  constexpr int LD = SY + 1;
+  // rows: SX lines of length SY, contiguous
+  Schedule<SY>::template run<SX, NT, DIR>(buf, LD, 1, twy);
+  // columns: SY lines of length SX, stride LD
+  Schedule<SX>::template run<SY, NT, DIR>(buf, 1, LD, twx);
+}
+
+}  // namespace pty

@@ -1,0 +1,368 @@
+// extern "C" entry points of libptycho_gb300.so (declared in include/ptycho_gb300.h).
+// Validates arguments, carves the caller's workspace and launches the kernels of
+// ptycho_position.cu and ptycho_reduce.cu on the caller's stream.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "../../include/ptycho_gb300.h"
+#include "ptycho_internal.h"
+
+namespace pty {
+namespace {
+
+thread_local char g_last_error[512] = "";
+
+int fail(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+  return fail(PTYCHO_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+}
+
+size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
+
+// ---- position-kernel timing: pairs of events recorded around each launch
+std::mutex g_timing_mu;
+bool g_timing_on = false;
+std::vector<cudaEvent_t> g_ev_pool;
+std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_ev_pairs;
+cudaEvent_t g_ev_pending = nullptr;
+
+cudaEvent_t take_event() {
+  if (!g_ev_pool.empty()) {
+    cudaEvent_t e = g_ev_pool.back();
+    g_ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+int check_geometry(const ptycho_geometry* g) {
+  if (!g) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "geometry is null");
+  if ((g->flags & ~PTYCHO_FLAG_MIXED_STATE) != 0)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "unknown bits in geometry.flags (0x%x)", g->flags);
+  if (g->num_slices < 1 || g->num_probes < 1)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "num_slices and num_probes must be >= 1");
+  if (g->num_slices > 1 && g->num_probes > 1)
+    return fail(PTYCHO_ERR_UNSUPPORTED, "mixed-state multislice is not supported");
+  if (g->num_probes > 16) return fail(PTYCHO_ERR_UNSUPPORTED, "at most 16 probe modes");
+  if (!roi_supported(g->roi_x, g->roi_y))
+    return fail(PTYCHO_ERR_UNSUPPORTED,
+                "ROI %dx%d has no fused kernel (supported: square 32, 48, 64, 96, 128)",
+                g->roi_x, g->roi_y);
+  if (g->object_x < g->roi_x || g->object_y < g->roi_y)
+    return fail(PTYCHO_ERR_UNSUPPORTED, "object %dx%d smaller than ROI %dx%d", g->object_x,
+                g->object_y, g->roi_x, g->roi_y);
+  if (g->object_is_potential != 0 && g->object_is_potential != 1)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "object_is_potential must be 0 or 1");
+  return PTYCHO_OK;
+}
+
+}  // namespace
+
+Workspace workspace_layout(int Sx, int Sy, int Px, int Py, int T, int M, int B) {
+  Workspace w{};
+  const size_t N = (size_t)Sx * Sy;
+  const size_t P = (size_t)Px * Py;
+  const size_t ntiles = (size_t)((Px + kTile - 1) / kTile) * ((Py + kTile - 1) / kTile);
+  const size_t nb = (N + kReduceThreads - 1) / kReduceThreads;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off = align256(off + bytes);
+    return o;
+  };
+  w.probe_spec = take(sizeof(float2) * M * N);
+  w.st_obj = take(sizeof(float2) * T * B * N);
+  w.st_nobj = take(sizeof(float) * T * B * N);
+  w.st_probe = take(sizeof(float2) * B * M * N);
+  w.st_nprobe = take(sizeof(float) * B * N);
+  w.scratch_f = take(T == 1 ? sizeof(float2) * B * M * N : 0);
+  w.pos_round = take(sizeof(int2) * B);
+  w.err = take(sizeof(float) * B);
+  w.obj_grad = take(sizeof(float2) * T * P);
+  w.obj_nrm = take(sizeof(float) * T * P);
+  w.tile_max = take(sizeof(float) * T * ntiles);
+  w.probe_part = take(sizeof(float2) * kProbeChunks * M * N);
+  w.probe_npart = take(sizeof(float) * kProbeChunks * N);
+  w.probe_bmax = take(sizeof(float) * nb);
+  w.probe_grad = take(sizeof(float2) * M * N);
+  w.probe_nrm = take(sizeof(float) * N);
+  w.com = take(sizeof(double) * 4);
+  w.red = take(sizeof(double) * 1024);
+  w.total = off;
+  return w;
+}
+
+void bind_workspace(BatchArgs& a, void* base, const Workspace& w) {
+  char* p = static_cast<char*>(base);
+  a.probe_spec = reinterpret_cast<float2*>(p + w.probe_spec);
+  a.st_obj = reinterpret_cast<float2*>(p + w.st_obj);
+  a.st_nobj = reinterpret_cast<float*>(p + w.st_nobj);
+  a.st_probe = reinterpret_cast<float2*>(p + w.st_probe);
+  a.st_nprobe = reinterpret_cast<float*>(p + w.st_nprobe);
+  a.scratch_f = reinterpret_cast<float2*>(p + w.scratch_f);
+  a.pos_round = reinterpret_cast<int2*>(p + w.pos_round);
+  a.err = reinterpret_cast<float*>(p + w.err);
+  a.obj_grad = reinterpret_cast<float2*>(p + w.obj_grad);
+  a.obj_nrm = reinterpret_cast<float*>(p + w.obj_nrm);
+  a.tile_max = reinterpret_cast<float*>(p + w.tile_max);
+  a.probe_part = reinterpret_cast<float2*>(p + w.probe_part);
+  a.probe_npart = reinterpret_cast<float*>(p + w.probe_npart);
+  a.probe_bmax = reinterpret_cast<float*>(p + w.probe_bmax);
+  a.probe_grad = reinterpret_cast<float2*>(p + w.probe_grad);
+  a.probe_nrm = reinterpret_cast<float*>(p + w.probe_nrm);
+  a.com = reinterpret_cast<double*>(p + w.com);
+  a.red = reinterpret_cast<float*>(p + w.red);
+}
+
+namespace {
+
+int prepare(const ptycho_geometry* g, int32_t batch, void* workspace, size_t workspace_bytes,
+            BatchArgs& a) {
+  int st = check_geometry(g);
+  if (st != PTYCHO_OK) return st;
+  if (batch < 1) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "batch must be >= 1 (got %d)", batch);
+  if (!workspace) return fail(PTYCHO_ERR_WORKSPACE, "workspace is null");
+  if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
+    return fail(PTYCHO_ERR_WORKSPACE, "workspace must be 256-byte aligned");
+  const Workspace w = workspace_layout(g->roi_x, g->roi_y, g->object_x, g->object_y,
+                                       g->num_slices, g->num_probes, batch);
+  if (workspace_bytes < w.total)
+    return fail(PTYCHO_ERR_WORKSPACE, "workspace of %zu bytes is smaller than the %zu needed",
+                workspace_bytes, w.total);
+  std::memset(&a, 0, sizeof(a));
+  a.Sx = g->roi_x;
+  a.Sy = g->roi_y;
+  a.Px = g->object_x;
+  a.Py = g->object_y;
+  a.T = g->num_slices;
+  a.M = g->num_probes;
+  a.potential = g->object_is_potential;
+  a.B = batch;
+  bind_workspace(a, workspace, w);
+  return PTYCHO_OK;
+}
+
+}  // namespace
+
+void timing_before(cudaStream_t s) {
+  std::lock_guard<std::mutex> lk(g_timing_mu);
+  if (!g_timing_on) return;
+  g_ev_pending = take_event();
+  cudaEventRecord(g_ev_pending, s);
+}
+
+void timing_after(cudaStream_t s) {
+  std::lock_guard<std::mutex> lk(g_timing_mu);
+  if (!g_timing_on || !g_ev_pending) return;
+  cudaEvent_t stop = take_event();
+  cudaEventRecord(stop, s);
+  g_ev_pairs.emplace_back(g_ev_pending, stop);
+  g_ev_pending = nullptr;
+}
+
+}  // namespace pty
+
+using namespace pty;
+
+extern "C" {
+
+int ptycho_abi_version(void) { return PTYCHO_ABI_VERSION; }
+
+const char* ptycho_last_error(void) { return g_last_error; }
+
+int ptycho_roi_supported(int32_t roi_x, int32_t roi_y) { return roi_supported(roi_x, roi_y) ? 1 : 0; }
+
+size_t ptycho_workspace_bytes(const ptycho_geometry* g, int32_t max_batch) {
+  if (!g || max_batch < 1) return 0;
+  return workspace_layout(g->roi_x, g->roi_y, g->object_x, g->object_y, g->num_slices,
+                          g->num_probes, max_batch)
+      .total;
+}
+
+static int run_batch(const ptycho_geometry* g, void* object, void* probe,
+                     const float* amplitudes, const int32_t* amplitude_rows,
+                     const float* positions_px, const int32_t* position_rows, int32_t batch,
+                     const float* detector_mask, const void* propagators, float* error_accum,
+                     void* workspace, size_t workspace_bytes, void* stream, BatchArgs& a) {
+  if (!object || !probe || !amplitudes || !positions_px || !error_accum)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "object, probe, amplitudes, positions and "
+                                             "error_accum must be non-null");
+  if (g && g->num_slices > 1 && !propagators)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "multislice needs propagators");
+  a.object = object;
+  a.probe = static_cast<float2*>(probe);
+  a.amplitudes = amplitudes;
+  a.amp_rows = amplitude_rows;
+  a.positions = positions_px;
+  a.pos_rows = position_rows;
+  a.det_mask = detector_mask;
+  a.props = static_cast<const float2*>(propagators);
+  a.error_accum = error_accum;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = launch_probe_spectrum(a, s);
+  if (e != cudaSuccess) return cuda_fail(e, "probe spectrum kernel");
+  e = launch_position_kernel(a, s);
+  if (e != cudaSuccess) return cuda_fail(e, "position kernel");
+  e = launch_reduce_and_update(a, s);
+  if (e != cudaSuccess) return cuda_fail(e, "reduce/update kernels");
+  return PTYCHO_OK;
+}
+
+int ptycho_gd_batch(const ptycho_geometry* g, void* object, void* probe,
+                    const float* amplitudes, const int32_t* amplitude_rows,
+                    const float* positions_px, const int32_t* position_rows, int32_t batch,
+                    float step_size, float normalization_min, int32_t fix_probe,
+                    const float* detector_mask, const void* propagators, float* error_accum,
+                    void* workspace, size_t workspace_bytes, void* stream) {
+  BatchArgs a;
+  int st = prepare(g, batch, workspace, workspace_bytes, a);
+  if (st != PTYCHO_OK) return st;
+  a.step = step_size;
+  a.norm_min = normalization_min;
+  a.fix_probe = fix_probe ? 1 : 0;
+  a.mixed_formula = (g->num_probes > 1 || (g->flags & PTYCHO_FLAG_MIXED_STATE)) ? 1 : 0;
+  return run_batch(g, object, probe, amplitudes, amplitude_rows, positions_px, position_rows,
+                   batch, detector_mask, propagators, error_accum, workspace, workspace_bytes,
+                   stream, a);
+}
+
+int ptycho_projection_batch(const ptycho_geometry* g, void* object, void* probe,
+                            const float* amplitudes, const int32_t* amplitude_rows,
+                            const float* positions_px, const int32_t* position_rows,
+                            int32_t batch, float projection_a, float projection_b,
+                            float projection_c, float normalization_min, int32_t fix_probe,
+                            void* exit_waves, int32_t exit_waves_valid, const void* propagators,
+                            float* error_accum, void* workspace, size_t workspace_bytes,
+                            void* stream) {
+  BatchArgs a;
+  int st = prepare(g, batch, workspace, workspace_bytes, a);
+  if (st != PTYCHO_OK) return st;
+  if (!exit_waves) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "exit_waves must be non-null");
+  a.projection = 1;
+  a.pa = projection_a;
+  a.pb = projection_b;
+  a.pc = projection_c;
+  a.norm_min = normalization_min;
+  a.fix_probe = fix_probe ? 1 : 0;
+  a.exit_waves = static_cast<float2*>(exit_waves);
+  a.ew_valid = exit_waves_valid ? 1 : 0;
+  a.mixed_formula = (g->num_probes > 1 || (g->flags & PTYCHO_FLAG_MIXED_STATE)) ? 1 : 0;
+  return run_batch(g, object, probe, amplitudes, amplitude_rows, positions_px, position_rows,
+                   batch, nullptr, propagators, error_accum, workspace, workspace_bytes, stream,
+                   a);
+}
+
+int ptycho_object_constraints(const ptycho_geometry* g, void* object, const uint8_t* mask,
+                              float shrinkage_rad, int32_t apply_shrinkage, int32_t pure_phase,
+                              int32_t positivity, void* workspace, size_t workspace_bytes,
+                              void* stream) {
+  BatchArgs a;
+  int st = prepare(g, 1, workspace, workspace_bytes, a);
+  if (st != PTYCHO_OK) return st;
+  if (!object) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "object is null");
+  a.object = object;
+  cudaError_t e = launch_object_constraints(a, mask, shrinkage_rad, apply_shrinkage, pure_phase,
+                                            positivity, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "object constraints");
+  return PTYCHO_OK;
+}
+
+int ptycho_probe_com_constraint(const ptycho_geometry* g, void* probe, void* workspace,
+                                size_t workspace_bytes, void* stream) {
+  BatchArgs a;
+  int st = prepare(g, 1, workspace, workspace_bytes, a);
+  if (st != PTYCHO_OK) return st;
+  if (!probe) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "probe is null");
+  a.probe = static_cast<float2*>(probe);
+  cudaError_t e = launch_probe_com(a, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "probe CoM constraint");
+  return PTYCHO_OK;
+}
+
+int ptycho_enable_kernel_timing(int32_t enable) {
+  std::lock_guard<std::mutex> lk(g_timing_mu);
+  g_timing_on = enable != 0;
+  return PTYCHO_OK;
+}
+
+int ptycho_kernel_timing(float* total_ms, int32_t* launches) {
+  if (!total_ms || !launches)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "total_ms and launches must be non-null");
+  std::lock_guard<std::mutex> lk(g_timing_mu);
+  float sum = 0.f;
+  int n = 0;
+  for (auto& pr : g_ev_pairs) {
+    cudaError_t e = cudaEventSynchronize(pr.second);
+    if (e != cudaSuccess) return cuda_fail(e, "timing event");
+    float ms = 0.f;
+    e = cudaEventElapsedTime(&ms, pr.first, pr.second);
+    if (e != cudaSuccess) return cuda_fail(e, "timing elapsed");
+    sum += ms;
+    ++n;
+    g_ev_pool.push_back(pr.first);
+    g_ev_pool.push_back(pr.second);
+  }
+  g_ev_pairs.clear();
+  *total_ms = sum;
+  *launches = n;
+  return PTYCHO_OK;
+}
+
+int ptycho_fp32_fma_probe(int32_t blocks, int32_t iters, float* sink, void* stream) {
+  if (blocks < 1 || iters < 1 || !sink)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "blocks, iters >= 1 and sink non-null required");
+  cudaError_t e = launch_fma_probe(blocks, iters, sink, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "fma probe");
+  return PTYCHO_OK;
+}
+
+int ptycho_probe_gram(const ptycho_geometry* g, const void* probe, void* gram, void* stream) {
+  int st = check_geometry(g);
+  if (st != PTYCHO_OK) return st;
+  if (!probe || !gram) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "probe and gram must be non-null");
+  BatchArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.Sx = g->roi_x;
+  a.Sy = g->roi_y;
+  a.M = g->num_probes;
+  cudaError_t e = launch_probe_gram(a, static_cast<const float2*>(probe),
+                                    static_cast<float2*>(gram), static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "probe Gram matrix");
+  return PTYCHO_OK;
+}
+
+int ptycho_probe_mix(const ptycho_geometry* g, const void* probe_in, const void* coeffs,
+                     void* probe_out, void* stream) {
+  int st = check_geometry(g);
+  if (st != PTYCHO_OK) return st;
+  if (!probe_in || !coeffs || !probe_out)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "probe_in, coeffs and probe_out must be non-null");
+  if (probe_in == probe_out) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "probe_out aliases probe_in");
+  BatchArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.Sx = g->roi_x;
+  a.Sy = g->roi_y;
+  a.M = g->num_probes;
+  cudaError_t e = launch_probe_mix(a, static_cast<const float2*>(probe_in),
+                                   static_cast<const float2*>(coeffs),
+                                   static_cast<float2*>(probe_out),
+                                   static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "probe mix");
+  return PTYCHO_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,87 @@
+// Internal declarations shared by the kernel and C-ABI translation units.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pty {
+
+constexpr int kTile = 32;          // object reduction tile (kTile x kTile pixels)
+constexpr int kProbeChunks = 16;   // batch chunks of the probe-gradient reduction
+constexpr int kReduceThreads = 256;
+
+// Per-batch kernel arguments (device pointers into caller buffers/workspace).
+struct BatchArgs {
+  int Sx, Sy, Px, Py, T, M;
+  int potential;           // object is float32 potential
+  int projection;          // projection-set update instead of gradient descent
+  int mixed_formula;       // |F|_tot ratio form (mixed-state class)
+  int B;
+  float step, norm_min;
+  float pa, pb, pc;        // projection parameters a, b, c
+  int fix_probe;
+  int ew_valid;
+
+  void* object;                 // (T,Px,Py) float2 or float
+  float2* probe;                // (M,N)
+  const float* amplitudes;      // (J,N)
+  const int32_t* amp_rows;      // (B) or null
+  const float* positions;       // (J,2)
+  const int32_t* pos_rows;      // (B) or null
+  const float* det_mask;        // (N) or null
+  const float2* props;          // (T-1,N) or null
+  float2* exit_waves;           // (J,M,N) or null
+  float* error_accum;           // scalar
+
+  // workspace
+  float2* probe_spec;   // (M,N)
+  float2* st_obj;       // (T,B,N)
+  float* st_nobj;       // (T,B,N)
+  float2* st_probe;     // (B,M,N)
+  float* st_nprobe;     // (B,N)
+  float2* scratch_f;    // (B,M,N) when M > 1
+  int2* pos_round;      // (B)
+  float* err;           // (B)
+  float2* obj_grad;     // (T,P)
+  float* obj_nrm;       // (T,P)
+  float* tile_max;      // (T,ntiles)
+  float2* probe_part;   // (chunks,M,N)
+  float* probe_npart;   // (chunks,N)
+  float* probe_bmax;    // (N/256)
+  float2* probe_grad;   // (M,N)
+  float* probe_nrm;     // (N)
+  double* com;          // (4) scratch for the probe CoM constraint
+  float* red;           // (1024) scratch for constraint reductions
+};
+
+struct Workspace {
+  size_t probe_spec, st_obj, st_nobj, st_probe, st_nprobe, scratch_f, pos_round, err,
+      obj_grad, obj_nrm, tile_max, probe_part, probe_npart, probe_bmax, probe_grad,
+      probe_nrm, com, red, total;
+};
+
+Workspace workspace_layout(int Sx, int Sy, int Px, int Py, int T, int M, int B);
+void bind_workspace(BatchArgs& a, void* base, const Workspace& w);
+
+bool roi_supported(int Sx, int Sy);
+
+// Position-kernel timing (instrumentation); implemented in ptycho_capi.cu.
+void timing_before(cudaStream_t s);
+void timing_after(cudaStream_t s);
+
+// Launchers (return cudaError_t of the last launch).
+cudaError_t launch_probe_spectrum(const BatchArgs& a, cudaStream_t s);
+cudaError_t launch_position_kernel(const BatchArgs& a, cudaStream_t s);
+cudaError_t launch_reduce_and_update(const BatchArgs& a, cudaStream_t s);
+cudaError_t launch_object_constraints(const BatchArgs& a, const uint8_t* mask,
+                                      float shrinkage, int apply_shrinkage,
+                                      int pure_phase, int positivity, cudaStream_t s);
+cudaError_t launch_probe_com(const BatchArgs& a, cudaStream_t s);
+cudaError_t launch_probe_gram(const BatchArgs& a, const float2* probe, float2* gram,
+                              cudaStream_t s);
+cudaError_t launch_fma_probe(int blocks, int iters, float* sink, cudaStream_t s);
+cudaError_t launch_probe_mix(const BatchArgs& a, const float2* in, const float2* coeffs,
+                             float2* out, cudaStream_t s);
+
+}  // namespace pty

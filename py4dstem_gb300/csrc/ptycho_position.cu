@@ -1,0 +1,461 @@
+// Fused per-position kernel: one thread block owns one scan position of the
+// batch and runs the whole forward model, Fourier projection and the per-position
+// half of the adjoint with the wave resident in shared memory.
+//
+// Per position b (reference operators in parentheses, py4DSTEM 0.14.18):
+//   shifted probe   P_m = IFFT2( FFT2(P_m) . exp(-2 pi i (kx dx + ky dy)) )
+//                                  (utils.py:468-533 fft_shift, ptychographic_methods.py:1482)
+//   object patch    O_s = object_s[(x0 + fx) mod Px, (y0 + fy) mod Py], exp(iV) for
+//                   potentials   (phase_base_class.py:1970-2003, ptychographic_methods.py:1489-1527)
+//   multislice      P_{s+1} = IFFT2( FFT2(P_s O_s) H_s )     (ptychographic_methods.py:2300-2351, 383-401)
+//   projection      F = FFT2(psi); err = sum (A - |F|)^2;
+//                   GD: chi = IFFT2(A F/|F| - F); mixed: chi_m = IFFT2((A/|F|tot) F_m - F_m)
+//                   projection sets: exit-wave update with (a,b,c)
+//                                  (ptychographic_methods.py:1576-1734, 2742-2904)
+//   adjoint terms   conj(P_s) chi_s, |P_s|^2 (object), conj(O) chi, |O|^2 (probe);
+//                   multislice back-transmits and back-propagates chi
+//                                  (ptychographic_methods.py:1818-1908, 2353-2565, 2906-3093)
+// The adjoint terms go to position-major staging buffers; ptycho_reduce.cu sums
+// them over positions in a fixed order.
+#include <cuda_runtime.h>
+
+#include "fft_smem.cuh"
+#include "ptycho_internal.h"
+
+namespace pty {
+namespace {
+
+__device__ __forceinline__ int pmod(int v, int m) {
+  int r = v % m;
+  return r < 0 ? r + m : r;
+}
+
+// numpy.fft.fftfreq(n, 1/n) as an integer: i for i < (n+1)/2, else i - n.
+__device__ __forceinline__ int fint(int i, int n) { return i < (n + 1) / 2 ? i : i - n; }
+
+template <int SX, int SY>
+struct Layout {
+  static constexpr int N = SX * SY;
+  static constexpr int LD = SY + 1;
+  static constexpr size_t smem_bytes(bool mixed) {
+    return sizeof(float2) * (size_t)(SX * LD + 2 * SX + 2 * SY) + (mixed ? sizeof(float) * N : 0);
+  }
+};
+
+__device__ __forceinline__ float2 load_object(const BatchArgs& a, int s, int ox, int oy) {
+  const size_t idx = ((size_t)s * a.Px + ox) * a.Py + oy;
+  if (a.potential) {
+    float sv, cv;
+    sincosf(reinterpret_cast<const float*>(a.object)[idx], &sv, &cv);
+    return make_float2(cv, sv);
+  }
+  return reinterpret_cast<const float2*>(a.object)[idx];
+}
+
+// Object-gradient term for one pixel: conj(P) chi for complex objects and
+// Re(-i conj(O) conj(P) chi) for potentials (stored in .x).
+__device__ __forceinline__ float2 object_term(int potential, float2 o, float2 p, float2 chi) {
+  if (potential) {
+    const float2 t = make_float2(-o.y, -o.x);          // -i * conj(O)
+    const float2 u = c_mul(t, make_float2(p.x, -p.y));  // * conj(P)
+    const float2 v = c_mul(u, chi);                     // * chi
+    return make_float2(v.x, 0.0f);
+  }
+  return c_conj_mul(p, chi);
+}
+
+// Block-wide deterministic sum (fixed shuffle tree, then warp order).
+template <int NT>
+__device__ __forceinline__ float block_sum(float v, float* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float t = 0.0f;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int w = 0; w < NT / 32; ++w) t += red[w];
+  }
+  return t;  // valid in thread 0
+}
+
+template <int SX, int SY, int NT>
+__global__ void __launch_bounds__(NT, 1) probe_spectrum_kernel(BatchArgs a) {
+  using L = Layout<SX, SY>;
+  extern __shared__ float4 smem4[];
+  float2* buf = reinterpret_cast<float2*>(smem4);
+  float2* twx = buf + SX * L::LD;
+  float2* twy = twx + SX;
+  fill_twiddles<SX, NT>(twx);
+  fill_twiddles<SY, NT>(twy);
+  const float2* src = a.probe + (size_t)blockIdx.x * L::N;
+  for (int e = threadIdx.x; e < L::N; e += NT) buf[(e / SY) * L::LD + e % SY] = src[e];
+  __syncthreads();
+  fft2d<SX, SY, NT, -1>(buf, twx, twy);
+  float2* dst = a.probe_spec + (size_t)blockIdx.x * L::N;
+  for (int e = threadIdx.x; e < L::N; e += NT) dst[e] = buf[(e / SY) * L::LD + e % SY];
+}
+
+template <int SX, int SY, int NT>
+__global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
+  using L = Layout<SX, SY>;
+  constexpr int N = L::N;
+  constexpr int LD = L::LD;
+  extern __shared__ float4 smem4[];
+  float2* buf = reinterpret_cast<float2*>(smem4);
+  float2* twx = buf + SX * LD;
+  float2* twy = twx + SX;
+  float2* rpx = twy + SY;
+  float2* rpy = rpx + SX;
+  float* itot = reinterpret_cast<float*>(rpy + SY);  // N floats, mixed only
+  __shared__ float red[NT / 32];
+
+  const int b = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int T = a.T;
+  const int M = a.M;
+  const int prow = a.pos_rows ? a.pos_rows[b] : b;
+  const int arow = a.amp_rows ? a.amp_rows[b] : b;
+  const float posx = a.positions[2 * prow];
+  const float posy = a.positions[2 * prow + 1];
+  const float rx = rintf(posx);  // numpy.round: half to even
+  const float ry = rintf(posy);
+  const float dx = posx - rx;
+  const float dy = posy - ry;
+  const int x0 = (int)rx;
+  const int y0 = (int)ry;
+  const float invN = 1.0f / (float)N;
+  const bool ps = a.projection != 0;
+  const float* amp = a.amplitudes + (size_t)arow * N;
+
+  fill_twiddles<SX, NT>(twx);
+  fill_twiddles<SY, NT>(twy);
+  // separable sub-pixel shift ramps exp(-2 pi i k d), phase formed in float32
+  for (int i = tid; i < SX; i += NT) {
+    const float k = (float)fint(i, SX) / (float)SX;
+    float s, c;
+    sincosf(__fmul_rn(__fmul_rn(-6.2831855f, k), dx), &s, &c);
+    rpx[i] = make_float2(c, s);
+  }
+  for (int i = tid; i < SY; i += NT) {
+    const float k = (float)fint(i, SY) / (float)SY;
+    float s, c;
+    sincosf(__fmul_rn(__fmul_rn(-6.2831855f, k), dy), &s, &c);
+    rpy[i] = make_float2(c, s);
+  }
+  if (tid == 0) a.pos_round[b] = make_int2(x0, y0);
+  __syncthreads();
+
+  auto obj_x = [&](int x) { return pmod(x0 + fint(x, SX), a.Px); };
+  auto obj_y = [&](int y) { return pmod(y0 + fint(y, SY), a.Py); };
+
+  // buf <- IFFT2(FFT2(P_m) . ramp) * 1/N  (sub-pixel shifted probe, mode m)
+  auto shifted_probe = [&](int m) {
+    const float2* spec = a.probe_spec + (size_t)m * N;
+    for (int e = tid; e < N; e += NT) {
+      const int x = e / SY, y = e % SY;
+      buf[x * LD + y] = c_mul(spec[e], c_mul(rpx[x], rpy[y]));
+    }
+    __syncthreads();
+    fft2d<SX, SY, NT, +1>(buf, twx, twy);
+  };
+
+  float err = 0.0f;
+  const float px_ = 1.0f - a.pa - a.pb;  // projection x
+  const float py_ = 1.0f - a.pc;          // projection y
+
+  if (T == 1) {
+    // ------------------------------------------------------------ single slice
+    const bool mixed = M > 1 || a.mixed_formula;
+    for (int m = 0; m < M; ++m) {
+      shifted_probe(m);
+      float2* pst = a.st_probe + ((size_t)b * M + m) * N;  // stash P_m
+      const float2* ew = a.exit_waves ? a.exit_waves + ((size_t)prow * M + m) * N : nullptr;
+      for (int e = tid; e < N; e += NT) {
+        const int x = e / SY, y = e % SY;
+        const float2 p = c_scale(buf[x * LD + y], invN);
+        const float2 o = load_object(a, 0, obj_x(x), obj_y(y));
+        pst[e] = p;
+        const float2 psi = c_mul(p, o);
+        float2 v = psi;
+        if (ps) {
+          const float2 w = a.ew_valid ? ew[e] : psi;
+          v = c_add(c_scale(psi, a.pc), c_scale(w, py_));
+        }
+        buf[x * LD + y] = v;
+      }
+      __syncthreads();
+      fft2d<SX, SY, NT, -1>(buf, twx, twy);
+      if (mixed) {
+        float2* f = a.scratch_f + ((size_t)b * M + m) * N;
+        for (int e = tid; e < N; e += NT) {
+          const float2 v = buf[(e / SY) * LD + e % SY];
+          f[e] = v;
+          // |F_m|^2 as numpy forms it: abs() then square
+          const float av = hypotf(v.x, v.y);
+          itot[e] = (m == 0 ? 0.0f : itot[e]) + av * av;
+        }
+        __syncthreads();
+      }
+    }
+
+    if (!mixed) {
+      // single probe: A exp(i angle F) - F (GD) or A exp(i angle F) (projection)
+      for (int e = tid; e < N; e += NT) {
+        const int idx = (e / SY) * LD + e % SY;
+        float2 f = buf[idx];
+        const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
+        if (a.det_mask) f = c_scale(f, mk);
+        const float af = hypotf(f.x, f.y);
+        const float A = amp[e];
+        const float d = A - af;
+        err += d * d;
+        const float2 ph = af > 0.0f ? make_float2(f.x / af, f.y / af) : make_float2(1.0f, 0.0f);
+        float2 r = c_scale(ph, A);
+        if (!ps) {
+          r = c_sub(r, f);
+          if (a.det_mask) r = c_scale(r, mk);
+        }
+        buf[idx] = r;
+      }
+      __syncthreads();
+      fft2d<SX, SY, NT, +1>(buf, twx, twy);
+    } else {
+      // mixed state: shared ratio A / sqrt(sum_m |F_m|^2), 0 where the model is 0
+      for (int e = tid; e < N; e += NT) {
+        const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
+        float tot = sqrtf(itot[e]);
+        if (a.det_mask) tot = sqrtf(itot[e] * mk * mk);
+        const float A = amp[e];
+        const float d = A - tot;
+        err += d * d;
+        itot[e] = tot == 0.0f ? 0.0f : A / tot;
+      }
+      __syncthreads();
+    }
+
+    // adjoint terms, mode by mode
+    for (int m = 0; m < M; ++m) {
+      if (mixed) {
+        const float2* f = a.scratch_f + ((size_t)b * M + m) * N;
+        for (int e = tid; e < N; e += NT) {
+          const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
+          float2 fv = f[e];
+          if (a.det_mask) fv = c_scale(fv, mk);
+          float2 r = c_scale(fv, itot[e]);
+          if (!ps) {
+            r = c_sub(r, fv);
+            if (a.det_mask) r = c_scale(r, mk);
+          }
+          buf[(e / SY) * LD + e % SY] = r;
+        }
+        __syncthreads();
+        fft2d<SX, SY, NT, +1>(buf, twx, twy);
+      }
+      float2* pst = a.st_probe + ((size_t)b * M + m) * N;
+      float2* ew = a.exit_waves ? a.exit_waves + ((size_t)prow * M + m) * N : nullptr;
+      float2* gobj = a.st_obj + (size_t)b * N;
+      float* nobj = a.st_nobj + (size_t)b * N;
+      for (int e = tid; e < N; e += NT) {
+        const int x = e / SY, y = e % SY;
+        float2 chi = c_scale(buf[x * LD + y], invN);
+        const float2 p = pst[e];
+        const float2 o = load_object(a, 0, obj_x(x), obj_y(y));
+        if (ps) {
+          const float2 psi = c_mul(p, o);
+          const float2 w = a.ew_valid ? ew[e] : psi;
+          chi = c_add(c_add(c_scale(w, px_), c_scale(psi, a.pa)), c_scale(chi, a.pb));
+          ew[e] = chi;
+        }
+        const float2 g = object_term(a.potential, o, p, chi);
+        const float pn = c_abs2(p);
+        if (m == 0) {
+          gobj[e] = g;
+          nobj[e] = pn;
+        } else {
+          gobj[e] = c_add(gobj[e], g);
+          nobj[e] = nobj[e] + pn;
+        }
+        pst[e] = c_conj_mul(o, chi);
+        if (m == 0) a.st_nprobe[(size_t)b * N + e] = c_abs2(o);
+      }
+      __syncthreads();
+    }
+  } else {
+    // ------------------------------------------------------------- multislice
+    shifted_probe(0);
+    for (int s = 0; s < T; ++s) {
+      float2* pst = a.st_obj + ((size_t)s * a.B + b) * N;  // stash P_s
+      for (int e = tid; e < N; e += NT) {
+        const int x = e / SY, y = e % SY;
+        float2 p = buf[x * LD + y];
+        p = c_scale(p, invN);
+        const float2 o = load_object(a, s, obj_x(x), obj_y(y));
+        pst[e] = p;
+        buf[x * LD + y] = c_mul(o, p);
+      }
+      __syncthreads();
+      if (s + 1 < T) {
+        fft2d<SX, SY, NT, -1>(buf, twx, twy);
+        const float2* h = a.props + (size_t)s * N;
+        for (int e = tid; e < N; e += NT) {
+          const int idx = (e / SY) * LD + e % SY;
+          buf[idx] = c_mul(buf[idx], h[e]);
+        }
+        __syncthreads();
+        fft2d<SX, SY, NT, +1>(buf, twx, twy);
+      }
+    }
+    // buf = psi_{T-1} (unscaled exit wave of the last slice)
+    const float2* ew_in = a.exit_waves ? a.exit_waves + (size_t)prow * N : nullptr;
+    if (ps) {
+      for (int e = tid; e < N; e += NT) {
+        const int idx = (e / SY) * LD + e % SY;
+        const float2 psi = buf[idx];
+        const float2 w = a.ew_valid ? ew_in[e] : psi;
+        buf[idx] = c_add(c_scale(psi, a.pc), c_scale(w, py_));
+      }
+      __syncthreads();
+    }
+    fft2d<SX, SY, NT, -1>(buf, twx, twy);
+    for (int e = tid; e < N; e += NT) {
+      const int idx = (e / SY) * LD + e % SY;
+      float2 f = buf[idx];
+      const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
+      if (a.det_mask) f = c_scale(f, mk);
+      const float af = hypotf(f.x, f.y);
+      const float A = amp[e];
+      const float d = A - af;
+      err += d * d;
+      const float2 ph = af > 0.0f ? make_float2(f.x / af, f.y / af) : make_float2(1.0f, 0.0f);
+      float2 r = c_scale(ph, A);
+      if (!ps) {
+        r = c_sub(r, f);
+        if (a.det_mask) r = c_scale(r, mk);
+      }
+      buf[idx] = r;
+    }
+    __syncthreads();
+    fft2d<SX, SY, NT, +1>(buf, twx, twy);
+    if (ps) {
+      // new exit wave of the last slice; psi recomputed from the stash
+      float2* ew = a.exit_waves + (size_t)prow * N;
+      const float2* pst = a.st_obj + ((size_t)(T - 1) * a.B + b) * N;
+      for (int e = tid; e < N; e += NT) {
+        const int x = e / SY, y = e % SY;
+        const float2 proj = c_scale(buf[x * LD + y], invN);
+        const float2 psi = c_mul(load_object(a, T - 1, obj_x(x), obj_y(y)), pst[e]);
+        const float2 w = a.ew_valid ? ew[e] : psi;
+        const float2 nw = c_add(c_add(c_scale(w, px_), c_scale(psi, a.pa)), c_scale(proj, a.pb));
+        ew[e] = nw;
+        buf[x * LD + y] = c_scale(nw, (float)N);  // keep buf in unscaled units
+      }
+      __syncthreads();
+    }
+    for (int s = T - 1; s >= 0; --s) {
+      float2* pst = a.st_obj + ((size_t)s * a.B + b) * N;
+      float* nst = a.st_nobj + ((size_t)s * a.B + b) * N;
+      for (int e = tid; e < N; e += NT) {
+        const int x = e / SY, y = e % SY;
+        const int idx = x * LD + y;
+        const float2 chi = c_scale(buf[idx], invN);
+        const float2 p = pst[e];
+        const float2 o = load_object(a, s, obj_x(x), obj_y(y));
+        pst[e] = object_term(a.potential, o, p, chi);
+        nst[e] = c_abs2(p);
+        const float2 bt = c_mul(chi, make_float2(o.x, -o.y));  // chi * conj(O_s)
+        if (s > 0) {
+          buf[idx] = bt;
+        } else {
+          a.st_probe[(size_t)b * N + e] = bt;
+          a.st_nprobe[(size_t)b * N + e] = c_abs2(o);
+        }
+      }
+      __syncthreads();
+      if (s > 0) {
+        fft2d<SX, SY, NT, -1>(buf, twx, twy);
+        const float2* h = a.props + (size_t)(s - 1) * N;
+        for (int e = tid; e < N; e += NT) {
+          const int idx = (e / SY) * LD + e % SY;
+          const float2 hv = h[e];
+          buf[idx] = c_mul(buf[idx], make_float2(hv.x, -hv.y));
+        }
+        __syncthreads();
+        fft2d<SX, SY, NT, +1>(buf, twx, twy);
+      }
+    }
+  }
+
+  const float tot = block_sum<NT>(err, red);
+  if (tid == 0) a.err[b] = tot;
+}
+
+template <int SX, int SY, int NT>
+cudaError_t launch_spectrum_t(const BatchArgs& a, cudaStream_t s) {
+  const size_t smem = Layout<SX, SY>::smem_bytes(false);
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(probe_spectrum_kernel<SX, SY, NT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)Layout<SX, SY>::smem_bytes(true));
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  probe_spectrum_kernel<SX, SY, NT><<<a.M, NT, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <int SX, int SY, int NT>
+cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
+  const bool mixed = a.T == 1 && (a.M > 1 || a.mixed_formula);
+  const size_t smem = Layout<SX, SY>::smem_bytes(mixed);
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(position_kernel<SX, SY, NT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)Layout<SX, SY>::smem_bytes(true));
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  timing_before(s);
+  position_kernel<SX, SY, NT><<<a.B, NT, smem, s>>>(a);
+  cudaError_t e = cudaGetLastError();
+  timing_after(s);
+  return e;
+}
+
+}  // namespace
+
+bool roi_supported(int Sx, int Sy) {
+  if (Sx != Sy) return false;
+  switch (Sx) {
+    case 32:
+    case 48:
+    case 64:
+    case 96:
+    case 128:
+      return true;
+    default:
+      return false;
+  }
+}
+
+#define PTY_DISPATCH(FN, A, S)                                   \
+  switch ((A).Sx) {                                              \
+    case 32: return FN<32, 32, 128>(A, S);                       \
+    case 48: return FN<48, 48, 192>(A, S);                       \
+    case 64: return FN<64, 64, 256>(A, S);                       \
+    case 96: return FN<96, 96, 384>(A, S);                       \
+    case 128: return FN<128, 128, 512>(A, S);                    \
+    default: return cudaErrorInvalidValue;                       \
+  }
+
+cudaError_t launch_probe_spectrum(const BatchArgs& a, cudaStream_t s) {
+  PTY_DISPATCH(launch_spectrum_t, a, s)
+}
+
+cudaError_t launch_position_kernel(const BatchArgs& a, cudaStream_t s) {
+  PTY_DISPATCH(launch_position_t, a, s)
+}
+
+}  // namespace pty

@@ -1,0 +1,292 @@
+"""Device state and the iteration driver of the GPU reconstruction.
+
+The host keeps what the reference keeps on the host: the iteration and batch
+loops, NumPy's global RNG for the position order (singleslice_ptychography.py:836-857)
+and the error bookkeeping. Every array operation of an iteration is a call into
+libptycho_gb300 on the current CUDA stream; torch is used only to own device
+memory and to name the stream.
+
+Per batch: ptycho_gd_batch / ptycho_projection_batch (forward, projection,
+adjoint, deterministic scatter, object and probe update). Per iteration:
+object constraints, probe centre-of-mass constraint and, for mixed states, the
+probe orthogonalisation (Gram matrix on the GPU, the M x M eigendecomposition on
+the host as numpy.linalg.eigh, mode mixing on the GPU).
+"""
+
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+
+from . import _native
+from .preprocess import generate_batches
+
+
+def _torch():
+    import torch
+
+    if not torch.cuda.is_available():
+        raise RuntimeError(
+            "py4dstem_gb300 reconstructs on a CUDA GPU only and none is available "
+            "(there is no CPU fallback)")
+    return torch
+
+
+def _ptr(t) -> Optional[int]:
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+@dataclass
+class DeviceState:
+    """All device buffers of one reconstruction."""
+
+    geometry: _native.Geometry
+    object: object
+    probe: object
+    amplitudes: object            # device (J,Sx,Sy) f32, or None when streamed
+    amplitudes_host: Optional[np.ndarray]
+    positions: object             # device (J,2) f32
+    order: object                 # device (J,) int32
+    workspace: object
+    workspace_bytes: int
+    error_accum: object
+    max_batch: int
+    propagators: object = None
+    det_mask: object = None
+    fov_mask_inverse: object = None
+    exit_waves: object = None
+    exit_waves_valid: bool = False
+    amp_stage: object = None      # device batch buffer when streaming from the host
+    amp_pinned: object = None     # two pinned host batch buffers (double-buffered)
+    amp_events: object = None     # copy-done events of the pinned buffers
+    amp_turn: int = 0
+    gram: object = None
+    probe_tmp: object = None
+    coeffs: object = None
+    launches: int = 0
+    extra: dict = field(default_factory=dict)
+
+
+def supported_roi(shape) -> bool:
+    return bool(_native.lib().ptycho_roi_supported(int(shape[0]), int(shape[1])))
+
+
+def make_geometry(roi_shape, object_shape, num_slices, num_probes, potential,
+                  mixed_state=False) -> _native.Geometry:
+    return _native.Geometry(int(roi_shape[0]), int(roi_shape[1]), int(object_shape[-2]),
+                            int(object_shape[-1]), int(num_slices), int(num_probes),
+                            1 if potential else 0,
+                            _native.FLAG_MIXED_STATE if mixed_state else 0)
+
+
+def create_state(*, roi_shape, object_array, probe_array, amplitudes, positions_px,
+                 num_slices, num_probes, potential, max_batch, storage="gpu",
+                 propagators=None, detector_mask=None, fov_mask_inverse=None,
+                 projection=False, mixed_state=False) -> DeviceState:
+    torch = _torch()
+    lib = _native.lib()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    geom = make_geometry(roi_shape, object_array.shape, num_slices, num_probes, potential,
+                         mixed_state or num_probes > 1)
+    if not lib.ptycho_roi_supported(geom.roi_x, geom.roi_y):
+        raise NotImplementedError(
+            f"no fused GPU kernel for a {geom.roi_x}x{geom.roi_y} region of interest "
+            "(supported: square 32, 48, 64, 96, 128)")
+    ws_bytes = int(lib.ptycho_workspace_bytes(ctypes.byref(geom), int(max_batch)))
+    if ws_bytes == 0:
+        raise ValueError("invalid geometry for the workspace query")
+    obj_np = np.ascontiguousarray(object_array)
+    obj = torch.from_numpy(obj_np).to(dev)
+    probe_np = np.ascontiguousarray(probe_array, dtype=np.complex64).reshape(
+        (num_probes,) + tuple(roi_shape))
+    probe = torch.from_numpy(probe_np).to(dev)
+    amps_dev = None
+    amps_host = None
+    amp_stage = amp_pinned = None
+    if storage == "gpu":
+        amps_dev = torch.from_numpy(np.ascontiguousarray(amplitudes, dtype=np.float32)).to(dev)
+    else:
+        amps_host = np.ascontiguousarray(amplitudes, dtype=np.float32)
+        amp_stage = torch.empty((max_batch,) + tuple(roi_shape), dtype=torch.float32, device=dev)
+        amp_pinned = [torch.empty((max_batch,) + tuple(roi_shape), dtype=torch.float32,
+                                  pin_memory=True) for _ in range(2)]
+    pos = torch.from_numpy(np.ascontiguousarray(positions_px, dtype=np.float32)).to(dev)
+    order = torch.arange(pos.shape[0], dtype=torch.int32, device=dev)
+    ws = torch.empty(ws_bytes + 256, dtype=torch.uint8, device=dev)
+    err = torch.zeros(1, dtype=torch.float32, device=dev)
+    st = DeviceState(geometry=geom, object=obj, probe=probe, amplitudes=amps_dev,
+                     amplitudes_host=amps_host, positions=pos, order=order, workspace=ws,
+                     workspace_bytes=ws_bytes, error_accum=err, max_batch=int(max_batch),
+                     amp_stage=amp_stage, amp_pinned=amp_pinned)
+    if propagators is not None:
+        st.propagators = torch.from_numpy(
+            np.ascontiguousarray(propagators, dtype=np.complex64)).to(dev)
+    if detector_mask is not None:
+        st.det_mask = torch.from_numpy(
+            np.ascontiguousarray(np.asarray(detector_mask), dtype=np.float32)).to(dev)
+    if fov_mask_inverse is not None:
+        st.fov_mask_inverse = torch.from_numpy(
+            np.ascontiguousarray(fov_mask_inverse, dtype=np.uint8)).to(dev)
+    if projection:
+        J = pos.shape[0]
+        st.exit_waves = torch.empty((J, num_probes) + tuple(roi_shape), dtype=torch.complex64,
+                                    device=dev)
+    if num_probes > 1:
+        st.gram = torch.empty((num_probes, num_probes), dtype=torch.complex64, device=dev)
+        st.probe_tmp = torch.empty_like(probe)
+        st.coeffs = torch.empty((num_probes, num_probes), dtype=torch.complex64, device=dev)
+    return st
+
+
+def _ws_ptr(st: DeviceState):
+    base = st.workspace.data_ptr()
+    aligned = (base + 255) & ~255
+    return ctypes.c_void_p(aligned)
+
+
+def _stream():
+    torch = _torch()
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def run_batch(st: DeviceState, start: int, end: int, host_order: np.ndarray, *,
+              projection=False, step_size=0.5, normalization_min=1.0, fix_probe=False,
+              projection_abc=(0.0, 0.0, 0.0)):
+    lib = _native.lib()
+    n = end - start
+    rows_ptr = ctypes.c_void_p(st.order.data_ptr() + 4 * start)
+    if st.amplitudes is not None:
+        amps_ptr, amp_rows = _ptr(st.amplitudes), rows_ptr
+    else:
+        # storage on the host: gather this batch's patterns and copy them over,
+        # like the reference's per-batch copy_to_device
+        torch = _torch()
+        if st.amp_events is None:
+            st.amp_events = [torch.cuda.Event(), torch.cuda.Event()]
+        k = st.amp_turn
+        st.amp_turn ^= 1
+        st.amp_events[k].synchronize()  # the previous copy out of this buffer is done
+        pinned = st.amp_pinned[k]
+        idx = host_order[start:end]
+        np.take(st.amplitudes_host, idx, axis=0, out=pinned.numpy()[:n])
+        st.amp_stage[:n].copy_(pinned[:n], non_blocking=True)
+        st.amp_events[k].record()
+        amps_ptr, amp_rows = _ptr(st.amp_stage), None
+    g = ctypes.byref(st.geometry)
+    props = _ptr(st.propagators)
+    if projection:
+        a, b, c = projection_abc
+        status = lib.ptycho_projection_batch(
+            g, _ptr(st.object), _ptr(st.probe), amps_ptr, amp_rows, _ptr(st.positions),
+            rows_ptr, n, float(a), float(b), float(c), float(normalization_min),
+            1 if fix_probe else 0, _ptr(st.exit_waves), 1 if st.exit_waves_valid else 0,
+            props, _ptr(st.error_accum), _ws_ptr(st), st.workspace_bytes, _stream())
+    else:
+        status = lib.ptycho_gd_batch(
+            g, _ptr(st.object), _ptr(st.probe), amps_ptr, amp_rows, _ptr(st.positions),
+            rows_ptr, n, float(step_size), float(normalization_min), 1 if fix_probe else 0,
+            _ptr(st.det_mask), props, _ptr(st.error_accum), _ws_ptr(st), st.workspace_bytes,
+            _stream())
+    _native.check(status)
+    st.launches += 4 if fix_probe else 7
+
+
+def run_iteration(st: DeviceState, host_order: np.ndarray, max_batch: int, **kw) -> None:
+    """One pass over all positions in `host_order` (already shuffled), batch by batch.
+    The batch errors accumulate into st.error_accum (float32 on the device)."""
+    torch = _torch()
+    st.order.copy_(torch.from_numpy(np.ascontiguousarray(host_order, dtype=np.int32)),
+                   non_blocking=False)
+    st.error_accum.zero_()
+    for start, end in generate_batches(int(host_order.shape[0]), max_batch):
+        run_batch(st, start, end, host_order, **kw)
+    if kw.get("projection"):
+        st.exit_waves_valid = True
+
+
+def object_constraints(st: DeviceState, *, shrinkage_rad: float, use_mask: bool,
+                       pure_phase: bool, positivity: bool) -> None:
+    lib = _native.lib()
+    apply_shrinkage = shrinkage_rad > 0.0 or use_mask
+    mask = _ptr(st.fov_mask_inverse) if use_mask else None
+    _native.check(lib.ptycho_object_constraints(
+        ctypes.byref(st.geometry), _ptr(st.object), mask, float(shrinkage_rad),
+        1 if apply_shrinkage else 0, 1 if pure_phase else 0, 1 if positivity else 0,
+        _ws_ptr(st), st.workspace_bytes, _stream()))
+    st.launches += 2 if use_mask else 1
+
+
+def probe_com_constraint(st: DeviceState) -> None:
+    lib = _native.lib()
+    _native.check(lib.ptycho_probe_com_constraint(
+        ctypes.byref(st.geometry), _ptr(st.probe), _ws_ptr(st), st.workspace_bytes, _stream()))
+    st.launches += 2
+
+
+def probe_orthogonalization(st: DeviceState) -> None:
+    """Gram matrix on the GPU, eigh of the M x M matrix on the host, mixing on the GPU
+    (ptychographic_constraints.py:1181-1216). Modes are ordered by decreasing
+    intensity; the intensity of mode i is the i-th eigenvalue."""
+    torch = _torch()
+    lib = _native.lib()
+    g = ctypes.byref(st.geometry)
+    _native.check(lib.ptycho_probe_gram(g, _ptr(st.probe), _ptr(st.gram), _stream()))
+    gram = st.gram.cpu().numpy()
+    upper = np.triu(gram)
+    evals, evecs = np.linalg.eigh(upper.astype(np.complex64), UPLO="U")
+    coeffs = evecs.T  # new mode i = sum_j evecs[j, i] P_j
+    # |new mode i|^2 = e_i^H G e_i = eigenvalue i: sort by decreasing intensity
+    order = np.argsort(evals, axis=None)[::-1]
+    coeffs = np.ascontiguousarray(coeffs[order], dtype=np.complex64)
+    st.coeffs.copy_(torch.from_numpy(coeffs))
+    _native.check(lib.ptycho_probe_mix(g, _ptr(st.probe), _ptr(st.coeffs),
+                                       _ptr(st.probe_tmp), _stream()))
+    st.probe.copy_(st.probe_tmp)
+    st.launches += 2
+
+
+def read_error(st: DeviceState) -> np.float32:
+    return np.float32(st.error_accum.item())
+
+
+class IterationDriver:
+    """Runs reconstruction iterations on a DeviceState: all batches of the
+    shuffled order, then the per-iteration constraints; the error is read back
+    (one device-to-host sync) only when asked for."""
+
+    def __init__(self, st: DeviceState, *, max_batch, projection=False, step_size=0.5,
+                 normalization_min=1.0, fix_probe=False, projection_abc=(0.0, 0.0, 0.0),
+                 shrinkage_rad=0.0, use_mask=False, pure_phase=False, positivity=True,
+                 fix_probe_com=True, orthogonalize_probe=False, mean_intensity=1.0):
+        self.st = st
+        self.max_batch = int(max_batch)
+        self.batch_kw = dict(projection=projection, step_size=step_size,
+                             normalization_min=normalization_min, fix_probe=fix_probe,
+                             projection_abc=projection_abc)
+        self.shrinkage_rad = shrinkage_rad
+        self.use_mask = use_mask
+        self.pure_phase = pure_phase
+        self.positivity = positivity
+        self.fix_probe_com = fix_probe_com and not fix_probe
+        self.orthogonalize = orthogonalize_probe and st.geometry.num_probes > 1
+        self.mixed_state = bool(st.geometry.flags & _native.FLAG_MIXED_STATE)
+        J = int(st.positions.shape[0])
+        self.norm = np.float32(mean_intensity) * J
+
+    def iterate(self, order: np.ndarray) -> None:
+        st = self.st
+        run_iteration(st, order, self.max_batch, **self.batch_kw)
+        object_constraints(st, shrinkage_rad=self.shrinkage_rad, use_mask=self.use_mask,
+                           pure_phase=self.pure_phase, positivity=self.positivity)
+        if self.fix_probe_com:
+            probe_com_constraint(st)
+        if self.orthogonalize:
+            probe_orthogonalization(st)
+
+    def error(self) -> np.float32:
+        """Normalised error of the last iteration: float32 sum over batches divided
+        by mean intensity x J (singleslice_ptychography.py:929-932)."""
+        return np.float32(read_error(self.st) / self.norm)

@@ -1,0 +1,112 @@
+"""Generate the golden fixtures of tests/golden/ from the unmodified reference.
+
+Each fixture holds a seeded synthetic datacube (py4dstem_gb300.synthetic), the
+arguments of the constructor / preprocess() / reconstruct() calls, and what the
+reference py4DSTEM 0.14.18 CPU path (loaded by oracle/refloader.py) returned:
+preprocessed state (mean intensity, positions, initial probe and object, FOV
+mask, per-pattern amplitude sums) and the reconstruction result (error per
+iteration, object, corner-centred probe).
+
+Run from the repository root in a container that has the reference checkout:
+
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py
+"""
+
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from oracle.refloader import load_reference  # noqa: E402
+from py4dstem_gb300 import synthetic  # noqa: E402
+
+PRE = dict(plot_center_of_mass=False, plot_rotation=False, plot_probe_overlaps=False,
+           force_com_rotation=0.0, force_com_transpose=False)
+
+CASES = {
+    # the CPU-runnable single-slice workload, full size
+    "ss_gd_32x32_det64": dict(
+        gen=dict(name="ss", seed=0, scan_shape=(32, 32), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=128),
+        cls="single", ctor=dict(object_fov_ang=(32.0, 32.0)),
+        rec=dict(num_iter=16, max_batch_size=64, step_size=0.5, seed_random=0)),
+    "ss_gd_potential": dict(
+        gen=dict(name="ssp", seed=11, scan_shape=(12, 12), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=96),
+        cls="single", ctor=dict(object_fov_ang=(24.0, 24.0), object_type="potential"),
+        rec=dict(num_iter=6, max_batch_size=36, step_size=0.5, seed_random=1)),
+    "ss_raar": dict(
+        gen=dict(name="ssr", seed=12, scan_shape=(12, 12), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=96),
+        cls="single", ctor=dict(object_fov_ang=(24.0, 24.0)),
+        rec=dict(num_iter=6, reconstruction_method="RAAR", reconstruction_parameter=0.5)),
+    "ms_gd_T3": dict(
+        gen=dict(name="ms", seed=13, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=96, num_slices=3, slice_thickness=20.0),
+        cls="multi", ctor=dict(object_fov_ang=(24.0, 24.0), num_slices=3, slice_thicknesses=20.0),
+        rec=dict(num_iter=6, max_batch_size=25, step_size=0.5, seed_random=2)),
+    "mixed_gd_M3": dict(
+        gen=dict(name="mx", seed=14, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=96, num_modes=3, mode_weights=(0.7, 0.2, 0.1)),
+        cls="mixed", ctor=dict(object_fov_ang=(24.0, 24.0), num_probes=3), global_seed=7,
+        rec=dict(num_iter=6, max_batch_size=25, step_size=0.5, seed_random=3)),
+}
+
+
+def make_case(ref, name, spec):
+    case = synthetic.make_scan(**spec["gen"])
+    data = case.datacube.data
+    assert np.array_equal(data, np.round(data)) and data.max() < 65535
+    q = case.datacube.calibration.get_Q_pixel_size()
+    r = case.datacube.calibration.get_R_pixel_size()
+    dc = ref.DataCube(data, r_pixel_size=r, r_pixel_units="A", q_pixel_size=q,
+                      q_pixel_units="mrad")
+    ctor = dict(energy=300e3, semiangle_cutoff=20.0, defocus=100.0, **spec["ctor"])
+    cls = {"single": ref.SingleslicePtychography, "multi": ref.MultislicePtychography,
+           "mixed": ref.MixedstatePtychography}[spec["cls"]]
+    if "global_seed" in spec:
+        np.random.seed(spec["global_seed"])
+    p = cls(datacube=dc, initial_scan_positions=case.scan_positions_ang, verbose=False,
+            device="cpu", **ctor)
+    p.preprocess(**PRE)
+    pre = dict(
+        mean_intensity=np.float32(p._mean_diffraction_intensity),
+        positions_px=p._positions_px.copy(),
+        probe_initial=p._probe.copy(),
+        object_initial=p._object.copy(),
+        fov_mask=p._object_fov_mask.copy(),
+        amplitude_sums=p._amplitudes.astype(np.float64).sum(axis=(-2, -1)),
+        amplitude_first=p._amplitudes[0].copy(),
+        amplitude_last=p._amplitudes[-1].copy(),
+    )
+    p.reconstruct(progress_bar=False, **spec["rec"])
+    out = dict(
+        error_iterations=np.asarray(p.error_iterations, dtype=np.float64),
+        object=p.object,
+        probe_corner=np.asarray(p._probe),
+    )
+    meta = dict(cls=spec["cls"], ctor=ctor, preprocess=PRE, reconstruct=spec["rec"],
+                global_seed=spec.get("global_seed"), r_pixel_size=r, q_pixel_size=q,
+                generator=spec["gen"])
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(
+        path, datacube=data.astype(np.uint16), scan_positions_ang=case.scan_positions_ang,
+        meta=json.dumps(meta), **{f"pre_{k}": v for k, v in pre.items()},
+        **{f"out_{k}": v for k, v in out.items()})
+    print(f"{name}: {os.path.getsize(path) / 1e6:.2f} MB, errors {out['error_iterations'][-3:]}")
+
+
+def main():
+    ref = load_reference()
+    for name, spec in CASES.items():
+        make_case(ref, name, spec)
+
+
+if __name__ == "__main__":
+    main()

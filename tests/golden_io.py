@@ -1,0 +1,75 @@
+"""Load the golden fixtures written by tests/golden/make_golden.py."""
+
+import glob
+import json
+import os
+
+import numpy as np
+
+from py4dstem_gb300 import DataCube
+from py4dstem_gb300 import ptychography as api
+from oracle.ptycho_np import State
+
+GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def names():
+    return sorted(os.path.splitext(os.path.basename(p))[0]
+                  for p in glob.glob(os.path.join(GOLDEN_DIR, "*.npz")))
+
+
+class Golden:
+    def __init__(self, name):
+        self.name = name
+        z = np.load(os.path.join(GOLDEN_DIR, f"{name}.npz"))
+        self.meta = json.loads(str(z["meta"]))
+        self.datacube_counts = z["datacube"].astype(np.float32)
+        self.scan_positions_ang = z["scan_positions_ang"]
+        self.pre = {k[4:]: z[k] for k in z.files if k.startswith("pre_")}
+        self.out = {k[4:]: z[k] for k in z.files if k.startswith("out_")}
+
+    def datacube(self):
+        return DataCube(self.datacube_counts.copy(), r_pixel_size=self.meta["r_pixel_size"],
+                        r_pixel_units="A", q_pixel_size=self.meta["q_pixel_size"],
+                        q_pixel_units="mrad")
+
+    def build(self, device="gpu", storage=None):
+        """Construct and preprocess the product class exactly as the reference was."""
+        m = self.meta
+        ctor = dict(m["ctor"])
+        if "object_fov_ang" in ctor:
+            ctor["object_fov_ang"] = tuple(ctor["object_fov_ang"])
+        cls = {"single": api.SingleslicePtychography, "multi": api.MultislicePtychography,
+               "mixed": api.MixedstatePtychography}[m["cls"]]
+        if m.get("global_seed") is not None:
+            np.random.seed(m["global_seed"])
+        p = cls(datacube=self.datacube(), initial_scan_positions=self.scan_positions_ang.copy(),
+                verbose=False, device=device, storage=storage, **ctor)
+        p.preprocess(**m["preprocess"])
+        return p
+
+    def state(self, p):
+        """Oracle state from a preprocessed product object."""
+        m = self.meta
+        return State(
+            amplitudes=p._amplitudes, positions_px=p._positions_px.copy(),
+            probe=np.array(p._probe, copy=True), object=np.array(p._object, copy=True),
+            mean_intensity=p._mean_diffraction_intensity,
+            fov_mask_inverse=p._object_fov_mask_inverse, object_type=p._object_type,
+            num_slices=m["ctor"].get("num_slices", 1), num_probes=m["ctor"].get("num_probes", 1),
+            mixed=m["cls"] == "mixed",
+            propagators=getattr(p, "_propagator_arrays", None) if m["cls"] == "multi" else None)
+
+    def oracle_kwargs(self):
+        from oracle.ptycho_np import method_abc
+
+        r = dict(self.meta["reconstruct"])
+        method, a, b, c = method_abc(r.pop("reconstruction_method", "GD"),
+                                     r.pop("reconstruction_parameter", 1.0))
+        return dict(method=method, a=a, b=b, c=c, **r)
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, dtype=np.complex128)
+    b = np.asarray(b, dtype=np.complex128)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))

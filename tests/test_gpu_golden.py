@@ -1,0 +1,90 @@
+"""End-to-end parity of the drop-in classes against the unmodified reference.
+
+Each golden fixture is reconstructed through the public API (constructor,
+preprocess(), reconstruct()) on the GPU and compared with what the reference's
+CPU path returned on the same datacube, seed and arguments.
+
+Tolerances. The reference itself is sensitive to floating-point rounding: with a
+uniform initial object the far field of the first iteration is exactly zero
+outside the probe aperture, so A*exp(i*angle(F)) takes a rounding-determined
+phase there. We measure that floor by re-running the oracle with every FFT
+evaluated in complex128 and rounded back to complex64 (a different, correct
+float32 FFT). The bar is the benchmark spec's tolerance (error per iteration 1e-5
+relative, object and probe 1e-4 relative L2) or 3x the measured floor,
+whichever is larger; for the 32x32-scan, 64^2-detector workload the north-star
+numbers are required as they stand. Each result's distance to the float64
+evaluation of the same model is printed.
+"""
+
+import numpy as np
+import pytest
+
+from golden_io import Golden, names, rel_l2
+from oracle.ptycho_np import Oracle
+
+pytestmark = pytest.mark.gpu
+
+STRICT = {"ss_gd_32x32_det64"}
+
+
+@pytest.mark.parametrize("name", names())
+def test_reconstruction_matches_reference(cuda, name):
+    g = Golden(name)
+    p = g.build(device="gpu")
+    state = g.state(p)
+    kw = g.oracle_kwargs()
+    p.reconstruct(progress_bar=False, **g.meta["reconstruct"])
+
+    ref_err = g.out["error_iterations"]
+    err = np.asarray(p.error_iterations)
+    d_err = float(np.max(np.abs(err - ref_err) / np.abs(ref_err)))
+    d_obj = rel_l2(p.object, g.out["object"])
+    d_probe = rel_l2(p._probe, g.out["probe_corner"])
+
+    floor = Oracle(state, fft_round_trip=True).reconstruct(**kw)
+    f_err = float(np.max(np.abs(np.asarray(floor.error_iterations) - ref_err) / ref_err))
+    f_obj = rel_l2(floor.object, g.out["object"])
+    f_probe = rel_l2(floor.probe, g.out["probe_corner"])
+    o64 = Oracle(state, "float64").reconstruct(**kw)
+    print(f"\n{name}: gpu-vs-ref err {d_err:.2e} obj {d_obj:.2e} probe {d_probe:.2e} | "
+          f"floor err {f_err:.2e} obj {f_obj:.2e} probe {f_probe:.2e} | "
+          f"gpu-vs-fp64 obj {rel_l2(p.object, o64.object):.2e} "
+          f"probe {rel_l2(p._probe, o64.probe):.2e} | "
+          f"ref-vs-fp64 obj {rel_l2(g.out['object'], o64.object):.2e}")
+    if name in STRICT:
+        tol_err, tol_obj, tol_probe = 1e-5, 1e-4, 1e-4
+    else:
+        tol_err = max(1e-5, 3 * f_err)
+        tol_obj = max(1e-4, 3 * f_obj)
+        tol_probe = max(1e-4, 3 * f_probe)
+    assert d_err <= tol_err
+    assert d_obj <= tol_obj
+    assert d_probe <= tol_probe
+
+
+def test_storage_cpu_matches_gpu(cuda):
+    g = Golden("ss_gd_potential")
+    a = g.build(device="gpu", storage="gpu")
+    b = g.build(device="gpu", storage="cpu")
+    a.reconstruct(progress_bar=False, **g.meta["reconstruct"])
+    b.reconstruct(progress_bar=False, **g.meta["reconstruct"])
+    np.testing.assert_array_equal(a.object, b.object)
+    np.testing.assert_array_equal(a._probe, b._probe)
+    assert a.error_iterations == b.error_iterations
+
+
+def test_continue_and_reset_semantics(cuda):
+    g = Golden("ss_gd_potential")
+    rec = dict(g.meta["reconstruct"])
+    n = rec.pop("num_iter")
+    a = g.build()
+    a.reconstruct(num_iter=n, progress_bar=False, **rec)
+    b = g.build()
+    b.reconstruct(num_iter=2, progress_bar=False, **rec)
+    b.reconstruct(num_iter=n - 2, progress_bar=False, reset=True, **rec)
+    assert len(b.error_iterations) == n - 2
+    c = g.build()
+    c.reconstruct(num_iter=n, progress_bar=False, **rec)
+    c.reconstruct(num_iter=1, progress_bar=False, **rec)  # continues
+    assert len(c.error_iterations) == n + 1
+    np.testing.assert_array_equal(a.error_iterations, c.error_iterations[:n])

@@ -1,0 +1,105 @@
+"""GPU parity of the fused kernels against the oracle on small seeded states.
+
+One or a few iterations from a non-uniform initial object, where the reference
+algorithm is well conditioned, so the GPU must agree with the float32 oracle to
+a few float32 ulps amplified by the iteration (tolerances written per test)."""
+
+import numpy as np
+import pytest
+
+from gpu_helpers import gpu_reconstruct, make_state, rel
+from oracle.ptycho_np import Oracle
+
+pytestmark = pytest.mark.gpu
+
+OFF = dict(fix_probe_com=False, fix_potential_baseline=False, orthogonalize_probe=False)
+
+
+def compare(state, tol_obj, tol_probe, tol_err, **kw):
+    o = Oracle(state).reconstruct(**kw)
+    g_obj, g_probe, g_err = gpu_reconstruct(state, **kw)
+    d_obj = rel(g_obj, o.object)
+    d_probe = rel(g_probe, o.probe)
+    d_err = float(np.max(np.abs(np.array(g_err) - np.array(o.error_iterations))
+                         / np.abs(np.array(o.error_iterations))))
+    print(f"obj {d_obj:.2e} probe {d_probe:.2e} err {d_err:.2e}")
+    assert d_obj < tol_obj, d_obj
+    assert d_probe < tol_probe, d_probe
+    assert d_err < tol_err, d_err
+    return g_obj, g_probe, g_err
+
+
+@pytest.mark.parametrize("S", [32, 48, 64, 96, 128])
+def test_single_slice_one_iteration(cuda, S):
+    st = make_state(S=S, J=25, seed=S)
+    compare(st, 2e-5, 2e-5, 2e-5, num_iter=1, max_batch_size=13, seed_random=1, **OFF)
+
+
+def test_potential_object(cuda):
+    st = make_state(S=64, J=25, potential=True, seed=3)
+    compare(st, 2e-5, 2e-5, 2e-5, num_iter=1, max_batch_size=9, seed_random=2, **OFF)
+
+
+@pytest.mark.parametrize("modes", [2, 3])
+def test_mixed_state(cuda, modes):
+    st = make_state(S=64, J=25, modes=modes, seed=4)
+    compare(st, 2e-5, 2e-5, 2e-5, num_iter=1, max_batch_size=10, seed_random=3, **OFF)
+
+
+def test_mixed_formula_single_mode(cuda):
+    st = make_state(S=32, J=16, modes=1, seed=5)
+    st.mixed = True
+    compare(st, 2e-5, 2e-5, 2e-5, num_iter=1, max_batch_size=8, seed_random=3, **OFF)
+
+
+@pytest.mark.parametrize("slices,potential", [(2, False), (3, False), (2, True)])
+def test_multislice(cuda, slices, potential):
+    st = make_state(S=64, J=16, slices=slices, potential=potential, seed=6 + slices)
+    compare(st, 2e-5, 2e-5, 2e-5, num_iter=1, max_batch_size=8, seed_random=4, **OFF)
+
+
+@pytest.mark.parametrize("method,abc", [("DM", (-1.0, 1.0, 2.0)), ("RAAR", (0.0, 0.5, 2.0)),
+                                        ("RRR", (-1.0, 1.0, 2.0)), ("SUPERFLIP", (0.0, 1.0, 2.0)),
+                                        ("GP", (0.3, 0.6, 1.4))])
+def test_projection_sets(cuda, method, abc):
+    st = make_state(S=32, J=16, seed=7)
+    a, b, c = abc
+    compare(st, 5e-5, 5e-5, 5e-5, num_iter=2, method="PS", a=a, b=b, c=c, **OFF)
+
+
+def test_projection_mixed_and_multislice(cuda):
+    st = make_state(S=32, J=16, modes=2, seed=8)
+    compare(st, 5e-5, 5e-5, 5e-5, num_iter=2, method="PS", a=0.0, b=0.5, c=2.0, **OFF)
+    st = make_state(S=32, J=16, slices=2, seed=9)
+    compare(st, 5e-5, 5e-5, 5e-5, num_iter=2, method="PS", a=-1.0, b=1.0, c=2.0, **OFF)
+
+
+def test_fix_probe_and_detector_mask(cuda):
+    st = make_state(S=64, J=16, seed=10)
+    mask = (np.random.default_rng(0).uniform(size=(64, 64)) > 0.1).astype(np.float32)
+    compare(st, 2e-5, 2e-5, 2e-5, num_iter=1, max_batch_size=8, seed_random=1, fix_probe=True,
+            detector_fourier_mask=mask, **OFF)
+
+
+def test_constraints_several_iterations(cuda):
+    st = make_state(S=64, J=25, seed=11)
+    compare(st, 1e-4, 1e-4, 2e-5, num_iter=4, max_batch_size=9, seed_random=5)
+    st = make_state(S=64, J=25, seed=12, potential=True)
+    compare(st, 1e-4, 1e-4, 2e-5, num_iter=3, max_batch_size=9, seed_random=5, shrinkage_rad=0.01)
+    st = make_state(S=32, J=16, modes=3, seed=13)
+    compare(st, 1e-4, 1e-4, 2e-5, num_iter=3, max_batch_size=8, seed_random=5)
+    st = make_state(S=32, J=16, seed=14)
+    compare(st, 1e-4, 1e-4, 2e-5, num_iter=3, max_batch_size=8, seed_random=5,
+            pure_phase_object=True)
+
+
+def test_deterministic_and_storage_independent(cuda):
+    st = make_state(S=64, J=25, seed=15)
+    kw = dict(num_iter=2, max_batch_size=7, seed_random=9)
+    a = gpu_reconstruct(st, **kw)
+    b = gpu_reconstruct(st, **kw)
+    c = gpu_reconstruct(st, storage="cpu", **kw)
+    for x, y in ((a, b), (a, c)):
+        np.testing.assert_array_equal(x[0], y[0])
+        np.testing.assert_array_equal(x[1], y[1])
+        assert x[2] == y[2]

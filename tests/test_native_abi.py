@@ -1,0 +1,99 @@
+"""The C-ABI library: builds, loads, exports every declared symbol, and rejects bad
+arguments on the host (no GPU call is made by these tests)."""
+
+import ctypes
+import os
+import re
+
+import pytest
+
+from py4dstem_gb300 import _native
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "ptycho_gb300.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(ptycho_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return _native.lib()
+
+
+def test_exports_every_declared_symbol(lib):
+    syms = declared_symbols()
+    assert len(syms) >= 10
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert set(syms) == set(_native.EXPORTED_SYMBOLS)
+
+
+def test_abi_version(lib):
+    assert lib.ptycho_abi_version() == 1
+
+
+@pytest.mark.parametrize("n,ok", [(32, 1), (48, 1), (64, 1), (96, 1), (128, 1), (80, 0),
+                                  (256, 0), (100, 0)])
+def test_roi_supported(lib, n, ok):
+    assert lib.ptycho_roi_supported(n, n) == ok
+    assert lib.ptycho_roi_supported(n, n * 2) == 0
+
+
+def geometry(roi=64, obj=128, T=1, M=1, potential=0):
+    return _native.Geometry(roi, roi, obj, obj, T, M, potential, 0)
+
+
+def test_workspace_size_grows_with_batch(lib):
+    g = geometry()
+    w1 = lib.ptycho_workspace_bytes(ctypes.byref(g), 1)
+    w64 = lib.ptycho_workspace_bytes(ctypes.byref(g), 64)
+    assert 0 < w1 < w64
+    # per-position staging: object term c64 + |P|^2 + probe term c64 + |O|^2 + F c64 = 32 B/px
+    assert w64 - w1 >= 63 * 64 * 64 * 32
+    assert lib.ptycho_workspace_bytes(None, 4) == 0
+    assert lib.ptycho_workspace_bytes(ctypes.byref(g), 0) == 0
+
+
+def _gd(lib, g, ws=None, wsb=0, batch=4):
+    dummy = ctypes.c_void_p(0x1000)
+    return lib.ptycho_gd_batch(ctypes.byref(g) if g is not None else None, dummy, dummy, dummy,
+                               None, dummy, None, batch, 0.5, 1.0, 0, None, None, dummy,
+                               ws, wsb, None)
+
+
+def test_rejects_null_geometry(lib):
+    assert _gd(lib, None) == 1
+    assert b"geometry" in lib.ptycho_last_error()
+
+
+def test_rejects_unsupported_roi(lib):
+    assert _gd(lib, geometry(roi=80)) == 2
+    assert b"80x80" in lib.ptycho_last_error()
+
+
+def test_rejects_object_smaller_than_roi(lib):
+    assert _gd(lib, geometry(roi=64, obj=48)) == 2
+
+
+def test_rejects_mixed_multislice(lib):
+    assert _gd(lib, geometry(T=2, M=2)) == 2
+
+
+def test_rejects_bad_batch_and_workspace(lib):
+    g = geometry()
+    assert _gd(lib, g, batch=0) == 1
+    assert _gd(lib, g, ws=None) == 3
+    assert _gd(lib, g, ws=ctypes.c_void_p(0x1001), wsb=1 << 30) == 3  # misaligned
+    assert _gd(lib, g, ws=ctypes.c_void_p(0x1000), wsb=16) == 3       # too small
+    assert b"smaller" in lib.ptycho_last_error()
+
+
+def test_rejects_unknown_flags(lib):
+    g = geometry()
+    g.flags = 2
+    assert _gd(lib, g) == 1
+    assert b"flags" in lib.ptycho_last_error()
