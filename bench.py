@@ -59,6 +59,8 @@ def parse_args(argv=None):
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
+    ap.add_argument("--schedule", type=int, default=0,
+                    help="128^2 kernel schedule: 0 default, 1 shared-memory, 2 register")
     return ap.parse_args(argv)
 
 
@@ -334,6 +336,7 @@ def run_ours(args):
     from py4dstem_gb300 import _native, engine
 
     lib = _native.lib()
+    lib.ptycho_set_kernel_schedule(128, args.schedule)
     seed = 1234 + rank
     t_setup = time.time()
     case = build_case(args.scan, seed, f"cuda:{local}")

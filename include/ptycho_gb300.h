@@ -164,6 +164,16 @@ int ptycho_enable_kernel_timing(int32_t enable);
 int ptycho_kernel_timing(float* total_ms, int32_t* launches);
 
 /*
+ * Kernel schedule for the fused per-position kernel of a given ROI edge length:
+ * 0 = library default, 1 = shared-memory Stockham passes (every ROI and
+ * variant), 2 = register-resident four-step transform (128 x 128 single-slice
+ * gradient descent only; other cases fall back to 1). Process-wide; results
+ * agree between schedules to float32 rounding. Returns the previous setting.
+ * No reference counterpart (tuning knob of this library's autotuner).
+ */
+int ptycho_set_kernel_schedule(int32_t roi, int32_t schedule);
+
+/*
  * FP32 throughput probe: `blocks` blocks of 256 threads each run `iters`
  * iterations of 8 independent FMA chains and write one float per thread to
  * `sink` (device, blocks*256 floats). 16 * blocks * 256 * iters flops. Used to

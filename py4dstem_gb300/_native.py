@@ -75,6 +75,7 @@ _SIGNATURES = {
     "ptycho_enable_kernel_timing": ([_i32], ctypes.c_int),
     "ptycho_kernel_timing": ([ctypes.POINTER(_f32), ctypes.POINTER(_i32)], ctypes.c_int),
     "ptycho_fp32_fma_probe": ([_i32, _i32, _vp, _vp], ctypes.c_int),
+    "ptycho_set_kernel_schedule": ([_i32, _i32], ctypes.c_int),
 }
 
 EXPORTED_SYMBOLS = tuple(_SIGNATURES)

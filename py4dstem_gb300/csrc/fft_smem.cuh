@@ -133,13 +133,22 @@ __device__ __forceinline__ void dft(float2 (&a)[R]) {
 }
 
 // Fill tw[m] = exp(-2 pi i m / L) for m < L (block-cooperative, no barrier).
+// Evaluated in double and rounded once, so every entry is the float32 nearest
+// to the exact root of unity (L values per block: negligible FP64 work).
 template <int L, int NT>
 __device__ __forceinline__ void fill_twiddles(float2* tw) {
   for (int m = threadIdx.x; m < L; m += NT) {
-    float s, c;
-    sincospif(2.0f * (float)m / (float)L, &s, &c);
-    tw[m] = make_float2(c, -s);
+    double s, c;
+    sincospi(2.0 * (double)m / (double)L, &s, &c);
+    tw[m] = make_float2((float)c, (float)-s);
   }
+}
+
+// exp(i phi) for a float32 phase, cos/sin evaluated in double and rounded once.
+__device__ __forceinline__ float2 cis_rounded(float phi) {
+  double s, c;
+  sincos((double)phi, &s, &c);
+  return make_float2((float)c, (float)s);
 }
 
 // One Stockham pass over NLINES lines of length L with radix R; NS is the length

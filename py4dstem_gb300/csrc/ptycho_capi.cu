@@ -85,6 +85,7 @@ Workspace workspace_layout(int Sx, int Sy, int Px, int Py, int T, int M, int B) 
     return o;
   };
   w.probe_spec = take(sizeof(float2) * M * N);
+  w.tw = take(sizeof(float2) * (Sx + Sy));
   w.st_obj = take(sizeof(float2) * T * B * N);
   w.st_nobj = take(sizeof(float) * T * B * N);
   w.st_probe = take(sizeof(float2) * B * M * N);
@@ -109,6 +110,7 @@ Workspace workspace_layout(int Sx, int Sy, int Px, int Py, int T, int M, int B) 
 void bind_workspace(BatchArgs& a, void* base, const Workspace& w) {
   char* p = static_cast<char*>(base);
   a.probe_spec = reinterpret_cast<float2*>(p + w.probe_spec);
+  a.tw = reinterpret_cast<float2*>(p + w.tw);
   a.st_obj = reinterpret_cast<float2*>(p + w.st_obj);
   a.st_nobj = reinterpret_cast<float*>(p + w.st_nobj);
   a.st_probe = reinterpret_cast<float2*>(p + w.st_probe);
@@ -215,7 +217,8 @@ static int run_batch(const ptycho_geometry* g, void* object, void* probe,
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   cudaError_t e = launch_probe_spectrum(a, s);
   if (e != cudaSuccess) return cuda_fail(e, "probe spectrum kernel");
-  e = launch_position_kernel(a, s);
+  a.staging_t = position_v2_eligible(a) ? 1 : 0;
+  e = a.staging_t ? launch_position_v2(a, s) : launch_position_kernel(a, s);
   if (e != cudaSuccess) return cuda_fail(e, "position kernel");
   e = launch_reduce_and_update(a, s);
   if (e != cudaSuccess) return cuda_fail(e, "reduce/update kernels");
@@ -291,6 +294,12 @@ int ptycho_probe_com_constraint(const ptycho_geometry* g, void* probe, void* wor
   cudaError_t e = launch_probe_com(a, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "probe CoM constraint");
   return PTYCHO_OK;
+}
+
+int ptycho_set_kernel_schedule(int32_t roi, int32_t schedule) {
+  if (schedule < 0 || schedule > 2)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "schedule must be 0, 1 or 2 (got %d)", schedule);
+  return set_schedule(roi, schedule);
 }
 
 int ptycho_enable_kernel_timing(int32_t enable) {

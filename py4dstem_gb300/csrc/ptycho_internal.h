@@ -7,7 +7,7 @@
 
 namespace pty {
 
-constexpr int kTile = 32;          // object reduction tile (kTile x kTile pixels)
+constexpr int kTile = 16;          // object reduction tile (kTile x kTile pixels)
 constexpr int kProbeChunks = 16;   // batch chunks of the probe-gradient reduction
 constexpr int kReduceThreads = 256;
 
@@ -22,6 +22,7 @@ struct BatchArgs {
   float pa, pb, pc;        // projection parameters a, b, c
   int fix_probe;
   int ew_valid;
+  int staging_t;           // staged per-position terms are y-major (e' = y * Sx + x)
 
   void* object;                 // (T,Px,Py) float2 or float
   float2* probe;                // (M,N)
@@ -36,6 +37,7 @@ struct BatchArgs {
 
   // workspace
   float2* probe_spec;   // (M,N)
+  float2* tw;           // (Sx + Sy) twiddle tables exp(-2 pi i m / S), x then y
   float2* st_obj;       // (T,B,N)
   float* st_nobj;       // (T,B,N)
   float2* st_probe;     // (B,M,N)
@@ -56,7 +58,7 @@ struct BatchArgs {
 };
 
 struct Workspace {
-  size_t probe_spec, st_obj, st_nobj, st_probe, st_nprobe, scratch_f, pos_round, err,
+  size_t probe_spec, tw, st_obj, st_nobj, st_probe, st_nprobe, scratch_f, pos_round, err,
       obj_grad, obj_nrm, tile_max, probe_part, probe_npart, probe_bmax, probe_grad,
       probe_nrm, com, red, total;
 };
@@ -73,6 +75,12 @@ void timing_after(cudaStream_t s);
 // Launchers (return cudaError_t of the last launch).
 cudaError_t launch_probe_spectrum(const BatchArgs& a, cudaStream_t s);
 cudaError_t launch_position_kernel(const BatchArgs& a, cudaStream_t s);
+// Register-resident 128 x 128 single-slice GD kernel (ptycho_gd128.cu).
+// set_schedule stores the preferred schedule for a ROI edge (0 default,
+// 1 shared-memory passes, 2 register-resident) and returns the previous one.
+int set_schedule(int roi, int schedule);
+bool position_v2_eligible(const BatchArgs& a);
+cudaError_t launch_position_v2(const BatchArgs& a, cudaStream_t s);
 cudaError_t launch_reduce_and_update(const BatchArgs& a, cudaStream_t s);
 cudaError_t launch_object_constraints(const BatchArgs& a, const uint8_t* mask,
                                       float shrinkage, int apply_shrinkage,

@@ -91,6 +91,10 @@ __global__ void __launch_bounds__(NT, 1) probe_spectrum_kernel(BatchArgs a) {
   const float2* src = a.probe + (size_t)blockIdx.x * L::N;
   for (int e = threadIdx.x; e < L::N; e += NT) buf[(e / SY) * L::LD + e % SY] = src[e];
   __syncthreads();
+  if (blockIdx.x == 0) {  // publish the tables for the position kernel of this batch
+    for (int i = threadIdx.x; i < SX; i += NT) a.tw[i] = twx[i];
+    for (int i = threadIdx.x; i < SY; i += NT) a.tw[SX + i] = twy[i];
+  }
   fft2d<SX, SY, NT, -1>(buf, twx, twy);
   float2* dst = a.probe_spec + (size_t)blockIdx.x * L::N;
   for (int e = threadIdx.x; e < L::N; e += NT) dst[e] = buf[(e / SY) * L::LD + e % SY];
@@ -128,33 +132,54 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
   const bool ps = a.projection != 0;
   const float* amp = a.amplitudes + (size_t)arow * N;
 
-  fill_twiddles<SX, NT>(twx);
-  fill_twiddles<SY, NT>(twy);
-  // separable sub-pixel shift ramps exp(-2 pi i k d), phase formed in float32
+  for (int i = tid; i < SX; i += NT) twx[i] = a.tw[i];  // tables from the spectrum kernel
+  for (int i = tid; i < SY; i += NT) twy[i] = a.tw[SX + i];
+  // separable sub-pixel shift ramps exp(-2 pi i k d): the phase is formed in
+  // float32 like the reference's complex64 expression, its cos/sin rounded once
   for (int i = tid; i < SX; i += NT) {
     const float k = (float)fint(i, SX) / (float)SX;
-    float s, c;
-    sincosf(__fmul_rn(__fmul_rn(-6.2831855f, k), dx), &s, &c);
-    rpx[i] = make_float2(c, s);
+    rpx[i] = cis_rounded(__fmul_rn(__fmul_rn(-6.2831855f, k), dx));
   }
   for (int i = tid; i < SY; i += NT) {
     const float k = (float)fint(i, SY) / (float)SY;
-    float s, c;
-    sincosf(__fmul_rn(__fmul_rn(-6.2831855f, k), dy), &s, &c);
-    rpy[i] = make_float2(c, s);
+    rpy[i] = cis_rounded(__fmul_rn(__fmul_rn(-6.2831855f, k), dy));
   }
   if (tid == 0) a.pos_round[b] = make_int2(x0, y0);
   __syncthreads();
 
-  auto obj_x = [&](int x) { return pmod(x0 + fint(x, SX), a.Px); };
-  auto obj_y = [&](int y) { return pmod(y0 + fint(y, SY), a.Py); };
+  // (c0 + fint(i)) mod P as base + ((i + S/2) mod S) with one wrap (P >= S)
+  const int bx = pmod(x0 - SX / 2, a.Px);
+  const int by = pmod(y0 - SY / 2, a.Py);
+  auto obj_x = [&](int x) {
+    const int t = bx + (x + SX / 2) % SX;
+    return t >= a.Px ? t - a.Px : t;
+  };
+  auto obj_y = [&](int y) {
+    const int t = by + (y + SY / 2) % SY;
+    return t >= a.Py ? t - a.Py : t;
+  };
+
+  // Elementwise phases walk e = tid + i * NT (PER samples per thread) in chunks of
+  // CH: all global loads of a chunk are issued before any of them is used, so a
+  // thread keeps CH L2 requests in flight instead of one.
+  constexpr int PER = N / NT;
+  constexpr int CH = PER % 8 == 0 ? 8 : (PER % 6 == 0 ? 6 : (PER % 4 == 0 ? 4 : 1));
+  static_assert(N % NT == 0 && PER % CH == 0, "samples per thread");
 
   // buf <- IFFT2(FFT2(P_m) . ramp) * 1/N  (sub-pixel shifted probe, mode m)
   auto shifted_probe = [&](int m) {
-    const float2* spec = a.probe_spec + (size_t)m * N;
-    for (int e = tid; e < N; e += NT) {
-      const int x = e / SY, y = e % SY;
-      buf[x * LD + y] = c_mul(spec[e], c_mul(rpx[x], rpy[y]));
+    const float2* __restrict__ spec = a.probe_spec + (size_t)m * N;
+#pragma unroll
+    for (int c0 = 0; c0 < PER; c0 += CH) {
+      float2 sv[CH];
+#pragma unroll
+      for (int i = 0; i < CH; ++i) sv[i] = __ldg(spec + tid + (c0 + i) * NT);
+#pragma unroll
+      for (int i = 0; i < CH; ++i) {
+        const int e = tid + (c0 + i) * NT;
+        const int x = e / SY, y = e % SY;
+        buf[x * LD + y] = c_mul(sv[i], c_mul(rpx[x], rpy[y]));
+      }
     }
     __syncthreads();
     fft2d<SX, SY, NT, +1>(buf, twx, twy);
@@ -171,18 +196,28 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
       shifted_probe(m);
       float2* pst = a.st_probe + ((size_t)b * M + m) * N;  // stash P_m
       const float2* ew = a.exit_waves ? a.exit_waves + ((size_t)prow * M + m) * N : nullptr;
-      for (int e = tid; e < N; e += NT) {
-        const int x = e / SY, y = e % SY;
-        const float2 p = c_scale(buf[x * LD + y], invN);
-        const float2 o = load_object(a, 0, obj_x(x), obj_y(y));
-        pst[e] = p;
-        const float2 psi = c_mul(p, o);
-        float2 v = psi;
-        if (ps) {
-          const float2 w = a.ew_valid ? ew[e] : psi;
-          v = c_add(c_scale(psi, a.pc), c_scale(w, py_));
+#pragma unroll
+      for (int c0 = 0; c0 < PER; c0 += CH) {
+        float2 ov[CH];
+#pragma unroll
+        for (int i = 0; i < CH; ++i) {
+          const int e = tid + (c0 + i) * NT;
+          ov[i] = load_object(a, 0, obj_x(e / SY), obj_y(e % SY));
         }
-        buf[x * LD + y] = v;
+#pragma unroll
+        for (int i = 0; i < CH; ++i) {
+          const int e = tid + (c0 + i) * NT;
+          const int x = e / SY, y = e % SY;
+          const float2 p = c_scale(buf[x * LD + y], invN);
+          pst[e] = p;
+          const float2 psi = c_mul(p, ov[i]);
+          float2 v = psi;
+          if (ps) {
+            const float2 w = a.ew_valid ? ew[e] : psi;
+            v = c_add(c_scale(psi, a.pc), c_scale(w, py_));
+          }
+          buf[x * LD + y] = v;
+        }
       }
       __syncthreads();
       fft2d<SX, SY, NT, -1>(buf, twx, twy);
@@ -201,22 +236,31 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
 
     if (!mixed) {
       // single probe: A exp(i angle F) - F (GD) or A exp(i angle F) (projection)
-      for (int e = tid; e < N; e += NT) {
+#pragma unroll
+      for (int c0 = 0; c0 < PER; c0 += CH) {
+      float av[CH];
+#pragma unroll
+      for (int i = 0; i < CH; ++i) av[i] = __ldg(amp + tid + (c0 + i) * NT);
+#pragma unroll
+      for (int i = 0; i < CH; ++i) {
+        const int e = tid + (c0 + i) * NT;
         const int idx = (e / SY) * LD + e % SY;
         float2 f = buf[idx];
         const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
         if (a.det_mask) f = c_scale(f, mk);
         const float af = hypotf(f.x, f.y);
-        const float A = amp[e];
+        const float A = av[i];
         const float d = A - af;
         err += d * d;
-        const float2 ph = af > 0.0f ? make_float2(f.x / af, f.y / af) : make_float2(1.0f, 0.0f);
-        float2 r = c_scale(ph, A);
+        // A exp(i angle F) (- F for gradient descent), one division per pixel
+        const float q = af > 0.0f ? A / af : 0.0f;
+        float2 r = af > 0.0f ? c_scale(f, q) : make_float2(A, 0.0f);
         if (!ps) {
-          r = c_sub(r, f);
+          r = af > 0.0f ? make_float2(fmaf(f.x, q, -f.x), fmaf(f.y, q, -f.y)) : c_sub(r, f);
           if (a.det_mask) r = c_scale(r, mk);
         }
         buf[idx] = r;
+      }
       }
       __syncthreads();
       fft2d<SX, SY, NT, +1>(buf, twx, twy);
@@ -256,11 +300,22 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
       float2* ew = a.exit_waves ? a.exit_waves + ((size_t)prow * M + m) * N : nullptr;
       float2* gobj = a.st_obj + (size_t)b * N;
       float* nobj = a.st_nobj + (size_t)b * N;
-      for (int e = tid; e < N; e += NT) {
+#pragma unroll
+      for (int c0 = 0; c0 < PER; c0 += CH) {
+      float2 ov[CH], pv[CH];
+#pragma unroll
+      for (int i = 0; i < CH; ++i) {
+        const int e = tid + (c0 + i) * NT;
+        ov[i] = load_object(a, 0, obj_x(e / SY), obj_y(e % SY));
+        pv[i] = pst[e];
+      }
+#pragma unroll
+      for (int i = 0; i < CH; ++i) {
+        const int e = tid + (c0 + i) * NT;
         const int x = e / SY, y = e % SY;
         float2 chi = c_scale(buf[x * LD + y], invN);
-        const float2 p = pst[e];
-        const float2 o = load_object(a, 0, obj_x(x), obj_y(y));
+        const float2 p = pv[i];
+        const float2 o = ov[i];
         if (ps) {
           const float2 psi = c_mul(p, o);
           const float2 w = a.ew_valid ? ew[e] : psi;
@@ -278,6 +333,7 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
         }
         pst[e] = c_conj_mul(o, chi);
         if (m == 0) a.st_nprobe[(size_t)b * N + e] = c_abs2(o);
+      }
       }
       __syncthreads();
     }
@@ -327,10 +383,11 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
       const float A = amp[e];
       const float d = A - af;
       err += d * d;
-      const float2 ph = af > 0.0f ? make_float2(f.x / af, f.y / af) : make_float2(1.0f, 0.0f);
-      float2 r = c_scale(ph, A);
+      // A exp(i angle F) (- F for gradient descent), one division per pixel
+      const float q = af > 0.0f ? A / af : 0.0f;
+      float2 r = af > 0.0f ? c_scale(f, q) : make_float2(A, 0.0f);
       if (!ps) {
-        r = c_sub(r, f);
+        r = af > 0.0f ? make_float2(fmaf(f.x, q, -f.x), fmaf(f.y, q, -f.y)) : c_sub(r, f);
         if (a.det_mask) r = c_scale(r, mk);
       }
       buf[idx] = r;
@@ -446,7 +503,7 @@ bool roi_supported(int Sx, int Sy) {
     case 48: return FN<48, 48, 192>(A, S);                       \
     case 64: return FN<64, 64, 256>(A, S);                       \
     case 96: return FN<96, 96, 384>(A, S);                       \
-    case 128: return FN<128, 128, 512>(A, S);                    \
+    case 128: return FN<128, 128, 1024>(A, S);                   \
     default: return cudaErrorInvalidValue;                       \
   }
 

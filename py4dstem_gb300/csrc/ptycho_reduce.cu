@@ -81,12 +81,12 @@ __global__ void __launch_bounds__(NT) object_reduce_kernel(BatchArgs a) {
   __shared__ int warp_base[NT / 32 + 1];
   __shared__ float red[NT / 32];
 
+  static_assert(kTile * kTile == NT, "one object pixel per thread");
   const int s = blockIdx.y;
-  const int ntx = (a.Px + kTile - 1) / kTile;
+  const int nty = (a.Py + kTile - 1) / kTile;
   const int tile = blockIdx.x;
-  const int tx0 = (tile / (((a.Py + kTile - 1) / kTile))) * kTile;
-  const int ty0 = (tile % (((a.Py + kTile - 1) / kTile))) * kTile;
-  (void)ntx;
+  const int tx0 = (tile / nty) * kTile;
+  const int ty0 = (tile % nty) * kTile;
   const int tw = min(kTile, a.Px - tx0);
   const int th = min(kTile, a.Py - ty0);
   const int N = a.Sx * a.Sy;
@@ -95,18 +95,16 @@ __global__ void __launch_bounds__(NT) object_reduce_kernel(BatchArgs a) {
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
 
-  // this thread's pixels: column ty0 + lane, rows tx0 + warp + 8k
-  constexpr int ROWS = kTile * kTile / NT;  // 4
-  float2 g[ROWS];
-  float n[ROWS];
-#pragma unroll
-  for (int k = 0; k < ROWS; ++k) {
-    g[k] = make_float2(0.f, 0.f);
-    n[k] = 0.f;
-  }
-  const int py = ty0 + lane;
-  const float2* st = a.st_obj + (size_t)s * a.B * N;
-  const float* sn = a.st_nobj + (size_t)s * a.B * N;
+  // this thread's pixel; consecutive lanes walk the staging's contiguous axis
+  const int row = a.staging_t ? tid % kTile : tid / kTile;
+  const int col = a.staging_t ? tid / kTile : tid % kTile;
+  const bool inside = row < tw && col < th;
+  const int px = tx0 + row;
+  const int py = ty0 + col;
+  float2 g = make_float2(0.f, 0.f);
+  float n = 0.f;
+  const float2* __restrict__ st = a.st_obj + (size_t)s * a.B * N;
+  const float* __restrict__ sn = a.st_nobj + (size_t)s * a.B * N;
 
   for (int c0 = 0; c0 < a.B; c0 += kListChunk) {
     const int cn = min(kListChunk, a.B - c0);
@@ -133,41 +131,46 @@ __global__ void __launch_bounds__(NT) object_reduce_kernel(BatchArgs a) {
       count = warp_base[NT / 32];
       __syncthreads();
     }
-    for (int li = 0; li < count; ++li) {
-      const int b = list[li];
-      const int2 r = a.pos_round[b];
-      const int ty = pmod(py - r.y - fminy, a.Py);
-      if (lane >= th || ty >= a.Sy) continue;
-      const int ly = fminy + ty < 0 ? fminy + ty + a.Sy : fminy + ty;
-      const float2* sb = st + (size_t)b * N;
-      const float* nb = sn + (size_t)b * N;
+    // Sum the staged terms in list (= batch) order. Loads are issued U at a time
+    // ahead of the adds so that several are in flight per thread.
+    constexpr int U = 8;
+    for (int l0 = 0; l0 < count; l0 += U) {
+      float2 v[U];
+      float w[U];
 #pragma unroll
-      for (int k = 0; k < ROWS; ++k) {
-        const int row = warp + 8 * k;
-        if (row >= tw) continue;
-        const int tx = pmod(tx0 + row - r.x - fminx, a.Px);
-        if (tx >= a.Sx) continue;
-        const int lx = fminx + tx < 0 ? fminx + tx + a.Sx : fminx + tx;
-        const int e = lx * a.Sy + ly;
-        const float2 v = sb[e];
-        g[k].x += v.x;
-        g[k].y += v.y;
-        n[k] += nb[e];
+      for (int u = 0; u < U; ++u) {
+        v[u] = make_float2(0.f, 0.f);
+        w[u] = 0.f;
+        if (l0 + u < count && inside) {
+          const int b = list[l0 + u];
+          const int2 r = a.pos_round[b];
+          const int tx = pmod(px - r.x - fminx, a.Px);
+          const int ty = pmod(py - r.y - fminy, a.Py);
+          if (tx < a.Sx && ty < a.Sy) {
+            const int lx = fminx + tx < 0 ? fminx + tx + a.Sx : fminx + tx;
+            const int ly = fminy + ty < 0 ? fminy + ty + a.Sy : fminy + ty;
+            const size_t e = (size_t)b * N + (a.staging_t ? ly * a.Sx + lx : lx * a.Sy + ly);
+            v[u] = st[e];
+            w[u] = sn[e];
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        g.x += v[u].x;
+        g.y += v[u].y;
+        n += w[u];
       }
     }
   }
 
   float m = 0.0f;
   const size_t P = (size_t)a.Px * a.Py;
-#pragma unroll
-  for (int k = 0; k < ROWS; ++k) {
-    const int row = warp + 8 * k;
-    if (row < tw && lane < th) {
-      const size_t o = (size_t)s * P + (size_t)(tx0 + row) * a.Py + py;
-      a.obj_grad[o] = g[k];
-      a.obj_nrm[o] = n[k];
-      m = fmaxf(m, n[k]);
-    }
+  if (inside) {
+    const size_t o = (size_t)s * P + (size_t)px * a.Py + py;
+    a.obj_grad[o] = g;
+    a.obj_nrm[o] = n;
+    m = n;
   }
   m = block_max(m, red);
   const int ntiles = gridDim.x;
@@ -235,17 +238,21 @@ __global__ void __launch_bounds__(NT) probe_reduce_kernel(BatchArgs a) {
   const int lo = c * per;
   const int hi = min(a.B, lo + per);
   if (e >= N) return;
+  const float2* __restrict__ sp = a.st_probe;
+  const float* __restrict__ snp = a.st_nprobe;
   for (int m = 0; m < a.M; ++m) {
     float2 acc = make_float2(0.f, 0.f);
+#pragma unroll 8
     for (int b = lo; b < hi; ++b) {
-      const float2 v = a.st_probe[((size_t)b * a.M + m) * N + e];
+      const float2 v = sp[((size_t)b * a.M + m) * N + e];
       acc.x += v.x;
       acc.y += v.y;
     }
     a.probe_part[((size_t)c * a.M + m) * N + e] = acc;
   }
   float n = 0.f;
-  for (int b = lo; b < hi; ++b) n += a.st_nprobe[(size_t)b * N + e];
+#pragma unroll 8
+  for (int b = lo; b < hi; ++b) n += snp[(size_t)b * N + e];
   a.probe_npart[(size_t)c * N + e] = n;
 }
 
@@ -281,11 +288,13 @@ __global__ void __launch_bounds__(NT) probe_update_kernel(BatchArgs a, int nbloc
   const float smax = block_max(m, red);
   const int e = blockIdx.x * NT + threadIdx.x;
   if (e >= N) return;
-  const float nrm = normaliser(a.probe_nrm[e], smax, a.norm_min);
+  // sums are in staging order; the probe is natural (x-major)
+  const int es = a.staging_t ? (e % a.Sy) * a.Sx + e / a.Sy : e;
+  const float nrm = normaliser(a.probe_nrm[es], smax, a.norm_min);
   const bool ms_order = a.T > 1;
   for (int mm = 0; mm < a.M; ++mm) {
     const size_t o = (size_t)mm * N + e;
-    const float2 g = a.probe_grad[o];
+    const float2 g = a.probe_grad[(size_t)mm * N + es];
     if (a.projection) {
       a.probe[o] = make_float2(__fmul_rn(g.x, nrm), __fmul_rn(g.y, nrm));
     } else {
@@ -423,16 +432,12 @@ __global__ void __launch_bounds__(NTF, 1) probe_shift_kernel(BatchArgs a) {
   for (int i = threadIdx.x; i < SX; i += NTF) {
     const int f = i < (SX + 1) / 2 ? i : i - SX;
     const float k = (float)f / (float)SX;
-    float s, c;
-    sincosf(__fmul_rn(__fmul_rn(-6.2831855f, k), dx), &s, &c);
-    rpx[i] = make_float2(c, s);
+    rpx[i] = cis_rounded(__fmul_rn(__fmul_rn(-6.2831855f, k), dx));
   }
   for (int i = threadIdx.x; i < SY; i += NTF) {
     const int f = i < (SY + 1) / 2 ? i : i - SY;
     const float k = (float)f / (float)SY;
-    float s, c;
-    sincosf(__fmul_rn(__fmul_rn(-6.2831855f, k), dy), &s, &c);
-    rpy[i] = make_float2(c, s);
+    rpy[i] = cis_rounded(__fmul_rn(__fmul_rn(-6.2831855f, k), dy));
   }
   float2* p = a.probe + (size_t)blockIdx.x * N;
   for (int e = threadIdx.x; e < N; e += NTF) buf[(e / SY) * LD + e % SY] = p[e];

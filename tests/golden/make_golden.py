@@ -30,33 +30,51 @@ PRE = dict(plot_center_of_mass=False, plot_rotation=False, plot_probe_overlaps=F
            force_com_rotation=0.0, force_com_transpose=False)
 
 CASES = {
-    # the CPU-runnable single-slice workload, full size
+    # the CPU-runnable single-slice workload, full size, default (uniform) start
     "ss_gd_32x32_det64": dict(
         gen=dict(name="ss", seed=0, scan_shape=(32, 32), step_ang=0.5, jitter_ang=0.05,
                  detector=64, object_px=128),
         cls="single", ctor=dict(object_fov_ang=(32.0, 32.0)),
         rec=dict(num_iter=16, max_batch_size=64, step_size=0.5, seed_random=0)),
+    # the smaller cases start from a seeded non-uniform object (`guess`): with a
+    # uniform start the first far field is exactly zero outside the aperture and
+    # the reference's result is set by FFT rounding noise there
     "ss_gd_potential": dict(
         gen=dict(name="ssp", seed=11, scan_shape=(12, 12), step_ang=0.5, jitter_ang=0.05,
                  detector=64, object_px=96),
         cls="single", ctor=dict(object_fov_ang=(24.0, 24.0), object_type="potential"),
+        guess=(96, 96),
         rec=dict(num_iter=6, max_batch_size=36, step_size=0.5, seed_random=1)),
-    "ss_raar": dict(
+    "ss_ap": dict(
         gen=dict(name="ssr", seed=12, scan_shape=(12, 12), step_ang=0.5, jitter_ang=0.05,
                  detector=64, object_px=96),
-        cls="single", ctor=dict(object_fov_ang=(24.0, 24.0)),
-        rec=dict(num_iter=6, reconstruction_method="RAAR", reconstruction_parameter=0.5)),
+        cls="single", ctor=dict(object_fov_ang=(24.0, 24.0)), guess=(96, 96),
+        rec=dict(num_iter=6, reconstruction_method="DM_AP", reconstruction_parameter=0.0)),
     "ms_gd_T3": dict(
         gen=dict(name="ms", seed=13, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
                  detector=64, object_px=96, num_slices=3, slice_thickness=20.0),
         cls="multi", ctor=dict(object_fov_ang=(24.0, 24.0), num_slices=3, slice_thicknesses=20.0),
+        guess=(3, 96, 96),
         rec=dict(num_iter=6, max_batch_size=25, step_size=0.5, seed_random=2)),
     "mixed_gd_M3": dict(
         gen=dict(name="mx", seed=14, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
                  detector=64, object_px=96, num_modes=3, mode_weights=(0.7, 0.2, 0.1)),
         cls="mixed", ctor=dict(object_fov_ang=(24.0, 24.0), num_probes=3), global_seed=7,
+        guess=(96, 96),
         rec=dict(num_iter=6, max_batch_size=25, step_size=0.5, seed_random=3)),
 }
+
+
+def smooth_guess(shape, seed, potential):
+    """Seeded smooth random phase (0.3 rad peak) as an initial object."""
+    rng = np.random.default_rng(seed)
+    f = rng.normal(size=shape)
+    k0 = np.fft.fftfreq(shape[-2])
+    k1 = np.fft.fftfreq(shape[-1])
+    g = np.exp(-(k0[:, None] ** 2 + k1[None] ** 2) * (shape[-1] / 8.0) ** 2)
+    ph = np.fft.ifft2(np.fft.fft2(f) * g).real
+    ph = 0.3 * ph / np.abs(ph).max()
+    return ph.astype(np.float32) if potential else np.exp(1j * ph).astype(np.complex64)
 
 
 def make_case(ref, name, spec):
@@ -70,10 +88,18 @@ def make_case(ref, name, spec):
     ctor = dict(energy=300e3, semiangle_cutoff=20.0, defocus=100.0, **spec["ctor"])
     cls = {"single": ref.SingleslicePtychography, "multi": ref.MultislicePtychography,
            "mixed": ref.MixedstatePtychography}[spec["cls"]]
+    extra = {}
+    guess = None
+    if "guess" in spec:
+        guess = smooth_guess(tuple(spec["guess"]), spec["gen"]["seed"] + 100,
+                             ctor.get("object_type") == "potential")
+        # the reference aliases the caller's array as its object and updates it
+        # in place, so it gets a copy and the fixture keeps the original
+        extra["initial_object_guess"] = guess.copy()
     if "global_seed" in spec:
         np.random.seed(spec["global_seed"])
     p = cls(datacube=dc, initial_scan_positions=case.scan_positions_ang, verbose=False,
-            device="cpu", **ctor)
+            device="cpu", **ctor, **extra)
     p.preprocess(**PRE)
     pre = dict(
         mean_intensity=np.float32(p._mean_diffraction_intensity),
@@ -95,9 +121,13 @@ def make_case(ref, name, spec):
                 global_seed=spec.get("global_seed"), r_pixel_size=r, q_pixel_size=q,
                 generator=spec["gen"])
     path = os.path.join(HERE, f"{name}.npz")
+    if guess is not None:
+        extra_arrays = {"initial_object_guess": guess}
+    else:
+        extra_arrays = {}
     np.savez_compressed(
         path, datacube=data.astype(np.uint16), scan_positions_ang=case.scan_positions_ang,
-        meta=json.dumps(meta), **{f"pre_{k}": v for k, v in pre.items()},
+        meta=json.dumps(meta), **extra_arrays, **{f"pre_{k}": v for k, v in pre.items()},
         **{f"out_{k}": v for k, v in out.items()})
     print(f"{name}: {os.path.getsize(path) / 1e6:.2f} MB, errors {out['error_iterations'][-3:]}")
 

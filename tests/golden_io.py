@@ -27,6 +27,12 @@ class Golden:
         self.scan_positions_ang = z["scan_positions_ang"]
         self.pre = {k[4:]: z[k] for k in z.files if k.startswith("pre_")}
         self.out = {k[4:]: z[k] for k in z.files if k.startswith("out_")}
+        self.guess = z["initial_object_guess"] if "initial_object_guess" in z.files else None
+
+    @property
+    def projection(self):
+        return self.meta["reconstruct"].get("reconstruction_method", "GD") not in (
+            "GD", "gradient-descent")
 
     def datacube(self):
         return DataCube(self.datacube_counts.copy(), r_pixel_size=self.meta["r_pixel_size"],
@@ -41,6 +47,8 @@ class Golden:
             ctor["object_fov_ang"] = tuple(ctor["object_fov_ang"])
         cls = {"single": api.SingleslicePtychography, "multi": api.MultislicePtychography,
                "mixed": api.MixedstatePtychography}[m["cls"]]
+        if self.guess is not None:
+            ctor["initial_object_guess"] = self.guess.copy()
         if m.get("global_seed") is not None:
             np.random.seed(m["global_seed"])
         p = cls(datacube=self.datacube(), initial_scan_positions=self.scan_positions_ang.copy(),

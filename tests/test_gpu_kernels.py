@@ -35,6 +35,39 @@ def test_single_slice_one_iteration(cuda, S):
     compare(st, 2e-5, 2e-5, 2e-5, num_iter=1, max_batch_size=13, seed_random=1, **OFF)
 
 
+@pytest.mark.parametrize("potential,masked,fix_probe", [(True, False, False), (False, True, False),
+                                                        (False, False, True)])
+def test_register_resident_128_variants(cuda, potential, masked, fix_probe):
+    """The 128^2 single-slice kernel (register-resident FFT) with each option."""
+    from py4dstem_gb300 import _native
+
+    lib = _native.lib()
+    st = make_state(S=128, J=20, potential=potential, seed=21)
+    mask = None
+    if masked:
+        mask = (np.random.default_rng(1).uniform(size=(128, 128)) > 0.05).astype(np.float32)
+    lib.ptycho_set_kernel_schedule(128, 2)
+    try:
+        compare(st, 2e-5, 2e-5, 2e-5, num_iter=2, max_batch_size=7, seed_random=2,
+                detector_fourier_mask=mask, fix_probe=fix_probe, **OFF)
+    finally:
+        lib.ptycho_set_kernel_schedule(128, 0)
+
+
+def test_both_128_schedules_agree_with_oracle(cuda):
+    """Shared-memory passes and the register-resident schedule at 128^2."""
+    from py4dstem_gb300 import _native
+
+    lib = _native.lib()
+    st = make_state(S=128, J=16, seed=23)
+    try:
+        for schedule in (1, 2):
+            lib.ptycho_set_kernel_schedule(128, schedule)
+            compare(st, 2e-5, 2e-5, 2e-5, num_iter=1, max_batch_size=8, seed_random=4, **OFF)
+    finally:
+        lib.ptycho_set_kernel_schedule(128, 0)
+
+
 def test_potential_object(cuda):
     st = make_state(S=64, J=25, potential=True, seed=3)
     compare(st, 2e-5, 2e-5, 2e-5, num_iter=1, max_batch_size=9, seed_random=2, **OFF)
@@ -49,6 +82,7 @@ def test_mixed_state(cuda, modes):
 def test_mixed_formula_single_mode(cuda):
     st = make_state(S=32, J=16, modes=1, seed=5)
     st.mixed = True
+    st.probe = st.probe[None]
     compare(st, 2e-5, 2e-5, 2e-5, num_iter=1, max_batch_size=8, seed_random=3, **OFF)
 
 
