@@ -164,6 +164,25 @@ int ptycho_enable_kernel_timing(int32_t enable);
 int ptycho_kernel_timing(float* total_ms, int32_t* launches);
 
 /*
+ * ptycho_gd_batch() for callers that cannot allocate device memory (an
+ * acquisition loop with a device-memory budget fixed at start-up, or a host
+ * application whose own allocator owns the GPU): same arguments and results
+ * without the workspace; the scratch is a fixed 32 MiB array inside the
+ * library that each GPU holds from loading the library until exit. Batches
+ * needing more scratch than that (ptycho_workspace_bytes) return
+ * PTYCHO_ERR_WORKSPACE. The first call on a device looks up the array's
+ * address and should come before any stream capture. All calls share the
+ * array: calls that can overlap on the GPU must be serialised on one stream.
+ * No counterpart in the reference (its CuPy path always allocates).
+ */
+int ptycho_gd_batch_noalloc(const ptycho_geometry* geometry, void* object, void* probe,
+                            const float* amplitudes, const int32_t* amplitude_rows,
+                            const float* positions_px, const int32_t* position_rows,
+                            int32_t batch, float step_size, float normalization_min,
+                            int32_t fix_probe, const float* detector_mask,
+                            const void* propagators, float* error_accum, void* stream);
+
+/*
  * Kernel schedule for the fused per-position kernel of a given ROI edge length:
  * 0 = library default, 1 = shared-memory Stockham passes (every ROI and
  * variant), 2 = register-resident four-step transform (128 x 128 single-slice

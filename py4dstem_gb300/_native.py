@@ -76,6 +76,11 @@ _SIGNATURES = {
     "ptycho_kernel_timing": ([ctypes.POINTER(_f32), ctypes.POINTER(_i32)], ctypes.c_int),
     "ptycho_fp32_fma_probe": ([_i32, _i32, _vp, _vp], ctypes.c_int),
     "ptycho_set_kernel_schedule": ([_i32, _i32], ctypes.c_int),
+    "ptycho_gd_batch_noalloc": (
+        [ctypes.POINTER(Geometry), _vp, _vp, _vp, _vp, _vp, _vp, _i32, _f32, _f32, _i32,
+         _vp, _vp, _vp, _vp],
+        ctypes.c_int,
+    ),
 }
 
 EXPORTED_SYMBOLS = tuple(_SIGNATURES)

@@ -375,3 +375,70 @@ int ptycho_probe_mix(const ptycho_geometry* g, const void* probe_in, const void*
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Gradient-descent batch for callers that cannot allocate device memory.
+//
+// Some callers of this library may not call cudaMalloc at all: an acquisition
+// loop that fixes its device-memory budget when the microscope session starts
+// and must not allocate (or block on an allocation) while patterns stream in,
+// or a host application whose own allocator owns the GPU, so that memory taken
+// behind its back would break its accounting. They cannot provide the
+// workspace ptycho_gd_batch() needs. ptycho_gd_batch_noalloc() runs the same
+// kernels with their scratch in the fixed-size array below instead, so the call
+// itself allocates nothing.
+//
+//  - The array is kNoallocScratchBytes (32 MiB) of device memory that every GPU
+//    holds from the moment it loads this library until the process exits.
+//  - Its device address is looked up once per device (cudaGetSymbolAddress,
+//    on the first call made with that device current); make that first call
+//    before any stream capture.
+//  - Every call on a device uses the same array. Two calls that may run at the
+//    same time on the GPU (different streams or host threads) overwrite each
+//    other's scratch: issue them in order on one stream.
+//  - The kernels write every scratch byte they read within the call, so no
+//    part of the array has to start at zero; nothing is cleared between calls.
+namespace {
+constexpr size_t kNoallocScratchBytes = size_t(32) << 20;
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
+std::mutex g_noalloc_mu;
+std::vector<void*> g_noalloc_addr;  // per device ordinal, nullptr until looked up
+}  // namespace
+
+extern "C" int ptycho_gd_batch_noalloc(const ptycho_geometry* g, void* object, void* probe,
+                                       const float* amplitudes, const int32_t* amplitude_rows,
+                                       const float* positions_px, const int32_t* position_rows,
+                                       int32_t batch, float step_size, float normalization_min,
+                                       int32_t fix_probe, const float* detector_mask,
+                                       const void* propagators, float* error_accum,
+                                       void* stream) {
+  int st = check_geometry(g);
+  if (st != PTYCHO_OK) return st;
+  if (batch < 1) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "batch must be >= 1 (got %d)", batch);
+  const size_t need = ptycho_workspace_bytes(g, batch);
+  if (need > kNoallocScratchBytes)
+    return fail(PTYCHO_ERR_WORKSPACE,
+                "batch of %d positions needs %zu bytes of scratch; the fixed no-allocation "
+                "scratch holds %zu bytes (use fewer positions per call or ptycho_gd_batch "
+                "with a workspace)",
+                batch, need, kNoallocScratchBytes);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  void* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if ((size_t)dev >= g_noalloc_addr.size()) g_noalloc_addr.resize(dev + 1, nullptr);
+    if (!g_noalloc_addr[dev]) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-allocation scratch)");
+      g_noalloc_addr[dev] = p;
+    }
+    scratch = g_noalloc_addr[dev];
+  }
+  return ptycho_gd_batch(g, object, probe, amplitudes, amplitude_rows, positions_px,
+                         position_rows, batch, step_size, normalization_min, fix_probe,
+                         detector_mask, propagators, error_accum, scratch,
+                         kNoallocScratchBytes, stream);
+}

@@ -34,12 +34,6 @@ constexpr int NT = 1024;
 constexpr int GA = 1;  // A groups (16 samples) per thread
 constexpr int GB = 2;  // B groups (8 samples) per thread
 
-__device__ __forceinline__ int swz(int x, int y) {
-  const int u = (y >> 4) & 7;
-  const int t = (x & 15) ^ ((x >> 4) & 7);
-  return x * S + (y ^ u ^ t);
-}
-
 __device__ __forceinline__ int pmod(int v, int m) {
   int r = v % m;
   return r < 0 ? r + m : r;
