@@ -11,7 +11,7 @@
 // Radix-R DFTs (R in {2,4,8,16}) are radix-2 decimation-in-frequency networks
 // fully unrolled in registers; R = 3 uses the standard 3-point butterfly. Their
 // internal twiddles are exact 16th roots of unity. Inter-pass twiddles come from
-// a per-block table exp(-2 pi i m / L), m < L, filled with sincospif().
+// a table exp(-2 pi i m / L), m < L, evaluated in double and rounded once.
 //
 // Conventions match numpy.fft: forward = exp(-2 pi i n k / L) unnormalised,
 // inverse = exp(+2 pi i n k / L); the caller applies the 1/(SX*SY) factor.
@@ -22,6 +22,8 @@
 namespace pty {
 
 // ---------------------------------------------------------------- complex ops
+// (Packed f32x2 forms of these were measured slower here: the register pairing
+// they need adds moves and spills in the radix passes.)
 __device__ __forceinline__ float2 c_add(float2 a, float2 b) {
   return make_float2(a.x + b.x, a.y + b.y);
 }
