@@ -51,7 +51,7 @@ WORKLOAD = "single-slice GD, 128x128 scan (J=16384), 128^2 detector, 512^2 objec
 def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--scan", type=int, default=128, help="scan side (positions = scan^2)")
@@ -59,6 +59,8 @@ def parse_args(argv=None):
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-cores", type=int, default=0,
+                    help="reference arm: limit the worker processes (0 = all host cores)")
     ap.add_argument("--schedule", type=int, default=0,
                     help="128^2 kernel schedule: 0 default, 1 shared-memory, 2 register")
     return ap.parse_args(argv)
@@ -95,19 +97,24 @@ class ClockSampler:
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index=0):
+    def __init__(self, gpu_index=0, period_ms=50):
         self.gpu_index = gpu_index
+        self.period_ms = period_ms
         self.proc = None
         self.lines = []
+        self.first = threading.Event()
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu_index}", f"--query-gpu={self.QUERY}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", str(self.period_ms)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # start the timed region only once sampling runs (bounded wait)
+            self.first.wait(timeout=5.0)
+            self.lines.clear()
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
@@ -115,6 +122,7 @@ class ClockSampler:
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+            self.first.set()
 
     def __exit__(self, *exc):
         if self.proc is not None:
@@ -148,12 +156,20 @@ class ClockSampler:
 
 # ------------------------------------------------------------------ workload
 def roofline_constants(n_pixels):
-    """Algorithmic work per single-slice GD position update (5 N log2 N flops per
-    complex 2D FFT, 3 FFTs, ~50 real flops of elementwise work per pixel; bytes:
-    amplitude read 4N + object patch 8N + object-term scatter 8N + |P|^2 scatter 4N)."""
-    flops = 3 * 5 * n_pixels * math.log2(n_pixels) + 50 * n_pixels
-    bytes_ = 24 * n_pixels
-    return flops, bytes_
+    """Algorithmic flops and bytes of one single-slice GD position update."""
+    from py4dstem_gb300 import roofline
+
+    return roofline.flops_per_position(n_pixels), roofline.bytes_per_position(n_pixels)
+
+
+def measured_hbm_gbs():
+    """Measured HBM copy bandwidth of this GPU model (MEASURED_PEAKS.json), else
+    the 6.8 TB/s fallback; returns (GB/s, source)."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (copy)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback 6.8 TB/s"
 
 
 def read_profile_traffic():
@@ -245,33 +261,48 @@ def _run_oracle_batch(o, idx):
     o.adjoint(patches, shifted, pos, ew, 0.5, 1.0, False, False)
 
 
+def bench_config(scan, batch, object_shape, world):
+    return {"workload": WORKLOAD, "positions": scan * scan, "batch": min(batch, scan * scan),
+            "detector": 128, "object": object_shape, "iterations_per_step": 1,
+            "l2": "inputs larger than L2 (1 GiB amplitudes)",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
 # ------------------------------------------------------------------ reference arm
-def _ref_worker(args):
-    scan, seed, seconds = args
-    import numpy as _np
+_REF = {}
 
+
+def _ref_init(scan, seed):
+    """Pool initializer: one small scan per worker process, preprocessed once."""
     from py4dstem_gb300 import synthetic
-    from oracle.ptycho_np import Oracle
+    from oracle.ptycho_np import Oracle, State
 
-    case = synthetic.make_scan("ref", seed, (scan, scan), 0.75, 0.05, 128, 512 if scan >= 128
-                               else int(2 ** math.ceil(math.log2(scan * 3 + 128))), dose=1e5,
+    seed = seed + os.getpid() % 1000
+    case = synthetic.make_scan("ref", seed, (scan, scan), 0.75, 0.05, 128,
+                               int(2 ** math.ceil(math.log2(scan * 3 + 128))), dose=1e5,
                                backend="numpy")
     p = preprocess(case, storage="cpu")
-    from oracle.ptycho_np import State
-
     st = State(amplitudes=p._amplitudes, positions_px=p._positions_px.copy(),
-               probe=_np.array(p._probe), object=_np.array(p._object),
+               probe=np.array(p._probe), object=np.array(p._object),
                mean_intensity=p._mean_diffraction_intensity,
                fov_mask_inverse=p._object_fov_mask_inverse)
-    o = Oracle(st)
-    J = p._num_diffraction_patterns
-    order = _np.random.default_rng(seed).permutation(J)
+    _REF["oracle"] = Oracle(st)
+    _REF["order"] = np.random.default_rng(seed).permutation(p._num_diffraction_patterns)
+    _REF["done"] = 0
+
+
+def _ref_step(seconds):
+    """Reference-algorithm GD batches of 64 positions for ~`seconds`."""
+    o, order = _REF["oracle"], _REF["order"]
+    J = len(order)
     done = 0
     t0 = time.perf_counter()
     while time.perf_counter() - t0 < seconds:
-        idx = order[(done % J):(done % J) + 64]
+        start = _REF["done"] % J
+        idx = order[start:start + 64]
         _run_oracle_batch(o, idx)
         done += len(idx)
+        _REF["done"] += len(idx)
     return done, time.perf_counter() - t0
 
 
@@ -282,14 +313,16 @@ def run_reference(args):
     import multiprocessing as mp
 
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    if args.ref_cores:
+        cores = min(cores, args.ref_cores)
     # small scans per worker keep the per-process setup short; the per-position
-    # work (128^2 detector) is the workload's
-    per_step = max(2.0, min(20.0, 60.0 / max(1, args.steps + args.warmup)))
+    # work (128^2 detector GD update) is the workload's
+    per_step = max(1.0, min(20.0, 60.0 / max(1, args.steps + args.warmup)))
     ctx = mp.get_context("spawn")
     values = []
-    with ctx.Pool(cores) as pool:
+    with ctx.Pool(cores, initializer=_ref_init, initargs=(16, 100)) as pool:
         for i in range(args.warmup + args.steps):
-            res = pool.map(_ref_worker, [(16, 100 + w + 1000 * i, per_step) for w in range(cores)])
+            res = pool.map(_ref_step, [per_step] * cores, chunksize=1)
             tot = sum(r[0] for r in res)
             wall = max(r[1] for r in res)
             if i >= args.warmup:
@@ -300,10 +333,12 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * 16384 / v,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample": "per-position GD updates at 128^2 detector"},
+        "config": bench_config(args.scan, args.batch, [512, 512] if args.scan >= 128 else None,
+                               args.gpus),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{cores} processes x ~{per_step:.0f} s of 64-position "
-                                   "batches of the 128^2-detector GD update"},
+                         "sample": f"{cores} processes x ~{per_step:.1f} s per step of "
+                                   "64-position batches of the 128^2-detector GD update "
+                                   "(16x16 scan per process)"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -406,9 +441,36 @@ def run_ours(args):
     kernel_avg_ms = kms.value / max(1, kn.value)
     nb = len(list(engine.generate_batches(J, B)))
     pos_per_launch = J / nb
-    achieved = flops_pos * pos_per_launch / (kernel_avg_ms * 1e-3) / 1e12
-    peak = fp32_peak_tflops(torch, lib) if rank == 0 else None
+    kernel_s = kernel_avg_ms * 1e-3
+    fp32_peak = fp32_peak_tflops(torch, lib) if rank == 0 else None
+    hbm_peak, hbm_source = measured_hbm_gbs()
     traffic = read_profile_traffic()
+    fp32_achieved = flops_pos * pos_per_launch / kernel_s / 1e12
+    hbm_achieved = bytes_pos * pos_per_launch / kernel_s / 1e9
+    from py4dstem_gb300 import roofline as _rl
+
+    bound_name, _ = _rl.bound(flops_pos, bytes_pos, fp32_peak or 77.0, hbm_peak)
+    kernel_name = ("gd128_kernel" if args.schedule == 2 else "position_kernel<128,128,1024>")
+    if bound_name == "hbm":
+        roof = {"bound": "hbm", "achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": hbm_achieved / hbm_peak, "peak_source": hbm_source + ", of measured"}
+    else:
+        roof = {"bound": "fp32", "achieved": fp32_achieved, "peak": fp32_peak,
+                "unit": "TFLOP/s", "frac": fp32_achieved / fp32_peak if fp32_peak else None,
+                "peak_source": "FP32 FMA probe measured live (ptycho_fp32_fma_probe), of measured"}
+    roof.update({
+        "traffic": traffic, "kernel": kernel_name, "kernel_avg_ms": kernel_avg_ms,
+        "kernel_launches": kn.value, "positions_per_launch": pos_per_launch,
+        "flops_per_position": flops_pos, "bytes_per_position": bytes_pos,
+        "other_roofline": ({"bound": "fp32", "achieved": fp32_achieved, "peak": fp32_peak,
+                            "unit": "TFLOP/s",
+                            "frac": fp32_achieved / fp32_peak if fp32_peak else None}
+                           if bound_name == "hbm" else
+                           {"bound": "hbm", "achieved": hbm_achieved, "peak": hbm_peak,
+                            "unit": "GB/s", "frac": hbm_achieved / hbm_peak}),
+        "traffic_source": "ncu dram__bytes_read+write of one launch "
+                          "(profiles/position_kernel_128_gd.md)",
+    })
 
     # e2e through the public API with host-resident inputs
     e2e = None
@@ -433,18 +495,9 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "positions": J, "batch": B, "detector": 128,
-                       "object": list(np.shape(p._object)), "iterations_per_step": 1,
-                       "l2": "inputs larger than L2 (1 GiB amplitudes)",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "config": bench_config(args.scan, B, list(np.shape(p._object)), world),
             "iterations_per_s": args.steps / (ms * 1e-3),
-            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak,
-                         "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
-                         "traffic": traffic, "kernel": "position_kernel<128,128,512>",
-                         "kernel_avg_ms": kernel_avg_ms, "kernel_launches": kn.value,
-                         "peak_source": "measured FP32 FMA probe (ptycho_fp32_fma_probe)",
-                         "flops_per_position": flops_pos, "bytes_per_position": bytes_pos,
-                         "positions_per_launch": pos_per_launch},
+            "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": launches,
