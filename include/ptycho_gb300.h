@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define PTYCHO_ABI_VERSION 1
+#define PTYCHO_ABI_VERSION 2
 
 enum ptycho_status {
   PTYCHO_OK = 0,
@@ -60,6 +60,10 @@ typedef struct ptycho_geometry {
 /* Use the mixed-state Fourier projection (shared ratio A/sqrt(sum_m |F_m|^2),
  * mixedstate class) even when num_probes == 1. Implied when num_probes > 1. */
 #define PTYCHO_FLAG_MIXED_STATE 1
+
+/* Single slice, gradient descent: keep each position's far field FFT2(P_m O)
+ * in the workspace for a following ptycho_position_correction() call. */
+#define PTYCHO_FLAG_KEEP_FARFIELD 2
 
 /* Library identity and capability queries. */
 int ptycho_abi_version(void);
@@ -112,6 +116,43 @@ int ptycho_projection_batch(const ptycho_geometry* geometry, void* object, void*
                             int32_t exit_waves_valid, const void* propagators,
                             float* error_accum, void* workspace,
                             size_t workspace_bytes, void* stream);
+
+/*
+ * Position correction of the batch just updated by ptycho_gd_batch() (called
+ * with PTYCHO_FLAG_KEEP_FARFIELD, the same geometry, workspace, amplitudes,
+ * rows and batch, and no other batch call on that workspace in between).
+ * Replaces _position_correction (ptychographic_methods.py:2071-2225): per
+ * position a 2x2 least-squares shift from the intensity change of one-pixel
+ * object shifts, using the object after the update, scaled by step_size,
+ * limited to max_update_px per call and to max_total_px from positions_initial
+ * (negative = no limit; pixels), and subtracted from positions_px[row] in place.
+ * The perturbed waves start, as in the reference, from the batch's shifted
+ * probes (single slice, mixed state) or from the updated unshifted probe
+ * propagated through all slices (multislice, multislice_ptychography.py:1026-1038;
+ * probe and propagators are read only then). A position whose 2x2 system is
+ * singular keeps its place (the reference raises LinAlgError).
+ */
+int ptycho_position_correction(const ptycho_geometry* geometry, const void* object,
+                               const void* probe, const void* propagators,
+                               const float* amplitudes, const int32_t* amplitude_rows,
+                               float* positions_px, const float* positions_initial,
+                               const int32_t* position_rows, int32_t batch, float step_size,
+                               double max_update_px, double max_total_px, void* workspace,
+                               size_t workspace_bytes, void* stream);
+
+/*
+ * Per-position self-consistency error sum_k (A - |F|)^2 of a forward-only pass
+ * (no update), written to errors[b] for the `batch` positions. Replaces the
+ * per-batch body of _return_self_consistency_errors
+ * (ptychographic_methods.py:2227-2291); the caller divides by the mean
+ * intensity. No detector mask (the reference applies none here).
+ */
+int ptycho_self_consistency_errors(const ptycho_geometry* geometry, const void* object,
+                                   const void* probe, const float* amplitudes,
+                                   const int32_t* amplitude_rows, const float* positions_px,
+                                   const int32_t* position_rows, int32_t batch,
+                                   const void* propagators, float* errors, void* workspace,
+                                   size_t workspace_bytes, void* stream);
 
 /*
  * Per-iteration object constraints, default-on subset: shrinkage by

@@ -42,6 +42,7 @@ class State:
     num_probes: int = 1             # >1 or mixed=True: mixed state
     mixed: bool = False
     propagators: Optional[np.ndarray] = None  # (T-1,Sx,Sy) complex64
+    sampling: tuple = (1.0, 1.0)    # real-space pixel size (A), for position limits
 
     def copy(self):
         return dataclasses.replace(
@@ -65,6 +66,8 @@ class Oracle:
         s = state
         self.amplitudes = np.asarray(s.amplitudes, dtype=self.f)
         self.positions_px = np.asarray(s.positions_px, dtype=np.float32).copy()
+        self.positions_initial = self.positions_px.copy()
+        self.sampling = tuple(s.sampling)
         self.object_type = s.object_type
         otype = self.f if s.object_type == "potential" else self.c
         self.object = np.asarray(s.object, dtype=otype).copy()
@@ -284,6 +287,72 @@ class Oracle:
             probe = g if projection else probe + step * g
         self.object, self.probe = obj, probe
 
+    # ------------------------------------------------------- position correction A16
+    def position_correction(self, rows, cols, shifted, ov, amps, pos, pos_init, step,
+                            max_update, max_total):
+        """ptychographic_methods.py:2071-2225 (without diffraction resampling): a
+        per-position 2x2 least-squares shift from the intensity change of one-pixel
+        object shifts, computed with the object after this batch's update, the
+        overlap of the forward pass and `shifted` (the forward pass's shifted probes,
+        or for multislice the updated probe)."""
+        fo = self.fft2(ov)
+        fo_conj = np.conj(fo)
+        estimated = self.farfield(fo) ** 2
+        measured = amps ** 2
+        flat = (measured.shape[0], -1)
+        difference = (measured - estimated).reshape(flat)
+        _, _, ov_dx = self.overlap((rows + 1) % self.object_shape[0], cols, shifted)
+        _, _, ov_dy = self.overlap(rows, (cols + 1) % self.object_shape[1], shifted)
+        fdx = fo - self.fft2(ov_dx)
+        fdy = fo - self.fft2(ov_dy)
+        pdx = 2 * np.real(fdx * fo_conj)
+        pdy = 2 * np.real(fdy * fo_conj)
+        if pdx.ndim == 4:
+            pdx = pdx.sum(1)
+            pdy = pdy.sum(1)
+        pdx = pdx.reshape(flat)
+        pdy = pdy.reshape(flat)
+        cm = np.dstack((pdx, pdy))
+        cm_t = cm.conj().swapaxes(-1, -2)
+        update = np.linalg.inv(cm_t @ cm) @ cm_t @ difference[..., None]
+        update = update[..., 0] * step
+        scale = np.sqrt(self.sampling[0] ** 2 + self.sampling[1] ** 2)
+        if max_update is not None:
+            max_update = max_update / scale
+            norms = np.linalg.norm(update, axis=1)
+            out = norms > max_update
+            update[out] /= norms[out, None] / max_update
+        if max_total is not None:
+            max_total = max_total / scale
+            deltas = (pos - pos_init) - update
+            out = np.linalg.norm(deltas, axis=1) > max_total
+            update[out] = 0
+        pos -= update
+        return pos
+
+    def positions_com_constraint(self):
+        """ptychographic_constraints.py:1292-1311."""
+        self.positions_px -= self.positions_px.mean(0) - self.positions_initial.mean(0)
+
+    # ------------------------------------------------------- self-consistency A19
+    def self_consistency_errors(self, max_batch_size=None):
+        """ptychographic_methods.py:2227-2291: per-position sum (A - |F|)^2 of a
+        forward-only pass in natural order, divided by the mean intensity."""
+        if max_batch_size is None:
+            max_batch_size = self.J
+        errors = np.array([])
+        for start, end in self.batches(self.J, max_batch_size):
+            pos = self.positions_px[start:end]
+            frac = pos - np.round(pos)
+            rows, cols = self.patch_indices(pos)
+            shifted = self.fft_shift(self.probe, frac)
+            _, _, ov = self.overlap(rows, cols, shifted)
+            ff = self.farfield(self.fft2(ov))
+            errors = np.hstack((errors, np.sum(np.abs(self.amplitudes[start:end] - ff) ** 2,
+                                               axis=(-2, -1))))
+        errors /= self.mean_intensity
+        return errors
+
     # ------------------------------------------------------------ constraints A17
     def object_constraints(self, shrinkage_rad, mask, pure_phase, positivity):
         """ptychographic_constraints.py:29-117, 411-464, 649-726 (default-on subset)."""
@@ -339,7 +408,9 @@ class Oracle:
                     seed_random=None, step_size=0.5, normalization_min=1.0, fix_probe=False,
                     fix_probe_com=True, orthogonalize_probe=True, shrinkage_rad=0.0,
                     fix_potential_baseline=True, pure_phase_object=False,
-                    object_positivity=True, detector_fourier_mask=None):
+                    object_positivity=True, detector_fourier_mask=None, fix_positions=True,
+                    fix_positions_com=True, positions_step_size=0.5,
+                    max_position_update_distance=None, max_position_total_distance=None):
         """singleslice_ptychography.py:606-996 (and the multislice / mixed-state twins)."""
         projection = method != "GD"
         J = self.J
@@ -370,6 +441,14 @@ class Oracle:
                     ew, be = self.gd_projection(amps, ov, detector_fourier_mask)
                 self.adjoint(patches, shifted, pos, ew, step_size, normalization_min, fix_probe,
                              projection)
+                if not fix_positions:
+                    # multislice passes the updated, unshifted probe
+                    # (multislice_ptychography.py:1026-1038)
+                    self.positions_px[idx] = self.position_correction(
+                        rows, cols, self.probe if self.num_slices > 1 else shifted, ov, amps,
+                        pos, self.positions_initial[idx],
+                        positions_step_size, max_position_update_distance,
+                        max_position_total_distance)
                 error += be
             error /= self.mean_intensity * J
             self.object_constraints(shrinkage_rad, mask,
@@ -379,6 +458,9 @@ class Oracle:
                 self.probe_com_constraint()
             if self.mixed and orthogonalize_probe:
                 self.probe_orthogonalization()
+            # phase_base_class.py:2179-2195 passes fix_positions_com and not fix_positions
+            if not fix_positions and not (fix_positions_com and not fix_positions):
+                self.positions_com_constraint()
             self.error_iterations.append(float(error))
         return self
 

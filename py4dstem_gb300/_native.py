@@ -14,6 +14,7 @@ from . import build as _build
 
 PTYCHO_OK = 0
 FLAG_MIXED_STATE = 1
+FLAG_KEEP_FARFIELD = 2
 _STATUS_NAMES = {
     1: "invalid argument",
     2: "unsupported geometry",
@@ -48,6 +49,7 @@ _vp = ctypes.c_void_p
 _i32 = ctypes.c_int32
 _f32 = ctypes.c_float
 _sz = ctypes.c_size_t
+_f64 = ctypes.c_double
 
 _SIGNATURES = {
     "ptycho_abi_version": ([], ctypes.c_int),
@@ -76,6 +78,15 @@ _SIGNATURES = {
     "ptycho_kernel_timing": ([ctypes.POINTER(_f32), ctypes.POINTER(_i32)], ctypes.c_int),
     "ptycho_fp32_fma_probe": ([_i32, _i32, _vp, _vp], ctypes.c_int),
     "ptycho_set_kernel_schedule": ([_i32, _i32], ctypes.c_int),
+    "ptycho_position_correction": (
+        [ctypes.POINTER(Geometry), _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _f32, _f64,
+         _f64, _vp, _sz, _vp],
+        ctypes.c_int,
+    ),
+    "ptycho_self_consistency_errors": (
+        [ctypes.POINTER(Geometry), _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _sz, _vp],
+        ctypes.c_int,
+    ),
     "ptycho_gd_batch_noalloc": (
         [ctypes.POINTER(Geometry), _vp, _vp, _vp, _vp, _vp, _vp, _i32, _f32, _f32, _i32,
          _vp, _vp, _vp, _vp],

@@ -51,7 +51,7 @@ cudaEvent_t take_event() {
 
 int check_geometry(const ptycho_geometry* g) {
   if (!g) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "geometry is null");
-  if ((g->flags & ~PTYCHO_FLAG_MIXED_STATE) != 0)
+  if ((g->flags & ~(PTYCHO_FLAG_MIXED_STATE | PTYCHO_FLAG_KEEP_FARFIELD)) != 0)
     return fail(PTYCHO_ERR_INVALID_ARGUMENT, "unknown bits in geometry.flags (0x%x)", g->flags);
   if (g->num_slices < 1 || g->num_probes < 1)
     return fail(PTYCHO_ERR_INVALID_ARGUMENT, "num_slices and num_probes must be >= 1");
@@ -72,7 +72,8 @@ int check_geometry(const ptycho_geometry* g) {
 
 }  // namespace
 
-Workspace workspace_layout(int Sx, int Sy, int Px, int Py, int T, int M, int B) {
+Workspace workspace_layout(int Sx, int Sy, int Px, int Py, int T, int M, int B,
+                           bool keep_farfield) {
   Workspace w{};
   const size_t N = (size_t)Sx * Sy;
   const size_t P = (size_t)Px * Py;
@@ -90,7 +91,7 @@ Workspace workspace_layout(int Sx, int Sy, int Px, int Py, int T, int M, int B) 
   w.st_nobj = take(sizeof(float) * T * B * N);
   w.st_probe = take(sizeof(float2) * B * M * N);
   w.st_nprobe = take(sizeof(float) * B * N);
-  w.scratch_f = take(T == 1 ? sizeof(float2) * B * M * N : 0);
+  w.scratch_f = take(T == 1 || keep_farfield ? sizeof(float2) * B * M * N : 0);
   w.pos_round = take(sizeof(int2) * B);
   w.err = take(sizeof(float) * B);
   w.obj_grad = take(sizeof(float2) * T * P);
@@ -141,7 +142,8 @@ int prepare(const ptycho_geometry* g, int32_t batch, void* workspace, size_t wor
   if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
     return fail(PTYCHO_ERR_WORKSPACE, "workspace must be 256-byte aligned");
   const Workspace w = workspace_layout(g->roi_x, g->roi_y, g->object_x, g->object_y,
-                                       g->num_slices, g->num_probes, batch);
+                                       g->num_slices, g->num_probes, batch,
+                                       (g->flags & PTYCHO_FLAG_KEEP_FARFIELD) != 0);
   if (workspace_bytes < w.total)
     return fail(PTYCHO_ERR_WORKSPACE, "workspace of %zu bytes is smaller than the %zu needed",
                 workspace_bytes, w.total);
@@ -191,7 +193,7 @@ int ptycho_roi_supported(int32_t roi_x, int32_t roi_y) { return roi_supported(ro
 size_t ptycho_workspace_bytes(const ptycho_geometry* g, int32_t max_batch) {
   if (!g || max_batch < 1) return 0;
   return workspace_layout(g->roi_x, g->roi_y, g->object_x, g->object_y, g->num_slices,
-                          g->num_probes, max_batch)
+                          g->num_probes, max_batch, (g->flags & PTYCHO_FLAG_KEEP_FARFIELD) != 0)
       .total;
 }
 
@@ -238,6 +240,7 @@ int ptycho_gd_batch(const ptycho_geometry* g, void* object, void* probe,
   a.norm_min = normalization_min;
   a.fix_probe = fix_probe ? 1 : 0;
   a.mixed_formula = (g->num_probes > 1 || (g->flags & PTYCHO_FLAG_MIXED_STATE)) ? 1 : 0;
+  a.keep_farfield = (g->flags & PTYCHO_FLAG_KEEP_FARFIELD) ? 1 : 0;
   return run_batch(g, object, probe, amplitudes, amplitude_rows, positions_px, position_rows,
                    batch, detector_mask, propagators, error_accum, workspace, workspace_bytes,
                    stream, a);
@@ -255,6 +258,9 @@ int ptycho_projection_batch(const ptycho_geometry* g, void* object, void* probe,
   int st = prepare(g, batch, workspace, workspace_bytes, a);
   if (st != PTYCHO_OK) return st;
   if (!exit_waves) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "exit_waves must be non-null");
+  if (g->flags & PTYCHO_FLAG_KEEP_FARFIELD)
+    return fail(PTYCHO_ERR_UNSUPPORTED, "PTYCHO_FLAG_KEEP_FARFIELD applies to gradient-descent "
+                                        "batches only");
   a.projection = 1;
   a.pa = projection_a;
   a.pb = projection_b;
@@ -267,6 +273,75 @@ int ptycho_projection_batch(const ptycho_geometry* g, void* object, void* probe,
   return run_batch(g, object, probe, amplitudes, amplitude_rows, positions_px, position_rows,
                    batch, nullptr, propagators, error_accum, workspace, workspace_bytes, stream,
                    a);
+}
+
+int ptycho_position_correction(const ptycho_geometry* g, const void* object,
+                               const void* probe, const void* propagators,
+                               const float* amplitudes, const int32_t* amplitude_rows,
+                               float* positions_px, const float* positions_initial,
+                               const int32_t* position_rows, int32_t batch, float step_size,
+                               double max_update_px, double max_total_px, void* workspace,
+                               size_t workspace_bytes, void* stream) {
+  BatchArgs a;
+  int st = prepare(g, batch, workspace, workspace_bytes, a);
+  if (st != PTYCHO_OK) return st;
+  if (!(g->flags & PTYCHO_FLAG_KEEP_FARFIELD))
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "position correction needs the far fields of a "
+                                             "batch run with PTYCHO_FLAG_KEEP_FARFIELD");
+  if (!object || !amplitudes || !positions_px || !positions_initial)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "object, amplitudes, positions_px and "
+                                             "positions_initial must be non-null");
+  if (g->num_slices > 1 && (!probe || !propagators))
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "multislice position correction needs the probe "
+                                             "and the propagators");
+  a.object = const_cast<void*>(object);
+  a.amplitudes = amplitudes;
+  a.amp_rows = amplitude_rows;
+  a.positions = positions_px;
+  a.positions_rw = positions_px;
+  a.positions_initial = positions_initial;
+  a.pos_rows = position_rows;
+  a.pc_step = step_size;
+  a.pc_max_update = max_update_px;
+  a.pc_max_total = max_total_px;
+  a.mixed_formula = (g->num_probes > 1 || (g->flags & PTYCHO_FLAG_MIXED_STATE)) ? 1 : 0;
+  a.probe = static_cast<float2*>(const_cast<void*>(probe));
+  a.props = static_cast<const float2*>(propagators);
+  cudaError_t e = launch_position_correction(a, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "position correction kernel");
+  return PTYCHO_OK;
+}
+
+int ptycho_self_consistency_errors(const ptycho_geometry* g, const void* object,
+                                   const void* probe, const float* amplitudes,
+                                   const int32_t* amplitude_rows, const float* positions_px,
+                                   const int32_t* position_rows, int32_t batch,
+                                   const void* propagators, float* errors, void* workspace,
+                                   size_t workspace_bytes, void* stream) {
+  BatchArgs a;
+  int st = prepare(g, batch, workspace, workspace_bytes, a);
+  if (st != PTYCHO_OK) return st;
+  if (!object || !probe || !amplitudes || !positions_px || !errors)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "object, probe, amplitudes, positions and errors "
+                                             "must be non-null");
+  if (g->num_slices > 1 && !propagators)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "multislice needs propagators");
+  a.forward_only = 1;
+  a.mixed_formula = (g->num_probes > 1 || (g->flags & PTYCHO_FLAG_MIXED_STATE)) ? 1 : 0;
+  a.object = const_cast<void*>(object);
+  a.probe = static_cast<float2*>(const_cast<void*>(probe));
+  a.amplitudes = amplitudes;
+  a.amp_rows = amplitude_rows;
+  a.positions = positions_px;
+  a.pos_rows = position_rows;
+  a.props = static_cast<const float2*>(propagators);
+  a.err = errors;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = launch_probe_spectrum(a, s);
+  if (e != cudaSuccess) return cuda_fail(e, "probe spectrum kernel");
+  e = launch_position_kernel(a, s);
+  if (e != cudaSuccess) return cuda_fail(e, "position kernel (forward only)");
+  return PTYCHO_OK;
 }
 
 int ptycho_object_constraints(const ptycho_geometry* g, void* object, const uint8_t* mask,

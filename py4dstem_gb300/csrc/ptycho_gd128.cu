@@ -442,7 +442,8 @@ int set_schedule(int roi, int schedule) {
 
 bool position_v2_eligible(const BatchArgs& a) {
   if (g_schedule_128 != 2) return false;
-  return a.Sx == S && a.Sy == S && a.T == 1 && a.M == 1 && !a.projection && !a.mixed_formula;
+  return a.Sx == S && a.Sy == S && a.T == 1 && a.M == 1 && !a.projection && !a.mixed_formula &&
+         !a.forward_only && !a.keep_farfield;
 }
 
 cudaError_t launch_position_v2(const BatchArgs& a, cudaStream_t s) {

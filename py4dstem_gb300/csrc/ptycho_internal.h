@@ -23,6 +23,8 @@ struct BatchArgs {
   int fix_probe;
   int ew_valid;
   int staging_t;           // staged per-position terms are y-major (e' = y * Sx + x)
+  int forward_only;        // forward model and per-position error only, no adjoint
+  int keep_farfield;       // single slice: keep FFT2(psi_m) of each position in scratch_f
 
   void* object;                 // (T,Px,Py) float2 or float
   float2* probe;                // (M,N)
@@ -35,6 +37,14 @@ struct BatchArgs {
   float2* exit_waves;           // (J,M,N) or null
   float* error_accum;           // scalar
 
+  // position correction (after the batch update; positions_rw is the positions
+  // array above, updated in place)
+  float* positions_rw;             // (J,2)
+  const float* positions_initial;  // (J,2)
+  float pc_step;                   // positions_step_size
+  double pc_max_update;            // pixels; < 0: no limit
+  double pc_max_total;             // pixels; < 0: no limit
+
   // workspace
   float2* probe_spec;   // (M,N)
   float2* tw;           // (Sx + Sy) twiddle tables exp(-2 pi i m / S), x then y
@@ -42,7 +52,7 @@ struct BatchArgs {
   float* st_nobj;       // (T,B,N)
   float2* st_probe;     // (B,M,N)
   float* st_nprobe;     // (B,N)
-  float2* scratch_f;    // (B,M,N) when M > 1
+  float2* scratch_f;    // (B,M,N) far fields FFT2(psi_m): single slice, or kept for A16
   int2* pos_round;      // (B)
   float* err;           // (B)
   float2* obj_grad;     // (T,P)
@@ -63,7 +73,8 @@ struct Workspace {
       probe_nrm, com, red, total;
 };
 
-Workspace workspace_layout(int Sx, int Sy, int Px, int Py, int T, int M, int B);
+Workspace workspace_layout(int Sx, int Sy, int Px, int Py, int T, int M, int B,
+                           bool keep_farfield);
 void bind_workspace(BatchArgs& a, void* base, const Workspace& w);
 
 bool roi_supported(int Sx, int Sy);
@@ -75,6 +86,7 @@ void timing_after(cudaStream_t s);
 // Launchers (return cudaError_t of the last launch).
 cudaError_t launch_probe_spectrum(const BatchArgs& a, cudaStream_t s);
 cudaError_t launch_position_kernel(const BatchArgs& a, cudaStream_t s);
+cudaError_t launch_position_correction(const BatchArgs& a, cudaStream_t s);
 // Register-resident 128 x 128 single-slice GD kernel (ptycho_gd128.cu).
 // set_schedule stores the preferred schedule for a ROI edge (0 default,
 // 1 shared-memory passes, 2 register-resident) and returns the previous one.

@@ -130,6 +130,7 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
   const int y0 = (int)ry;
   const float invN = 1.0f / (float)N;
   const bool ps = a.projection != 0;
+  const bool fwd = a.forward_only != 0;  // per-position error only (block-uniform)
   const float* amp = a.amplitudes + (size_t)arow * N;
 
   for (int i = tid; i < SX; i += NT) twx[i] = a.tw[i];  // tables from the spectrum kernel
@@ -246,6 +247,7 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
         const int e = tid + (c0 + i) * NT;
         const int idx = (e / SY) * LD + e % SY;
         float2 f = buf[idx];
+        if (a.keep_farfield) a.scratch_f[(size_t)b * N + e] = f;  // unmasked, for A16
         const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
         if (a.det_mask) f = c_scale(f, mk);
         const float af = hypotf(f.x, f.y);
@@ -262,8 +264,10 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
         buf[idx] = r;
       }
       }
-      __syncthreads();
-      fft2d<SX, SY, NT, +1>(buf, twx, twy);
+      if (!fwd) {
+        __syncthreads();
+        fft2d<SX, SY, NT, +1>(buf, twx, twy);
+      }
     } else {
       // mixed state: shared ratio A / sqrt(sum_m |F_m|^2), 0 where the model is 0
       for (int e = tid; e < N; e += NT) {
@@ -279,7 +283,7 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
     }
 
     // adjoint terms, mode by mode
-    for (int m = 0; m < M; ++m) {
+    for (int m = 0; m < (fwd ? 0 : M); ++m) {
       if (mixed) {
         const float2* f = a.scratch_f + ((size_t)b * M + m) * N;
         for (int e = tid; e < N; e += NT) {
@@ -377,6 +381,7 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
     for (int e = tid; e < N; e += NT) {
       const int idx = (e / SY) * LD + e % SY;
       float2 f = buf[idx];
+      if (a.keep_farfield) a.scratch_f[(size_t)b * N + e] = f;  // unmasked, for A16
       const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
       if (a.det_mask) f = c_scale(f, mk);
       const float af = hypotf(f.x, f.y);
@@ -392,6 +397,7 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
       }
       buf[idx] = r;
     }
+    if (fwd) goto done;
     __syncthreads();
     fft2d<SX, SY, NT, +1>(buf, twx, twy);
     if (ps) {
@@ -443,8 +449,228 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
     }
   }
 
+done:
   const float tot = block_sum<NT>(err, red);
   if (tid == 0) a.err[b] = tot;
+}
+
+// Position correction of one batch (ptychographic_methods.py:2071-2225), run
+// after the batch's object update. One block per position:
+//   F0_m = FFT2(P_m O_old)        kept by the forward pass in scratch_f
+//   Fx_m = FFT2(P_m O_new[x+1,y]),  Fy_m = FFT2(P_m O_new[x,y+1])
+//   gx = sum_m 2 Re((F0_m - Fx_m) conj(F0_m)),  gy likewise
+//   d  = A^2 - |F0|^2             (|F0|^2 = sum_m |F0_m|^2 for mixed state)
+//   (ux, uy) = step * inv([gx gy]^T [gx gy]) [gx gy]^T d
+// then the per-update and total-distance limits, and positions -= u.
+// P_m is recomputed from the batch's probe spectrum exactly as the forward pass
+// formed it. gx and gy go to the |P|^2 / |O|^2 staging rows, which the batch's
+// reductions have consumed by now. The 2x2 normal equations are summed in
+// double (per-thread float partials, then a fixed-order block sum).
+template <int NT>
+__device__ __forceinline__ void block_sum5(double (&v)[5], double (*red)[NT / 32]) {
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    double x = v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      double t = 0.0;
+      for (int w = 0; w < NT / 32; ++w) t += red[k][w];
+      v[k] = t;
+    }
+  }
+}
+
+template <int SX, int SY, int NT>
+__global__ void __launch_bounds__(NT, 1) position_correction_kernel(BatchArgs a) {
+  using L = Layout<SX, SY>;
+  constexpr int N = L::N;
+  constexpr int LD = L::LD;
+  extern __shared__ float4 smem4[];
+  float2* buf = reinterpret_cast<float2*>(smem4);
+  float2* twx = buf + SX * LD;
+  float2* twy = twx + SX;
+  float2* rpx = twy + SY;
+  float2* rpy = rpx + SX;
+  __shared__ double red[5][NT / 32];
+
+  const int b = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int M = a.M;
+  const int prow = a.pos_rows ? a.pos_rows[b] : b;
+  const int arow = a.amp_rows ? a.amp_rows[b] : b;
+  const float posx = a.positions_rw[2 * prow];
+  const float posy = a.positions_rw[2 * prow + 1];
+  const float rx = rintf(posx);
+  const float ry = rintf(posy);
+  const float dx = posx - rx;
+  const float dy = posy - ry;
+  const int x0 = (int)rx;
+  const int y0 = (int)ry;
+  const float invN = 1.0f / (float)N;
+
+  for (int i = tid; i < SX; i += NT) twx[i] = a.tw[i];
+  for (int i = tid; i < SY; i += NT) twy[i] = a.tw[SX + i];
+  for (int i = tid; i < SX; i += NT) {
+    const float k = (float)fint(i, SX) / (float)SX;
+    rpx[i] = cis_rounded(__fmul_rn(__fmul_rn(-6.2831855f, k), dx));
+  }
+  for (int i = tid; i < SY; i += NT) {
+    const float k = (float)fint(i, SY) / (float)SY;
+    rpy[i] = cis_rounded(__fmul_rn(__fmul_rn(-6.2831855f, k), dy));
+  }
+  __syncthreads();
+
+  const int bx = pmod(x0 - SX / 2, a.Px);
+  const int by = pmod(y0 - SY / 2, a.Py);
+  auto obj_x = [&](int x) {
+    const int t = bx + (x + SX / 2) % SX;
+    return t >= a.Px ? t - a.Px : t;
+  };
+  auto obj_y = [&](int y) {
+    const int t = by + (y + SY / 2) % SY;
+    return t >= a.Py ? t - a.Py : t;
+  };
+
+  float* gx = a.st_nobj + (size_t)b * N;
+  float* gy = a.st_nprobe + (size_t)b * N;
+  const float2* f0 = a.scratch_f + (size_t)b * M * N;
+  const int T = a.T;
+  // object pixel of ROI sample (x, y) with the patch moved one pixel along dir
+  auto moved = [&](int dir, int x, int y, int& ox, int& oy) {
+    ox = obj_x(x);
+    oy = obj_y(y);
+    if (dir == 0) ox = ox + 1 == a.Px ? 0 : ox + 1;
+    else oy = oy + 1 == a.Py ? 0 : oy + 1;
+  };
+  for (int m = 0; m < M; ++m) {
+    const float2* __restrict__ spec = a.probe_spec + (size_t)m * N;
+    for (int dir = 0; dir < 2; ++dir) {
+      if (T == 1) {
+        // P_m shifted as in the forward pass, times the moved object patch
+        for (int e = tid; e < N; e += NT) {
+          const int x = e / SY, y = e % SY;
+          buf[x * LD + y] = c_mul(spec[e], c_mul(rpx[x], rpy[y]));
+        }
+        __syncthreads();
+        fft2d<SX, SY, NT, +1>(buf, twx, twy);
+        for (int e = tid; e < N; e += NT) {
+          const int x = e / SY, y = e % SY;
+          int ox, oy;
+          moved(dir, x, y, ox, oy);
+          const float2 p = c_scale(buf[x * LD + y], invN);
+          buf[x * LD + y] = c_mul(p, load_object(a, 0, ox, oy));
+        }
+        __syncthreads();
+      } else {
+        // multislice: the updated, unshifted probe through all moved slices
+        for (int s = 0; s < T; ++s) {
+          for (int e = tid; e < N; e += NT) {
+            const int x = e / SY, y = e % SY;
+            int ox, oy;
+            moved(dir, x, y, ox, oy);
+            const float2 p = s == 0 ? a.probe[e] : c_scale(buf[x * LD + y], invN);
+            buf[x * LD + y] = c_mul(load_object(a, s, ox, oy), p);
+          }
+          __syncthreads();
+          if (s + 1 < T) {
+            fft2d<SX, SY, NT, -1>(buf, twx, twy);
+            const float2* h = a.props + (size_t)s * N;
+            for (int e = tid; e < N; e += NT) {
+              const int idx = (e / SY) * LD + e % SY;
+              buf[idx] = c_mul(buf[idx], h[e]);
+            }
+            __syncthreads();
+            fft2d<SX, SY, NT, +1>(buf, twx, twy);
+          }
+        }
+      }
+      fft2d<SX, SY, NT, -1>(buf, twx, twy);
+      float* g = dir == 0 ? gx : gy;
+      for (int e = tid; e < N; e += NT) {
+        const float2 f = buf[(e / SY) * LD + e % SY];
+        const float2 r = f0[(size_t)m * N + e];
+        const float2 d = c_sub(r, f);
+        const float v = 2.0f * __fadd_rn(__fmul_rn(d.x, r.x), __fmul_rn(d.y, r.y));
+        g[e] = m == 0 ? v : g[e] + v;
+      }
+      __syncthreads();  // buf is rewritten by the next pass
+    }
+  }
+
+  const float* amp = a.amplitudes + (size_t)arow * N;
+  const bool mixed = M > 1 || a.mixed_formula;
+  float sxx = 0.f, sxy = 0.f, syy = 0.f, sxd = 0.f, syd = 0.f;
+  for (int e = tid; e < N; e += NT) {
+    float est;
+    if (mixed) {
+      float t = 0.0f;
+      for (int m = 0; m < M; ++m) {
+        const float2 r = f0[(size_t)m * N + e];
+        const float av = hypotf(r.x, r.y);
+        t += av * av;
+      }
+      const float amp_tot = sqrtf(t);
+      est = amp_tot * amp_tot;
+    } else {
+      const float2 r = f0[e];
+      const float af = hypotf(r.x, r.y);
+      est = af * af;
+    }
+    const float A = amp[e];
+    const float d = __fsub_rn(__fmul_rn(A, A), est);
+    const float px = gx[e], py = gy[e];
+    sxx = fmaf(px, px, sxx);
+    sxy = fmaf(px, py, sxy);
+    syy = fmaf(py, py, syy);
+    sxd = fmaf(px, d, sxd);
+    syd = fmaf(py, d, syd);
+  }
+  double s5[5] = {sxx, sxy, syy, sxd, syd};
+  block_sum5<NT>(s5, red);
+  if (tid == 0) {
+    const double det = s5[0] * s5[2] - s5[1] * s5[1];
+    float ux = 0.0f, uy = 0.0f;
+    if (det != 0.0 && isfinite(det)) {  // the reference's inverse fails on a singular system
+      ux = __fmul_rn((float)((s5[2] * s5[3] - s5[1] * s5[4]) / det), a.pc_step);
+      uy = __fmul_rn((float)((s5[0] * s5[4] - s5[1] * s5[3]) / det), a.pc_step);
+    }
+    if (a.pc_max_update >= 0.0) {
+      const float n = sqrtf(__fadd_rn(__fmul_rn(ux, ux), __fmul_rn(uy, uy)));
+      if ((double)n > a.pc_max_update) {
+        const double r = (double)n / a.pc_max_update;
+        ux = (float)((double)ux / r);
+        uy = (float)((double)uy / r);
+      }
+    }
+    if (a.pc_max_total >= 0.0) {
+      const float ddx = __fsub_rn(__fsub_rn(posx, a.positions_initial[2 * prow]), ux);
+      const float ddy = __fsub_rn(__fsub_rn(posy, a.positions_initial[2 * prow + 1]), uy);
+      const float dist = sqrtf(__fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(ddy, ddy)));
+      if ((double)dist > a.pc_max_total) ux = uy = 0.0f;
+    }
+    a.positions_rw[2 * prow] = __fsub_rn(posx, ux);
+    a.positions_rw[2 * prow + 1] = __fsub_rn(posy, uy);
+  }
+}
+
+template <int SX, int SY, int NT>
+cudaError_t launch_correction_t(const BatchArgs& a, cudaStream_t s) {
+  const size_t smem = Layout<SX, SY>::smem_bytes(false);
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(position_correction_kernel<SX, SY, NT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  position_correction_kernel<SX, SY, NT><<<a.B, NT, smem, s>>>(a);
+  return cudaGetLastError();
 }
 
 template <int SX, int SY, int NT>
@@ -513,6 +739,10 @@ cudaError_t launch_probe_spectrum(const BatchArgs& a, cudaStream_t s) {
 
 cudaError_t launch_position_kernel(const BatchArgs& a, cudaStream_t s) {
   PTY_DISPATCH(launch_position_t, a, s)
+}
+
+cudaError_t launch_position_correction(const BatchArgs& a, cudaStream_t s) {
+  PTY_DISPATCH(launch_correction_t, a, s)
 }
 
 }  // namespace pty

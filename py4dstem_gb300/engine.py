@@ -66,6 +66,7 @@ class DeviceState:
     gram: object = None
     probe_tmp: object = None
     coeffs: object = None
+    positions_initial: object = None  # device (J,2) f32 when positions are corrected
     launches: int = 0
     extra: dict = field(default_factory=dict)
 
@@ -85,12 +86,14 @@ def make_geometry(roi_shape, object_shape, num_slices, num_probes, potential,
 def create_state(*, roi_shape, object_array, probe_array, amplitudes, positions_px,
                  num_slices, num_probes, potential, max_batch, storage="gpu",
                  propagators=None, detector_mask=None, fov_mask_inverse=None,
-                 projection=False, mixed_state=False) -> DeviceState:
+                 projection=False, mixed_state=False, positions_initial=None) -> DeviceState:
     torch = _torch()
     lib = _native.lib()
     dev = torch.device("cuda", torch.cuda.current_device())
     geom = make_geometry(roi_shape, object_array.shape, num_slices, num_probes, potential,
                          mixed_state or num_probes > 1)
+    if positions_initial is not None:
+        geom.flags |= _native.FLAG_KEEP_FARFIELD
     if not lib.ptycho_roi_supported(geom.roi_x, geom.roi_y):
         raise NotImplementedError(
             f"no fused GPU kernel for a {geom.roi_x}x{geom.roi_y} region of interest "
@@ -134,6 +137,9 @@ def create_state(*, roi_shape, object_array, probe_array, amplitudes, positions_
         J = pos.shape[0]
         st.exit_waves = torch.empty((J, num_probes) + tuple(roi_shape), dtype=torch.complex64,
                                     device=dev)
+    if positions_initial is not None:
+        st.positions_initial = torch.from_numpy(
+            np.ascontiguousarray(positions_initial, dtype=np.float32)).to(dev)
     if num_probes > 1:
         st.gram = torch.empty((num_probes, num_probes), dtype=torch.complex64, device=dev)
         st.probe_tmp = torch.empty_like(probe)
@@ -152,14 +158,13 @@ def _stream():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
-def run_batch(st: DeviceState, start: int, end: int, host_order: np.ndarray, *,
-              projection=False, step_size=0.5, normalization_min=1.0, fix_probe=False,
-              projection_abc=(0.0, 0.0, 0.0)):
-    lib = _native.lib()
+def _batch_amplitudes(st: DeviceState, start: int, end: int, host_order: np.ndarray):
+    """(amplitudes pointer, amplitude rows pointer) of one batch: the resident
+    array indexed by the order rows, or this batch's patterns copied from the host."""
     n = end - start
     rows_ptr = ctypes.c_void_p(st.order.data_ptr() + 4 * start)
     if st.amplitudes is not None:
-        amps_ptr, amp_rows = _ptr(st.amplitudes), rows_ptr
+        return _ptr(st.amplitudes), rows_ptr
     else:
         # storage on the host: gather this batch's patterns and copy them over,
         # like the reference's per-batch copy_to_device
@@ -174,7 +179,16 @@ def run_batch(st: DeviceState, start: int, end: int, host_order: np.ndarray, *,
         np.take(st.amplitudes_host, idx, axis=0, out=pinned.numpy()[:n])
         st.amp_stage[:n].copy_(pinned[:n], non_blocking=True)
         st.amp_events[k].record()
-        amps_ptr, amp_rows = _ptr(st.amp_stage), None
+        return _ptr(st.amp_stage), None
+
+
+def run_batch(st: DeviceState, start: int, end: int, host_order: np.ndarray, *,
+              projection=False, step_size=0.5, normalization_min=1.0, fix_probe=False,
+              projection_abc=(0.0, 0.0, 0.0), position_correction=None):
+    lib = _native.lib()
+    n = end - start
+    rows_ptr = ctypes.c_void_p(st.order.data_ptr() + 4 * start)
+    amps_ptr, amp_rows = _batch_amplitudes(st, start, end, host_order)
     g = ctypes.byref(st.geometry)
     props = _ptr(st.propagators)
     if projection:
@@ -192,6 +206,45 @@ def run_batch(st: DeviceState, start: int, end: int, host_order: np.ndarray, *,
             _stream())
     _native.check(status)
     st.launches += 4 if fix_probe else 7
+    if position_correction is not None:
+        pc = position_correction
+        none = -1.0
+        status = lib.ptycho_position_correction(
+            g, _ptr(st.object), _ptr(st.probe), props, amps_ptr, amp_rows, _ptr(st.positions),
+            _ptr(st.positions_initial), rows_ptr, n, float(pc["step_size"]),
+            none if pc["max_update_px"] is None else float(pc["max_update_px"]),
+            none if pc["max_total_px"] is None else float(pc["max_total_px"]),
+            _ws_ptr(st), st.workspace_bytes, _stream())
+        _native.check(status)
+        st.launches += 1
+
+
+def positions_com_constraint(st: DeviceState) -> None:
+    """positions -= mean(positions) - mean(initial positions)
+    (ptychographic_constraints.py:1292-1311)."""
+    st.positions -= st.positions.mean(0) - st.positions_initial.mean(0)
+
+
+def self_consistency_errors(st: DeviceState, max_batch: int) -> np.ndarray:
+    """Per-position sum (A - |F|)^2 of a forward-only pass over the positions in
+    natural order, batch by batch (ptychographic_methods.py:2227-2291); float32."""
+    torch = _torch()
+    lib = _native.lib()
+    J = int(st.positions.shape[0])
+    natural = np.arange(J)
+    st.order.copy_(torch.arange(J, dtype=torch.int32, device=st.order.device))
+    out = torch.empty(J, dtype=torch.float32, device=st.order.device)
+    g = ctypes.byref(st.geometry)
+    for start, end in generate_batches(J, max_batch):
+        amps_ptr, amp_rows = _batch_amplitudes(st, start, end, natural)
+        rows_ptr = ctypes.c_void_p(st.order.data_ptr() + 4 * start)
+        _native.check(lib.ptycho_self_consistency_errors(
+            g, _ptr(st.object), _ptr(st.probe), amps_ptr, amp_rows, _ptr(st.positions),
+            rows_ptr, end - start, _ptr(st.propagators),
+            ctypes.c_void_p(out.data_ptr() + 4 * start), _ws_ptr(st), st.workspace_bytes,
+            _stream()))
+        st.launches += 2
+    return out.cpu().numpy()
 
 
 def run_iteration(st: DeviceState, host_order: np.ndarray, max_batch: int, **kw) -> None:
@@ -260,12 +313,17 @@ class IterationDriver:
     def __init__(self, st: DeviceState, *, max_batch, projection=False, step_size=0.5,
                  normalization_min=1.0, fix_probe=False, projection_abc=(0.0, 0.0, 0.0),
                  shrinkage_rad=0.0, use_mask=False, pure_phase=False, positivity=True,
-                 fix_probe_com=True, orthogonalize_probe=False, mean_intensity=1.0):
+                 fix_probe_com=True, orthogonalize_probe=False, mean_intensity=1.0,
+                 position_correction=None):
         self.st = st
         self.max_batch = int(max_batch)
+        if position_correction is not None and st.positions_initial is None:
+            raise ValueError("position correction needs a state created with positions_initial")
         self.batch_kw = dict(projection=projection, step_size=step_size,
                              normalization_min=normalization_min, fix_probe=fix_probe,
-                             projection_abc=projection_abc)
+                             projection_abc=projection_abc,
+                             position_correction=position_correction)
+        self.positions_com = bool(position_correction and position_correction["center_of_mass"])
         self.shrinkage_rad = shrinkage_rad
         self.use_mask = use_mask
         self.pure_phase = pure_phase
@@ -285,6 +343,8 @@ class IterationDriver:
             probe_com_constraint(st)
         if self.orthogonalize:
             probe_orthogonalization(st)
+        if self.positions_com:
+            positions_com_constraint(st)
 
     def error(self) -> np.float32:
         """Normalised error of the last iteration: float32 sum over batches divided

@@ -373,7 +373,8 @@ class _PtychographyBase(PreprocessMixin):
                           reconstruction_parameter_a, reconstruction_parameter_b,
                           reconstruction_parameter_c, max_batch_size, seed_random, step_size,
                           normalization_min, fix_probe_com, fix_probe, fix_positions,
-                          pure_phase_object, object_positivity, shrinkage_rad,
+                          fix_positions_com, positions_step_size, max_position_update_distance,
+                          max_position_total_distance, pure_phase_object, object_positivity, shrinkage_rad,
                           fix_potential_baseline, detector_fourier_mask, store_iterations,
                           reset, device, clear_fft_cache, object_type,
                           orthogonalize_probe=False, unsupported=None):
@@ -386,9 +387,13 @@ class _PtychographyBase(PreprocessMixin):
             reconstruction_parameter_b, reconstruction_parameter_c, step_size)
         self._report(num_iter, use_projection, reconstruction_method, parameter, pa, pb, pc,
                      normalization_min, max_batch_size, step_size)
-        self._unsupported(fix_positions=not fix_positions, **(unsupported or {}))
+        self._unsupported(**(unsupported or {}))
         if use_projection and detector_fourier_mask is not None:
             raise NotImplementedError()
+        correct_positions = not fix_positions
+        if correct_positions and use_projection:
+            raise NotImplementedError(
+                "position correction (fix_positions=False) runs with gradient descent only")
 
         J = self._num_diffraction_patterns
         shuffled = np.arange(J)
@@ -409,7 +414,8 @@ class _PtychographyBase(PreprocessMixin):
             propagators=getattr(self, "_propagator_arrays", None) if self._multislice else None,
             detector_mask=detector_fourier_mask,
             fov_mask_inverse=self._object_fov_mask_inverse if use_mask else None,
-            projection=use_projection, mixed_state=self._mixed)
+            projection=use_projection, mixed_state=self._mixed,
+            positions_initial=self._positions_px_initial if correct_positions else None)
         if use_projection and self._exit_waves is not None:
             import torch
 
@@ -425,7 +431,14 @@ class _PtychographyBase(PreprocessMixin):
             pure_phase=pure_phase_object and self._object_type == "complex",
             positivity=object_positivity, fix_probe_com=fix_probe_com,
             orthogonalize_probe=orthogonalize_probe,
-            mean_intensity=self._mean_diffraction_intensity)
+            mean_intensity=self._mean_diffraction_intensity,
+            position_correction=(dict(
+                step_size=positions_step_size,
+                max_update_px=self._distance_px(max_position_update_distance),
+                max_total_px=self._distance_px(max_position_total_distance),
+                # the reference passes fix_positions_com and not fix_positions on
+                # (singleslice_ptychography.py:956, ptychographic_constraints.py:1355-1377)
+                center_of_mass=not fix_positions_com) if correct_positions else None))
         error = np.float32(0.0)
         for _ in range(num_iter):
             if not use_projection:
@@ -441,6 +454,8 @@ class _PtychographyBase(PreprocessMixin):
 
         self._object = st.object.cpu().numpy()
         self._probe = st.probe.cpu().numpy().reshape(np.shape(self._probe))
+        if correct_positions:
+            self._positions_px = st.positions.cpu().numpy()
         self.object = self._object.copy()
         self.probe = self.probe_centered
         self.error = error.item()
@@ -449,6 +464,32 @@ class _PtychographyBase(PreprocessMixin):
         else:
             self._exit_waves = None
         return self
+
+    def _distance_px(self, distance_ang):
+        """A distance limit in A as pixels, like the reference's
+        distance / sqrt(sx^2 + sy^2) (ptychographic_methods.py:2191-2213); None stays None."""
+        if distance_ang is None:
+            return None
+        return float(distance_ang / np.sqrt(self.sampling[0] ** 2 + self.sampling[1] ** 2))
+
+    def _return_self_consistency_errors(self, max_batch_size=None):
+        """Per-position self-consistency errors of the current object and probe
+        (ptychographic_methods.py:2227-2291): sum (A - |F|)^2 of a forward-only GPU
+        pass in natural position order, divided by the mean intensity (float64)."""
+        potential = self._object_type == "potential"
+        J = self._num_diffraction_patterns
+        max_batch_size = J if max_batch_size is None else int(max_batch_size)
+        st = engine.create_state(
+            roi_shape=tuple(self._region_of_interest_shape),
+            object_array=np.asarray(self._object, dtype=np.float32 if potential else np.complex64),
+            probe_array=self._probe, amplitudes=self._amplitudes,
+            positions_px=self._positions_px, num_slices=self._num_slices,
+            num_probes=self._num_probes, potential=potential, max_batch=max_batch_size,
+            storage=self._storage,
+            propagators=getattr(self, "_propagator_arrays", None) if self._multislice else None,
+            mixed_state=self._mixed)
+        errors = engine.self_consistency_errors(st, max_batch_size)
+        return errors.astype(np.float64) / self._mean_diffraction_intensity
 
     def _fresnel_propagators(self):
         """(T-1, Sx, Sy) complex64 Fresnel propagators with optional tilt
@@ -611,12 +652,16 @@ class SingleslicePtychography(_PtychographyBase):
             max_batch_size=max_batch_size, seed_random=seed_random, step_size=step_size,
             normalization_min=normalization_min, fix_probe_com=fix_probe_com,
             fix_probe=fix_probe, fix_positions=fix_positions,
+            fix_positions_com=fix_positions_com, positions_step_size=positions_step_size,
+            max_position_update_distance=max_position_update_distance,
+            max_position_total_distance=max_position_total_distance,
             pure_phase_object=pure_phase_object, object_positivity=object_positivity,
             shrinkage_rad=shrinkage_rad, fix_potential_baseline=fix_potential_baseline,
             detector_fourier_mask=detector_fourier_mask, store_iterations=store_iterations,
             reset=reset, device=device, clear_fft_cache=clear_fft_cache,
             object_type=object_type,
             unsupported=dict(
+                global_affine_transformation=global_affine_transformation and not fix_positions,
                 fix_probe_aperture=fix_probe_aperture and not fix_probe,
                 constrain_probe_amplitude=constrain_probe_amplitude and not fix_probe,
                 constrain_probe_fourier_amplitude=constrain_probe_fourier_amplitude
@@ -742,12 +787,16 @@ class MixedstatePtychography(_PtychographyBase):
             max_batch_size=max_batch_size, seed_random=seed_random, step_size=step_size,
             normalization_min=normalization_min, fix_probe_com=fix_probe_com,
             fix_probe=fix_probe, fix_positions=fix_positions,
+            fix_positions_com=fix_positions_com, positions_step_size=positions_step_size,
+            max_position_update_distance=max_position_update_distance,
+            max_position_total_distance=max_position_total_distance,
             pure_phase_object=pure_phase_object, object_positivity=object_positivity,
             shrinkage_rad=shrinkage_rad, fix_potential_baseline=fix_potential_baseline,
             detector_fourier_mask=detector_fourier_mask, store_iterations=store_iterations,
             reset=reset, device=device, clear_fft_cache=clear_fft_cache,
             object_type=object_type, orthogonalize_probe=orthogonalize_probe,
             unsupported=dict(
+                global_affine_transformation=global_affine_transformation and not fix_positions,
                 fix_probe_aperture=fix_probe_aperture and not fix_probe,
                 constrain_probe_amplitude=constrain_probe_amplitude and not fix_probe,
                 constrain_probe_fourier_amplitude=constrain_probe_fourier_amplitude
@@ -885,12 +934,16 @@ class MultislicePtychography(_PtychographyBase):
             max_batch_size=max_batch_size, seed_random=seed_random, step_size=step_size,
             normalization_min=normalization_min, fix_probe_com=fix_probe_com,
             fix_probe=fix_probe, fix_positions=fix_positions,
+            fix_positions_com=fix_positions_com, positions_step_size=positions_step_size,
+            max_position_update_distance=max_position_update_distance,
+            max_position_total_distance=max_position_total_distance,
             pure_phase_object=pure_phase_object, object_positivity=object_positivity,
             shrinkage_rad=shrinkage_rad, fix_potential_baseline=fix_potential_baseline,
             detector_fourier_mask=detector_fourier_mask, store_iterations=store_iterations,
             reset=reset, device=device, clear_fft_cache=clear_fft_cache,
             object_type=object_type,
             unsupported=dict(
+                global_affine_transformation=global_affine_transformation and not fix_positions,
                 fix_probe_aperture=fix_probe_aperture and not fix_probe,
                 constrain_probe_amplitude=constrain_probe_amplitude and not fix_probe,
                 constrain_probe_fourier_amplitude=constrain_probe_fourier_amplitude

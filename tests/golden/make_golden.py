@@ -5,7 +5,8 @@ arguments of the constructor / preprocess() / reconstruct() calls, and what the
 reference py4DSTEM 0.14.18 CPU path (loaded by oracle/refloader.py) returned:
 preprocessed state (mean intensity, positions, initial probe and object, FOV
 mask, per-pattern amplitude sums) and the reconstruction result (error per
-iteration, object, corner-centred probe).
+iteration, object, corner-centred probe, final positions, and the per-position
+self-consistency errors of the final state).
 
 Run from the repository root in a container that has the reference checkout:
 
@@ -56,6 +57,31 @@ CASES = {
         cls="multi", ctor=dict(object_fov_ang=(24.0, 24.0), num_slices=3, slice_thicknesses=20.0),
         guess=(3, 96, 96),
         rec=dict(num_iter=6, max_batch_size=25, step_size=0.5, seed_random=2)),
+    # position correction (fix_positions=False) from perturbed scan positions,
+    # with both distance limits and the positions centre-of-mass constraint
+    "ss_gd_poscorr": dict(
+        gen=dict(name="ssc", seed=15, scan_shape=(12, 12), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=96),
+        cls="single", ctor=dict(object_fov_ang=(24.0, 24.0)), guess=(96, 96),
+        perturb_ang=0.15,
+        rec=dict(num_iter=6, max_batch_size=36, step_size=0.5, seed_random=4,
+                 fix_positions=False, fix_positions_com=False, positions_step_size=0.5,
+                 max_position_update_distance=0.1, max_position_total_distance=0.3)),
+    "ms_gd_poscorr": dict(
+        gen=dict(name="msc", seed=17, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=96, num_slices=2, slice_thickness=20.0),
+        cls="multi", ctor=dict(object_fov_ang=(24.0, 24.0), num_slices=2, slice_thicknesses=20.0),
+        guess=(2, 96, 96), perturb_ang=0.15,
+        rec=dict(num_iter=5, max_batch_size=25, step_size=0.5, seed_random=6,
+                 fix_positions=False, positions_step_size=0.5,
+                 max_position_total_distance=0.5)),
+    "mixed_gd_poscorr": dict(
+        gen=dict(name="mxc", seed=16, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=96, num_modes=2, mode_weights=(0.8, 0.2)),
+        cls="mixed", ctor=dict(object_fov_ang=(24.0, 24.0), num_probes=2), global_seed=8,
+        guess=(96, 96), perturb_ang=0.15,
+        rec=dict(num_iter=5, max_batch_size=25, step_size=0.5, seed_random=5,
+                 fix_positions=False, positions_step_size=0.25)),
     "mixed_gd_M3": dict(
         gen=dict(name="mx", seed=14, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
                  detector=64, object_px=96, num_modes=3, mode_weights=(0.7, 0.2, 0.1)),
@@ -96,9 +122,14 @@ def make_case(ref, name, spec):
         # the reference aliases the caller's array as its object and updates it
         # in place, so it gets a copy and the fixture keeps the original
         extra["initial_object_guess"] = guess.copy()
+    positions = case.scan_positions_ang
+    if "perturb_ang" in spec:
+        rng = np.random.default_rng(spec["gen"]["seed"] + 200)
+        positions = positions + rng.uniform(-spec["perturb_ang"], spec["perturb_ang"],
+                                            positions.shape)
     if "global_seed" in spec:
         np.random.seed(spec["global_seed"])
-    p = cls(datacube=dc, initial_scan_positions=case.scan_positions_ang, verbose=False,
+    p = cls(datacube=dc, initial_scan_positions=positions, verbose=False,
             device="cpu", **ctor, **extra)
     p.preprocess(**PRE)
     pre = dict(
@@ -116,6 +147,9 @@ def make_case(ref, name, spec):
         error_iterations=np.asarray(p.error_iterations, dtype=np.float64),
         object=p.object,
         probe_corner=np.asarray(p._probe),
+        positions_px=np.asarray(p._positions_px).copy(),
+        self_consistency_errors=p._return_self_consistency_errors(
+            max_batch_size=spec["rec"].get("max_batch_size")),
     )
     meta = dict(cls=spec["cls"], ctor=ctor, preprocess=PRE, reconstruct=spec["rec"],
                 global_seed=spec.get("global_seed"), r_pixel_size=r, q_pixel_size=q,
@@ -126,7 +160,7 @@ def make_case(ref, name, spec):
     else:
         extra_arrays = {}
     np.savez_compressed(
-        path, datacube=data.astype(np.uint16), scan_positions_ang=case.scan_positions_ang,
+        path, datacube=data.astype(np.uint16), scan_positions_ang=positions,
         meta=json.dumps(meta), **extra_arrays, **{f"pre_{k}": v for k, v in pre.items()},
         **{f"out_{k}": v for k, v in out.items()})
     print(f"{name}: {os.path.getsize(path) / 1e6:.2f} MB, errors {out['error_iterations'][-3:]}")

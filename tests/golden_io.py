@@ -66,7 +66,8 @@ class Golden:
             fov_mask_inverse=p._object_fov_mask_inverse, object_type=p._object_type,
             num_slices=m["ctor"].get("num_slices", 1), num_probes=m["ctor"].get("num_probes", 1),
             mixed=m["cls"] == "mixed",
-            propagators=getattr(p, "_propagator_arrays", None) if m["cls"] == "multi" else None)
+            propagators=getattr(p, "_propagator_arrays", None) if m["cls"] == "multi" else None,
+            sampling=tuple(p.sampling))
 
     def oracle_kwargs(self):
         from oracle.ptycho_np import method_abc

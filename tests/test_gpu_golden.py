@@ -60,6 +60,29 @@ def test_reconstruction_matches_reference(cuda, name):
     assert d_err <= tol_err
     assert d_obj <= tol_obj
     assert d_probe <= tol_probe
+    # position correction fixtures move the positions; the others leave them alone
+    d_pos = float(np.max(np.abs(p._positions_px - g.out["positions_px"])))
+    f_pos = float(np.max(np.abs(floor.positions_px - g.out["positions_px"])))
+    print(f"{name}: positions gpu-vs-ref {d_pos:.2e} px, floor {f_pos:.2e} px")
+    assert d_pos <= max(1e-4, k * f_pos)
+
+
+@pytest.mark.parametrize("name", names())
+def test_self_consistency_errors_match_reference(cuda, name):
+    """Per-position errors of the reference's final state (A19): float64 values
+    within 1e-5 relative of the reference (its own rounding floor is ~4e-7)."""
+    g = Golden(name)
+    p = g.build(device="gpu")
+    p._object = np.array(g.out["object"], copy=True)
+    p._probe = np.array(g.out["probe_corner"], copy=True)
+    p._positions_px = np.array(g.out["positions_px"], copy=True)
+    e = p._return_self_consistency_errors(
+        max_batch_size=g.meta["reconstruct"].get("max_batch_size"))
+    ref = g.out["self_consistency_errors"]
+    assert e.dtype == np.float64 and e.shape == ref.shape
+    rel = np.abs(e - ref) / ref
+    print(f"\n{name}: self-consistency max rel {rel.max():.2e} mean {rel.mean():.2e}")
+    assert rel.max() <= 1e-5
 
 
 def test_storage_cpu_matches_gpu(cuda):

@@ -72,8 +72,11 @@ def test_unsupported_options_raise_before_gpu():
     g = Golden("ss_gd_potential")
     p = g.build()
     with pytest.raises(NotImplementedError):
-        p.reconstruct(num_iter=1, fix_positions=False)
+        p.reconstruct(num_iter=1, fix_positions=False, global_affine_transformation=True)
+    with pytest.raises(NotImplementedError):
+        p.reconstruct(num_iter=1, fix_positions=False, reconstruction_method="DM_AP")
     with pytest.raises(NotImplementedError):
         p.reconstruct(num_iter=1, gaussian_filter_sigma=0.5)
+
     with pytest.raises(ValueError):
         p.reconstruct(num_iter=1, reconstruction_method="DM_AP", max_batch_size=4)

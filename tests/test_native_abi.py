@@ -33,7 +33,7 @@ def test_exports_every_declared_symbol(lib):
 
 
 def test_abi_version(lib):
-    assert lib.ptycho_abi_version() == 1
+    assert lib.ptycho_abi_version() == 2
 
 
 @pytest.mark.parametrize("n,ok", [(32, 1), (48, 1), (64, 1), (96, 1), (128, 1), (80, 0),
@@ -94,6 +94,57 @@ def test_rejects_bad_batch_and_workspace(lib):
 
 def test_rejects_unknown_flags(lib):
     g = geometry()
-    g.flags = 2
+    g.flags = 4
     assert _gd(lib, g) == 1
     assert b"flags" in lib.ptycho_last_error()
+
+
+def test_keep_farfield_is_gd_only(lib):
+    g = geometry()
+    g.flags = _native.FLAG_KEEP_FARFIELD
+    dummy = ctypes.c_void_p(0x1000)
+    st = lib.ptycho_projection_batch(ctypes.byref(g), dummy, dummy, dummy, None, dummy, None, 4,
+                                     0.0, 1.0, 1.0, 1.0, 0, dummy, 0, None, dummy,
+                                     ctypes.c_void_p(0x1000), 1 << 40, None)
+    assert st == 2 and b"gradient-descent" in lib.ptycho_last_error()
+
+
+def _pc(lib, g, ws=ctypes.c_void_p(0x1000), wsb=1 << 40, initial=ctypes.c_void_p(0x1000)):
+    dummy = ctypes.c_void_p(0x1000)
+    return lib.ptycho_position_correction(ctypes.byref(g), dummy, None, None, dummy, None,
+                                          dummy, initial, None, 4, 0.5, -1.0, -1.0, ws, wsb,
+                                          None)
+
+
+def test_position_correction_argument_checks(lib):
+    g = geometry()
+    assert _pc(lib, g) == 1  # far fields were not kept
+    assert b"KEEP_FARFIELD" in lib.ptycho_last_error()
+    g.flags = _native.FLAG_KEEP_FARFIELD
+    assert _pc(lib, g, initial=None) == 1
+    assert b"positions_initial" in lib.ptycho_last_error()
+    assert _pc(lib, g, ws=None) == 3
+    g = geometry(T=3)
+    g.flags = _native.FLAG_KEEP_FARFIELD
+    assert _pc(lib, g) == 1
+    assert b"propagators" in lib.ptycho_last_error()
+
+
+def test_keep_farfield_workspace(lib):
+    g = geometry(T=3)
+    base = lib.ptycho_workspace_bytes(ctypes.byref(g), 8)
+    g.flags = _native.FLAG_KEEP_FARFIELD
+    # multislice keeps one far field (c64) per position only when asked to
+    assert lib.ptycho_workspace_bytes(ctypes.byref(g), 8) >= base + 8 * 64 * 64 * 8
+
+
+def test_self_consistency_argument_checks(lib):
+    dummy = ctypes.c_void_p(0x1000)
+    g = geometry()
+    st = lib.ptycho_self_consistency_errors(ctypes.byref(g), dummy, dummy, dummy, None, dummy,
+                                            None, 4, None, None, dummy, 1 << 40, None)
+    assert st == 1 and b"errors" in lib.ptycho_last_error()
+    g = geometry(T=3)
+    st = lib.ptycho_self_consistency_errors(ctypes.byref(g), dummy, dummy, dummy, None, dummy,
+                                            None, 4, None, dummy, dummy, 1 << 40, None)
+    assert st == 1 and b"propagators" in lib.ptycho_last_error()

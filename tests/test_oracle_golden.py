@@ -39,6 +39,10 @@ def test_oracle_reproduces_reference(name):
                                   g.out["error_iterations"])
     np.testing.assert_array_equal(o.object, g.out["object"])
     np.testing.assert_array_equal(o.probe, g.out["probe_corner"])
+    np.testing.assert_array_equal(o.positions_px, g.out["positions_px"])
+    np.testing.assert_array_equal(
+        o.self_consistency_errors(g.meta["reconstruct"].get("max_batch_size")),
+        g.out["self_consistency_errors"])
 
 
 def test_oracle_float64_close_to_float32():
