@@ -11,7 +11,7 @@
 // Radix-R DFTs (R in {2,4,8,16}) are radix-2 decimation-in-frequency networks
 // fully unrolled in registers; R = 3 uses the standard 3-point butterfly. Their
 // internal twiddles are exact 16th roots of unity. Inter-pass twiddles come from
-// a table exp(-2 pi i m / L), m < L, evaluated in double and rounded once.
+// a table exp(-2 pi i m / L), m < L, computed at compile time and rounded once.
 //
 // Conventions match numpy.fft: forward = exp(-2 pi i n k / L) unnormalised,
 // inverse = exp(+2 pi i n k / L); the caller applies the 1/(SX*SY) factor.
@@ -134,16 +134,60 @@ __device__ __forceinline__ void dft(float2 (&a)[R]) {
   }
 }
 
-// Fill tw[m] = exp(-2 pi i m / L) for m < L (block-cooperative, no barrier).
-// Evaluated in double and rounded once, so every entry is the float32 nearest
-// to the exact root of unity (L values per block: negligible FP64 work).
+// Twiddle tables exp(-2 pi i m / L), m < L, evaluated at compile time: the
+// angle is reduced to a quarter turn by integer arithmetic (exact), cos and sin
+// of x = (pi/2) r/L in [0, pi/2) are summed as Taylor series in double (16 terms:
+// truncation below 1e-20), and each entry is rounded once to float. Every entry
+// equals the float nearest to the exact root of unity (checked against 40-digit
+// values for L = 32, 48, 64, 96, 128).
+namespace twiddle_detail {
+constexpr double kHalfPi = 1.57079632679489661923;
+constexpr double sin_series(double x) {
+  double term = x, sum = x;
+  for (int k = 1; k < 16; ++k) {
+    term *= -x * x / ((2.0 * k) * (2.0 * k + 1.0));
+    sum += term;
+  }
+  return sum;
+}
+constexpr double cos_series(double x) {
+  double term = 1.0, sum = 1.0;
+  for (int k = 1; k < 16; ++k) {
+    term *= -x * x / ((2.0 * k - 1.0) * (2.0 * k));
+    sum += term;
+  }
+  return sum;
+}
+template <int L>
+struct Table {
+  float2 v[L];
+};
+template <int L>
+constexpr Table<L> make_table() {
+  Table<L> t{};
+  for (int m = 0; m < L; ++m) {
+    const int q = (4 * m) / L;  // quarter turns
+    const int r = 4 * m - q * L;
+    const double x = kHalfPi * (double)r / (double)L;
+    const double c0 = cos_series(x), s0 = sin_series(x);
+    double c = c0, s = s0;
+    if (q == 1) { c = -s0; s = c0; }
+    if (q == 2) { c = -c0; s = -s0; }
+    if (q == 3) { c = s0; s = -c0; }
+    t.v[m].x = (float)c;
+    t.v[m].y = (float)-s;
+  }
+  return t;
+}
+template <int L>
+__device__ const Table<L> kTable = make_table<L>();
+}  // namespace twiddle_detail
+
+// Fill tw[m] = exp(-2 pi i m / L) for m < L from the table (block-cooperative,
+// no barrier).
 template <int L, int NT>
 __device__ __forceinline__ void fill_twiddles(float2* tw) {
-  for (int m = threadIdx.x; m < L; m += NT) {
-    double s, c;
-    sincospi(2.0 * (double)m / (double)L, &s, &c);
-    tw[m] = make_float2((float)c, (float)-s);
-  }
+  for (int m = threadIdx.x; m < L; m += NT) tw[m] = twiddle_detail::kTable<L>.v[m];
 }
 
 // exp(i phi) for a float32 phase, cos/sin evaluated in double and rounded once.

@@ -3,7 +3,7 @@
 //
 // Object side (replaces _sum_overlapping_patches_bincounts, phase_base_class.py:1905-1968,
 // and the update lines of _gradient_descent_adjoint / _projection_sets_adjoint):
-//   object_reduce_kernel   one block per 32x32 object tile (and slice). It lists,
+//   object_reduce_kernel   one block per 16x16 object tile (and slice). It lists,
 //                          in batch order, the positions whose patch touches the
 //                          tile, then sums their staged terms pixel by pixel in
 //                          that order. Every staged value is read exactly once.
@@ -11,7 +11,14 @@
 //                          O += step G N_O (GD) or O = G N_O (projection sets).
 // Probe side: a chunked fixed-order sum over the batch, then the same
 // normaliser with max over the probe pixels.
+// The two sides read disjoint staging buffers and write disjoint state, so the
+// probe side runs on a helper stream concurrently with the object side (fork and
+// join through events on the caller's stream).
 #include <cuda_runtime.h>
+
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "fft_smem.cuh"
 #include "ptycho_internal.h"
@@ -519,21 +526,65 @@ cudaError_t launch_fma_probe(int blocks, int iters, float* sink, cudaStream_t s)
   return cudaGetLastError();
 }
 
+namespace {
+
+// Helper stream and fork/join events per (device, caller stream), created on
+// the first batch issued on that stream and kept for the life of the process.
+struct ForkJoin {
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr;
+  cudaEvent_t join = nullptr;
+};
+std::mutex g_fork_mu;
+std::map<std::pair<int, cudaStream_t>, ForkJoin> g_fork;
+
+cudaError_t fork_join_for(cudaStream_t s, ForkJoin& out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(g_fork_mu);
+  ForkJoin& fj = g_fork[std::make_pair(dev, s)];
+  if (!fj.side) {
+    int prio = 0;
+    if (s != nullptr && (e = cudaStreamGetPriority(s, &prio)) != cudaSuccess) return e;
+    ForkJoin n;
+    if ((e = cudaStreamCreateWithPriority(&n.side, cudaStreamNonBlocking, prio)) != cudaSuccess)
+      return e;
+    if ((e = cudaEventCreateWithFlags(&n.fork, cudaEventDisableTiming)) != cudaSuccess) return e;
+    if ((e = cudaEventCreateWithFlags(&n.join, cudaEventDisableTiming)) != cudaSuccess) return e;
+    fj = n;
+  }
+  out = fj;
+  return cudaSuccess;
+}
+
+}  // namespace
+
 cudaError_t launch_reduce_and_update(const BatchArgs& a, cudaStream_t s) {
   const int ntx = (a.Px + kTile - 1) / kTile;
   const int nty = (a.Py + kTile - 1) / kTile;
   const int ntiles = ntx * nty;
+  ForkJoin fj;
+  cudaError_t e;
+  if (!a.fix_probe) {
+    // probe side on the helper stream, after everything issued so far on s
+    if ((e = fork_join_for(s, fj)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(fj.fork, s)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(fj.side, fj.fork, 0)) != cudaSuccess) return e;
+    const int N = a.Sx * a.Sy;
+    const int nb = (N + NT - 1) / NT;
+    probe_reduce_kernel<<<dim3(nb, kProbeChunks), NT, 0, fj.side>>>(a);
+    probe_finalize_kernel<<<nb, NT, 0, fj.side>>>(a);
+    probe_update_kernel<<<nb, NT, 0, fj.side>>>(a, nb);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(fj.join, fj.side)) != cudaSuccess) return e;
+  }
   object_reduce_kernel<<<dim3(ntiles, a.T), NT, 0, s>>>(a);
   const size_t P = (size_t)a.Px * a.Py;
   object_update_kernel<<<dim3((unsigned)((P + NT - 1) / NT), a.T), NT, 0, s>>>(a, ntiles);
-  if (!a.fix_probe) {
-    const int N = a.Sx * a.Sy;
-    const int nb = (N + NT - 1) / NT;
-    probe_reduce_kernel<<<dim3(nb, kProbeChunks), NT, 0, s>>>(a);
-    probe_finalize_kernel<<<nb, NT, 0, s>>>(a);
-    probe_update_kernel<<<nb, NT, 0, s>>>(a, nb);
-  }
-  return cudaGetLastError();
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (!a.fix_probe && (e = cudaStreamWaitEvent(s, fj.join, 0)) != cudaSuccess) return e;
+  return cudaSuccess;
 }
 
 cudaError_t launch_object_constraints(const BatchArgs& a, const uint8_t* mask, float shrinkage,
