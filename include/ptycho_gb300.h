@@ -141,6 +141,23 @@ int ptycho_position_correction(const ptycho_geometry* geometry, const void* obje
                                size_t workspace_bytes, void* stream);
 
 /*
+ * Loss and gradients of one batch, without an update (the backward of an
+ * autograd function over the forward model). loss[0] = sum over the batch of
+ * sum_k (A - |F|)^2 (the batch error of _gradient_descent_fourier_projection,
+ * ptychographic_methods.py:1576-1635, 2742-2804); object_grad (T,Px,Py) complex64
+ * (float32 for potentials) and probe_grad (M,Sx,Sy) complex64 (NULL: skipped)
+ * receive dloss/dRe + i dloss/dIm (for potentials dloss/dV), i.e. -2N times the
+ * summed adjoint terms of _gradient_descent_adjoint (ptychographic_methods.py:
+ * 1818-1908, 2353-2458, 2906-3000) before their normalisation and step.
+ */
+int ptycho_gd_gradient(const ptycho_geometry* geometry, const void* object, const void* probe,
+                       const float* amplitudes, const int32_t* amplitude_rows,
+                       const float* positions_px, const int32_t* position_rows, int32_t batch,
+                       const float* detector_mask, const void* propagators, void* object_grad,
+                       void* probe_grad, float* loss, void* workspace, size_t workspace_bytes,
+                       void* stream);
+
+/*
  * Per-position self-consistency error sum_k (A - |F|)^2 of a forward-only pass
  * (no update), written to errors[b] for the `batch` positions. Replaces the
  * per-batch body of _return_self_consistency_errors

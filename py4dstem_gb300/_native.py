@@ -83,6 +83,11 @@ _SIGNATURES = {
          _f64, _vp, _sz, _vp],
         ctypes.c_int,
     ),
+    "ptycho_gd_gradient": (
+        [ctypes.POINTER(Geometry), _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _vp, _vp,
+         _vp, _sz, _vp],
+        ctypes.c_int,
+    ),
     "ptycho_self_consistency_errors": (
         [ctypes.POINTER(Geometry), _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _sz, _vp],
         ctypes.c_int,

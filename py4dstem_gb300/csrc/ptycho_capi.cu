@@ -97,6 +97,8 @@ Workspace workspace_layout(int Sx, int Sy, int Px, int Py, int T, int M, int B,
   w.obj_grad = take(sizeof(float2) * T * P);
   w.obj_nrm = take(sizeof(float) * T * P);
   w.tile_max = take(sizeof(float) * T * ntiles);
+  w.obj_part = take(sizeof(float2) * kObjSplit * T * P);
+  w.obj_npart = take(sizeof(float) * kObjSplit * T * P);
   w.probe_part = take(sizeof(float2) * kProbeChunks * M * N);
   w.probe_npart = take(sizeof(float) * kProbeChunks * N);
   w.probe_bmax = take(sizeof(float) * nb);
@@ -122,6 +124,8 @@ void bind_workspace(BatchArgs& a, void* base, const Workspace& w) {
   a.obj_grad = reinterpret_cast<float2*>(p + w.obj_grad);
   a.obj_nrm = reinterpret_cast<float*>(p + w.obj_nrm);
   a.tile_max = reinterpret_cast<float*>(p + w.tile_max);
+  a.obj_part = reinterpret_cast<float2*>(p + w.obj_part);
+  a.obj_npart = reinterpret_cast<float*>(p + w.obj_npart);
   a.probe_part = reinterpret_cast<float2*>(p + w.probe_part);
   a.probe_npart = reinterpret_cast<float*>(p + w.probe_npart);
   a.probe_bmax = reinterpret_cast<float*>(p + w.probe_bmax);
@@ -341,6 +345,39 @@ int ptycho_self_consistency_errors(const ptycho_geometry* g, const void* object,
   if (e != cudaSuccess) return cuda_fail(e, "probe spectrum kernel");
   e = launch_position_kernel(a, s);
   if (e != cudaSuccess) return cuda_fail(e, "position kernel (forward only)");
+  return PTYCHO_OK;
+}
+
+int ptycho_gd_gradient(const ptycho_geometry* g, const void* object, const void* probe,
+                       const float* amplitudes, const int32_t* amplitude_rows,
+                       const float* positions_px, const int32_t* position_rows, int32_t batch,
+                       const float* detector_mask, const void* propagators, void* object_grad,
+                       void* probe_grad, float* loss, void* workspace, size_t workspace_bytes,
+                       void* stream) {
+  BatchArgs a;
+  int st = prepare(g, batch, workspace, workspace_bytes, a);
+  if (st != PTYCHO_OK) return st;
+  if (!object || !probe || !amplitudes || !positions_px || !object_grad || !loss)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "object, probe, amplitudes, positions, object_grad "
+                                             "and loss must be non-null");
+  if (g->num_slices > 1 && !propagators)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "multislice needs propagators");
+  a.mixed_formula = (g->num_probes > 1 || (g->flags & PTYCHO_FLAG_MIXED_STATE)) ? 1 : 0;
+  a.object = const_cast<void*>(object);
+  a.probe = static_cast<float2*>(const_cast<void*>(probe));
+  a.amplitudes = amplitudes;
+  a.amp_rows = amplitude_rows;
+  a.positions = positions_px;
+  a.pos_rows = position_rows;
+  a.det_mask = detector_mask;
+  a.props = static_cast<const float2*>(propagators);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = launch_probe_spectrum(a, s);
+  if (e != cudaSuccess) return cuda_fail(e, "probe spectrum kernel");
+  e = launch_position_kernel(a, s);  // natural staging order (the shared-memory schedule)
+  if (e != cudaSuccess) return cuda_fail(e, "position kernel");
+  e = launch_gradient(a, object_grad, static_cast<float2*>(probe_grad), loss, s);
+  if (e != cudaSuccess) return cuda_fail(e, "gradient kernels");
   return PTYCHO_OK;
 }
 

@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(NT, 1) gd128_kernel(BatchArgs a) {
             mk = a.det_mask[x * S + 8 * j + m.n2];
             f = c_scale(f, mk);
           }
-          const float af = hypotf(f.x, f.y);
+          const float af = c_abs(f);
           const float d = A[j] - af;
           err += d * d;
           // A exp(i angle F) - F = F (A/|F| - 1); A - F where F = 0 (angle 0)

@@ -9,6 +9,7 @@ namespace pty {
 
 constexpr int kTile = 16;          // object reduction tile (kTile x kTile pixels)
 constexpr int kProbeChunks = 16;   // batch chunks of the probe-gradient reduction
+constexpr int kObjSplit = 4;       // position-list chunks per object tile (partial sums)
 constexpr int kReduceThreads = 256;
 
 // Per-batch kernel arguments (device pointers into caller buffers/workspace).
@@ -58,6 +59,8 @@ struct BatchArgs {
   float2* obj_grad;     // (T,P)
   float* obj_nrm;       // (T,P)
   float* tile_max;      // (T,ntiles)
+  float2* obj_part;     // (kObjSplit,T,P) partial object-term sums
+  float* obj_npart;     // (kObjSplit,T,P) partial |P|^2 sums
   float2* probe_part;   // (chunks,M,N)
   float* probe_npart;   // (chunks,N)
   float* probe_bmax;    // (N/256)
@@ -69,7 +72,7 @@ struct BatchArgs {
 
 struct Workspace {
   size_t probe_spec, tw, st_obj, st_nobj, st_probe, st_nprobe, scratch_f, pos_round, err,
-      obj_grad, obj_nrm, tile_max, probe_part, probe_npart, probe_bmax, probe_grad,
+      obj_grad, obj_nrm, tile_max, obj_part, obj_npart, probe_part, probe_npart, probe_bmax, probe_grad,
       probe_nrm, com, red, total;
 };
 
@@ -94,6 +97,9 @@ int set_schedule(int roi, int schedule);
 bool position_v2_eligible(const BatchArgs& a);
 cudaError_t launch_position_v2(const BatchArgs& a, cudaStream_t s);
 cudaError_t launch_reduce_and_update(const BatchArgs& a, cudaStream_t s);
+// Loss and object / probe gradients of a batch (no update); probe_grad may be null.
+cudaError_t launch_gradient(const BatchArgs& a, void* object_grad, float2* probe_grad,
+                            float* loss, cudaStream_t s);
 cudaError_t launch_object_constraints(const BatchArgs& a, const uint8_t* mask,
                                       float shrinkage, int apply_shrinkage,
                                       int pure_phase, int positivity, cudaStream_t s);

@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
         if (a.keep_farfield) a.scratch_f[(size_t)b * N + e] = f;  // unmasked, for A16
         const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
         if (a.det_mask) f = c_scale(f, mk);
-        const float af = hypotf(f.x, f.y);
+        const float af = c_abs(f);
         const float A = av[i];
         const float d = A - af;
         err += d * d;
@@ -384,7 +384,7 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
       if (a.keep_farfield) a.scratch_f[(size_t)b * N + e] = f;  // unmasked, for A16
       const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
       if (a.det_mask) f = c_scale(f, mk);
-      const float af = hypotf(f.x, f.y);
+      const float af = c_abs(f);
       const float A = amp[e];
       const float d = A - af;
       err += d * d;

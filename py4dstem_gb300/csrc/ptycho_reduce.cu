@@ -3,10 +3,13 @@
 //
 // Object side (replaces _sum_overlapping_patches_bincounts, phase_base_class.py:1905-1968,
 // and the update lines of _gradient_descent_adjoint / _projection_sets_adjoint):
-//   object_reduce_kernel   one block per 16x16 object tile (and slice). It lists,
-//                          in batch order, the positions whose patch touches the
-//                          tile, then sums their staged terms pixel by pixel in
-//                          that order. Every staged value is read exactly once.
+//   object_reduce_kernel   one block per 16x16 object tile, slice and list chunk.
+//                          It lists, in batch order, the positions whose patch
+//                          touches the tile, then sums the staged terms of its
+//                          chunk (kObjSplit contiguous chunks of that list) pixel
+//                          by pixel in list order. Every staged value is read once.
+//   object_combine_kernel  adds the chunk sums in chunk order (fixed, so the
+//                          result is deterministic) and takes the tile maximum.
 //   object_update_kernel   N_O = 1/sqrt(1e-16 + ((1-m) S)^2 + (m max S)^2);
 //                          O += step G N_O (GD) or O = G N_O (projection sets).
 // Probe side: a chunked fixed-order sum over the batch, then the same
@@ -80,16 +83,17 @@ __device__ __forceinline__ float normaliser(float s, float smax, float m) {
 }
 
 // ------------------------------------------------------------------ object side
-constexpr int kListChunk = 4096;
+constexpr int kListChunk = 2048;
 
 __global__ void __launch_bounds__(NT) object_reduce_kernel(BatchArgs a) {
   __shared__ int list[kListChunk];
+  __shared__ int list_d[kListChunk];  // (dx << 16) | dy: tile origin in patch coordinates
   __shared__ int warp_count[NT / 32];
   __shared__ int warp_base[NT / 32 + 1];
-  __shared__ float red[NT / 32];
 
   static_assert(kTile * kTile == NT, "one object pixel per thread");
   const int s = blockIdx.y;
+  const int chunk = blockIdx.z;
   const int nty = (a.Py + kTile - 1) / kTile;
   const int tile = blockIdx.x;
   const int tx0 = (tile / nty) * kTile;
@@ -120,10 +124,11 @@ __global__ void __launch_bounds__(NT) object_reduce_kernel(BatchArgs a) {
     for (int base = 0; base < cn; base += NT) {
       const int i = base + tid;
       bool hit = false;
+      int dx = 0, dy = 0;
       if (i < cn) {
         const int2 r = a.pos_round[c0 + i];
-        const int dx = pmod(tx0 - (r.x + fminx), a.Px);
-        const int dy = pmod(ty0 - (r.y + fminy), a.Py);
+        dx = pmod(tx0 - (r.x + fminx), a.Px);
+        dy = pmod(ty0 - (r.y + fminy), a.Py);
         hit = (dx < a.Sx || dx + tw - 1 >= a.Px) && (dy < a.Sy || dy + th - 1 >= a.Py);
       }
       const unsigned bal = __ballot_sync(0xffffffffu, hit);
@@ -134,25 +139,36 @@ __global__ void __launch_bounds__(NT) object_reduce_kernel(BatchArgs a) {
         for (int w = 0; w < NT / 32; ++w) warp_base[w + 1] = warp_base[w] + warp_count[w];
       }
       __syncthreads();
-      if (hit) list[warp_base[warp] + __popc(bal & ((1u << lane) - 1u))] = c0 + i;
+      if (hit) {
+        const int slot = warp_base[warp] + __popc(bal & ((1u << lane) - 1u));
+        list[slot] = c0 + i;
+        list_d[slot] = (dx << 16) | dy;
+      }
       count = warp_base[NT / 32];
       __syncthreads();
     }
-    // Sum the staged terms in list (= batch) order. Loads are issued U at a time
-    // ahead of the adds so that several are in flight per thread.
+    // Sum this block's chunk of the list in list (= batch) order. Loads are
+    // issued U at a time ahead of the adds so that several are in flight.
     constexpr int U = 8;
-    for (int l0 = 0; l0 < count; l0 += U) {
+    const int per = (count + kObjSplit - 1) / kObjSplit;
+    const int lo = chunk * per;
+    const int hi = min(count, lo + per);
+    for (int l0 = lo; l0 < hi; l0 += U) {
       float2 v[U];
       float w[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         v[u] = make_float2(0.f, 0.f);
         w[u] = 0.f;
-        if (l0 + u < count && inside) {
+        if (l0 + u < hi && inside) {
+          // patch coordinates of this pixel: (tile origin in the patch) + offset,
+          // one wrap at most since the tile edge (16) is below the object size
           const int b = list[l0 + u];
-          const int2 r = a.pos_round[b];
-          const int tx = pmod(px - r.x - fminx, a.Px);
-          const int ty = pmod(py - r.y - fminy, a.Py);
+          const int d = list_d[l0 + u];
+          int tx = (d >> 16) + row;
+          int ty = (d & 0xffff) + col;
+          if (tx >= a.Px) tx -= a.Px;
+          if (ty >= a.Py) ty -= a.Py;
           if (tx < a.Sx && ty < a.Sy) {
             const int lx = fminx + tx < 0 ? fminx + tx + a.Sx : fminx + tx;
             const int ly = fminy + ty < 0 ? fminy + ty + a.Sy : fminy + ty;
@@ -171,17 +187,43 @@ __global__ void __launch_bounds__(NT) object_reduce_kernel(BatchArgs a) {
     }
   }
 
-  float m = 0.0f;
-  const size_t P = (size_t)a.Px * a.Py;
   if (inside) {
+    const size_t P = (size_t)a.Px * a.Py;
+    const size_t o = ((size_t)chunk * a.T + s) * P + (size_t)px * a.Py + py;
+    a.obj_part[o] = g;
+    a.obj_npart[o] = n;
+  }
+}
+
+__global__ void __launch_bounds__(NT) object_combine_kernel(BatchArgs a) {
+  __shared__ float red[NT / 32];
+  const int s = blockIdx.y;
+  const int nty = (a.Py + kTile - 1) / kTile;
+  const int tile = blockIdx.x;
+  const int tx0 = (tile / nty) * kTile;
+  const int ty0 = (tile % nty) * kTile;
+  const int px = tx0 + threadIdx.x / kTile;
+  const int py = ty0 + threadIdx.x % kTile;
+  float m = 0.0f;
+  if (px < a.Px && py < a.Py) {
+    const size_t P = (size_t)a.Px * a.Py;
     const size_t o = (size_t)s * P + (size_t)px * a.Py + py;
+    float2 g = a.obj_part[o];
+    float n = a.obj_npart[o];
+#pragma unroll
+    for (int k = 1; k < kObjSplit; ++k) {
+      const size_t ok = ((size_t)k * a.T + s) * P + (size_t)px * a.Py + py;
+      const float2 gk = a.obj_part[ok];
+      g.x += gk.x;
+      g.y += gk.y;
+      n += a.obj_npart[ok];
+    }
     a.obj_grad[o] = g;
     a.obj_nrm[o] = n;
     m = n;
   }
   m = block_max(m, red);
-  const int ntiles = gridDim.x;
-  if (tid == 0) a.tile_max[s * ntiles + tile] = m;
+  if (threadIdx.x == 0) a.tile_max[s * gridDim.x + tile] = m;
 }
 
 __global__ void __launch_bounds__(NT) object_update_kernel(BatchArgs a, int ntiles) {
@@ -313,6 +355,43 @@ __global__ void __launch_bounds__(NT) probe_update_kernel(BatchArgs a, int nbloc
       }
       const float2 v = a.probe[o];
       a.probe[o] = make_float2(__fadd_rn(v.x, u.x), __fadd_rn(v.y, u.y));
+    }
+  }
+}
+
+// ------------------------------------------------------------- gradient export
+// Loss and gradients of one batch without an update (the autograd backward):
+// loss = sum_b err_b in batch order; object and probe gradients are the summed
+// adjoint terms times `scale` (-2N: the adjoint terms are -1/(2N) times the
+// gradient of the loss with respect to the real and imaginary parts).
+__global__ void __launch_bounds__(NT) gradient_export_kernel(BatchArgs a, void* object_grad,
+                                                            float2* probe_grad, float* loss,
+                                                            float scale) {
+  __shared__ float red[NT / 32];
+  if (blockIdx.x == 0) {
+    float e = 0.0f;
+    const int per = (a.B + NT - 1) / NT;
+    const int lo = threadIdx.x * per;
+    const int hi = min(a.B, lo + per);
+    for (int i = lo; i < hi; ++i) e += a.err[i];
+    const float tot = block_sum_all(e, red);
+    if (threadIdx.x == 0) loss[0] = tot;
+  }
+  const size_t TP = (size_t)a.T * a.Px * a.Py;
+  const size_t MN = (size_t)a.M * a.Sx * a.Sy;
+  const size_t stride = (size_t)gridDim.x * NT;
+  for (size_t i = (size_t)blockIdx.x * NT + threadIdx.x; i < TP; i += stride) {
+    const float2 g = a.obj_grad[i];
+    if (a.potential) {
+      reinterpret_cast<float*>(object_grad)[i] = scale * g.x;
+    } else {
+      reinterpret_cast<float2*>(object_grad)[i] = make_float2(scale * g.x, scale * g.y);
+    }
+  }
+  if (probe_grad) {
+    for (size_t i = (size_t)blockIdx.x * NT + threadIdx.x; i < MN; i += stride) {
+      const float2 g = a.probe_grad[i];
+      probe_grad[i] = make_float2(scale * g.x, scale * g.y);
     }
   }
 }
@@ -579,12 +658,31 @@ cudaError_t launch_reduce_and_update(const BatchArgs& a, cudaStream_t s) {
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = cudaEventRecord(fj.join, fj.side)) != cudaSuccess) return e;
   }
-  object_reduce_kernel<<<dim3(ntiles, a.T), NT, 0, s>>>(a);
+  object_reduce_kernel<<<dim3(ntiles, a.T, kObjSplit), NT, 0, s>>>(a);
+  object_combine_kernel<<<dim3(ntiles, a.T), NT, 0, s>>>(a);
   const size_t P = (size_t)a.Px * a.Py;
   object_update_kernel<<<dim3((unsigned)((P + NT - 1) / NT), a.T), NT, 0, s>>>(a, ntiles);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (!a.fix_probe && (e = cudaStreamWaitEvent(s, fj.join, 0)) != cudaSuccess) return e;
   return cudaSuccess;
+}
+
+cudaError_t launch_gradient(const BatchArgs& a, void* object_grad, float2* probe_grad,
+                            float* loss, cudaStream_t s) {
+  const int ntx = (a.Px + kTile - 1) / kTile;
+  const int nty = (a.Py + kTile - 1) / kTile;
+  const int ntiles = ntx * nty;
+  object_reduce_kernel<<<dim3(ntiles, a.T, kObjSplit), NT, 0, s>>>(a);
+  object_combine_kernel<<<dim3(ntiles, a.T), NT, 0, s>>>(a);
+  if (probe_grad) {
+    const int N = a.Sx * a.Sy;
+    const int nb = (N + NT - 1) / NT;
+    probe_reduce_kernel<<<dim3(nb, kProbeChunks), NT, 0, s>>>(a);
+    probe_finalize_kernel<<<nb, NT, 0, s>>>(a);
+  }
+  const float scale = -2.0f * (float)(a.Sx * a.Sy);
+  gradient_export_kernel<<<1024, NT, 0, s>>>(a, object_grad, probe_grad, loss, scale);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_object_constraints(const BatchArgs& a, const uint8_t* mask, float shrinkage,

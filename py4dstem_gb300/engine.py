@@ -205,7 +205,7 @@ def run_batch(st: DeviceState, start: int, end: int, host_order: np.ndarray, *,
             _ptr(st.det_mask), props, _ptr(st.error_accum), _ws_ptr(st), st.workspace_bytes,
             _stream())
     _native.check(status)
-    st.launches += 4 if fix_probe else 7
+    st.launches += 5 if fix_probe else 8
     if position_correction is not None:
         pc = position_correction
         none = -1.0
