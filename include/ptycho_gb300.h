@@ -146,9 +146,12 @@ int ptycho_position_correction(const ptycho_geometry* geometry, const void* obje
  * sum_k (A - |F|)^2 (the batch error of _gradient_descent_fourier_projection,
  * ptychographic_methods.py:1576-1635, 2742-2804); object_grad (T,Px,Py) complex64
  * (float32 for potentials) and probe_grad (M,Sx,Sy) complex64 (NULL: skipped)
- * receive dloss/dRe + i dloss/dIm (for potentials dloss/dV), i.e. -2N times the
- * summed adjoint terms of _gradient_descent_adjoint (ptychographic_methods.py:
- * 1818-1908, 2353-2458, 2906-3000) before their normalisation and step.
+ * receive dloss/dRe + i dloss/dIm (for potentials dloss/dV). The object gradient
+ * is -2N times the summed adjoint terms of _gradient_descent_adjoint
+ * (ptychographic_methods.py:1818-1908, 2353-2458, 2906-3000) before their
+ * normalisation and step. The probe gradient is exact: each position's term
+ * conj(O) chi goes back through the adjoint of its sub-pixel shift before the sum
+ * (the reference's probe update sums the unshifted terms).
  */
 int ptycho_gd_gradient(const ptycho_geometry* geometry, const void* object, const void* probe,
                        const float* amplitudes, const int32_t* amplitude_rows,
@@ -210,6 +213,27 @@ int ptycho_probe_gram(const ptycho_geometry* geometry, const void* probe, void* 
  */
 int ptycho_probe_mix(const ptycho_geometry* geometry, const void* probe_in,
                      const void* coeffs, void* probe_out, void* stream);
+
+/*
+ * Mixed-state orthogonalisation entirely on the device (for graph capture):
+ * Gram matrix, eigen-decomposition of the M x M Hermitian matrix (cyclic Jacobi
+ * in double, M <= 16) and mixing, in place on `probe`. Modes come out ordered by
+ * decreasing intensity like _probe_orthogonalization_constraint
+ * (ptychographic_constraints.py:1181-1216); each eigenvector's phase is fixed so
+ * that its largest component is real and positive, so the modes may differ from
+ * the reference's LAPACK eigenvectors by a constant phase per mode (to which the
+ * mixed-state model is invariant).
+ */
+int ptycho_probe_orthogonalize(const ptycho_geometry* geometry, void* probe, void* workspace,
+                               size_t workspace_bytes, void* stream);
+
+/*
+ * Creates, for batches issued on `stream`, the helper stream and events on which
+ * the probe-side reductions of a batch run concurrently with the object side.
+ * A batch call makes them on first use; call this for every stream before
+ * capturing batch calls on it in a CUDA graph (creation cannot be captured).
+ */
+int ptycho_prepare_stream(void* stream);
 
 /*
  * Instrumentation. When enabled, every launch of the fused per-position kernel

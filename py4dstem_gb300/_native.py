@@ -74,6 +74,8 @@ _SIGNATURES = {
         [ctypes.POINTER(Geometry), _vp, _vp, _sz, _vp], ctypes.c_int),
     "ptycho_probe_gram": ([ctypes.POINTER(Geometry), _vp, _vp, _vp], ctypes.c_int),
     "ptycho_probe_mix": ([ctypes.POINTER(Geometry), _vp, _vp, _vp, _vp], ctypes.c_int),
+    "ptycho_probe_orthogonalize": ([ctypes.POINTER(Geometry), _vp, _vp, _sz, _vp], ctypes.c_int),
+    "ptycho_prepare_stream": ([_vp], ctypes.c_int),
     "ptycho_enable_kernel_timing": ([_i32], ctypes.c_int),
     "ptycho_kernel_timing": ([ctypes.POINTER(_f32), ctypes.POINTER(_i32)], ctypes.c_int),
     "ptycho_fp32_fma_probe": ([_i32, _i32, _vp, _vp], ctypes.c_int),

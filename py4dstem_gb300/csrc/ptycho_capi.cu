@@ -371,6 +371,7 @@ int ptycho_gd_gradient(const ptycho_geometry* g, const void* object, const void*
   a.pos_rows = position_rows;
   a.det_mask = detector_mask;
   a.props = static_cast<const float2*>(propagators);
+  a.exact_probe_grad = probe_grad ? 1 : 0;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   cudaError_t e = launch_probe_spectrum(a, s);
   if (e != cudaSuccess) return cuda_fail(e, "probe spectrum kernel");
@@ -405,6 +406,12 @@ int ptycho_probe_com_constraint(const ptycho_geometry* g, void* probe, void* wor
   a.probe = static_cast<float2*>(probe);
   cudaError_t e = launch_probe_com(a, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "probe CoM constraint");
+  return PTYCHO_OK;
+}
+
+int ptycho_prepare_stream(void* stream) {
+  cudaError_t e = prepare_stream(static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "helper stream");
   return PTYCHO_OK;
 }
 
@@ -463,6 +470,22 @@ int ptycho_probe_gram(const ptycho_geometry* g, const void* probe, void* gram, v
   cudaError_t e = launch_probe_gram(a, static_cast<const float2*>(probe),
                                     static_cast<float2*>(gram), static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "probe Gram matrix");
+  return PTYCHO_OK;
+}
+
+int ptycho_probe_orthogonalize(const ptycho_geometry* g, void* probe, void* workspace,
+                               size_t workspace_bytes, void* stream) {
+  BatchArgs a;
+  int st = prepare(g, 1, workspace, workspace_bytes, a);
+  if (st != PTYCHO_OK) return st;
+  if (!probe) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "probe is null");
+  a.probe = static_cast<float2*>(probe);
+  // scratch: the probe-gradient rows (M x N) and the constraint scratch (Gram, coefficients)
+  float2* gram = reinterpret_cast<float2*>(a.red);
+  float2* coeffs = gram + 16 * 16;
+  cudaError_t e = launch_probe_orthogonalize(a, a.probe_grad, gram, coeffs,
+                                             static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "probe orthogonalisation");
   return PTYCHO_OK;
 }
 

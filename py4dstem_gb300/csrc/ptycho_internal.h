@@ -26,6 +26,7 @@ struct BatchArgs {
   int staging_t;           // staged per-position terms are y-major (e' = y * Sx + x)
   int forward_only;        // forward model and per-position error only, no adjoint
   int keep_farfield;       // single slice: keep FFT2(psi_m) of each position in scratch_f
+  int exact_probe_grad;    // probe term through the adjoint of the sub-pixel shift
 
   void* object;                 // (T,Px,Py) float2 or float
   float2* probe;                // (M,N)
@@ -90,12 +91,15 @@ void timing_after(cudaStream_t s);
 cudaError_t launch_probe_spectrum(const BatchArgs& a, cudaStream_t s);
 cudaError_t launch_position_kernel(const BatchArgs& a, cudaStream_t s);
 cudaError_t launch_position_correction(const BatchArgs& a, cudaStream_t s);
+cudaError_t launch_probe_inverse(const BatchArgs& a, cudaStream_t s);
 // Register-resident 128 x 128 single-slice GD kernel (ptycho_gd128.cu).
 // set_schedule stores the preferred schedule for a ROI edge (0 default,
 // 1 shared-memory passes, 2 register-resident) and returns the previous one.
 int set_schedule(int roi, int schedule);
 bool position_v2_eligible(const BatchArgs& a);
 cudaError_t launch_position_v2(const BatchArgs& a, cudaStream_t s);
+// Creates the helper stream and events that batches issued on s use (idempotent).
+cudaError_t prepare_stream(cudaStream_t s);
 cudaError_t launch_reduce_and_update(const BatchArgs& a, cudaStream_t s);
 // Loss and object / probe gradients of a batch (no update); probe_grad may be null.
 cudaError_t launch_gradient(const BatchArgs& a, void* object_grad, float2* probe_grad,
@@ -107,6 +111,10 @@ cudaError_t launch_probe_com(const BatchArgs& a, cudaStream_t s);
 cudaError_t launch_probe_gram(const BatchArgs& a, const float2* probe, float2* gram,
                               cudaStream_t s);
 cudaError_t launch_fma_probe(int blocks, int iters, float* sink, cudaStream_t s);
+// Gram matrix, device eigen-decomposition and mixing of the probe modes, all on
+// stream s (no host round trip; capturable in a CUDA graph).
+cudaError_t launch_probe_orthogonalize(const BatchArgs& a, float2* scratch_probe, float2* gram,
+                                       float2* coeffs, cudaStream_t s);
 cudaError_t launch_probe_mix(const BatchArgs& a, const float2* in, const float2* coeffs,
                              float2* out, cudaStream_t s);
 

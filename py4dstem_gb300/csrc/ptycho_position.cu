@@ -186,6 +186,22 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
     fft2d<SX, SY, NT, +1>(buf, twx, twy);
   };
 
+  // Exact probe gradient (autograd backward): the probe reaches position b
+  // through the sub-pixel shift S_b = IFFT2 diag(ramp) FFT2, so its term is
+  // S_b^H (conj(O) chi) = IFFT2(conj(ramp) FFT2(conj(O) chi)). The reference's
+  // update omits S_b^H; here the FFT2 and the conj(ramp) are applied per position
+  // and the IFFT2 once to the batch sum. buf holds conj(O) chi on entry.
+  const bool exact = a.exact_probe_grad != 0;
+  auto unshift_probe_term = [&](float2* dst) {
+    fft2d<SX, SY, NT, -1>(buf, twx, twy);
+    for (int e = tid; e < N; e += NT) {
+      const int x = e / SY, y = e % SY;
+      const float2 r = c_mul(rpx[x], rpy[y]);
+      dst[e] = c_mul(buf[x * LD + y], make_float2(r.x, -r.y));
+    }
+    __syncthreads();
+  };
+
   float err = 0.0f;
   const float px_ = 1.0f - a.pa - a.pb;  // projection x
   const float py_ = 1.0f - a.pc;          // projection y
@@ -335,11 +351,13 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
           gobj[e] = c_add(gobj[e], g);
           nobj[e] = nobj[e] + pn;
         }
-        pst[e] = c_conj_mul(o, chi);
+        const float2 yv = c_conj_mul(o, chi);
+        if (exact) buf[x * LD + y] = yv; else pst[e] = yv;
         if (m == 0) a.st_nprobe[(size_t)b * N + e] = c_abs2(o);
       }
       }
       __syncthreads();
+      if (exact) unshift_probe_term(pst);
     }
   } else {
     // ------------------------------------------------------------- multislice
@@ -427,14 +445,14 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
         pst[e] = object_term(a.potential, o, p, chi);
         nst[e] = c_abs2(p);
         const float2 bt = c_mul(chi, make_float2(o.x, -o.y));  // chi * conj(O_s)
-        if (s > 0) {
-          buf[idx] = bt;
-        } else {
-          a.st_probe[(size_t)b * N + e] = bt;
+        if (s > 0 || exact) buf[idx] = bt;
+        if (s == 0) {
+          if (!exact) a.st_probe[(size_t)b * N + e] = bt;
           a.st_nprobe[(size_t)b * N + e] = c_abs2(o);
         }
       }
       __syncthreads();
+      if (s == 0 && exact) unshift_probe_term(a.st_probe + (size_t)b * N);
       if (s > 0) {
         fft2d<SX, SY, NT, -1>(buf, twx, twy);
         const float2* h = a.props + (size_t)(s - 1) * N;
@@ -673,6 +691,39 @@ cudaError_t launch_correction_t(const BatchArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// probe_grad[m] <- IFFT2(probe_grad[m]) for every mode (one block per mode):
+// the last step of the exact probe gradient, applied to the batch sum.
+template <int SX, int SY, int NT>
+__global__ void __launch_bounds__(NT, 1) probe_inverse_kernel(BatchArgs a) {
+  using L = Layout<SX, SY>;
+  extern __shared__ float4 smem4[];
+  float2* buf = reinterpret_cast<float2*>(smem4);
+  float2* twx = buf + SX * L::LD;
+  float2* twy = twx + SX;
+  fill_twiddles<SX, NT>(twx);
+  fill_twiddles<SY, NT>(twy);
+  float2* g = a.probe_grad + (size_t)blockIdx.x * L::N;
+  for (int e = threadIdx.x; e < L::N; e += NT) buf[(e / SY) * L::LD + e % SY] = g[e];
+  __syncthreads();
+  fft2d<SX, SY, NT, +1>(buf, twx, twy);
+  const float invN = 1.0f / (float)L::N;
+  for (int e = threadIdx.x; e < L::N; e += NT) g[e] = c_scale(buf[(e / SY) * L::LD + e % SY], invN);
+}
+
+template <int SX, int SY, int NT>
+cudaError_t launch_probe_inverse_t(const BatchArgs& a, cudaStream_t s) {
+  const size_t smem = Layout<SX, SY>::smem_bytes(false);
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(probe_inverse_kernel<SX, SY, NT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  probe_inverse_kernel<SX, SY, NT><<<a.M, NT, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
 template <int SX, int SY, int NT>
 cudaError_t launch_spectrum_t(const BatchArgs& a, cudaStream_t s) {
   const size_t smem = Layout<SX, SY>::smem_bytes(false);
@@ -743,6 +794,10 @@ cudaError_t launch_position_kernel(const BatchArgs& a, cudaStream_t s) {
 
 cudaError_t launch_position_correction(const BatchArgs& a, cudaStream_t s) {
   PTY_DISPATCH(launch_correction_t, a, s)
+}
+
+cudaError_t launch_probe_inverse(const BatchArgs& a, cudaStream_t s) {
+  PTY_DISPATCH(launch_probe_inverse_t, a, s)
 }
 
 }  // namespace pty

@@ -583,6 +583,102 @@ __global__ void __launch_bounds__(NT) probe_mix_kernel(int M, int N, const float
   out[(size_t)i * N + e] = acc;
 }
 
+// Eigen-decomposition of the M x M Hermitian Gram matrix on the device (cyclic
+// Jacobi in double, one thread; M <= 16), then the mixing coefficients of the
+// orthogonalised modes: mode i = sum_j coeffs[i*M+j] P_j with the eigenvectors
+// ordered by decreasing eigenvalue (= decreasing mode intensity), each
+// eigenvector's phase fixed so that its largest component is real and positive.
+// Rotation of pair (p, q): remove the phase of g_pq, then the real Jacobi
+// rotation t = sgn(tau)/(|tau| + sqrt(1 + tau^2)), tau = (g_qq - g_pp)/(2|g_pq|).
+// At most 32 sweeps; each sweep visits every pair once.
+__global__ void probe_eigh_kernel(int M, const float2* gram, float2* coeffs) {
+  __shared__ double2 A[16][16];
+  __shared__ double2 V[16][16];
+  __shared__ double w[16];
+  __shared__ int order[16];
+  if (threadIdx.x != 0) return;
+  for (int i = 0; i < M; ++i)
+    for (int j = 0; j < M; ++j) {
+      // upper triangle is the reference's input (eigh with UPLO='U')
+      const float2 g = i <= j ? gram[i * M + j] : gram[j * M + i];
+      A[i][j] = i <= j ? make_double2(g.x, g.y) : make_double2(g.x, -g.y);
+      if (i == j) A[i][j].y = 0.0;
+      V[i][j] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+    }
+  for (int sweep = 0; sweep < 32; ++sweep) {
+    double off = 0.0, diag = 0.0;
+    for (int i = 0; i < M; ++i) {
+      diag += A[i][i].x * A[i][i].x;
+      for (int j = i + 1; j < M; ++j) off += A[i][j].x * A[i][j].x + A[i][j].y * A[i][j].y;
+    }
+    if (off <= 1e-30 * diag || off == 0.0) break;
+    for (int p = 0; p < M - 1; ++p) {
+      for (int q = p + 1; q < M; ++q) {
+        const double re = A[p][q].x, im = A[p][q].y;
+        const double mag = sqrt(re * re + im * im);
+        if (mag == 0.0) continue;
+        const double ephr = re / mag, ephi = im / mag;  // e^{i phi}
+        const double tau = (A[q][q].x - A[p][p].x) / (2.0 * mag);
+        const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+        const double c = 1.0 / sqrt(1.0 + t * t);
+        const double sn = t * c;
+        // J = [[c, s], [-s e^{-i phi}, c e^{-i phi}]] on columns (p, q): A <- J^H A J
+        for (int k = 0; k < M; ++k) {  // columns
+          const double2 akp = A[k][p], akq = A[k][q];
+          const double2 aq = make_double2(akq.x * ephr + akq.y * ephi, akq.y * ephr - akq.x * ephi);
+          A[k][p] = make_double2(c * akp.x - sn * aq.x, c * akp.y - sn * aq.y);
+          A[k][q] = make_double2(sn * akp.x + c * aq.x, sn * akp.y + c * aq.y);
+          const double2 vkp = V[k][p], vkq = V[k][q];
+          const double2 vq = make_double2(vkq.x * ephr + vkq.y * ephi, vkq.y * ephr - vkq.x * ephi);
+          V[k][p] = make_double2(c * vkp.x - sn * vq.x, c * vkp.y - sn * vq.y);
+          V[k][q] = make_double2(sn * vkp.x + c * vq.x, sn * vkp.y + c * vq.y);
+        }
+        for (int k = 0; k < M; ++k) {  // rows: conjugate of the column transform
+          const double2 apk = A[p][k], aqk = A[q][k];
+          const double2 aq = make_double2(aqk.x * ephr - aqk.y * ephi, aqk.y * ephr + aqk.x * ephi);
+          A[p][k] = make_double2(c * apk.x - sn * aq.x, c * apk.y - sn * aq.y);
+          A[q][k] = make_double2(sn * apk.x + c * aq.x, sn * apk.y + c * aq.y);
+        }
+        A[p][q] = make_double2(0.0, 0.0);
+        A[q][p] = make_double2(0.0, 0.0);
+        A[p][p].y = 0.0;
+        A[q][q].y = 0.0;
+      }
+    }
+  }
+  for (int i = 0; i < M; ++i) {
+    w[i] = A[i][i].x;
+    order[i] = i;
+  }
+  for (int i = 1; i < M; ++i) {  // stable insertion sort, decreasing eigenvalue
+    const int o = order[i];
+    int k = i - 1;
+    while (k >= 0 && w[order[k]] < w[o]) {
+      order[k + 1] = order[k];
+      --k;
+    }
+    order[k + 1] = o;
+  }
+  for (int i = 0; i < M; ++i) {
+    const int col = order[i];
+    int big = 0;
+    double bmag = -1.0;
+    for (int j = 0; j < M; ++j) {
+      const double mg = V[j][col].x * V[j][col].x + V[j][col].y * V[j][col].y;
+      if (mg > bmag) {
+        bmag = mg;
+        big = j;
+      }
+    }
+    const double bm = sqrt(bmag);
+    const double pr = V[big][col].x / bm, pi = -V[big][col].y / bm;  // e^{-i arg}
+    for (int j = 0; j < M; ++j) {
+      const double2 v = V[j][col];
+      coeffs[i * M + j] = make_float2((float)(v.x * pr - v.y * pi), (float)(v.x * pi + v.y * pr));
+    }
+  }
+}
+
 __global__ void __launch_bounds__(256) fma_probe_kernel(int iters, float* sink) {
   float a[8];
 #pragma unroll
@@ -639,6 +735,11 @@ cudaError_t fork_join_for(cudaStream_t s, ForkJoin& out) {
 
 }  // namespace
 
+cudaError_t prepare_stream(cudaStream_t s) {
+  ForkJoin fj;
+  return fork_join_for(s, fj);
+}
+
 cudaError_t launch_reduce_and_update(const BatchArgs& a, cudaStream_t s) {
   const int ntx = (a.Px + kTile - 1) / kTile;
   const int nty = (a.Py + kTile - 1) / kTile;
@@ -679,6 +780,10 @@ cudaError_t launch_gradient(const BatchArgs& a, void* object_grad, float2* probe
     const int nb = (N + NT - 1) / NT;
     probe_reduce_kernel<<<dim3(nb, kProbeChunks), NT, 0, s>>>(a);
     probe_finalize_kernel<<<nb, NT, 0, s>>>(a);
+    if (a.exact_probe_grad) {
+      cudaError_t e = launch_probe_inverse(a, s);
+      if (e != cudaSuccess) return e;
+    }
   }
   const float scale = -2.0f * (float)(a.Sx * a.Sy);
   gradient_export_kernel<<<1024, NT, 0, s>>>(a, object_grad, probe_grad, loss, scale);
@@ -714,6 +819,19 @@ cudaError_t launch_probe_gram(const BatchArgs& a, const float2* probe, float2* g
                               cudaStream_t s) {
   probe_gram_kernel<<<a.M * a.M, NT, 0, s>>>(a.M, a.Sx * a.Sy, probe, gram);
   return cudaGetLastError();
+}
+
+cudaError_t launch_probe_orthogonalize(const BatchArgs& a, float2* scratch_probe, float2* gram,
+                                       float2* coeffs, cudaStream_t s) {
+  const int N = a.Sx * a.Sy;
+  probe_gram_kernel<<<a.M * a.M, NT, 0, s>>>(a.M, N, a.probe, gram);
+  probe_eigh_kernel<<<1, 32, 0, s>>>(a.M, gram, coeffs);
+  probe_mix_kernel<<<dim3((N + NT - 1) / NT, a.M), NT, 0, s>>>(a.M, N, a.probe, coeffs,
+                                                               scratch_probe);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyAsync(a.probe, scratch_probe, sizeof(float2) * a.M * N,
+                         cudaMemcpyDeviceToDevice, s);
 }
 
 cudaError_t launch_probe_mix(const BatchArgs& a, const float2* in, const float2* coeffs,

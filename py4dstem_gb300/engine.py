@@ -247,14 +247,23 @@ def self_consistency_errors(st: DeviceState, max_batch: int) -> np.ndarray:
     return out.cpu().numpy()
 
 
-def run_iteration(st: DeviceState, host_order: np.ndarray, max_batch: int, **kw) -> None:
+def run_iteration(st: DeviceState, host_order: Optional[np.ndarray], max_batch: int,
+                  **kw) -> None:
     """One pass over all positions in `host_order` (already shuffled), batch by batch.
-    The batch errors accumulate into st.error_accum (float32 on the device)."""
+    The batch errors accumulate into st.error_accum (float32 on the device).
+    host_order=None uses the order already in st.order (no host transfer: the
+    form that a CUDA graph can capture; device-resident amplitudes only)."""
     torch = _torch()
-    st.order.copy_(torch.from_numpy(np.ascontiguousarray(host_order, dtype=np.int32)),
-                   non_blocking=False)
+    if host_order is None:
+        if st.amplitudes is None:
+            raise ValueError("an iteration without a host order needs device-resident amplitudes")
+        n = int(st.positions.shape[0])
+    else:
+        st.order.copy_(torch.from_numpy(np.ascontiguousarray(host_order, dtype=np.int32)),
+                       non_blocking=False)
+        n = int(host_order.shape[0])
     st.error_accum.zero_()
-    for start, end in generate_batches(int(host_order.shape[0]), max_batch):
+    for start, end in generate_batches(n, max_batch):
         run_batch(st, start, end, host_order, **kw)
     if kw.get("projection"):
         st.exit_waves_valid = True
@@ -279,13 +288,22 @@ def probe_com_constraint(st: DeviceState) -> None:
     st.launches += 2
 
 
-def probe_orthogonalization(st: DeviceState) -> None:
+def probe_orthogonalization(st: DeviceState, on_device: bool = False) -> None:
     """Gram matrix on the GPU, eigh of the M x M matrix on the host, mixing on the GPU
     (ptychographic_constraints.py:1181-1216). Modes are ordered by decreasing
-    intensity; the intensity of mode i is the i-th eigenvalue."""
+    intensity; the intensity of mode i is the i-th eigenvalue.
+
+    on_device=True runs the eigen-decomposition on the GPU too (no host round
+    trip, capturable in a CUDA graph); its eigenvectors carry a fixed phase
+    convention, so modes may differ from the host path by one phase per mode."""
     torch = _torch()
     lib = _native.lib()
     g = ctypes.byref(st.geometry)
+    if on_device:
+        _native.check(lib.ptycho_probe_orthogonalize(g, _ptr(st.probe), _ws_ptr(st),
+                                                      st.workspace_bytes, _stream()))
+        st.launches += 3
+        return
     _native.check(lib.ptycho_probe_gram(g, _ptr(st.probe), _ptr(st.gram), _stream()))
     gram = st.gram.cpu().numpy()
     upper = np.triu(gram)
@@ -314,8 +332,9 @@ class IterationDriver:
                  normalization_min=1.0, fix_probe=False, projection_abc=(0.0, 0.0, 0.0),
                  shrinkage_rad=0.0, use_mask=False, pure_phase=False, positivity=True,
                  fix_probe_com=True, orthogonalize_probe=False, mean_intensity=1.0,
-                 position_correction=None):
+                 position_correction=None, device_orthogonalization=False):
         self.st = st
+        self.device_orthogonalization = bool(device_orthogonalization)
         self.max_batch = int(max_batch)
         if position_correction is not None and st.positions_initial is None:
             raise ValueError("position correction needs a state created with positions_initial")
@@ -334,7 +353,8 @@ class IterationDriver:
         J = int(st.positions.shape[0])
         self.norm = np.float32(mean_intensity) * J
 
-    def iterate(self, order: np.ndarray) -> None:
+    def iterate(self, order: Optional[np.ndarray]) -> None:
+        """One iteration; order=None takes the order already in st.order."""
         st = self.st
         run_iteration(st, order, self.max_batch, **self.batch_kw)
         object_constraints(st, shrinkage_rad=self.shrinkage_rad, use_mask=self.use_mask,
@@ -342,7 +362,7 @@ class IterationDriver:
         if self.fix_probe_com:
             probe_com_constraint(st)
         if self.orthogonalize:
-            probe_orthogonalization(st)
+            probe_orthogonalization(st, on_device=self.device_orthogonalization)
         if self.positions_com:
             positions_com_constraint(st)
 

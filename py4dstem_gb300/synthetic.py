@@ -336,3 +336,19 @@ def mixed_state_case(seed=0, scan=32, detector=64, num_modes=4, backend="numpy",
     case.reconstruct_kwargs = dict(num_iter=16, max_batch_size=64, step_size=0.5,
                                    seed_random=seed)
     return case
+
+
+def multiscan_cases(seed=0, num_scans=16, num_modes=4, backend="torch", device="cuda",
+                    grid_range=(24, 96), detectors=(64, 96, 128)):
+    """Independent mixed-state scans of uneven sizes: square grids drawn uniformly
+    from grid_range, detectors from `detectors`, M probe modes (weights
+    0.7/0.15/0.1/0.05), 1e4 e-/pattern, 0.5 A step. Returns ScanCases; each
+    carries its mode probes as the initial probe guess."""
+    rng = np.random.default_rng(seed)
+    cases = []
+    for k in range(num_scans):
+        n = int(rng.integers(grid_range[0], grid_range[1] + 1))
+        det = int(rng.choice(detectors))
+        cases.append(mixed_state_case(seed=seed * 1000 + k, scan=n, detector=det,
+                                      num_modes=num_modes, backend=backend, device=device))
+    return cases
