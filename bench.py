@@ -13,9 +13,10 @@ each iteration).
   value  device-resident amplitudes (1 GiB f32, larger than L2), K iterations
          timed with CUDA events between barriers;
   e2e    the public API: K calls of reconstruct(num_iter=1) on a
-         SingleslicePtychography whose amplitudes live in pinned host memory;
-         each call uploads the step's inputs and reads object, probe and error
-         back.
+         SingleslicePtychography with storage="cpu" whose amplitudes live in
+         page-locked host memory; each call uploads object, probe and positions,
+         its kernels read all amplitudes from host memory over the CPU-GPU link,
+         and it reads object, probe and error back.
 
 `--impl reference` times the reference algorithm (the float32 NumPy restatement
 in oracle/, which reproduces the reference CPU path bit for bit) on the host
@@ -481,7 +482,10 @@ def run_ours(args):
     e2e = None
     if not args.no_e2e:
         pe = p  # preprocessed above; the engine run did not modify its host state
+        # amplitudes in page-locked host memory, storage="cpu": every step the
+        # kernels read all of them from the host (over the CPU-GPU link)
         pe._amplitudes = torch.from_numpy(np.ascontiguousarray(pe._amplitudes)).pin_memory().numpy()
+        pe._storage = "cpu"
         rec = dict(max_batch_size=B, seed_random=seed, progress_bar=False)
         for _ in range(max(1, args.warmup)):
             pe.reconstruct(num_iter=1, **rec)
@@ -492,7 +496,9 @@ def run_ours(args):
                   np.asarray(pe._probe).nbytes + pe._positions_px.nbytes)
         d2h = int(np.asarray(pe._object).nbytes + np.asarray(pe._probe).nbytes + 4)
         e2e = {"value": world * J * args.steps / (e_ms * 1e-3), "unit": UNIT,
-               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "mode": "reconstruct(num_iter=1) per step, storage='cpu': amplitudes in "
+                       "page-locked host memory, read in place by the kernels"}
 
     if rank == 0:
         line = {

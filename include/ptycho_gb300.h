@@ -228,6 +228,16 @@ int ptycho_probe_orthogonalize(const ptycho_geometry* geometry, void* probe, voi
                                size_t workspace_bytes, void* stream);
 
 /*
+ * *device = the device address of host memory [host, host + bytes) when that
+ * range is page-locked and mapped (the GPU then reads it in place, over the
+ * CPU-GPU link), else NULL. Lets a caller pass host-resident amplitudes to the
+ * batch calls without a copy; the reference's storage="cpu" mode keeps them on
+ * the host and copies each batch (copy_to_device in reconstruct,
+ * singleslice_ptychography.py:873-875).
+ */
+int ptycho_mapped_host_pointer(const void* host, size_t bytes, void** device);
+
+/*
  * Creates, for batches issued on `stream`, the helper stream and events on which
  * the probe-side reductions of a batch run concurrently with the object side.
  * A batch call makes them on first use; call this for every stream before

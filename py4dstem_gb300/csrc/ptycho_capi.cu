@@ -409,6 +409,30 @@ int ptycho_probe_com_constraint(const ptycho_geometry* g, void* probe, void* wor
   return PTYCHO_OK;
 }
 
+int ptycho_mapped_host_pointer(const void* host, size_t bytes, void** device) {
+  if (!device) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "device must be non-null");
+  *device = nullptr;
+  if (!host || bytes == 0) return PTYCHO_OK;
+  cudaPointerAttributes first, last;
+  if (cudaPointerGetAttributes(&first, host) != cudaSuccess) {
+    cudaGetLastError();  // no device or an unknown pointer: not mapped
+    return PTYCHO_OK;
+  }
+  if (first.type != cudaMemoryTypeHost || first.devicePointer == nullptr) return PTYCHO_OK;
+  // the whole range must lie in one page-locked, mapped allocation
+  const char* end = static_cast<const char*>(host) + bytes - 1;
+  if (cudaPointerGetAttributes(&last, end) != cudaSuccess) {
+    cudaGetLastError();
+    return PTYCHO_OK;
+  }
+  if (last.type != cudaMemoryTypeHost || last.devicePointer == nullptr ||
+      static_cast<const char*>(last.devicePointer) !=
+          static_cast<const char*>(first.devicePointer) + bytes - 1)
+    return PTYCHO_OK;
+  *device = first.devicePointer;
+  return PTYCHO_OK;
+}
+
 int ptycho_prepare_stream(void* stream) {
   cudaError_t e = prepare_stream(static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "helper stream");

@@ -59,6 +59,7 @@ class DeviceState:
     fov_mask_inverse: object = None
     exit_waves: object = None
     exit_waves_valid: bool = False
+    amp_mapped: Optional[int] = None  # device address of page-locked host amplitudes
     amp_stage: object = None      # device batch buffer when streaming from the host
     amp_pinned: object = None     # two pinned host batch buffers (double-buffered)
     amp_events: object = None     # copy-done events of the pinned buffers
@@ -109,13 +110,17 @@ def create_state(*, roi_shape, object_array, probe_array, amplitudes, positions_
     amps_dev = None
     amps_host = None
     amp_stage = amp_pinned = None
+    mapped = None
     if storage == "gpu":
         amps_dev = torch.from_numpy(np.ascontiguousarray(amplitudes, dtype=np.float32)).to(dev)
     else:
         amps_host = np.ascontiguousarray(amplitudes, dtype=np.float32)
-        amp_stage = torch.empty((max_batch,) + tuple(roi_shape), dtype=torch.float32, device=dev)
-        amp_pinned = [torch.empty((max_batch,) + tuple(roi_shape), dtype=torch.float32,
-                                  pin_memory=True) for _ in range(2)]
+        mapped = mapped_host_address(amps_host)
+        if mapped is None:
+            amp_stage = torch.empty((max_batch,) + tuple(roi_shape), dtype=torch.float32,
+                                    device=dev)
+            amp_pinned = [torch.empty((max_batch,) + tuple(roi_shape), dtype=torch.float32,
+                                      pin_memory=True) for _ in range(2)]
     pos = torch.from_numpy(np.ascontiguousarray(positions_px, dtype=np.float32)).to(dev)
     order = torch.arange(pos.shape[0], dtype=torch.int32, device=dev)
     ws = torch.empty(ws_bytes + 256, dtype=torch.uint8, device=dev)
@@ -123,7 +128,7 @@ def create_state(*, roi_shape, object_array, probe_array, amplitudes, positions_
     st = DeviceState(geometry=geom, object=obj, probe=probe, amplitudes=amps_dev,
                      amplitudes_host=amps_host, positions=pos, order=order, workspace=ws,
                      workspace_bytes=ws_bytes, error_accum=err, max_batch=int(max_batch),
-                     amp_stage=amp_stage, amp_pinned=amp_pinned)
+                     amp_stage=amp_stage, amp_pinned=amp_pinned, amp_mapped=mapped)
     if propagators is not None:
         st.propagators = torch.from_numpy(
             np.ascontiguousarray(propagators, dtype=np.complex64)).to(dev)
@@ -158,13 +163,30 @@ def _stream():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
+def mapped_host_address(array: np.ndarray) -> Optional[int]:
+    """Device address of a page-locked host array (the GPU reads it directly over
+    the CPU-GPU link), or None when the array lives in pageable memory."""
+    lib = _native.lib()
+    if array.nbytes == 0:
+        return None
+    dev = ctypes.c_void_p()
+    _native.check(lib.ptycho_mapped_host_pointer(ctypes.c_void_p(array.ctypes.data),
+                                                  ctypes.c_size_t(array.nbytes),
+                                                  ctypes.byref(dev)))
+    return dev.value or None
+
+
 def _batch_amplitudes(st: DeviceState, start: int, end: int, host_order: np.ndarray):
     """(amplitudes pointer, amplitude rows pointer) of one batch: the resident
-    array indexed by the order rows, or this batch's patterns copied from the host."""
+    array indexed by the order rows; page-locked host amplitudes read in place by
+    the kernels (indexed the same way); or this batch's patterns gathered on the
+    host and copied over."""
     n = end - start
     rows_ptr = ctypes.c_void_p(st.order.data_ptr() + 4 * start)
     if st.amplitudes is not None:
         return _ptr(st.amplitudes), rows_ptr
+    if st.amp_mapped is not None:
+        return ctypes.c_void_p(st.amp_mapped), rows_ptr
     else:
         # storage on the host: gather this batch's patterns and copy them over,
         # like the reference's per-batch copy_to_device
@@ -255,8 +277,9 @@ def run_iteration(st: DeviceState, host_order: Optional[np.ndarray], max_batch: 
     form that a CUDA graph can capture; device-resident amplitudes only)."""
     torch = _torch()
     if host_order is None:
-        if st.amplitudes is None:
-            raise ValueError("an iteration without a host order needs device-resident amplitudes")
+        if st.amplitudes is None and st.amp_mapped is None:
+            raise ValueError("an iteration without a host order needs device-resident or "
+                             "page-locked amplitudes")
         n = int(st.positions.shape[0])
     else:
         st.order.copy_(torch.from_numpy(np.ascontiguousarray(host_order, dtype=np.int32)),

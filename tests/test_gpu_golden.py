@@ -96,6 +96,24 @@ def test_storage_cpu_matches_gpu(cuda):
     assert a.error_iterations == b.error_iterations
 
 
+def test_storage_cpu_page_locked_matches_gpu(cuda):
+    """Host amplitudes in page-locked memory are read in place by the kernels."""
+    torch = cuda
+    from py4dstem_gb300 import engine
+
+    g = Golden("ss_gd_potential")
+    a = g.build(device="gpu", storage="gpu")
+    b = g.build(device="gpu", storage="cpu")
+    b._amplitudes = torch.from_numpy(np.ascontiguousarray(b._amplitudes)).pin_memory().numpy()
+    assert engine.mapped_host_address(b._amplitudes) is not None
+    assert engine.mapped_host_address(np.ones(16, np.float32)) is None  # pageable
+    a.reconstruct(progress_bar=False, **g.meta["reconstruct"])
+    b.reconstruct(progress_bar=False, **g.meta["reconstruct"])
+    np.testing.assert_array_equal(a.object, b.object)
+    np.testing.assert_array_equal(a._probe, b._probe)
+    assert a.error_iterations == b.error_iterations
+
+
 def test_continue_and_reset_semantics(cuda):
     g = Golden("ss_gd_potential")
     rec = dict(g.meta["reconstruct"])
