@@ -472,22 +472,12 @@ done:
   if (tid == 0) a.err[b] = tot;
 }
 
-// 128 x 128 (one block per SM) is persistent: a grid of as many blocks as fit
-// on the GPU walks the batch, block k taking positions k, k + gridDim.x, ...
-// Each position ends with a block barrier (the error sum), after which the next
-// may overwrite the shared wave. Smaller ROIs run one block per position (the
-// loop form costs them registers).
-template <int SX, int SY, int NT>
-constexpr bool kPersistent = SX == 128 && SY == 128;
-
+// One block per position. (A persistent form, one block per SM walking the
+// batch, measured 2% slower at 128 x 128 and was dropped.)
 template <int SX, int SY, int NT>
 __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
   __shared__ float red[NT / 32];
-  if constexpr (kPersistent<SX, SY, NT>) {
-    for (int b = blockIdx.x; b < a.B; b += gridDim.x) position_one<SX, SY, NT>(a, b, red);
-  } else {
-    position_one<SX, SY, NT>(a, blockIdx.x, red);
-  }
+  position_one<SX, SY, NT>(a, blockIdx.x, red);
 }
 
 // Position correction of one batch (ptychographic_methods.py:2071-2225), run
@@ -762,29 +752,15 @@ cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
   const bool mixed = a.T == 1 && (a.M > 1 || a.mixed_formula);
   const size_t smem = Layout<SX, SY>::smem_bytes(mixed);
   static bool configured = false;
-  static int resident[2] = {0, 0};  // resident blocks on the GPU, without / with the mixed buffer
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(position_kernel<SX, SY, NT>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)Layout<SX, SY>::smem_bytes(true));
     if (e != cudaSuccess) return e;
-    int dev = 0, sms = 0;
-    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
-      return e;
-    for (int k = 0; k < 2; ++k) {
-      int per_sm = 0;
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &per_sm, position_kernel<SX, SY, NT>, NT, Layout<SX, SY>::smem_bytes(k == 1));
-      if (e != cudaSuccess) return e;
-      resident[k] = (per_sm > 0 ? per_sm : 1) * sms;
-    }
     configured = true;
   }
-  const int cap = kPersistent<SX, SY, NT> ? resident[mixed ? 1 : 0] : a.B;
-  const int grid = a.B < cap ? a.B : cap;
   timing_before(s);
-  position_kernel<SX, SY, NT><<<grid, NT, smem, s>>>(a);
+  position_kernel<SX, SY, NT><<<a.B, NT, smem, s>>>(a);
   cudaError_t e = cudaGetLastError();
   timing_after(s);
   return e;
