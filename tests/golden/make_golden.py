@@ -82,6 +82,19 @@ CASES = {
         guess=(96, 96), perturb_ang=0.15,
         rec=dict(num_iter=5, max_batch_size=25, step_size=0.5, seed_random=5,
                  fix_positions=False, positions_step_size=0.25)),
+    # the benchmark's 128^2 detector (radix-16/8 transforms) on a small scan
+    "ss_gd_det128": dict(
+        gen=dict(name="s128", seed=18, scan_shape=(6, 6), step_ang=0.5, jitter_ang=0.05,
+                 detector=128, object_px=192),
+        cls="single", ctor=dict(object_fov_ang=(48.0, 48.0)), guess=(192, 192),
+        rec=dict(num_iter=4, max_batch_size=18, step_size=0.5, seed_random=7)),
+    # a 96^2 detector (radix-8/4/3 transforms) with a detector Fourier mask
+    "ss_gd_det96_mask": dict(
+        gen=dict(name="s96", seed=19, scan_shape=(8, 8), step_ang=0.5, jitter_ang=0.05,
+                 detector=96, object_px=128),
+        cls="single", ctor=dict(object_fov_ang=(32.0, 32.0)), guess=(128, 128),
+        mask_seed=5,
+        rec=dict(num_iter=4, max_batch_size=16, step_size=0.5, seed_random=8)),
     "mixed_gd_M3": dict(
         gen=dict(name="mx", seed=14, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
                  detector=64, object_px=96, num_modes=3, mode_weights=(0.7, 0.2, 0.1)),
@@ -142,7 +155,17 @@ def make_case(ref, name, spec):
         amplitude_first=p._amplitudes[0].copy(),
         amplitude_last=p._amplitudes[-1].copy(),
     )
-    p.reconstruct(progress_bar=False, **spec["rec"])
+    rec = dict(spec["rec"])
+    if "mask_seed" in spec:
+        # corner-centred Fourier mask with ~3% dead pixels, used as given
+        mrng = np.random.default_rng(spec["mask_seed"])
+        det = spec["gen"]["detector"]
+        mask = (mrng.random((det, det)) > 0.03).astype(np.float32)
+        extra_arrays_mask = {"detector_fourier_mask": mask}
+        rec["detector_fourier_mask"] = mask.copy()
+    else:
+        extra_arrays_mask = {}
+    p.reconstruct(progress_bar=False, **rec)
     out = dict(
         error_iterations=np.asarray(p.error_iterations, dtype=np.float64),
         object=p.object,
@@ -159,6 +182,7 @@ def make_case(ref, name, spec):
         extra_arrays = {"initial_object_guess": guess}
     else:
         extra_arrays = {}
+    extra_arrays.update(extra_arrays_mask)
     np.savez_compressed(
         path, datacube=data.astype(np.uint16), scan_positions_ang=positions,
         meta=json.dumps(meta), **extra_arrays, **{f"pre_{k}": v for k, v in pre.items()},

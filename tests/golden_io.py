@@ -28,6 +28,14 @@ class Golden:
         self.pre = {k[4:]: z[k] for k in z.files if k.startswith("pre_")}
         self.out = {k[4:]: z[k] for k in z.files if k.startswith("out_")}
         self.guess = z["initial_object_guess"] if "initial_object_guess" in z.files else None
+        self.mask = z["detector_fourier_mask"] if "detector_fourier_mask" in z.files else None
+
+    def rec_kwargs(self):
+        """reconstruct() arguments of the fixture (the detector mask included)."""
+        r = dict(self.meta["reconstruct"])
+        if self.mask is not None:
+            r["detector_fourier_mask"] = self.mask.copy()
+        return r
 
     @property
     def projection(self):
@@ -72,7 +80,7 @@ class Golden:
     def oracle_kwargs(self):
         from oracle.ptycho_np import method_abc
 
-        r = dict(self.meta["reconstruct"])
+        r = self.rec_kwargs()
         method, a, b, c = method_abc(r.pop("reconstruction_method", "GD"),
                                      r.pop("reconstruction_parameter", 1.0))
         return dict(method=method, a=a, b=b, c=c, **r)

@@ -33,7 +33,7 @@ def test_reconstruction_matches_reference(cuda, name):
     p = g.build(device="gpu")
     state = g.state(p)
     kw = g.oracle_kwargs()
-    p.reconstruct(progress_bar=False, **g.meta["reconstruct"])
+    p.reconstruct(progress_bar=False, **g.rec_kwargs())
 
     ref_err = g.out["error_iterations"]
     err = np.asarray(p.error_iterations)
