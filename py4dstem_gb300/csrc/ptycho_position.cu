@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(NT, 1) probe_spectrum_kernel(BatchArgs a) {
 
 // Everything of one scan position b (see the file header); the block's shared
 // memory holds the wave, the tables and the ramps. `red` is the block-sum scratch.
-template <int SX, int SY, int NT>
+template <int SX, int SY, int NT, bool kGd>
 __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, float* red) {
   using L = Layout<SX, SY>;
   constexpr int N = L::N;
@@ -116,8 +116,8 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
   float* itot = reinterpret_cast<float*>(rpy + SY);  // N floats, mixed only
 
   const int tid = threadIdx.x;
-  const int T = a.T;
-  const int M = a.M;
+  const int T = kGd ? 1 : a.T;
+  const int M = kGd ? 1 : a.M;
   const int prow = a.pos_rows ? a.pos_rows[b] : b;
   const int arow = a.amp_rows ? a.amp_rows[b] : b;
   const float posx = a.positions[2 * prow];
@@ -129,8 +129,8 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
   const int x0 = (int)rx;
   const int y0 = (int)ry;
   const float invN = 1.0f / (float)N;
-  const bool ps = a.projection != 0;
-  const bool fwd = a.forward_only != 0;  // per-position error only (block-uniform)
+  const bool ps = !kGd && a.projection != 0;
+  const bool fwd = !kGd && a.forward_only != 0;  // per-position error only (block-uniform)
   const float* amp = a.amplitudes + (size_t)arow * N;
 
   for (int i = tid; i < SX; i += NT) twx[i] = a.tw[i];  // tables from the spectrum kernel
@@ -191,7 +191,7 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
   // S_b^H (conj(O) chi) = IFFT2(conj(ramp) FFT2(conj(O) chi)). The reference's
   // update omits S_b^H; here the FFT2 and the conj(ramp) are applied per position
   // and the IFFT2 once to the batch sum. buf holds conj(O) chi on entry.
-  const bool exact = a.exact_probe_grad != 0;
+  const bool exact = !kGd && a.exact_probe_grad != 0;
   auto unshift_probe_term = [&](float2* dst) {
     fft2d<SX, SY, NT, -1>(buf, twx, twy);
     for (int e = tid; e < N; e += NT) {
@@ -208,7 +208,7 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
 
   if (T == 1) {
     // ------------------------------------------------------------ single slice
-    const bool mixed = M > 1 || a.mixed_formula;
+    const bool mixed = !kGd && (M > 1 || a.mixed_formula);
     for (int m = 0; m < M; ++m) {
       shifted_probe(m);
       float2* pst = a.st_probe + ((size_t)b * M + m) * N;  // stash P_m
@@ -263,7 +263,7 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
         const int e = tid + (c0 + i) * NT;
         const int idx = (e / SY) * LD + e % SY;
         float2 f = buf[idx];
-        if (a.keep_farfield) a.scratch_f[(size_t)b * N + e] = f;  // unmasked, for A16
+        if (!kGd && a.keep_farfield) a.scratch_f[(size_t)b * N + e] = f;  // unmasked, for A16
         const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
         if (a.det_mask) f = c_scale(f, mk);
         const float af = c_abs(f);
@@ -474,10 +474,10 @@ done:
 
 // One block per position. (A persistent form, one block per SM walking the
 // batch, measured 2% slower at 128 x 128 and was dropped.)
-template <int SX, int SY, int NT>
+template <int SX, int SY, int NT, bool kGd>
 __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
   __shared__ float red[NT / 32];
-  position_one<SX, SY, NT>(a, blockIdx.x, red);
+  position_one<SX, SY, NT, kGd>(a, blockIdx.x, red);
 }
 
 // Position correction of one batch (ptychographic_methods.py:2071-2225), run
@@ -753,14 +753,23 @@ cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
   const size_t smem = Layout<SX, SY>::smem_bytes(mixed);
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(position_kernel<SX, SY, NT>,
+    cudaError_t e = cudaFuncSetAttribute(position_kernel<SX, SY, NT, false>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)Layout<SX, SY>::smem_bytes(true));
     if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(position_kernel<SX, SY, NT, true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)Layout<SX, SY>::smem_bytes(false));
+    if (e != cudaSuccess) return e;
     configured = true;
   }
+  // the plain single-slice, single-probe gradient-descent batch has its own
+  // instantiation with the other modes compiled out (fewer live registers)
+  const bool plain = a.T == 1 && a.M == 1 && !a.mixed_formula && !a.projection &&
+                     !a.forward_only && !a.keep_farfield && !a.exact_probe_grad;
   timing_before(s);
-  position_kernel<SX, SY, NT><<<a.B, NT, smem, s>>>(a);
+  if (plain) position_kernel<SX, SY, NT, true><<<a.B, NT, smem, s>>>(a);
+  else position_kernel<SX, SY, NT, false><<<a.B, NT, smem, s>>>(a);
   cudaError_t e = cudaGetLastError();
   timing_after(s);
   return e;
