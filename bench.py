@@ -62,7 +62,7 @@ def parse_args(argv=None):
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
     ap.add_argument("--ref-cores", type=int, default=0,
                     help="reference arm: limit the worker processes (0 = all host cores)")
-    ap.add_argument("--workload", choices=["gd128", "multiscan"], default="gd128",
+    ap.add_argument("--workload", choices=["gd128", "multiscan", "multislice"], default="gd128",
                     help="gd128: the single-slice 128^2-detector workload (default); multiscan: "
                          "16 mixed-state scans of uneven sizes in one graph-captured launch")
     ap.add_argument("--scans", type=int, default=16, help="multiscan: number of scans")
@@ -589,12 +589,82 @@ def run_multiscan(args):
     return 0
 
 
+# ------------------------------------------------------------------ multislice
+def run_multislice(args):
+    """The multislice workload: 8 slices of 20 A, 64x64 scan at 0.4 A, 128^2
+    detector, 300 kV, 25 mrad, defocus 50 A, GD with batch 256; value = position
+    updates/s (one step = one full iteration, device-resident amplitudes)."""
+    rank, world, local = dist_env()
+    if world > 1:
+        print(json.dumps({"workload": "multislice", "unavailable": "single-GPU workload"}))
+        return 0
+    import torch
+
+    torch.cuda.set_device(local)
+    from py4dstem_gb300 import MultislicePtychography, engine, roofline, synthetic
+
+    c = synthetic.multislice_case(seed=3, num_slices=8, scan=64, backend="torch",
+                                  device=f"cuda:{local}", object_px=256)
+    p = MultislicePtychography(datacube=c.datacube, verbose=False, device="gpu",
+                               **c.ctor_kwargs)
+    p.preprocess(max_batch_size=256, **c.preprocess_kwargs)
+    J = p._num_diffraction_patterns
+    B = 256
+    st = engine.create_state(
+        roi_shape=tuple(p._region_of_interest_shape), object_array=np.asarray(p._object),
+        probe_array=p._probe, amplitudes=p._amplitudes, positions_px=p._positions_px,
+        num_slices=p._num_slices, num_probes=1, potential=False, max_batch=B, storage="gpu",
+        propagators=p._propagator_arrays,
+        fov_mask_inverse=p._object_fov_mask_inverse)
+    drv = engine.IterationDriver(st, max_batch=B, step_size=0.5, normalization_min=1.0,
+                                 use_mask=bool(p._object_fov_mask_inverse.sum() > 0),
+                                 mean_intensity=p._mean_diffraction_intensity)
+    rng = np.random.RandomState(3)
+    order = np.arange(J)
+
+    def step():
+        rng.shuffle(order)
+        drv.iterate(order)
+        drv.error()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        ev0.record()
+        for _ in range(args.steps):
+            step()
+        ev1.record()
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    n = 128 * 128
+    line = {
+        "metric": "position updates/s (multislice T=8, 128^2 det)",
+        "value": J * args.steps / (ms * 1e-3), "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "multislice", "slices": 8, "positions": J, "batch": B,
+                   "detector": 128, "object": list(np.shape(p._object))},
+        "flops_per_position": roofline.flops_per_position(n, num_slices=8),
+        "achieved_tflops": roofline.flops_per_position(n, num_slices=8) * J * args.steps
+        / (ms * 1e-3) / 1e12,
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main(argv=None):
     args = parse_args(argv)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "multiscan":
         return run_multiscan(args)
+    if args.workload == "multislice":
+        return run_multislice(args)
     return run_ours(args)
 
 

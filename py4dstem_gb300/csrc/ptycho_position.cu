@@ -102,8 +102,15 @@ __global__ void __launch_bounds__(NT, 1) probe_spectrum_kernel(BatchArgs a) {
 
 // Everything of one scan position b (see the file header); the block's shared
 // memory holds the wave, the tables and the ramps. `red` is the block-sum scratch.
-template <int SX, int SY, int NT, bool kGd>
+// kMode fixes at compile time what the batch is (fewer live registers, fewer
+// spills): 0 any, 1 single slice / single probe, 2 single-slice mixed state,
+// 3 multislice / single probe; modes 1-3 are gradient descent with no
+// projection sets, forward-only pass, kept far fields or exact probe gradient.
+template <int SX, int SY, int NT, int kMode>
 __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, float* red) {
+  constexpr bool kPlain = kMode != 0;
+  constexpr bool kT1 = kMode == 1 || kMode == 2;
+  constexpr bool kM1 = kMode == 1 || kMode == 3;
   using L = Layout<SX, SY>;
   constexpr int N = L::N;
   constexpr int LD = L::LD;
@@ -116,8 +123,8 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
   float* itot = reinterpret_cast<float*>(rpy + SY);  // N floats, mixed only
 
   const int tid = threadIdx.x;
-  const int T = kGd ? 1 : a.T;
-  const int M = kGd ? 1 : a.M;
+  const int T = kT1 ? 1 : a.T;
+  const int M = kM1 ? 1 : a.M;
   const int prow = a.pos_rows ? a.pos_rows[b] : b;
   const int arow = a.amp_rows ? a.amp_rows[b] : b;
   const float posx = a.positions[2 * prow];
@@ -129,8 +136,8 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
   const int x0 = (int)rx;
   const int y0 = (int)ry;
   const float invN = 1.0f / (float)N;
-  const bool ps = !kGd && a.projection != 0;
-  const bool fwd = !kGd && a.forward_only != 0;  // per-position error only (block-uniform)
+  const bool ps = !kPlain && a.projection != 0;
+  const bool fwd = !kPlain && a.forward_only != 0;  // per-position error only (block-uniform)
   const float* amp = a.amplitudes + (size_t)arow * N;
 
   for (int i = tid; i < SX; i += NT) twx[i] = a.tw[i];  // tables from the spectrum kernel
@@ -191,7 +198,7 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
   // S_b^H (conj(O) chi) = IFFT2(conj(ramp) FFT2(conj(O) chi)). The reference's
   // update omits S_b^H; here the FFT2 and the conj(ramp) are applied per position
   // and the IFFT2 once to the batch sum. buf holds conj(O) chi on entry.
-  const bool exact = !kGd && a.exact_probe_grad != 0;
+  const bool exact = !kPlain && a.exact_probe_grad != 0;
   auto unshift_probe_term = [&](float2* dst) {
     fft2d<SX, SY, NT, -1>(buf, twx, twy);
     for (int e = tid; e < N; e += NT) {
@@ -208,7 +215,7 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
 
   if (T == 1) {
     // ------------------------------------------------------------ single slice
-    const bool mixed = !kGd && (M > 1 || a.mixed_formula);
+    const bool mixed = kMode == 2 || (kMode == 0 && (M > 1 || a.mixed_formula));
     for (int m = 0; m < M; ++m) {
       shifted_probe(m);
       float2* pst = a.st_probe + ((size_t)b * M + m) * N;  // stash P_m
@@ -263,7 +270,7 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
         const int e = tid + (c0 + i) * NT;
         const int idx = (e / SY) * LD + e % SY;
         float2 f = buf[idx];
-        if (!kGd && a.keep_farfield) a.scratch_f[(size_t)b * N + e] = f;  // unmasked, for A16
+        if (!kPlain && a.keep_farfield) a.scratch_f[(size_t)b * N + e] = f;  // unmasked, for A16
         const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
         if (a.det_mask) f = c_scale(f, mk);
         const float af = c_abs(f);
@@ -474,10 +481,10 @@ done:
 
 // One block per position. (A persistent form, one block per SM walking the
 // batch, measured 2% slower at 128 x 128 and was dropped.)
-template <int SX, int SY, int NT, bool kGd>
+template <int SX, int SY, int NT, int kMode>
 __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
   __shared__ float red[NT / 32];
-  position_one<SX, SY, NT, kGd>(a, blockIdx.x, red);
+  position_one<SX, SY, NT, kMode>(a, blockIdx.x, red);
 }
 
 // Position correction of one batch (ptychographic_methods.py:2071-2225), run
@@ -753,23 +760,28 @@ cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
   const size_t smem = Layout<SX, SY>::smem_bytes(mixed);
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(position_kernel<SX, SY, NT, false>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)Layout<SX, SY>::smem_bytes(true));
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(position_kernel<SX, SY, NT, true>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)Layout<SX, SY>::smem_bytes(false));
+    const int bytes = (int)Layout<SX, SY>::smem_bytes(true);
+    const cudaFuncAttribute attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t e = cudaFuncSetAttribute(position_kernel<SX, SY, NT, 0>, attr, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(position_kernel<SX, SY, NT, 1>, attr, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(position_kernel<SX, SY, NT, 2>, attr, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(position_kernel<SX, SY, NT, 3>, attr, bytes);
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  // the plain single-slice, single-probe gradient-descent batch has its own
-  // instantiation with the other modes compiled out (fewer live registers)
-  const bool plain = a.T == 1 && a.M == 1 && !a.mixed_formula && !a.projection &&
-                     !a.forward_only && !a.keep_farfield && !a.exact_probe_grad;
+  // plain gradient-descent batches run an instantiation with the other modes
+  // compiled out (see position_one)
+  const bool plain = !a.projection && !a.forward_only && !a.keep_farfield && !a.exact_probe_grad;
+  const int mode = !plain ? 0
+                   : a.T == 1 ? (a.M == 1 && !a.mixed_formula ? 1 : 2)
+                   : (a.M == 1 ? 3 : 0);
   timing_before(s);
-  if (plain) position_kernel<SX, SY, NT, true><<<a.B, NT, smem, s>>>(a);
-  else position_kernel<SX, SY, NT, false><<<a.B, NT, smem, s>>>(a);
+  switch (mode) {
+    case 1: position_kernel<SX, SY, NT, 1><<<a.B, NT, smem, s>>>(a); break;
+    case 2: position_kernel<SX, SY, NT, 2><<<a.B, NT, smem, s>>>(a); break;
+    case 3: position_kernel<SX, SY, NT, 3><<<a.B, NT, smem, s>>>(a); break;
+    default: position_kernel<SX, SY, NT, 0><<<a.B, NT, smem, s>>>(a); break;
+  }
   cudaError_t e = cudaGetLastError();
   timing_after(s);
   return e;
