@@ -456,7 +456,7 @@ def run_ours(args):
     from py4dstem_gb300 import roofline as _rl
 
     bound_name, _ = _rl.bound(flops_pos, bytes_pos, fp32_peak or 77.0, hbm_peak)
-    kernel_name = ("gd128_kernel" if args.schedule == 2 else "position_kernel<128,128,1024>")
+    kernel_name = ("gd128_kernel" if args.schedule == 2 else "position_kernel<128,128,1024,1>")
     if bound_name == "hbm":
         roof = {"bound": "hbm", "achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": hbm_achieved / hbm_peak, "peak_source": hbm_source + ", of measured"}
