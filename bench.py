@@ -407,9 +407,11 @@ def run_ours(args):
     order = np.arange(J)
     errors = []
 
+    np.random.shuffle(order)
+
     def step():
-        np.random.shuffle(order)
         drv.iterate(order)
+        np.random.shuffle(order)  # the next iteration's order, while the GPU works
         errors.append(float(drv.error()))  # per-iteration read-back, as the reference
 
     for _ in range(args.warmup):
@@ -622,9 +624,11 @@ def run_multislice(args):
     rng = np.random.RandomState(3)
     order = np.arange(J)
 
+    rng.shuffle(order)
+
     def step():
-        rng.shuffle(order)
         drv.iterate(order)
+        rng.shuffle(order)
         drv.error()
 
     for _ in range(args.warmup):

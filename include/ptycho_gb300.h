@@ -65,6 +65,16 @@ typedef struct ptycho_geometry {
  * in the workspace for a following ptycho_position_correction() call. */
 #define PTYCHO_FLAG_KEEP_FARFIELD 2
 
+/* Batch chaining within one iteration (batch calls on one workspace and stream):
+ * PTYCHO_FLAG_PREPARE_SPECTRUM: after the probe update, compute the spectrum of
+ * the updated probe into the workspace (on the helper stream, concurrently with
+ * the object update) for the next batch call;
+ * PTYCHO_FLAG_SPECTRUM_READY: the workspace already holds the spectrum of the
+ * current probe (prepared by the previous batch call, or the probe is fixed),
+ * so the call skips its own. The probe must not change in between. */
+#define PTYCHO_FLAG_SPECTRUM_READY 4
+#define PTYCHO_FLAG_PREPARE_SPECTRUM 8
+
 /* Library identity and capability queries. */
 int ptycho_abi_version(void);
 const char* ptycho_last_error(void);

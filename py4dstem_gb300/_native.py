@@ -15,6 +15,8 @@ from . import build as _build
 PTYCHO_OK = 0
 FLAG_MIXED_STATE = 1
 FLAG_KEEP_FARFIELD = 2
+FLAG_SPECTRUM_READY = 4
+FLAG_PREPARE_SPECTRUM = 8
 _STATUS_NAMES = {
     1: "invalid argument",
     2: "unsupported geometry",

@@ -51,7 +51,8 @@ cudaEvent_t take_event() {
 
 int check_geometry(const ptycho_geometry* g) {
   if (!g) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "geometry is null");
-  if ((g->flags & ~(PTYCHO_FLAG_MIXED_STATE | PTYCHO_FLAG_KEEP_FARFIELD)) != 0)
+  if ((g->flags & ~(PTYCHO_FLAG_MIXED_STATE | PTYCHO_FLAG_KEEP_FARFIELD |
+                    PTYCHO_FLAG_SPECTRUM_READY | PTYCHO_FLAG_PREPARE_SPECTRUM)) != 0)
     return fail(PTYCHO_ERR_INVALID_ARGUMENT, "unknown bits in geometry.flags (0x%x)", g->flags);
   if (g->num_slices < 1 || g->num_probes < 1)
     return fail(PTYCHO_ERR_INVALID_ARGUMENT, "num_slices and num_probes must be >= 1");
@@ -221,8 +222,10 @@ static int run_batch(const ptycho_geometry* g, void* object, void* probe,
   a.props = static_cast<const float2*>(propagators);
   a.error_accum = error_accum;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e = launch_probe_spectrum(a, s);
+  cudaError_t e = cudaSuccess;
+  if (!(g->flags & PTYCHO_FLAG_SPECTRUM_READY)) e = launch_probe_spectrum(a, s);
   if (e != cudaSuccess) return cuda_fail(e, "probe spectrum kernel");
+  a.prepare_spectrum = (g->flags & PTYCHO_FLAG_PREPARE_SPECTRUM) && !a.fix_probe ? 1 : 0;
   a.staging_t = position_v2_eligible(a) ? 1 : 0;
   e = a.staging_t ? launch_position_v2(a, s) : launch_position_kernel(a, s);
   if (e != cudaSuccess) return cuda_fail(e, "position kernel");

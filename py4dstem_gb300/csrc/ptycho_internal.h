@@ -27,6 +27,7 @@ struct BatchArgs {
   int forward_only;        // forward model and per-position error only, no adjoint
   int keep_farfield;       // single slice: keep FFT2(psi_m) of each position in scratch_f
   int exact_probe_grad;    // probe term through the adjoint of the sub-pixel shift
+  int prepare_spectrum;    // after the probe update, the next batch's probe spectrum
 
   void* object;                 // (T,Px,Py) float2 or float
   float2* probe;                // (M,N)

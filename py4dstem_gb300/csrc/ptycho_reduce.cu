@@ -757,6 +757,8 @@ cudaError_t launch_reduce_and_update(const BatchArgs& a, cudaStream_t s) {
     probe_finalize_kernel<<<nb, NT, 0, fj.side>>>(a);
     probe_update_kernel<<<nb, NT, 0, fj.side>>>(a, nb);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // the next batch's spectrum of the updated probe, off the critical path
+    if (a.prepare_spectrum && (e = launch_probe_spectrum(a, fj.side)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(fj.join, fj.side)) != cudaSuccess) return e;
   }
   object_reduce_kernel<<<dim3(ntiles, a.T, kObjSplit), NT, 0, s>>>(a);

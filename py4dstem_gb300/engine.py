@@ -64,6 +64,9 @@ class DeviceState:
     amp_pinned: object = None     # two pinned host batch buffers (double-buffered)
     amp_events: object = None     # copy-done events of the pinned buffers
     amp_turn: int = 0
+    order_pinned: object = None   # two pinned host buffers for the per-iteration order
+    order_events: object = None
+    order_turn: int = 0
     gram: object = None
     probe_tmp: object = None
     coeffs: object = None
@@ -282,12 +285,44 @@ def run_iteration(st: DeviceState, host_order: Optional[np.ndarray], max_batch: 
                              "page-locked amplitudes")
         n = int(st.positions.shape[0])
     else:
-        st.order.copy_(torch.from_numpy(np.ascontiguousarray(host_order, dtype=np.int32)),
-                       non_blocking=False)
+        # the order goes through one of two pinned buffers and an asynchronous copy
+        # on the stream: the call returns at once and the caller may reuse (shuffle)
+        # its array while the GPU still works on the previous iteration
         n = int(host_order.shape[0])
+        if st.order_pinned is None:
+            cap = int(st.order.shape[0])
+            st.order_pinned = [torch.empty(cap, dtype=torch.int32, pin_memory=True)
+                               for _ in range(2)]
+            st.order_events = [None, None]
+        k = st.order_turn
+        st.order_turn ^= 1
+        if st.order_events[k] is not None:
+            st.order_events[k].synchronize()  # the copy out of this buffer has run
+        st.order_pinned[k].numpy()[:n] = host_order
+        st.order[:n].copy_(st.order_pinned[k][:n], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record()
+        st.order_events[k] = ev
     st.error_accum.zero_()
-    for start, end in generate_batches(n, max_batch):
-        run_batch(st, start, end, host_order, **kw)
+    # batch chaining: each batch computes the next batch's probe spectrum right
+    # after its probe update (concurrently with the object update); with a fixed
+    # probe the first batch's spectrum serves them all. Position correction reads
+    # the batch's own spectrum after the update, so it does not chain.
+    batches = list(generate_batches(n, max_batch))
+    fixed = bool(kw.get("fix_probe"))
+    chain = not fixed and kw.get("position_correction") is None
+    base = st.geometry.flags & ~(_native.FLAG_SPECTRUM_READY | _native.FLAG_PREPARE_SPECTRUM)
+    try:
+        for i, (start, end) in enumerate(batches):
+            flags = base
+            if i > 0 and (chain or fixed):
+                flags |= _native.FLAG_SPECTRUM_READY
+            if chain and i + 1 < len(batches):
+                flags |= _native.FLAG_PREPARE_SPECTRUM
+            st.geometry.flags = flags
+            run_batch(st, start, end, host_order, **kw)
+    finally:
+        st.geometry.flags = base
     if kw.get("projection"):
         st.exit_waves_valid = True
 

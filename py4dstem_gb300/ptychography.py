@@ -440,10 +440,14 @@ class _PtychographyBase(PreprocessMixin):
                 # (singleslice_ptychography.py:956, ptychographic_constraints.py:1355-1377)
                 center_of_mass=not fix_positions_com) if correct_positions else None))
         error = np.float32(0.0)
-        for _ in range(num_iter):
-            if not use_projection:
-                np.random.shuffle(shuffled)
+        if num_iter > 0 and not use_projection:
+            np.random.shuffle(shuffled)
+        for it in range(num_iter):
             driver.iterate(shuffled)
+            # the next iteration's shuffle (same global-RNG sequence as the
+            # reference) runs on the host while the GPU works on this one
+            if it + 1 < num_iter and not use_projection:
+                np.random.shuffle(shuffled)
             error = driver.error()
             self.error_iterations.append(error.item())
             if store_iterations:

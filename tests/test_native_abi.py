@@ -94,7 +94,7 @@ def test_rejects_bad_batch_and_workspace(lib):
 
 def test_rejects_unknown_flags(lib):
     g = geometry()
-    g.flags = 4
+    g.flags = 16
     assert _gd(lib, g) == 1
     assert b"flags" in lib.ptycho_last_error()
 
