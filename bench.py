@@ -399,30 +399,28 @@ def run_ours(args):
         probe_array=p._probe, amplitudes=p._amplitudes, positions_px=p._positions_px,
         num_slices=1, num_probes=1, potential=False, max_batch=B, storage="gpu",
         fov_mask_inverse=p._object_fov_mask_inverse)
-    drv = engine.IterationDriver(
-        st, max_batch=B, step_size=0.5, normalization_min=1.0,
-        use_mask=bool(p._object_fov_mask_inverse.sum() > 0),
-        mean_intensity=p._mean_diffraction_intensity)
+    driver_kw = dict(max_batch=B, step_size=0.5, normalization_min=1.0,
+                     use_mask=bool(p._object_fov_mask_inverse.sum() > 0),
+                     mean_intensity=p._mean_diffraction_intensity)
+    # each iteration replays one CUDA graph of all its kernels (captured during
+    # the warm-up)
+    drv = engine.IterationDriver(st, graph=True, **driver_kw)
     np.random.seed(seed)
     order = np.arange(J)
     errors = []
 
     np.random.shuffle(order)
 
-    def step():
-        drv.iterate(order)
+    def step(d=drv):
+        d.iterate(order)
         np.random.shuffle(order)  # the next iteration's order, while the GPU works
-        errors.append(float(drv.error()))  # per-iteration read-back, as the reference
+        errors.append(float(d.error()))  # per-iteration read-back, as the reference
 
-    for _ in range(args.warmup):
+    for _ in range(max(args.warmup, 2)):
         step()
     torch.cuda.synchronize()
-    lib.ptycho_enable_kernel_timing(1)
     import ctypes
 
-    ms_dummy = ctypes.c_float()
-    n_dummy = ctypes.c_int32()
-    lib.ptycho_kernel_timing(ctypes.byref(ms_dummy), ctypes.byref(n_dummy))  # clear
     launches0 = st.launches
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
@@ -439,6 +437,16 @@ def run_ours(args):
     dev_ms = ev0.elapsed_time(ev1)
     ms = reduce_max(dev_ms)
     launches = st.launches - launches0
+    # position-kernel time: CUDA events around each launch, in two more
+    # iterations issued without the graph (outside the timed region)
+    ms_dummy = ctypes.c_float()
+    n_dummy = ctypes.c_int32()
+    lib.ptycho_kernel_timing(ctypes.byref(ms_dummy), ctypes.byref(n_dummy))  # clear
+    lib.ptycho_enable_kernel_timing(1)
+    drv_t = engine.IterationDriver(st, graph=False, **driver_kw)
+    for _ in range(2):
+        step(drv_t)
+    torch.cuda.synchronize()
     lib.ptycho_enable_kernel_timing(0)
     kms = ctypes.c_float()
     kn = ctypes.c_int32()

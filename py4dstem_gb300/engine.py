@@ -272,6 +272,28 @@ def self_consistency_errors(st: DeviceState, max_batch: int) -> np.ndarray:
     return out.cpu().numpy()
 
 
+def upload_order(st: DeviceState, host_order: np.ndarray) -> None:
+    """Copy the iteration's position order to the device through one of two pinned
+    buffers and an asynchronous copy on the current stream: the call returns at
+    once and the caller may reuse (shuffle) its array while the GPU still works."""
+    torch = _torch()
+    n = int(host_order.shape[0])
+    if st.order_pinned is None:
+        cap = int(st.order.shape[0])
+        st.order_pinned = [torch.empty(cap, dtype=torch.int32, pin_memory=True)
+                           for _ in range(2)]
+        st.order_events = [None, None]
+    k = st.order_turn
+    st.order_turn ^= 1
+    if st.order_events[k] is not None:
+        st.order_events[k].synchronize()  # the copy out of this buffer has run
+    st.order_pinned[k].numpy()[:n] = host_order
+    st.order[:n].copy_(st.order_pinned[k][:n], non_blocking=True)
+    ev = torch.cuda.Event()
+    ev.record()
+    st.order_events[k] = ev
+
+
 def run_iteration(st: DeviceState, host_order: Optional[np.ndarray], max_batch: int,
                   **kw) -> None:
     """One pass over all positions in `host_order` (already shuffled), batch by batch.
@@ -285,24 +307,8 @@ def run_iteration(st: DeviceState, host_order: Optional[np.ndarray], max_batch: 
                              "page-locked amplitudes")
         n = int(st.positions.shape[0])
     else:
-        # the order goes through one of two pinned buffers and an asynchronous copy
-        # on the stream: the call returns at once and the caller may reuse (shuffle)
-        # its array while the GPU still works on the previous iteration
         n = int(host_order.shape[0])
-        if st.order_pinned is None:
-            cap = int(st.order.shape[0])
-            st.order_pinned = [torch.empty(cap, dtype=torch.int32, pin_memory=True)
-                               for _ in range(2)]
-            st.order_events = [None, None]
-        k = st.order_turn
-        st.order_turn ^= 1
-        if st.order_events[k] is not None:
-            st.order_events[k].synchronize()  # the copy out of this buffer has run
-        st.order_pinned[k].numpy()[:n] = host_order
-        st.order[:n].copy_(st.order_pinned[k][:n], non_blocking=True)
-        ev = torch.cuda.Event()
-        ev.record()
-        st.order_events[k] = ev
+        upload_order(st, host_order)
     st.error_accum.zero_()
     # batch chaining: each batch computes the next batch's probe spectrum right
     # after its probe update (concurrently with the object update); with a fixed
@@ -390,9 +396,12 @@ class IterationDriver:
                  normalization_min=1.0, fix_probe=False, projection_abc=(0.0, 0.0, 0.0),
                  shrinkage_rad=0.0, use_mask=False, pure_phase=False, positivity=True,
                  fix_probe_com=True, orthogonalize_probe=False, mean_intensity=1.0,
-                 position_correction=None, device_orthogonalization=False):
+                 position_correction=None, device_orthogonalization=False,
+                 graph=False):
         self.st = st
         self.device_orthogonalization = bool(device_orthogonalization)
+        self.graph = None
+        self.calls = 0
         self.max_batch = int(max_batch)
         if position_correction is not None and st.positions_initial is None:
             raise ValueError("position correction needs a state created with positions_initial")
@@ -410,11 +419,52 @@ class IterationDriver:
         self.mixed_state = bool(st.geometry.flags & _native.FLAG_MIXED_STATE)
         J = int(st.positions.shape[0])
         self.norm = np.float32(mean_intensity) * J
+        # CUDA-graph replay of whole iterations: every kernel of an iteration in
+        # one launch. Needs device-resident or page-locked amplitudes and, for
+        # mixed states, the device eigen-decomposition (no host step inside).
+        self.use_graph = bool(graph) and (st.amplitudes is not None or st.amp_mapped is not None) \
+            and (not self.orthogonalize or self.device_orthogonalization)
+
+    def _issue(self) -> None:
+        st = self.st
+        run_iteration(st, None, self.max_batch, **self.batch_kw)
+        self._constraints()
 
     def iterate(self, order: Optional[np.ndarray]) -> None:
         """One iteration; order=None takes the order already in st.order."""
         st = self.st
+        self.calls += 1
+        if self.use_graph and order is not None:
+            torch = _torch()
+            upload_order(st, order)
+            if self.graph is None and self.calls >= 2:
+                # the first iteration ran eagerly (library set-up for the stream);
+                # capture the second on a side stream, then replay it from now on
+                side = torch.cuda.Stream()
+                _native.check(_native.lib().ptycho_prepare_stream(
+                    ctypes.c_void_p(side.cuda_stream)))
+                side.wait_stream(torch.cuda.current_stream())
+                g = torch.cuda.CUDAGraph()
+                before = st.launches
+                with torch.cuda.graph(g, stream=side):
+                    self._issue()
+                torch.cuda.current_stream().wait_stream(side)
+                self.graph = g
+                self.graph_launches = st.launches - before
+                st.launches -= self.graph_launches  # counted again at each replay
+            if self.graph is not None:
+                self.graph.replay()
+                st.launches += self.graph_launches
+            else:
+                self._issue()
+            if self.batch_kw.get("projection"):
+                st.exit_waves_valid = True
+            return
         run_iteration(st, order, self.max_batch, **self.batch_kw)
+        self._constraints()
+
+    def _constraints(self) -> None:
+        st = self.st
         object_constraints(st, shrinkage_rad=self.shrinkage_rad, use_mask=self.use_mask,
                            pure_phase=self.pure_phase, positivity=self.positivity)
         if self.fix_probe_com:

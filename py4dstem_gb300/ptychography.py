@@ -133,6 +133,8 @@ class _PtychographyBase(PreprocessMixin):
         if storage not in ("cpu", "gpu"):
             raise ValueError(f"storage must be either 'cpu' or 'gpu', not {storage}")
         self._storage = storage
+        # replay each iteration from one captured CUDA graph (eager issue when False)
+        self._graph_iterations = True
         return self
 
     def set_save_defaults(self, save_datacube=False, save_exit_waves=False,
@@ -431,7 +433,7 @@ class _PtychographyBase(PreprocessMixin):
             pure_phase=pure_phase_object and self._object_type == "complex",
             positivity=object_positivity, fix_probe_com=fix_probe_com,
             orthogonalize_probe=orthogonalize_probe,
-            mean_intensity=self._mean_diffraction_intensity,
+            mean_intensity=self._mean_diffraction_intensity, graph=self._graph_iterations,
             position_correction=(dict(
                 step_size=positions_step_size,
                 max_update_px=self._distance_px(max_position_update_distance),
