@@ -55,6 +55,10 @@ def parse_args(argv=None):
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-preprocess-timing", action="store_true",
+                    help="skip the device / host preprocess() timing")
+    ap.add_argument("--preprocess-host-patterns", type=int, default=2048,
+                    help="patterns in the host preprocess() timing sample")
     ap.add_argument("--scan", type=int, default=128, help="scan side (positions = scan^2)")
     ap.add_argument("--batch", type=int, default=1024)
     ap.add_argument("--no-e2e", action="store_true")
@@ -199,14 +203,54 @@ def build_case(scan, seed, device):
     return case
 
 
-def preprocess(case, storage):
+def preprocess(case, storage, device="gpu"):
     from py4dstem_gb300 import SingleslicePtychography
 
     kw = dict(case.ctor_kwargs)
-    p = SingleslicePtychography(datacube=case.datacube, verbose=False, device="gpu",
+    p = SingleslicePtychography(datacube=case.datacube, verbose=False, device=device,
                                 storage=storage, **kw)
     p.preprocess(max_batch_size=1024, **case.preprocess_kwargs)
     return p
+
+
+def preprocess_timing(case, host_patterns):
+    """preprocess() with the rotation search (no forced rotation): on the device
+    for the whole scan (wall time, synchronised; the library is already loaded),
+    and the host NumPy path (device="cpu") on the first scan rows holding about
+    `host_patterns` patterns, scaled to the whole scan by the pattern count."""
+    import torch
+
+    from py4dstem_gb300 import DataCube, SingleslicePtychography
+
+    pre_kw = {k: v for k, v in case.preprocess_kwargs.items()
+              if k not in ("force_com_rotation", "force_com_transpose")}
+    kw = dict(case.ctor_kwargs)
+
+    def run(datacube, positions, device):
+        c = dict(kw, initial_scan_positions=positions)
+        p = SingleslicePtychography(datacube=datacube, verbose=False, device=device,
+                                    storage="gpu" if device == "gpu" else "cpu", **c)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        p.preprocess(max_batch_size=1024, **pre_kw)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
+
+    data = case.datacube.data
+    rx, ry = data.shape[:2]
+    J = rx * ry
+    dev_s = run(case.datacube, case.scan_positions_ang, "gpu")
+    rows = max(3, min(rx, host_patterns // ry))
+    sub = DataCube(np.ascontiguousarray(data[:rows]), r_pixel_size=case.datacube.calibration
+                   .get_R_pixel_size(), r_pixel_units="A",
+                   q_pixel_size=case.datacube.calibration.get_Q_pixel_size(), q_pixel_units="mrad")
+    n_host = rows * ry
+    host_s = run(sub, case.scan_positions_ang[:n_host], "cpu")
+    return {"device_s": dev_s, "patterns": J, "host_sample_s": host_s,
+            "host_sample_patterns": n_host, "host_s_scaled": host_s * J / n_host,
+            "speedup_vs_host_scaled": host_s * J / n_host / dev_s,
+            "steps": "intensities upload, centre of mass, plane fit, rotation search "
+                     "(179 angles x 2), corner-centring + sqrt, probe, probe overlap + FOV mask"}
 
 
 def fp32_peak_tflops(torch, lib):
@@ -287,7 +331,7 @@ def _ref_init(scan, seed):
     case = synthetic.make_scan("ref", seed, (scan, scan), 0.75, 0.05, 128,
                                int(2 ** math.ceil(math.log2(scan * 3 + 128))), dose=1e5,
                                backend="numpy")
-    p = preprocess(case, storage="cpu")
+    p = preprocess(case, storage="cpu", device="cpu")  # host NumPy preprocess
     st = State(amplitudes=p._amplitudes, positions_px=p._positions_px.copy(),
                probe=np.array(p._probe), object=np.array(p._object),
                mean_intensity=p._mean_diffraction_intensity,
@@ -383,6 +427,9 @@ def run_ours(args):
     case = build_case(args.scan, seed, f"cuda:{local}")
     p = preprocess(case, storage="gpu")
     setup_s = time.time() - t_setup
+    pre_timing = None
+    if rank == 0 and world == 1 and not args.no_preprocess_timing:
+        pre_timing = preprocess_timing(case, args.preprocess_host_patterns)
 
     # CPU baseline on rank 0 at N=1 only, before any timing (single core)
     cpu = None
@@ -396,7 +443,8 @@ def run_ours(args):
     B = min(args.batch, J)
     st = engine.create_state(
         roi_shape=tuple(p._region_of_interest_shape), object_array=np.asarray(p._object),
-        probe_array=p._probe, amplitudes=p._amplitudes, positions_px=p._positions_px,
+        probe_array=p._probe, amplitudes=p._amplitudes_for_state(),
+        positions_px=p._positions_px,
         num_slices=1, num_probes=1, potential=False, max_batch=B, storage="gpu",
         fov_mask_inverse=p._object_fov_mask_inverse)
     driver_kw = dict(max_batch=B, step_size=0.5, normalization_min=1.0,
@@ -525,6 +573,7 @@ def run_ours(args):
             "clocks": clocks.summary(),
             "final_error": errors[-1] if errors else None,
             "setup_s": setup_s,
+            "preprocess": pre_timing,
             "wall_ms_timed": wall_ms,
         }
         print(json.dumps(line), flush=True)

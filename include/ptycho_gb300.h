@@ -238,6 +238,66 @@ int ptycho_probe_orthogonalize(const ptycho_geometry* geometry, void* probe, voi
                                size_t workspace_bytes, void* stream);
 
 /*
+ * Preprocessing (one-time, before the reconstruction loop). Sums follow the
+ * order of NumPy's float32 pairwise add.reduce over each contiguous run, and
+ * products and quotients are rounded once each, so the results carry the bits
+ * of the reference's float32 NumPy evaluation of the same inputs.
+ */
+
+/*
+ * Intensity centre of mass of each (qx, qy) pattern of `intensities`
+ * (num_patterns, qx, qy) float32: com_x = sum(I kx)/sum(I), com_y = sum(I ky)/sum(I)
+ * with kx, ky the pixel indices and I = pattern * mask (mask (qx, qy) float32
+ * or NULL). Replaces the vectorised centre of mass of
+ * _calculate_intensities_center_of_mass (phase_base_class.py:613-700).
+ * qx * qy <= 40000.
+ */
+int ptycho_pattern_com(const float* intensities, int32_t num_patterns, int32_t qx, int32_t qy,
+                       const float* mask, float* com_x, float* com_y, void* stream);
+
+/*
+ * Rotation search of the real/reciprocal-space rotation: for every angle a
+ * (cos_angles[a], sin_angles[a], float32) and t = 0 (as is) / 1 (x and y
+ * exchanged), values[t * num_angles + a] = the mean over the scan interior of
+ * |curl| (or |div| when maximize_divergence) of the centre-of-mass field
+ * (com_x, com_y) (scan_x, scan_y) rotated by that angle. The caller takes the
+ * arg-min (arg-max) exactly as _solve_for_center_of_mass_relative_rotation
+ * (phase_base_class.py:1086-1182) does.
+ */
+int ptycho_rotation_search(const float* com_x, const float* com_y, int32_t scan_x,
+                           int32_t scan_y, const float* cos_angles, const float* sin_angles,
+                           int32_t num_angles, int32_t maximize_divergence, float* values,
+                           void* stream);
+
+/*
+ * Corner-centring and square root: output pattern o takes source pattern
+ * rows[o] (rows NULL: pattern o), shifts it periodically and bilinearly by
+ * (-com_fitted_x[rows[o]], -com_fitted_y[rows[o]]), writes the sum of the
+ * shifted pattern to pattern_sums[o] and sqrt(max(shifted, 0)) to amplitudes
+ * (num_out, qx, qy), or, with crop_w > 0, its four crop_w x crop_w corners as a
+ * (2 crop_w, 2 crop_w) pattern. The mean diffraction intensity is the float32
+ * running sum of pattern_sums in order, divided by num_out. Replaces
+ * _normalize_diffraction_intensities (phase_base_class.py:1347-1460).
+ * qx * qy <= 20000.
+ */
+int ptycho_normalize_patterns(const float* intensities, int32_t qx, int32_t qy,
+                              const int32_t* rows, int32_t num_out, const float* com_fitted_x,
+                              const float* com_fitted_y, int32_t crop_w, float* amplitudes,
+                              float* pattern_sums, void* stream);
+
+/*
+ * Probe-overlap map: overlap (Px, Py) float32 = sum over all positions of
+ * |P shifted to the position|^2 scattered into the object grid (probe mode 0,
+ * positions in batches of at most max_batch, near-equal sizes, the larger
+ * first). The map the preprocessing blurs and thresholds into the object
+ * field-of-view mask (singleslice_ptychography.py:504-540). Uses the workspace
+ * of ptycho_workspace_bytes(geometry, max_batch).
+ */
+int ptycho_probe_overlap(const ptycho_geometry* geometry, const void* probe,
+                         const float* positions_px, int32_t num_positions, int32_t max_batch,
+                         float* overlap, void* workspace, size_t workspace_bytes, void* stream);
+
+/*
  * *device = the device address of host memory [host, host + bytes) when that
  * range is page-locked and mapped (the GPU then reads it in place, over the
  * CPU-GPU link), else NULL. Lets a caller pass host-resident amplitudes to the

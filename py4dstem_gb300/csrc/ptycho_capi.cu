@@ -536,6 +536,103 @@ int ptycho_probe_mix(const ptycho_geometry* g, const void* probe_in, const void*
   return PTYCHO_OK;
 }
 
+// ----------------------------------------------------------------- preprocess
+int ptycho_pattern_com(const float* intensities, int32_t num_patterns, int32_t qx, int32_t qy,
+                       const float* mask, float* com_x, float* com_y, void* stream) {
+  if (!intensities || !com_x || !com_y)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "intensities, com_x and com_y must be non-null");
+  if (num_patterns < 0 || qx < 1 || qy < 1)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "bad pattern count or shape (%d, %d x %d)",
+                num_patterns, qx, qy);
+  if (num_patterns == 0) return PTYCHO_OK;
+  cudaError_t e = launch_pattern_com(intensities, num_patterns, qx, qy, mask, com_x, com_y,
+                                     static_cast<cudaStream_t>(stream));
+  if (e == cudaErrorInvalidValue)
+    return fail(PTYCHO_ERR_UNSUPPORTED, "%d x %d patterns do not fit one block's shared memory",
+                qx, qy);
+  if (e != cudaSuccess) return cuda_fail(e, "pattern centre-of-mass kernel");
+  return PTYCHO_OK;
+}
+
+int ptycho_rotation_search(const float* com_x, const float* com_y, int32_t scan_x,
+                           int32_t scan_y, const float* cos_angles, const float* sin_angles,
+                           int32_t num_angles, int32_t maximize_divergence, float* values,
+                           void* stream) {
+  if (!com_x || !com_y || !cos_angles || !sin_angles || !values)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "null pointer argument");
+  if (scan_x < 3 || scan_y < 3 || num_angles < 1)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT,
+                "the rotation search needs a scan of at least 3 x 3 and one angle "
+                "(got %d x %d, %d angles)", scan_x, scan_y, num_angles);
+  cudaError_t e = launch_rotation_search(com_x, com_y, scan_x, scan_y, cos_angles, sin_angles,
+                                         num_angles, maximize_divergence ? 1 : 0, values,
+                                         static_cast<cudaStream_t>(stream));
+  if (e == cudaErrorInvalidValue)
+    return fail(PTYCHO_ERR_UNSUPPORTED, "a %d x %d scan is too large for the rotation search",
+                scan_x, scan_y);
+  if (e != cudaSuccess) return cuda_fail(e, "rotation search kernel");
+  return PTYCHO_OK;
+}
+
+int ptycho_normalize_patterns(const float* intensities, int32_t qx, int32_t qy,
+                              const int32_t* rows, int32_t num_out, const float* com_fitted_x,
+                              const float* com_fitted_y, int32_t crop_w, float* amplitudes,
+                              float* pattern_sums, void* stream) {
+  if (!intensities || !com_fitted_x || !com_fitted_y || !amplitudes || !pattern_sums)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "null pointer argument");
+  if (num_out < 0 || qx < 1 || qy < 1)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "bad pattern count or shape (%d, %d x %d)",
+                num_out, qx, qy);
+  if (crop_w < 0 || 2 * crop_w > qx || 2 * crop_w > qy)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "crop width %d does not fit %d x %d patterns",
+                crop_w, qx, qy);
+  if (num_out == 0) return PTYCHO_OK;
+  cudaError_t e = launch_pattern_normalize(intensities, qx, qy, rows, num_out, com_fitted_x,
+                                           com_fitted_y, crop_w, amplitudes, pattern_sums,
+                                           static_cast<cudaStream_t>(stream));
+  if (e == cudaErrorInvalidValue)
+    return fail(PTYCHO_ERR_UNSUPPORTED, "%d x %d patterns do not fit one block's shared memory",
+                qx, qy);
+  if (e != cudaSuccess) return cuda_fail(e, "pattern normalisation kernel");
+  return PTYCHO_OK;
+}
+
+int ptycho_probe_overlap(const ptycho_geometry* g, const void* probe, const float* positions_px,
+                         int32_t num_positions, int32_t max_batch, float* overlap,
+                         void* workspace, size_t workspace_bytes, void* stream) {
+  BatchArgs a;
+  int st = prepare(g, max_batch, workspace, workspace_bytes, a);
+  if (st != PTYCHO_OK) return st;
+  if (!probe || !positions_px || !overlap)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "probe, positions_px and overlap must be non-null");
+  if (num_positions < 0)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "num_positions must be >= 0 (got %d)", num_positions);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t P = (size_t)g->object_x * g->object_y;
+  cudaError_t e = cudaMemsetAsync(overlap, 0, sizeof(float) * P, s);
+  if (e != cudaSuccess) return cuda_fail(e, "overlap clear");
+  if (num_positions == 0) return PTYCHO_OK;
+  a.probe = static_cast<float2*>(const_cast<void*>(probe));
+  a.M = 1;
+  a.T = 1;
+  a.nobj_only = 1;
+  if ((e = launch_probe_spectrum(a, s)) != cudaSuccess) return cuda_fail(e, "probe spectrum");
+  // near-equal batches, the larger ones first (utils.py:539-589)
+  const int nb = (num_positions + max_batch - 1) / max_batch;
+  const int base = num_positions / nb, extra = num_positions % nb;
+  int start = 0;
+  for (int k = 0; k < nb; ++k) {
+    const int size = base + (k < extra ? 1 : 0);
+    a.positions = positions_px + 2 * (size_t)start;
+    a.B = size;
+    if ((e = launch_probe_intensity(a, s)) != cudaSuccess) return cuda_fail(e, "probe intensity");
+    if ((e = launch_overlap_accumulate(a, overlap, s)) != cudaSuccess)
+      return cuda_fail(e, "overlap accumulation");
+    start += size;
+  }
+  return PTYCHO_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------

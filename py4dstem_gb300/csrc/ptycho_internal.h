@@ -28,6 +28,7 @@ struct BatchArgs {
   int keep_farfield;       // single slice: keep FFT2(psi_m) of each position in scratch_f
   int exact_probe_grad;    // probe term through the adjoint of the sub-pixel shift
   int prepare_spectrum;    // after the probe update, the next batch's probe spectrum
+  int nobj_only;           // object reduction of the |P|^2 terms alone (probe overlap)
 
   void* object;                 // (T,Px,Py) float2 or float
   float2* probe;                // (M,N)
@@ -93,6 +94,10 @@ cudaError_t launch_probe_spectrum(const BatchArgs& a, cudaStream_t s);
 cudaError_t launch_position_kernel(const BatchArgs& a, cudaStream_t s);
 cudaError_t launch_position_correction(const BatchArgs& a, cudaStream_t s);
 cudaError_t launch_probe_inverse(const BatchArgs& a, cudaStream_t s);
+// |P_b|^2 of the shifted probe (mode 0) of every batch position into st_nobj.
+cudaError_t launch_probe_intensity(const BatchArgs& a, cudaStream_t s);
+// overlap += sum over the batch of the staged |P_b|^2, scattered into the object grid.
+cudaError_t launch_overlap_accumulate(const BatchArgs& a, float* overlap, cudaStream_t s);
 // Register-resident 128 x 128 single-slice GD kernel (ptycho_gd128.cu).
 // set_schedule stores the preferred schedule for a ROI edge (0 default,
 // 1 shared-memory passes, 2 register-resident) and returns the previous one.
@@ -118,5 +123,15 @@ cudaError_t launch_probe_orthogonalize(const BatchArgs& a, float2* scratch_probe
                                        float2* coeffs, cudaStream_t s);
 cudaError_t launch_probe_mix(const BatchArgs& a, const float2* in, const float2* coeffs,
                              float2* out, cudaStream_t s);
+
+// Preprocessing kernels (ptycho_preprocess.cu).
+cudaError_t launch_pattern_com(const float* in, int num, int Qx, int Qy, const float* mask,
+                               float* cx, float* cy, cudaStream_t s);
+cudaError_t launch_rotation_search(const float* nx, const float* ny, int R0, int R1,
+                                   const float* cos_a, const float* sin_a, int A, int div,
+                                   float* vals, cudaStream_t s);
+cudaError_t launch_pattern_normalize(const float* in, int Qx, int Qy, const int32_t* rows,
+                                     int num_out, const float* cfx, const float* cfy,
+                                     int crop_w, float* amps, float* sums, cudaStream_t s);
 
 }  // namespace pty

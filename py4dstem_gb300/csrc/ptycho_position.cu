@@ -725,6 +725,70 @@ __global__ void __launch_bounds__(NT, 1) probe_inverse_kernel(BatchArgs a) {
   for (int e = threadIdx.x; e < L::N; e += NT) g[e] = c_scale(buf[(e / SY) * L::LD + e % SY], invN);
 }
 
+// |P_b|^2 of the sub-pixel shifted probe (mode 0) of batch position b, staged like
+// the position kernel's |P|^2 term; summed over positions it is the probe-overlap
+// map the preprocessing thresholds into the field-of-view mask
+// (singleslice_ptychography.py:504-526: ifft2(fft2(P) ramp), abs() squared).
+template <int SX, int SY, int NT>
+__global__ void __launch_bounds__(NT, 1) probe_intensity_kernel(BatchArgs a) {
+  using L = Layout<SX, SY>;
+  constexpr int N = L::N;
+  constexpr int LD = L::LD;
+  extern __shared__ float4 smem4[];
+  float2* buf = reinterpret_cast<float2*>(smem4);
+  float2* twx = buf + SX * LD;
+  float2* twy = twx + SX;
+  float2* rpx = twy + SY;
+  float2* rpy = rpx + SX;
+  const int tid = threadIdx.x;
+  const int b = blockIdx.x;
+  const float posx = a.positions[2 * b];
+  const float posy = a.positions[2 * b + 1];
+  const float rx = rintf(posx);
+  const float ry = rintf(posy);
+  const float dx = posx - rx;
+  const float dy = posy - ry;
+  for (int i = tid; i < SX; i += NT) twx[i] = a.tw[i];
+  for (int i = tid; i < SY; i += NT) twy[i] = a.tw[SX + i];
+  for (int i = tid; i < SX; i += NT) {
+    const float k = (float)fint(i, SX) / (float)SX;
+    rpx[i] = cis_rounded(__fmul_rn(__fmul_rn(-6.2831855f, k), dx));
+  }
+  for (int i = tid; i < SY; i += NT) {
+    const float k = (float)fint(i, SY) / (float)SY;
+    rpy[i] = cis_rounded(__fmul_rn(__fmul_rn(-6.2831855f, k), dy));
+  }
+  if (tid == 0) a.pos_round[b] = make_int2((int)rx, (int)ry);
+  __syncthreads();
+  for (int e = tid; e < N; e += NT) {
+    const int x = e / SY, y = e % SY;
+    buf[x * LD + y] = c_mul(__ldg(a.probe_spec + e), c_mul(rpx[x], rpy[y]));
+  }
+  __syncthreads();
+  fft2d<SX, SY, NT, +1>(buf, twx, twy);
+  const float invN = 1.0f / (float)N;
+  float* dst = a.st_nobj + (size_t)b * N;
+  for (int e = tid; e < N; e += NT) {
+    const float2 p = c_scale(buf[(e / SY) * LD + e % SY], invN);
+    const float av = hypotf(p.x, p.y);
+    dst[e] = av * av;
+  }
+}
+
+template <int SX, int SY, int NT>
+cudaError_t launch_probe_intensity_t(const BatchArgs& a, cudaStream_t s) {
+  const size_t smem = Layout<SX, SY>::smem_bytes(false);
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(probe_intensity_kernel<SX, SY, NT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  probe_intensity_kernel<SX, SY, NT><<<a.B, NT, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
 template <int SX, int SY, int NT>
 cudaError_t launch_probe_inverse_t(const BatchArgs& a, cudaStream_t s) {
   const size_t smem = Layout<SX, SY>::smem_bytes(false);
@@ -827,6 +891,10 @@ cudaError_t launch_position_correction(const BatchArgs& a, cudaStream_t s) {
 
 cudaError_t launch_probe_inverse(const BatchArgs& a, cudaStream_t s) {
   PTY_DISPATCH(launch_probe_inverse_t, a, s)
+}
+
+cudaError_t launch_probe_intensity(const BatchArgs& a, cudaStream_t s) {
+  PTY_DISPATCH(launch_probe_intensity_t, a, s)
 }
 
 }  // namespace pty

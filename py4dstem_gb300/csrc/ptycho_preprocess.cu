@@ -1,0 +1,333 @@
+// One-time preprocessing of the diffraction data on the device: the per-pattern
+// centre of mass, the real/reciprocal rotation search and the corner-centring /
+// square-root normalisation that py4DSTEM 0.14.18 runs before the reconstruction
+// loop (phase_base_class.py:613-767, 1086-1182, 1347-1460).
+//
+// The reference evaluates these in float32 NumPy. Every sum here reproduces the
+// order NumPy's float32 add.reduce uses for a contiguous run of n values
+// (numpy/_core/src/umath/loops_utils.h.src, pairwise_sum; the reduction's
+// identity 0 is added in front): runs of at most 128 values are summed with 8
+// interleaved accumulators, longer runs split in two halves at a multiple of 8.
+// Products, quotients and the bilinear weights are formed with the same single
+// roundings (no contraction into FMAs), so the results are the reference's bits.
+//
+// Kernels (one block per pattern, or per angle and transpose):
+//   pattern_com_kernel        sum I, sum I kx, sum I ky of the (masked) pattern
+//   rotation_search_kernel    mean |curl| (or |div|) of the rotated CoM field
+//   pattern_normalize_kernel  periodic bilinear shift by -CoM, pattern sum,
+//                             sqrt(max(., 0)) with the optional corner crop
+#include <cuda_runtime.h>
+
+#include "ptycho_internal.h"
+
+namespace pty {
+namespace {
+
+constexpr int kPwBlock = 128;  // PW_BLOCKSIZE of NumPy's pairwise sum
+constexpr int kPreThreads = 256;
+
+__host__ __device__ __forceinline__ int pw_half(int n) {
+  int h = n / 2;
+  return h - h % 8;
+}
+
+// Leaves of the pairwise tree over n values, left to right (one thread).
+__device__ int pairwise_leaves(int n, int* lo, int* len) {
+  int slo[40], sn[40];
+  int sp = 0, k = 0;
+  slo[sp] = 0;
+  sn[sp] = n;
+  ++sp;
+  while (sp > 0) {
+    --sp;
+    const int l = slo[sp], m = sn[sp];
+    if (m <= kPwBlock) {
+      lo[k] = l;
+      len[k] = m;
+      ++k;
+      continue;
+    }
+    const int h = pw_half(m);
+    slo[sp] = l + h;  // right half, taken after the left one
+    sn[sp] = m - h;
+    ++sp;
+    slo[sp] = l;
+    sn[sp] = h;
+    ++sp;
+  }
+  return k;
+}
+
+// Sum of one leaf [l, l + m) of values f(i).
+template <typename F>
+__device__ __forceinline__ float leaf_sum(const F& f, int l, int m) {
+  if (m < 8) {
+    float r = 0.0f;
+    for (int i = 0; i < m; ++i) r = __fadd_rn(r, f(l + i));
+    return r;
+  }
+  float r[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) r[j] = f(l + j);
+  int i = 8;
+  for (; i < m - (m % 8); i += 8) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) r[j] = __fadd_rn(r[j], f(l + i + j));
+  }
+  float res = __fadd_rn(__fadd_rn(__fadd_rn(r[0], r[1]), __fadd_rn(r[2], r[3])),
+                        __fadd_rn(__fadd_rn(r[4], r[5]), __fadd_rn(r[6], r[7])));
+  for (; i < m; ++i) res = __fadd_rn(res, f(l + i));
+  return res;
+}
+
+// Combines the leaf sums of the tree over n values in tree order (one thread).
+// Post-order walk with an explicit stack: each frame is a node still waiting for
+// its right half.
+__device__ float pairwise_combine(int n, const float* leaf) {
+  int fn[40];      // size of the node's right half
+  float fv[40];    // value of its left half
+  int sp = 0, k = 0;
+  int m = n;
+  for (;;) {
+    // descend along left halves to a leaf
+    while (m > kPwBlock) {
+      const int h = pw_half(m);
+      fn[sp] = m - h;
+      fv[sp] = 0.0f;
+      ++sp;
+      m = h;
+    }
+    float v = leaf[k++];
+    // climb: a finished left half starts its right sibling; a finished right
+    // half completes its parent
+    for (;;) {
+      if (sp == 0) return v;
+      if (fn[sp - 1] > 0) {  // v is a left half
+        fv[sp - 1] = v;
+        m = fn[sp - 1];
+        fn[sp - 1] = -1;
+        break;
+      }
+      --sp;  // v is a right half
+      v = __fadd_rn(fv[sp], v);
+    }
+  }
+}
+
+__device__ __forceinline__ int pmod(int v, int m) {
+  int r = v % m;
+  return r < 0 ? r + m : r;
+}
+
+// ------------------------------------------------------------ centre of mass
+// cx[p] = sum(I kx) / sum(I), cy[p] = sum(I ky) / sum(I) with I = pattern * mask
+// (phase_base_class.py:646-672): kx, ky are the pixel indices along x and y.
+__global__ void __launch_bounds__(kPreThreads) pattern_com_kernel(
+    const float* __restrict__ in, int Qx, int Qy, const float* __restrict__ mask,
+    int max_leaves, float* __restrict__ cx, float* __restrict__ cy) {
+  extern __shared__ float4 smem4[];
+  const int N = Qx * Qy;
+  float* pat = reinterpret_cast<float*>(smem4);
+  float* leaf = pat + N;                                        // 3 * max_leaves
+  int* llo = reinterpret_cast<int*>(leaf + 3 * max_leaves);     // max_leaves
+  int* llen = llo + max_leaves;                                 // max_leaves
+  __shared__ int nleaves;
+  const float* src = in + (size_t)blockIdx.x * N;
+  for (int e = threadIdx.x; e < N; e += kPreThreads) {
+    float v = src[e];
+    if (mask) v = __fmul_rn(v, mask[e]);
+    pat[e] = v;
+  }
+  if (threadIdx.x == 0) nleaves = pairwise_leaves(N, llo, llen);
+  __syncthreads();
+  const int L = nleaves;
+  for (int t = threadIdx.x; t < 3 * L; t += kPreThreads) {
+    const int q = t / L, j = t - q * L;
+    float s;
+    if (q == 0) {
+      s = leaf_sum([&](int e) { return pat[e]; }, llo[j], llen[j]);
+    } else if (q == 1) {
+      s = leaf_sum([&](int e) { return __fmul_rn(pat[e], (float)(e / Qy)); }, llo[j], llen[j]);
+    } else {
+      s = leaf_sum([&](int e) { return __fmul_rn(pat[e], (float)(e % Qy)); }, llo[j], llen[j]);
+    }
+    leaf[q * max_leaves + j] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const float s0 = __fadd_rn(0.0f, pairwise_combine(N, leaf));
+    const float s1 = __fadd_rn(0.0f, pairwise_combine(N, leaf + max_leaves));
+    const float s2 = __fadd_rn(0.0f, pairwise_combine(N, leaf + 2 * max_leaves));
+    cx[blockIdx.x] = __fdiv_rn(s1, s0);
+    cy[blockIdx.x] = __fdiv_rn(s2, s0);
+  }
+}
+
+// ----------------------------------------------------------- rotation search
+// vals[t * A + a] = mean over the interior of |d cy/dx - d cx/dy| (curl) or
+// |d cx/dx + d cy/dy| (divergence, `div` != 0) of the CoM field rotated by angle
+// a (cos_a, sin_a) and, for t = 1, with x and y exchanged
+// (phase_base_class.py:1086-1182; central differences over two pixels).
+__global__ void __launch_bounds__(kPreThreads) rotation_search_kernel(
+    const float* __restrict__ nx, const float* __restrict__ ny, int R0, int R1,
+    const float* __restrict__ cos_a, const float* __restrict__ sin_a, int A, int div,
+    int max_leaves, float* __restrict__ vals) {
+  extern __shared__ float4 smem4[];
+  float* leaf = reinterpret_cast<float*>(smem4);
+  int* llo = reinterpret_cast<int*>(leaf + max_leaves);
+  int* llen = llo + max_leaves;
+  __shared__ int nleaves;
+  const int a = blockIdx.x % A;
+  const int t = blockIdx.x / A;
+  const float c = cos_a[a], s = sin_a[a];
+  const int W = R1 - 2;
+  const int n = (R0 - 2) * W;
+  auto rx = [&](int i, int j) {
+    const float X = nx[i * R1 + j], Y = ny[i * R1 + j];
+    return t ? __fsub_rn(__fmul_rn(c, Y), __fmul_rn(s, X))
+             : __fsub_rn(__fmul_rn(c, X), __fmul_rn(s, Y));
+  };
+  auto ry = [&](int i, int j) {
+    const float X = nx[i * R1 + j], Y = ny[i * R1 + j];
+    return t ? __fadd_rn(__fmul_rn(s, Y), __fmul_rn(c, X))
+             : __fadd_rn(__fmul_rn(s, X), __fmul_rn(c, Y));
+  };
+  auto value = [&](int e) {
+    const int i = e / W, j = e - (e / W) * W;
+    if (div) {
+      const float gxx = __fsub_rn(rx(i + 2, j + 1), rx(i, j + 1));
+      const float gyy = __fsub_rn(ry(i + 1, j + 2), ry(i + 1, j));
+      return fabsf(__fadd_rn(gxx, gyy));
+    }
+    const float gxy = __fsub_rn(rx(i + 1, j + 2), rx(i + 1, j));
+    const float gyx = __fsub_rn(ry(i + 2, j + 1), ry(i, j + 1));
+    return fabsf(__fsub_rn(gyx, gxy));
+  };
+  if (threadIdx.x == 0) nleaves = pairwise_leaves(n, llo, llen);
+  __syncthreads();
+  for (int j = threadIdx.x; j < nleaves; j += kPreThreads) leaf[j] = leaf_sum(value, llo[j], llen[j]);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const float sum = __fadd_rn(0.0f, pairwise_combine(n, leaf));
+    vals[blockIdx.x] = __fdiv_rn(sum, (float)n);
+  }
+}
+
+// ------------------------------------------------------------- normalisation
+// Output pattern o takes source pattern rows[o] (all patterns in order when
+// rows is null), shifts it periodically and bilinearly by (-cfx, -cfy)
+// (preprocess/utils.py:59-120 bilinear branch: four rolled copies weighted
+// (1-wx)(1-wy), wx(1-wy), (1-wx)wy, wx wy, added in that order), stores its sum
+// in sums[o] and sqrt(max(shifted, 0)) in amps, cropped to the four crop_w x
+// crop_w corners when crop_w > 0 (phase_base_class.py:1385-1445).
+__global__ void __launch_bounds__(kPreThreads) pattern_normalize_kernel(
+    const float* __restrict__ in, int Qx, int Qy, const int32_t* __restrict__ rows,
+    const float* __restrict__ cfx, const float* __restrict__ cfy, int crop_w, int max_leaves,
+    float* __restrict__ amps, float* __restrict__ sums) {
+  extern __shared__ float4 smem4[];
+  const int N = Qx * Qy;
+  float* pat = reinterpret_cast<float*>(smem4);
+  float* sh = pat + N;
+  float* leaf = sh + N;
+  int* llo = reinterpret_cast<int*>(leaf + max_leaves);
+  int* llen = llo + max_leaves;
+  __shared__ int nleaves;
+  const int o = blockIdx.x;
+  const int r = rows ? rows[o] : o;
+  const float* src = in + (size_t)r * N;
+  for (int e = threadIdx.x; e < N; e += kPreThreads) pat[e] = src[e];
+  if (threadIdx.x == 0) nleaves = pairwise_leaves(N, llo, llen);
+
+  const float xs = -cfx[r], ys = -cfy[r];
+  const float xf = floorf(xs), yf = floorf(ys);
+  const float wx = __fsub_rn(xs, xf), wy = __fsub_rn(ys, yf);
+  const float ux = __fsub_rn(1.0f, wx), uy = __fsub_rn(1.0f, wy);
+  const float w00 = __fmul_rn(ux, uy), w10 = __fmul_rn(wx, uy);
+  const float w01 = __fmul_rn(ux, wy), w11 = __fmul_rn(wx, wy);
+  const int ix = (int)xf, iy = (int)yf;
+  __syncthreads();
+  for (int e = threadIdx.x; e < N; e += kPreThreads) {
+    const int i = e / Qy, j = e - (e / Qy) * Qy;
+    const int i0 = pmod(i - ix, Qx), i1 = pmod(i - ix - 1, Qx);
+    const int j0 = pmod(j - iy, Qy), j1 = pmod(j - iy - 1, Qy);
+    float v = __fmul_rn(pat[i0 * Qy + j0], w00);
+    v = __fadd_rn(v, __fmul_rn(pat[i1 * Qy + j0], w10));
+    v = __fadd_rn(v, __fmul_rn(pat[i0 * Qy + j1], w01));
+    v = __fadd_rn(v, __fmul_rn(pat[i1 * Qy + j1], w11));
+    sh[e] = v;
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < nleaves; j += kPreThreads)
+    leaf[j] = leaf_sum([&](int e) { return sh[e]; }, llo[j], llen[j]);
+  // amplitudes (numpy.maximum keeps its first argument unless it is below the second)
+  const int Cx = crop_w > 0 ? 2 * crop_w : Qx;
+  const int Cy = crop_w > 0 ? 2 * crop_w : Qy;
+  float* dst = amps + (size_t)o * Cx * Cy;
+  for (int e = threadIdx.x; e < Cx * Cy; e += kPreThreads) {
+    const int u = e / Cy, w = e - (e / Cy) * Cy;
+    const int x = crop_w > 0 && u >= crop_w ? Qx - Cx + u : u;
+    const int y = crop_w > 0 && w >= crop_w ? Qy - Cy + w : w;
+    float v = sh[x * Qy + y];
+    if (!(v >= 0.0f) && !isnan(v)) v = 0.0f;
+    dst[e] = __fsqrt_rn(v);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) sums[o] = __fadd_rn(0.0f, pairwise_combine(N, leaf));
+}
+
+// Number of leaves of the pairwise tree over n values (host side, for sizing).
+int pairwise_leaf_count(int n) {
+  if (n <= kPwBlock) return 1;
+  const int h = pw_half(n);
+  return pairwise_leaf_count(h) + pairwise_leaf_count(n - h);
+}
+
+cudaError_t set_smem(const void* fn, size_t bytes) {
+  return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+}  // namespace
+
+size_t preprocess_smem_limit() { return 227 * 1024; }
+
+cudaError_t launch_pattern_com(const float* in, int num, int Qx, int Qy, const float* mask,
+                               float* cx, float* cy, cudaStream_t s) {
+  const int N = Qx * Qy;
+  const int L = pairwise_leaf_count(N);
+  const size_t smem = sizeof(float) * ((size_t)N + 3 * L) + sizeof(int) * 2 * L;
+  if (smem > preprocess_smem_limit()) return cudaErrorInvalidValue;
+  cudaError_t e = set_smem((const void*)pattern_com_kernel, smem);
+  if (e != cudaSuccess) return e;
+  pattern_com_kernel<<<num, kPreThreads, smem, s>>>(in, Qx, Qy, mask, L, cx, cy);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rotation_search(const float* nx, const float* ny, int R0, int R1,
+                                   const float* cos_a, const float* sin_a, int A, int div,
+                                   float* vals, cudaStream_t s) {
+  const int n = (R0 - 2) * (R1 - 2);
+  const int L = pairwise_leaf_count(n);
+  const size_t smem = sizeof(float) * L + sizeof(int) * 2 * (size_t)L;
+  if (smem > preprocess_smem_limit()) return cudaErrorInvalidValue;
+  cudaError_t e = set_smem((const void*)rotation_search_kernel, smem);
+  if (e != cudaSuccess) return e;
+  rotation_search_kernel<<<2 * A, kPreThreads, smem, s>>>(nx, ny, R0, R1, cos_a, sin_a, A, div,
+                                                          L, vals);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pattern_normalize(const float* in, int Qx, int Qy, const int32_t* rows,
+                                     int num_out, const float* cfx, const float* cfy,
+                                     int crop_w, float* amps, float* sums, cudaStream_t s) {
+  const int N = Qx * Qy;
+  const int L = pairwise_leaf_count(N);
+  const size_t smem = sizeof(float) * (2 * (size_t)N + L) + sizeof(int) * 2 * L;
+  if (smem > preprocess_smem_limit()) return cudaErrorInvalidValue;
+  cudaError_t e = set_smem((const void*)pattern_normalize_kernel, smem);
+  if (e != cudaSuccess) return e;
+  pattern_normalize_kernel<<<num_out, kPreThreads, smem, s>>>(in, Qx, Qy, rows, cfx, cfy,
+                                                              crop_w, L, amps, sums);
+  return cudaGetLastError();
+}
+
+}  // namespace pty

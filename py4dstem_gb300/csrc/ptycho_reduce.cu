@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(NT) object_reduce_kernel(BatchArgs a) {
             const int lx = fminx + tx < 0 ? fminx + tx + a.Sx : fminx + tx;
             const int ly = fminy + ty < 0 ? fminy + ty + a.Sy : fminy + ty;
             const size_t e = (size_t)b * N + (a.staging_t ? ly * a.Sx + lx : lx * a.Sy + ly);
-            v[u] = st[e];
+            if (!a.nobj_only) v[u] = st[e];
             w[u] = sn[e];
           }
         }
@@ -276,6 +276,19 @@ __global__ void __launch_bounds__(NT) object_update_kernel(BatchArgs a, int ntil
       obj[o] = make_float2(__fadd_rn(v.x, u.x), __fadd_rn(v.y, u.y));
     }
   }
+}
+
+// overlap += the batch's |P|^2 sums (chunk partials added in chunk order): the
+// probe-overlap map of the preprocessing, one batch at a time
+// (singleslice_ptychography.py:504-526).
+__global__ void __launch_bounds__(NT) overlap_accumulate_kernel(BatchArgs a, float* overlap) {
+  const size_t P = (size_t)a.Px * a.Py;
+  const size_t i = (size_t)blockIdx.x * NT + threadIdx.x;
+  if (i >= P) return;
+  float n = a.obj_npart[i];
+#pragma unroll
+  for (int k = 1; k < kObjSplit; ++k) n += a.obj_npart[(size_t)k * P + i];
+  overlap[i] = overlap[i] + n;
 }
 
 // ------------------------------------------------------------------- probe side
@@ -768,6 +781,15 @@ cudaError_t launch_reduce_and_update(const BatchArgs& a, cudaStream_t s) {
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (!a.fix_probe && (e = cudaStreamWaitEvent(s, fj.join, 0)) != cudaSuccess) return e;
   return cudaSuccess;
+}
+
+cudaError_t launch_overlap_accumulate(const BatchArgs& a, float* overlap, cudaStream_t s) {
+  const int ntx = (a.Px + kTile - 1) / kTile;
+  const int nty = (a.Py + kTile - 1) / kTile;
+  object_reduce_kernel<<<dim3(ntx * nty, 1, kObjSplit), NT, 0, s>>>(a);
+  const size_t P = (size_t)a.Px * a.Py;
+  overlap_accumulate_kernel<<<(unsigned)((P + NT - 1) / NT), NT, 0, s>>>(a, overlap);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_gradient(const BatchArgs& a, void* object_grad, float2* probe_grad,

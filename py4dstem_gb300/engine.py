@@ -114,7 +114,12 @@ def create_state(*, roi_shape, object_array, probe_array, amplitudes, positions_
     amps_host = None
     amp_stage = amp_pinned = None
     mapped = None
-    if storage == "gpu":
+    if isinstance(amplitudes, torch.Tensor) and storage != "gpu":
+        amplitudes = amplitudes.cpu().numpy()
+    if isinstance(amplitudes, torch.Tensor):
+        # device amplitudes (from the device preprocessing) are used in place
+        amps_dev = amplitudes.to(device=dev, dtype=torch.float32).contiguous()
+    elif storage == "gpu":
         amps_dev = torch.from_numpy(np.ascontiguousarray(amplitudes, dtype=np.float32)).to(dev)
     else:
         amps_host = np.ascontiguousarray(amplitudes, dtype=np.float32)

@@ -268,7 +268,7 @@ class PreprocessMixin:
 
     # -- centre of mass --------------------------------------------------------
     def _intensities_center_of_mass(self, intensities, dp_mask, fit_function, com_shifts,
-                                    com_measured, vectorized):
+                                    com_measured, vectorized, intensities_dev=None):
         rs = self._reciprocal_sampling
         if com_measured:
             cmx = np.asarray(com_measured[0], dtype=np.float32)
@@ -280,7 +280,14 @@ class PreprocessMixin:
             kx = np.arange(intensities.shape[-2], dtype=np.float32)
             ky = np.arange(intensities.shape[-1], dtype=np.float32)
             kya, kxa = np.meshgrid(ky, kx)
-            if vectorized:
+            if intensities_dev is not None:
+                # both branches below give these bits for a 0/1 mask
+                from . import device_preprocess
+
+                cx, cy = device_preprocess.pattern_com(intensities_dev, dp_mask)
+                cmx = cx.reshape(intensities.shape[:2])
+                cmy = cy.reshape(intensities.shape[:2])
+            elif vectorized:
                 im = intensities * dp_mask if dp_mask is not None else intensities
                 isum = np.sum(im, axis=(-2, -1))
                 cmx = np.sum(im * kxa[None, None], axis=(-2, -1)) / isum
@@ -334,6 +341,19 @@ class PreprocessMixin:
         return (np.cos(angle) * nx - np.sin(angle) * ny,
                 np.sin(angle) * nx + np.cos(angle) * ny)
 
+    def _rotation_values(self, cnx, cny, rad, maximize_divergence):
+        """Mean |curl| (|div|) of the CoM field rotated by each angle of rad
+        (A,1,1), untransposed and transposed: two (A,) float32 arrays."""
+        if self._device == "gpu":
+            from . import device_preprocess
+
+            vals = device_preprocess.rotation_values(
+                np.asarray(cnx, dtype=np.float32), np.asarray(cny, dtype=np.float32),
+                np.cos(rad), np.sin(rad), maximize_divergence)
+            return vals[0], vals[1]
+        return tuple(self._curl_or_div(*self._rotated(cnx[None], cny[None], rad, t),
+                                       maximize_divergence, axis=(-2, -1)) for t in (False, True))
+
     def _solve_rotation(self, cnx, cny, rotation_angles_deg, maximize_divergence,
                         force_com_rotation, force_com_transpose):
         verbose = self._verbose
@@ -371,15 +391,11 @@ class PreprocessMixin:
                 if verbose:
                     warnings.warn(f"Transpose of intensities forced to {force_com_transpose}.",
                                   UserWarning)
-                vals = self._curl_or_div(*self._rotated(cnx[None], cny[None], rad, best_t),
-                                         maximize_divergence, axis=(-2, -1))
+                vals = self._rotation_values(cnx, cny, rad, maximize_divergence)[int(best_t)]
                 i = pick(vals).item()
                 best_deg, best_rad = deg[i], rad_flat[i]
             else:
-                v0 = self._curl_or_div(*self._rotated(cnx[None], cny[None], rad, False),
-                                       maximize_divergence, axis=(-2, -1))
-                v1 = self._curl_or_div(*self._rotated(cnx[None], cny[None], rad, True),
-                                       maximize_divergence, axis=(-2, -1))
+                v0, v1 = self._rotation_values(cnx, cny, rad, maximize_divergence)
                 i0 = pick(v0).item()
                 i1 = pick(v1).item()
                 keep0 = v0[i0] >= v1[i1] if maximize_divergence else v0[i0] <= v1[i1]
@@ -396,24 +412,46 @@ class PreprocessMixin:
         return best_rad, best_t, com_x, com_y
 
     # -- amplitudes ------------------------------------------------------------
+    @staticmethod
+    def _crop_geometry(pattern_shape, cfx, cfy, crop_patterns):
+        """(crop width, crop mask, cropped shape) of the corner crop
+        (phase_base_class.py:1385-1400); width 0 and no mask without cropping."""
+        if not crop_patterns:
+            return 0, None, tuple(pattern_shape)
+        crop_x = int(np.minimum(pattern_shape[0] - cfx.max(), cfx.min()))
+        crop_y = int(np.minimum(pattern_shape[1] - cfy.max(), cfy.min()))
+        w = int(np.minimum(crop_y, crop_x))
+        crop_mask = np.zeros(pattern_shape, dtype="bool")
+        crop_mask[:w, :w] = True
+        crop_mask[-w:, :w] = True
+        crop_mask[:w:, -w:] = True
+        crop_mask[-w:, -w:] = True
+        return w, crop_mask, (w * 2, w * 2)
+
+    def _normalize_intensities_device(self, intensities_dev, com_fitted_x, com_fitted_y,
+                                      positions_mask, crop_patterns):
+        """Device amplitudes, float32 mean intensity, crop mask and shape; the
+        same values as _normalize_intensities (the caller's datacube is left
+        unmodified)."""
+        from . import device_preprocess
+
+        cfx = np.asarray(com_fitted_x)
+        cfy = np.asarray(com_fitted_y)
+        w, crop_mask, crop_shape = self._crop_geometry(tuple(intensities_dev.shape[-2:]), cfx,
+                                                       cfy, crop_patterns)
+        if crop_patterns and (w < 1 or 2 * w > min(intensities_dev.shape[-2:])):
+            raise NotImplementedError(
+                f"corner crop of width {w} on {tuple(intensities_dev.shape[-2:])} patterns")
+        amps, mean = device_preprocess.normalize_patterns(intensities_dev, cfx, cfy,
+                                                          positions_mask, w)
+        return amps, mean, crop_mask, crop_shape
+
     def _normalize_intensities(self, intensities, com_fitted_x, com_fitted_y,
                                positions_mask, crop_patterns, in_place):
         diff = intensities if in_place else intensities.copy()
         cfx = np.asarray(com_fitted_x)
         cfy = np.asarray(com_fitted_y)
-        if crop_patterns:
-            crop_x = int(np.minimum(diff.shape[2] - cfx.max(), cfx.min()))
-            crop_y = int(np.minimum(diff.shape[3] - cfy.max(), cfy.min()))
-            w = np.minimum(crop_y, crop_x)
-            crop_mask = np.zeros(diff.shape[-2:], dtype="bool")
-            crop_mask[:w, :w] = True
-            crop_mask[-w:, :w] = True
-            crop_mask[:w:, -w:] = True
-            crop_mask[-w:, -w:] = True
-            crop_shape = (w * 2, w * 2)
-        else:
-            crop_mask = None
-            crop_shape = diff.shape[-2:]
+        _, crop_mask, crop_shape = self._crop_geometry(diff.shape[-2:], cfx, cfy, crop_patterns)
 
         # mean intensity accumulates in float32 pattern by pattern, like the reference
         mean_intensity = 0
@@ -590,6 +628,11 @@ class PreprocessMixin:
         return np.reshape(counts, shape).astype(np.float32)
 
     def _probe_overlap(self, probe_single, max_batch_size):
+        if self._device == "gpu":
+            from . import device_preprocess
+
+            return device_preprocess.probe_overlap(probe_single, self._positions_px,
+                                                   self._object_shape, max_batch_size)
         if max_batch_size is None:
             max_batch_size = self._num_diffraction_patterns
         overlap = np.zeros(self._object_shape, dtype=np.float32)

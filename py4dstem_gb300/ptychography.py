@@ -114,27 +114,69 @@ class _PtychographyBase(PreprocessMixin):
         self._verbose = verbose
         self._preprocessed = False
         self._exit_waves = None
+        # replay each iteration from one captured CUDA graph (eager issue when False)
+        self._graph_iterations = True
 
     def set_device(self, device, clear_fft_cache):
         if clear_fft_cache is not None:
             self._clear_fft_cache = clear_fft_cache
         if device is None:
             return self
-        if device == "cpu":
-            raise ValueError(
-                "py4dstem_gb300 reconstructs on the GPU only: use device='gpu' "
-                "(the CPU path is the reference implementation)")
-        if device != "gpu":
+        if device not in ("cpu", "gpu"):
             raise ValueError(f"device must be either 'cpu' or 'gpu', not {device}")
         self._device = device
         return self
+
+    def _require_gpu(self):
+        """device="cpu" runs preprocess() on the host (NumPy); everything after it
+        runs on the GPU only."""
+        if self._device != "gpu":
+            raise ValueError(
+                "py4dstem_gb300 reconstructs on the GPU only: pass device='gpu' "
+                "(device='cpu' runs preprocess() on the host; the CPU reconstruction is "
+                "the reference implementation)")
+
+    # Amplitudes preprocessed on the device stay there; the host copy is made
+    # the first time something asks for it.
+    @property
+    def _amplitudes(self):
+        host = self.__dict__.get("_amplitudes_host")
+        if host is None and self.__dict__.get("_amplitudes_device") is not None:
+            host = self._amplitudes_device.cpu().numpy()
+            self.__dict__["_amplitudes_host"] = host
+        return host
+
+    @_amplitudes.setter
+    def _amplitudes(self, value):
+        self.__dict__["_amplitudes_host"] = value
+        self.__dict__["_amplitudes_device"] = None
+
+    def _set_device_amplitudes(self, amps):
+        if self._storage == "cpu":
+            # host storage: one copy into page-locked memory, which the batch
+            # kernels read in place; the device copy is released
+            import torch
+
+            host = torch.empty(tuple(amps.shape), dtype=amps.dtype, pin_memory=True)
+            host.copy_(amps)
+            self.__dict__["_amplitudes_host"] = host.numpy()
+            self.__dict__["_amplitudes_device"] = None
+            return
+        self.__dict__["_amplitudes_host"] = None
+        self.__dict__["_amplitudes_device"] = amps
+
+    def _amplitudes_for_state(self):
+        """The amplitudes as create_state takes them: the device tensor when the
+        preprocessing left one and storage is "gpu", else the host array."""
+        dev = self.__dict__.get("_amplitudes_device")
+        if dev is not None and self._storage == "gpu":
+            return dev
+        return self._amplitudes
 
     def set_storage(self, storage):
         if storage not in ("cpu", "gpu"):
             raise ValueError(f"storage must be either 'cpu' or 'gpu', not {storage}")
         self._storage = storage
-        # replay each iteration from one captured CUDA graph (eager issue when False)
-        self._graph_iterations = True
         return self
 
     def set_save_defaults(self, save_datacube=False, save_exit_waves=False,
@@ -232,31 +274,47 @@ class _PtychographyBase(PreprocessMixin):
         if self._semiangle_cutoff_pixels:
             self._semiangle_cutoff = self._semiangle_cutoff_pixels * self._angular_sampling[0]
 
+        # device="gpu": the per-pattern steps run on the device copy of the patterns
+        intensities_dev = None
+        if self._device == "gpu":
+            from . import device_preprocess
+
+            intensities_dev = device_preprocess.upload_intensities(intensities)
+
         (self._com_measured_x, self._com_measured_y, self._com_fitted_x, self._com_fitted_y,
          self._com_normalized_x, self._com_normalized_y) = self._intensities_center_of_mass(
             intensities, self._dp_mask, fit_function, force_com_shifts, force_com_measured,
-            vectorized_com_calculation)
+            vectorized_com_calculation, intensities_dev)
 
         (self._rotation_best_rad, self._rotation_best_transpose, self._com_x,
          self._com_y) = self._solve_rotation(
             self._com_normalized_x, self._com_normalized_y, rotation_angles_deg,
             maximize_divergence, force_com_rotation, force_com_transpose)
 
-        (self._amplitudes, self._mean_diffraction_intensity, self._crop_mask,
-         self._crop_mask_shape) = self._normalize_intensities(
-            intensities, self._com_fitted_x, self._com_fitted_y, self._positions_mask,
-            crop_patterns, in_place_datacube_modification)
+        if intensities_dev is not None:
+            (amps, self._mean_diffraction_intensity, self._crop_mask,
+             self._crop_mask_shape) = self._normalize_intensities_device(
+                intensities_dev, self._com_fitted_x, self._com_fitted_y, self._positions_mask,
+                crop_patterns)
+            del intensities_dev
+            self._set_device_amplitudes(amps)
+        else:
+            (self._amplitudes, self._mean_diffraction_intensity, self._crop_mask,
+             self._crop_mask_shape) = self._normalize_intensities(
+                intensities, self._com_fitted_x, self._com_fitted_y, self._positions_mask,
+                crop_patterns, in_place_datacube_modification)
         del intensities
 
-        self._num_diffraction_patterns = self._amplitudes.shape[0]
-        self._amplitudes_shape = np.array(self._amplitudes.shape[-2:])
+        amp_shape = tuple(self._amplitudes_for_state().shape)
+        self._num_diffraction_patterns = amp_shape[0]
+        self._amplitudes_shape = np.array(amp_shape[-2:])
         if region_of_interest_shape is not None and tuple(region_of_interest_shape) != tuple(
                 self._amplitudes_shape):
             raise NotImplementedError(
                 "region_of_interest_shape different from the detector shape "
                 "(exit-wave resampling) is not implemented")
         self._resample_exit_waves = False
-        self._region_of_interest_shape = np.array(self._amplitudes.shape[-2:])
+        self._region_of_interest_shape = np.array(amp_shape[-2:])
 
         self._positions_px, self._object_padding_px = self._scan_positions_in_pixels(
             self._scan_positions, self._positions_mask, self._object_padding_px,
@@ -381,6 +439,7 @@ class _PtychographyBase(PreprocessMixin):
                           reset, device, clear_fft_cache, object_type,
                           orthogonalize_probe=False, unsupported=None):
         self.set_device(device, clear_fft_cache)
+        self._require_gpu()
         self._reset_reconstruction(store_iterations, reset)
         if object_type is not None:
             self._switch_object_type(object_type)
@@ -409,7 +468,7 @@ class _PtychographyBase(PreprocessMixin):
         use_mask = bool(fix_potential_baseline and self._object_fov_mask_inverse.sum() > 0)
         st = engine.create_state(
             roi_shape=tuple(self._region_of_interest_shape), object_array=obj,
-            probe_array=self._probe, amplitudes=self._amplitudes,
+            probe_array=self._probe, amplitudes=self._amplitudes_for_state(),
             positions_px=self._positions_px, num_slices=self._num_slices,
             num_probes=self._num_probes, potential=potential, max_batch=int(max_batch_size),
             storage=self._storage,
@@ -482,13 +541,14 @@ class _PtychographyBase(PreprocessMixin):
         """Per-position self-consistency errors of the current object and probe
         (ptychographic_methods.py:2227-2291): sum (A - |F|)^2 of a forward-only GPU
         pass in natural position order, divided by the mean intensity (float64)."""
+        self._require_gpu()
         potential = self._object_type == "potential"
         J = self._num_diffraction_patterns
         max_batch_size = J if max_batch_size is None else int(max_batch_size)
         st = engine.create_state(
             roi_shape=tuple(self._region_of_interest_shape),
             object_array=np.asarray(self._object, dtype=np.float32 if potential else np.complex64),
-            probe_array=self._probe, amplitudes=self._amplitudes,
+            probe_array=self._probe, amplitudes=self._amplitudes_for_state(),
             positions_px=self._positions_px, num_slices=self._num_slices,
             num_probes=self._num_probes, potential=potential, max_batch=max_batch_size,
             storage=self._storage,

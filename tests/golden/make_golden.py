@@ -104,6 +104,87 @@ CASES = {
 }
 
 
+# preprocess-only fixtures ("prep_" prefix): the rotation search, masks, crop and
+# the other centre-of-mass options that the reconstruction fixtures fix
+PRE_CASES = {
+    "prep_rotation_curl": dict(
+        gen=dict(name="prc", seed=21, scan_shape=(16, 16), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=128),
+        ctor=dict(object_fov_ang=(32.0, 32.0)), scan_positions=True,
+        pre=dict(plot_center_of_mass=False, plot_rotation=False, plot_probe_overlaps=False)),
+    "prep_rotation_div_masks": dict(
+        gen=dict(name="prd", seed=22, scan_shape=(14, 18), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=128),
+        ctor=dict(object_fov_ang=(32.0, 32.0)), scan_positions=False, positions_mask_seed=3,
+        dp_mask_radius=24,
+        pre=dict(plot_center_of_mass=False, plot_rotation=False, plot_probe_overlaps=False,
+                 maximize_divergence=True, rotation_angles_deg=list(range(-60, 61, 4)),
+                 fit_function="parabola")),
+    "prep_crop_loop_com": dict(
+        gen=dict(name="prx", seed=23, scan_shape=(12, 12), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=128),
+        ctor=dict(object_fov_ang=(32.0, 32.0)), scan_positions=True,
+        # the forced centre (24.6 px) makes the corner crop 48 x 48, a region of
+        # interest the fused kernels support
+        pre=dict(plot_center_of_mass=False, plot_rotation=False, plot_probe_overlaps=False,
+                 force_com_transpose=True, crop_patterns=True, force_com_shifts=[24.6, 24.6],
+                 vectorized_com_calculation=False)),
+}
+
+
+def make_pre_case(ref, name, spec):
+    case = synthetic.make_scan(**spec["gen"])
+    data = case.datacube.data
+    assert np.array_equal(data, np.round(data)) and data.max() < 65535
+    q = case.datacube.calibration.get_Q_pixel_size()
+    r = case.datacube.calibration.get_R_pixel_size()
+    dc = ref.DataCube(data, r_pixel_size=r, r_pixel_units="A", q_pixel_size=q,
+                      q_pixel_units="mrad")
+    ctor = dict(energy=300e3, semiangle_cutoff=20.0, defocus=100.0, **spec["ctor"])
+    arrays = {}
+    kw = {}
+    if spec["scan_positions"]:
+        kw["initial_scan_positions"] = case.scan_positions_ang
+    if "positions_mask_seed" in spec:
+        mrng = np.random.default_rng(spec["positions_mask_seed"])
+        pmask = mrng.random(data.shape[:2]) > 0.1
+        arrays["positions_mask"] = pmask
+        kw["positions_mask"] = pmask.copy()
+    pre = dict(spec["pre"])
+    if "dp_mask_radius" in spec:
+        qx, qy = data.shape[-2:]
+        x, y = np.meshgrid(np.arange(qx) - qx / 2, np.arange(qy) - qy / 2, indexing="ij")
+        dmask = (x ** 2 + y ** 2) < spec["dp_mask_radius"] ** 2
+        arrays["dp_mask"] = dmask
+        pre["dp_mask"] = dmask.copy()
+    p = ref.SingleslicePtychography(datacube=dc, verbose=False, device="cpu", **ctor, **kw)
+    p.preprocess(**pre)
+    out = dict(
+        com_measured_x=np.asarray(p._com_measured_x), com_measured_y=np.asarray(p._com_measured_y),
+        com_fitted_x=np.asarray(p._com_fitted_x), com_fitted_y=np.asarray(p._com_fitted_y),
+        com_normalized_x=np.asarray(p._com_normalized_x),
+        com_normalized_y=np.asarray(p._com_normalized_y),
+        rotation_best_rad=np.float64(p._rotation_best_rad),
+        rotation_best_transpose=np.bool_(p._rotation_best_transpose),
+        mean_intensity=np.float32(p._mean_diffraction_intensity),
+        positions_px=p._positions_px.copy(),
+        probe_initial=p._probe.copy(),
+        fov_mask=p._object_fov_mask.copy(),
+        amplitudes=p._amplitudes.copy(),
+    )
+    meta = dict(cls="single", ctor=ctor, preprocess={k: v for k, v in pre.items()
+                                                     if k != "dp_mask"},
+                r_pixel_size=r, q_pixel_size=q, generator=spec["gen"],
+                scan_positions=spec["scan_positions"])
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(path, datacube=data.astype(np.uint16),
+                        scan_positions_ang=case.scan_positions_ang, meta=json.dumps(meta),
+                        **arrays, **{f"pre_{k}": v for k, v in out.items()})
+    print(f"{name}: {os.path.getsize(path) / 1e6:.2f} MB, rotation "
+          f"{np.rad2deg(out['rotation_best_rad']):.1f} deg, transpose "
+          f"{bool(out['rotation_best_transpose'])}")
+
+
 def smooth_guess(shape, seed, potential):
     """Seeded smooth random phase (0.3 rad peak) as an initial object."""
     rng = np.random.default_rng(seed)
@@ -192,8 +273,13 @@ def make_case(ref, name, spec):
 
 def main():
     ref = load_reference()
+    only = set(sys.argv[1:])
     for name, spec in CASES.items():
-        make_case(ref, name, spec)
+        if not only or name in only:
+            make_case(ref, name, spec)
+    for name, spec in PRE_CASES.items():
+        if not only or name in only:
+            make_pre_case(ref, name, spec)
 
 
 if __name__ == "__main__":

@@ -13,9 +13,75 @@ from oracle.ptycho_np import State
 GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-def names():
+def _all_names():
     return sorted(os.path.splitext(os.path.basename(p))[0]
                   for p in glob.glob(os.path.join(GOLDEN_DIR, "*.npz")))
+
+
+def names():
+    """Reconstruction fixtures."""
+    return [n for n in _all_names() if not n.startswith("prep_")]
+
+
+def prep_names():
+    """Preprocess-only fixtures."""
+    return [n for n in _all_names() if n.startswith("prep_")]
+
+
+class PrepGolden:
+    """A preprocess-only fixture: datacube, options and the reference's
+    preprocessed state."""
+
+    def __init__(self, name):
+        self.name = name
+        z = np.load(os.path.join(GOLDEN_DIR, f"{name}.npz"))
+        self.meta = json.loads(str(z["meta"]))
+        self.datacube_counts = z["datacube"].astype(np.float32)
+        self.scan_positions_ang = z["scan_positions_ang"]
+        self.positions_mask = z["positions_mask"] if "positions_mask" in z.files else None
+        self.dp_mask = z["dp_mask"] if "dp_mask" in z.files else None
+        self.pre = {k[4:]: z[k] for k in z.files if k.startswith("pre_")}
+
+    def build(self, device="gpu", storage=None):
+        m = self.meta
+        ctor = dict(m["ctor"])
+        if "object_fov_ang" in ctor:
+            ctor["object_fov_ang"] = tuple(ctor["object_fov_ang"])
+        kw = {}
+        if m["scan_positions"]:
+            kw["initial_scan_positions"] = self.scan_positions_ang.copy()
+        if self.positions_mask is not None:
+            kw["positions_mask"] = self.positions_mask.copy()
+        dc = DataCube(self.datacube_counts.copy(), r_pixel_size=m["r_pixel_size"],
+                      r_pixel_units="A", q_pixel_size=m["q_pixel_size"], q_pixel_units="mrad")
+        p = api.SingleslicePtychography(datacube=dc, verbose=False, device=device,
+                                        storage=storage, **ctor, **kw)
+        pre = dict(m["preprocess"])
+        if self.dp_mask is not None:
+            pre["dp_mask"] = self.dp_mask.copy()
+        p.preprocess(**pre)
+        return p
+
+    def check(self, p, fov_mask=True, probe_exact=True):
+        """Assert that a preprocessed object holds the reference's bits. The
+        initial probe is NumPy FFT work on the host, whose float32 bits may differ
+        between CPU architectures for sizes that are not powers of two:
+        probe_exact=False compares it to 1e-6."""
+        r = self.pre
+        for key in ("com_measured_x", "com_measured_y", "com_fitted_x", "com_fitted_y",
+                    "com_normalized_x", "com_normalized_y"):
+            np.testing.assert_array_equal(np.asarray(getattr(p, "_" + key)), r[key], err_msg=key)
+        assert np.float64(p._rotation_best_rad) == r["rotation_best_rad"]
+        assert bool(p._rotation_best_transpose) == bool(r["rotation_best_transpose"])
+        assert np.float32(p._mean_diffraction_intensity) == r["mean_intensity"]
+        np.testing.assert_array_equal(p._positions_px, r["positions_px"])
+        if probe_exact:
+            np.testing.assert_array_equal(p._probe, r["probe_initial"])
+        else:
+            assert rel_l2(p._probe, r["probe_initial"]) < 1e-6
+        np.testing.assert_array_equal(p._amplitudes, r["amplitudes"])
+        if fov_mask:
+            np.testing.assert_array_equal(p._object_fov_mask, r["fov_mask"])
 
 
 class Golden:

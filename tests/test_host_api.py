@@ -42,7 +42,7 @@ def test_constructor_validation():
     with pytest.raises(ValueError):
         SingleslicePtychography(energy=300e3, not_an_aberration=1.0)
     with pytest.raises(ValueError):
-        SingleslicePtychography(energy=300e3, device="cpu")
+        SingleslicePtychography(energy=300e3, device="tpu")
     with pytest.raises(ValueError):
         SingleslicePtychography(energy=300e3, storage="disk")
     with pytest.raises(ValueError):
@@ -70,13 +70,28 @@ def test_unsupported_options_raise_before_gpu():
     from golden_io import Golden
 
     g = Golden("ss_gd_potential")
-    p = g.build()
+    p = g.build(device="cpu")
+    kw = dict(num_iter=1, device="gpu")
     with pytest.raises(NotImplementedError):
-        p.reconstruct(num_iter=1, fix_positions=False, global_affine_transformation=True)
+        p.reconstruct(fix_positions=False, global_affine_transformation=True, **kw)
     with pytest.raises(NotImplementedError):
-        p.reconstruct(num_iter=1, fix_positions=False, reconstruction_method="DM_AP")
+        p.reconstruct(fix_positions=False, reconstruction_method="DM_AP", **kw)
     with pytest.raises(NotImplementedError):
-        p.reconstruct(num_iter=1, gaussian_filter_sigma=0.5)
+        p.reconstruct(gaussian_filter_sigma=0.5, **kw)
 
     with pytest.raises(ValueError):
-        p.reconstruct(num_iter=1, reconstruction_method="DM_AP", max_batch_size=4)
+        p.reconstruct(reconstruction_method="DM_AP", max_batch_size=4, **kw)
+
+
+def test_device_cpu_preprocesses_on_host_and_refuses_to_reconstruct():
+    """device="cpu" is the reference's NumPy preprocessing; the reconstruction
+    itself runs on the GPU only and says so."""
+    from golden_io import Golden
+
+    g = Golden("ss_gd_32x32_det64")
+    p = g.build(device="cpu")
+    assert p._preprocessed and p._amplitudes.shape[0] == 32 * 32
+    with pytest.raises(ValueError, match="GPU only"):
+        p.reconstruct(num_iter=1)
+    with pytest.raises(ValueError, match="GPU only"):
+        p._return_self_consistency_errors()

@@ -11,14 +11,14 @@ The golden fixtures hold what the unmodified py4DSTEM 0.14.18 CPU path returned
 import numpy as np
 import pytest
 
-from golden_io import Golden, names
+from golden_io import Golden, PrepGolden, names, prep_names
 from oracle.ptycho_np import Oracle
 
 
 @pytest.mark.parametrize("name", names())
 def test_preprocess_matches_reference(name):
     g = Golden(name)
-    p = g.build(device="gpu")  # preprocess is host code: no GPU is touched here
+    p = g.build(device="cpu")  # device="cpu": the host preprocess, no GPU
     assert np.float32(p._mean_diffraction_intensity) == g.pre["mean_intensity"]
     np.testing.assert_array_equal(p._positions_px, g.pre["positions_px"])
     np.testing.assert_array_equal(p._probe, g.pre["probe_initial"])
@@ -30,10 +30,19 @@ def test_preprocess_matches_reference(name):
     np.testing.assert_array_equal(p._amplitudes[-1], g.pre["amplitude_last"])
 
 
+@pytest.mark.parametrize("name", prep_names())
+def test_preprocess_options_match_reference(name):
+    """Rotation search (curl and divergence, custom angles, forced transpose),
+    detector and positions masks, corner crop, per-pattern centre of mass and the
+    surface fits: the host preprocess gives the reference's bits."""
+    g = PrepGolden(name)
+    g.check(g.build(device="cpu"))
+
+
 @pytest.mark.parametrize("name", names())
 def test_oracle_reproduces_reference(name):
     g = Golden(name)
-    p = g.build(device="gpu")
+    p = g.build(device="cpu")
     o = Oracle(g.state(p)).reconstruct(**g.oracle_kwargs())
     np.testing.assert_array_equal(np.asarray(o.error_iterations, dtype=np.float64),
                                   g.out["error_iterations"])
@@ -48,7 +57,7 @@ def test_oracle_reproduces_reference(name):
 def test_oracle_float64_close_to_float32():
     """The FP64 evaluation of the same model stays within the float32 noise floor."""
     g = Golden("ms_gd_T3")
-    p = g.build(device="gpu")
+    p = g.build(device="cpu")
     o32 = Oracle(g.state(p)).reconstruct(**g.oracle_kwargs())
     o64 = Oracle(g.state(p), "float64").reconstruct(**g.oracle_kwargs())
     e32 = np.asarray(o32.error_iterations)
