@@ -16,6 +16,12 @@
 //   rotation_search_kernel    mean |curl| (or |div|) of the rotated CoM field
 //   pattern_normalize_kernel  periodic bilinear shift by -CoM, pattern sum,
 //                             sqrt(max(., 0)) with the optional corner crop
+// When every split of the summation tree halves a multiple of 16 (all square
+// detectors of 32..128 pixels), the tree is perfect: 2^d leaves of equal length
+// l. The fast kernels then give each of a leaf's 8 accumulator chains its own
+// lane (8 lanes per leaf, chains combined by shuffles in NumPy's order) and add
+// the leaves level by level in parallel. Other sizes take the *_general
+// kernels, in which one thread walks the tree.
 #include <cuda_runtime.h>
 
 #include "ptycho_internal.h"
@@ -122,7 +128,7 @@ __device__ __forceinline__ int pmod(int v, int m) {
 // ------------------------------------------------------------ centre of mass
 // cx[p] = sum(I kx) / sum(I), cy[p] = sum(I ky) / sum(I) with I = pattern * mask
 // (phase_base_class.py:646-672): kx, ky are the pixel indices along x and y.
-__global__ void __launch_bounds__(kPreThreads) pattern_com_kernel(
+__global__ void __launch_bounds__(kPreThreads) pattern_com_general_kernel(
     const float* __restrict__ in, int Qx, int Qy, const float* __restrict__ mask,
     int max_leaves, float* __restrict__ cx, float* __restrict__ cy) {
   extern __shared__ float4 smem4[];
@@ -220,7 +226,7 @@ __global__ void __launch_bounds__(kPreThreads) rotation_search_kernel(
 // (1-wx)(1-wy), wx(1-wy), (1-wx)wy, wx wy, added in that order), stores its sum
 // in sums[o] and sqrt(max(shifted, 0)) in amps, cropped to the four crop_w x
 // crop_w corners when crop_w > 0 (phase_base_class.py:1385-1445).
-__global__ void __launch_bounds__(kPreThreads) pattern_normalize_kernel(
+__global__ void __launch_bounds__(kPreThreads) pattern_normalize_general_kernel(
     const float* __restrict__ in, int Qx, int Qy, const int32_t* __restrict__ rows,
     const float* __restrict__ cfx, const float* __restrict__ cfy, int crop_w, int max_leaves,
     float* __restrict__ amps, float* __restrict__ sums) {
@@ -275,11 +281,198 @@ __global__ void __launch_bounds__(kPreThreads) pattern_normalize_kernel(
   if (threadIdx.x == 0) sums[o] = __fadd_rn(0.0f, pairwise_combine(N, leaf));
 }
 
+
+// ------------------------------------------------------- perfect-tree kernels
+// Chain j (0..7) of a leaf of length l starting at element `lo`: r = a[lo + j],
+// then r += a[lo + j + 8 k] for k = 1 .. l/8 - 1 (values from `val`). Lane j of
+// an 8-lane group holds chain j; the group's lane 0 gets the leaf sum
+// ((r0 + r1) + (r2 + r3)) + ((r4 + r5) + (r6 + r7)) plus the l % 8 tail in order.
+template <typename V>
+__device__ __forceinline__ float leaf_chain_sum(const V& val, int lo, int l) {
+  const int j = threadIdx.x & 7;
+  const int groups = l >> 3;
+  float r = val(lo + j);
+  for (int k = 1; k < groups; ++k) r = __fadd_rn(r, val(lo + j + 8 * k));
+  float o = __shfl_down_sync(0xffffffffu, r, 1, 8);
+  if ((j & 1) == 0) r = __fadd_rn(r, o);
+  o = __shfl_down_sync(0xffffffffu, r, 2, 8);
+  if ((j & 3) == 0) r = __fadd_rn(r, o);
+  o = __shfl_down_sync(0xffffffffu, r, 4, 8);
+  if (j == 0) {
+    r = __fadd_rn(r, o);
+    for (int i = groups * 8; i < l; ++i) r = __fadd_rn(r, val(lo + i));
+  }
+  return r;
+}
+
+// In-place pairwise sum of q arrays of L = 2^levels leaf sums each (arrays at
+// vals + q * L): level by level, vals[j] += vals[j + s]; the totals land in
+// vals[q * L]. Called by all threads of the block.
+__device__ __forceinline__ void tree_add(float* vals, int q, int L) {
+  for (int s = 1; s < L; s <<= 1) {
+    const int pairs = L / (2 * s);
+    for (int t = threadIdx.x; t < q * pairs; t += blockDim.x) {
+      const int a = t / pairs, k = t - (t / pairs) * pairs;
+      float* v = vals + a * L + 2 * s * k;
+      v[0] = __fadd_rn(v[0], v[s]);
+    }
+    __syncthreads();
+  }
+}
+
+// Centre of mass, perfect tree: block = 8 L threads (at least one warp), one
+// pattern per block, lane group g sums leaf g of the three quantities straight
+// from global memory (each warp load covers four 32-byte runs).
+__global__ void __launch_bounds__(1024) pattern_com_kernel(
+    const float* __restrict__ in, int Qx, int Qy, const float* __restrict__ mask, int leaf,
+    int L, float* __restrict__ cx, float* __restrict__ cy) {
+  __shared__ float vals[3 * 128];
+  const int N = Qx * Qy;
+  const int g = threadIdx.x >> 3;
+  const float* src = in + (size_t)blockIdx.x * N;
+  // lanes past the last leaf (blocks of one warp) sum elements 0..7 and drop
+  // the result: every lane of a warp takes part in the shuffles
+  const int lo = g < L ? g * leaf : 0;
+  const int len = g < L ? leaf : 8;
+  auto inten = [&](int e) {
+    const float v = __ldg(src + e);
+    return mask ? __fmul_rn(v, __ldg(mask + e)) : v;
+  };
+  const float s0 = leaf_chain_sum(inten, lo, len);
+  const float s1 = leaf_chain_sum(
+      [&](int e) { return __fmul_rn(inten(e), (float)(e / Qy)); }, lo, len);
+  const float s2 = leaf_chain_sum(
+      [&](int e) { return __fmul_rn(inten(e), (float)(e - (e / Qy) * Qy)); }, lo, len);
+  if (g < L && (threadIdx.x & 7) == 0) {
+    vals[g] = s0;
+    vals[L + g] = s1;
+    vals[2 * L + g] = s2;
+  }
+  __syncthreads();
+  tree_add(vals, 3, L);
+  if (threadIdx.x == 0) {
+    const float t0 = __fadd_rn(0.0f, vals[0]);
+    cx[blockIdx.x] = __fdiv_rn(__fadd_rn(0.0f, vals[L]), t0);
+    cy[blockIdx.x] = __fdiv_rn(__fadd_rn(0.0f, vals[2 * L]), t0);
+  }
+}
+
+// Normalisation, perfect tree: block = 8 L threads, one pattern per block. The
+// pattern is staged in shared memory, each thread forms its l/8 shifted values
+// (elements tid + k blockDim) in registers, writes them back in place, then the
+// lane groups sum the leaves and every thread writes its amplitudes.
+constexpr int kMaxPerThread = 16;  // l / 8 <= 128 / 8
+
+__global__ void __launch_bounds__(1024) pattern_normalize_kernel(
+    const float* __restrict__ in, int Qx, int Qy, const int32_t* __restrict__ rows,
+    const float* __restrict__ cfx, const float* __restrict__ cfy, int crop_w, int leaf, int L,
+    float* __restrict__ amps, float* __restrict__ sums) {
+  extern __shared__ float4 smem4[];
+  __shared__ float vals[128];
+  float* pat = reinterpret_cast<float*>(smem4);
+  const int N = Qx * Qy;
+  const int NT = blockDim.x;
+  const int tid = threadIdx.x;
+  const int o = blockIdx.x;
+  const int r = rows ? rows[o] : o;
+  const float* src = in + (size_t)r * N;
+  if ((N & 3) == 0 && (reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+    const float4* s4 = reinterpret_cast<const float4*>(src);
+    for (int e = tid; e < N / 4; e += NT) smem4[e] = __ldg(s4 + e);
+  } else {
+    for (int e = tid; e < N; e += NT) pat[e] = __ldg(src + e);
+  }
+
+  const float xs = -cfx[r], ys = -cfy[r];
+  const float xf = floorf(xs), yf = floorf(ys);
+  const float wx = __fsub_rn(xs, xf), wy = __fsub_rn(ys, yf);
+  const float ux = __fsub_rn(1.0f, wx), uy = __fsub_rn(1.0f, wy);
+  const float w00 = __fmul_rn(ux, uy), w10 = __fmul_rn(wx, uy);
+  const float w01 = __fmul_rn(ux, wy), w11 = __fmul_rn(wx, wy);
+  const int ixm = pmod((int)xf, Qx), iym = pmod((int)yf, Qy);
+  __syncthreads();
+
+  // shifted values of elements e = tid + k NT, (i, j) advanced incrementally
+  const int per = (N + NT - 1) / NT;
+  const int di = NT / Qy, dj = NT - (NT / Qy) * Qy;
+  float v[kMaxPerThread];
+  {
+    int i = tid / Qy, j = tid - (tid / Qy) * Qy;
+#pragma unroll
+    for (int k = 0; k < kMaxPerThread; ++k) {
+      if (k < per && tid + k * NT < N) {
+        int i0 = i - ixm;
+        if (i0 < 0) i0 += Qx;
+        int i1 = i0 - 1;
+        if (i1 < 0) i1 += Qx;
+        int j0 = j - iym;
+        if (j0 < 0) j0 += Qy;
+        int j1 = j0 - 1;
+        if (j1 < 0) j1 += Qy;
+        float t = __fmul_rn(pat[i0 * Qy + j0], w00);
+        t = __fadd_rn(t, __fmul_rn(pat[i1 * Qy + j0], w10));
+        t = __fadd_rn(t, __fmul_rn(pat[i0 * Qy + j1], w01));
+        t = __fadd_rn(t, __fmul_rn(pat[i1 * Qy + j1], w11));
+        v[k] = t;
+      }
+      i += di;
+      j += dj;
+      if (j >= Qy) {
+        j -= Qy;
+        ++i;
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < kMaxPerThread; ++k)
+    if (k < per && tid + k * NT < N) pat[tid + k * NT] = v[k];
+  __syncthreads();
+
+  const int g = tid >> 3;
+  const float ls = leaf_chain_sum([&](int e) { return pat[e]; }, g < L ? g * leaf : 0,
+                                  g < L ? leaf : 8);
+  if (g < L && (tid & 7) == 0) vals[g] = ls;
+
+  // amplitudes (numpy.maximum keeps its first argument unless it is below the second)
+  const int Cx = crop_w > 0 ? 2 * crop_w : Qx;
+  const int Cy = crop_w > 0 ? 2 * crop_w : Qy;
+  float* dst = amps + (size_t)o * Cx * Cy;
+  for (int e = tid; e < Cx * Cy; e += NT) {
+    int x = e / Cy, y = e - (e / Cy) * Cy;
+    if (crop_w > 0) {
+      if (x >= crop_w) x += Qx - Cx;
+      if (y >= crop_w) y += Qy - Cy;
+    }
+    float a = pat[x * Qy + y];
+    if (!(a >= 0.0f) && !isnan(a)) a = 0.0f;
+    dst[e] = __fsqrt_rn(a);
+  }
+  __syncthreads();
+  tree_add(vals, 1, L);
+  if (tid == 0) sums[o] = __fadd_rn(0.0f, vals[0]);
+}
+
 // Number of leaves of the pairwise tree over n values (host side, for sizing).
 int pairwise_leaf_count(int n) {
   if (n <= kPwBlock) return 1;
   const int h = pw_half(n);
   return pairwise_leaf_count(h) + pairwise_leaf_count(n - h);
+}
+
+// Perfect tree over n values: every split halves a multiple of 16, down to
+// 2^levels leaves of length leaf (8 <= leaf <= 128); at most 128 leaves (the
+// fast kernels run 8 lanes per leaf in one block of at most 1024 threads).
+bool pairwise_perfect(int n, int& leaf, int& levels) {
+  levels = 0;
+  while (n > kPwBlock) {
+    if (n % 16 != 0) return false;
+    n /= 2;
+    ++levels;
+  }
+  if (n < 8 || levels > 7) return false;
+  leaf = n;
+  return true;
 }
 
 cudaError_t set_smem(const void* fn, size_t bytes) {
@@ -293,12 +486,19 @@ size_t preprocess_smem_limit() { return 227 * 1024; }
 cudaError_t launch_pattern_com(const float* in, int num, int Qx, int Qy, const float* mask,
                                float* cx, float* cy, cudaStream_t s) {
   const int N = Qx * Qy;
+  int leaf = 0, levels = 0;
+  if (pairwise_perfect(N, leaf, levels)) {
+    const int L = 1 << levels;
+    const int threads = 8 * L < 32 ? 32 : 8 * L;
+    pattern_com_kernel<<<num, threads, 0, s>>>(in, Qx, Qy, mask, leaf, L, cx, cy);
+    return cudaGetLastError();
+  }
   const int L = pairwise_leaf_count(N);
   const size_t smem = sizeof(float) * ((size_t)N + 3 * L) + sizeof(int) * 2 * L;
   if (smem > preprocess_smem_limit()) return cudaErrorInvalidValue;
-  cudaError_t e = set_smem((const void*)pattern_com_kernel, smem);
+  cudaError_t e = set_smem((const void*)pattern_com_general_kernel, smem);
   if (e != cudaSuccess) return e;
-  pattern_com_kernel<<<num, kPreThreads, smem, s>>>(in, Qx, Qy, mask, L, cx, cy);
+  pattern_com_general_kernel<<<num, kPreThreads, smem, s>>>(in, Qx, Qy, mask, L, cx, cy);
   return cudaGetLastError();
 }
 
@@ -320,12 +520,23 @@ cudaError_t launch_pattern_normalize(const float* in, int Qx, int Qy, const int3
                                      int num_out, const float* cfx, const float* cfy,
                                      int crop_w, float* amps, float* sums, cudaStream_t s) {
   const int N = Qx * Qy;
+  int leaf = 0, levels = 0;
+  if (pairwise_perfect(N, leaf, levels)) {
+    const int L = 1 << levels;
+    const int threads = 8 * L < 32 ? 32 : 8 * L;
+    const size_t smem = sizeof(float) * (size_t)N;
+    cudaError_t e = set_smem((const void*)pattern_normalize_kernel, smem);
+    if (e != cudaSuccess) return e;
+    pattern_normalize_kernel<<<num_out, threads, smem, s>>>(in, Qx, Qy, rows, cfx, cfy, crop_w,
+                                                            leaf, L, amps, sums);
+    return cudaGetLastError();
+  }
   const int L = pairwise_leaf_count(N);
   const size_t smem = sizeof(float) * (2 * (size_t)N + L) + sizeof(int) * 2 * L;
   if (smem > preprocess_smem_limit()) return cudaErrorInvalidValue;
-  cudaError_t e = set_smem((const void*)pattern_normalize_kernel, smem);
+  cudaError_t e = set_smem((const void*)pattern_normalize_general_kernel, smem);
   if (e != cudaSuccess) return e;
-  pattern_normalize_kernel<<<num_out, kPreThreads, smem, s>>>(in, Qx, Qy, rows, cfx, cfy,
+  pattern_normalize_general_kernel<<<num_out, kPreThreads, smem, s>>>(in, Qx, Qy, rows, cfx, cfy,
                                                               crop_w, L, amps, sums);
   return cudaGetLastError();
 }
