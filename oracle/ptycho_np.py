@@ -165,7 +165,19 @@ class Oracle:
 
     # ------------------------------------------------------------- forward A7-A12
     def overlap(self, rows, cols, shifted):
-        """ptychographic_methods.py:1489-1527 (2D), 2300-2351 (2.5D), 2696-2734 (mixed)."""
+        """ptychographic_methods.py:1489-1527 (2D), 2300-2351 (2.5D), 2696-2734 (mixed),
+        3102-3160 (2.5D mixed)."""
+        if self.num_slices > 1 and self.mixed:
+            patches = self.object[:, rows, cols]
+            if self.object_type == "potential":
+                patches = np.exp(1j * patches)
+            probes = np.empty((self.num_slices,) + shifted.shape, dtype=patches.dtype)
+            probes[0] = shifted
+            for s in range(self.num_slices):
+                ov = np.expand_dims(patches[s], axis=1) * probes[s]
+                if s + 1 < self.num_slices:
+                    probes[s + 1] = self.ifft2(self.fft2(ov) * self.propagators[s])
+            return probes, patches, ov
         if self.num_slices > 1:
             patches = self.object[:, rows, cols]
             if self.object_type == "potential":
@@ -233,8 +245,36 @@ class Oracle:
         return np.conj(probe) * chi
 
     def adjoint(self, patches, shifted, positions_px, ew, step, m, fix_probe, projection):
-        """ptychographic_methods.py:1818-2069 (2D), 2353-2565 (2.5D), 2906-3093 (mixed)."""
+        """ptychographic_methods.py:1818-2069 (2D), 2353-2565 (2.5D), 2906-3093 (mixed),
+        3162-3340 (2.5D mixed)."""
         obj, probe = self.object, self.probe
+        if self.num_slices > 1 and self.mixed:
+            ew = ew.copy() if projection else ew
+            for s in reversed(range(self.num_slices)):
+                pr = shifted[s]
+                op = patches[s]
+                pn = np.zeros_like(obj[s])
+                upd = np.zeros_like(obj[s])
+                for i in range(self.num_probes):
+                    pn += self.scatter(np.abs(pr[:, i]) ** 2, positions_px)
+                    term = self.scatter(self._obj_term(op, pr[:, i], ew[:, i]), positions_px)
+                    upd += term if projection else step * term
+                pn = self._normaliser(pn, m)
+                if projection:
+                    obj[s] = upd * pn
+                else:
+                    obj[s] += upd * pn
+                ew *= np.expand_dims(np.conj(op), axis=1)
+                if s > 0:
+                    ew = self.ifft2(self.fft2(ew) * np.conj(self.propagators[s - 1]))
+                elif not fix_probe:
+                    on = self._normaliser(np.sum(np.abs(op) ** 2, axis=0), m)
+                    if projection:
+                        probe = np.sum(ew, axis=0) * on[None]
+                    else:
+                        probe += step * np.sum(ew, axis=0) * on[None]
+            self.object, self.probe = obj, probe
+            return
         if self.num_slices > 1:
             ew = ew.copy() if projection else ew
             for s in reversed(range(self.num_slices)):

@@ -167,7 +167,8 @@ def load_reference(root: str | None = None):
     """Import the reference phase classes and return them in a namespace.
 
     Returns an object with attributes ``SingleslicePtychography``,
-    ``MultislicePtychography``, ``MixedstatePtychography``, ``DataCube`` (the
+    ``MultislicePtychography``, ``MixedstatePtychography``,
+    ``MixedstateMultislicePtychography``, ``DataCube`` (the
     duck type above), ``utils`` (``process/phase/utils.py``) and ``root``.
     """
     root = root or os.environ.get("PY4DSTEM_REFERENCE", DEFAULT_REFERENCE_ROOT)
@@ -225,12 +226,15 @@ def load_reference(root: str | None = None):
         "py4DSTEM.process.phase.singleslice_ptychography")
     multi = importlib.import_module("py4DSTEM.process.phase.multislice_ptychography")
     mixed = importlib.import_module("py4DSTEM.process.phase.mixedstate_ptychography")
+    mixed_multi = importlib.import_module(
+        "py4DSTEM.process.phase.mixedstate_multislice_ptychography")
     phase_utils = importlib.import_module("py4DSTEM.process.phase.utils")
 
     ns = types.SimpleNamespace(
         SingleslicePtychography=single.SingleslicePtychography,
         MultislicePtychography=multi.MultislicePtychography,
         MixedstatePtychography=mixed.MixedstatePtychography,
+        MixedstateMultislicePtychography=mixed_multi.MixedstateMultislicePtychography,
         DataCube=DataCube,
         utils=phase_utils,
         root=root,

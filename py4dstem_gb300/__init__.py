@@ -1,6 +1,7 @@
 """GB300-native (sm_103a) iterative ptychography: a drop-in for the per-position
 forward/adjoint loop of py4DSTEM's SingleslicePtychography,
-MultislicePtychography and MixedstatePtychography.
+MultislicePtychography, MixedstatePtychography and
+MixedstateMultislicePtychography.
 
 Host code (this package) keeps the reference's Python API and preprocessing;
 the reconstruction loop runs in libptycho_gb300.so (csrc/, C ABI in
@@ -9,12 +10,14 @@ include/ptycho_gb300.h).
 
 from .datacube import Calibration, DataCube
 from .optics import ComplexProbe, electron_wavelength_angstrom
-from .ptychography import MixedstatePtychography, MultislicePtychography, SingleslicePtychography
+from .ptychography import (MixedstateMultislicePtychography, MixedstatePtychography,
+                           MultislicePtychography, SingleslicePtychography)
 
 __all__ = [
     "Calibration",
     "ComplexProbe",
     "DataCube",
+    "MixedstateMultislicePtychography",
     "MixedstatePtychography",
     "MultislicePtychography",
     "SingleslicePtychography",

@@ -56,8 +56,6 @@ int check_geometry(const ptycho_geometry* g) {
     return fail(PTYCHO_ERR_INVALID_ARGUMENT, "unknown bits in geometry.flags (0x%x)", g->flags);
   if (g->num_slices < 1 || g->num_probes < 1)
     return fail(PTYCHO_ERR_INVALID_ARGUMENT, "num_slices and num_probes must be >= 1");
-  if (g->num_slices > 1 && g->num_probes > 1)
-    return fail(PTYCHO_ERR_UNSUPPORTED, "mixed-state multislice is not supported");
   if (g->num_probes > 16) return fail(PTYCHO_ERR_UNSUPPORTED, "at most 16 probe modes");
   if (!roi_supported(g->roi_x, g->roi_y))
     return fail(PTYCHO_ERR_UNSUPPORTED,
@@ -92,7 +90,9 @@ Workspace workspace_layout(int Sx, int Sy, int Px, int Py, int T, int M, int B,
   w.st_nobj = take(sizeof(float) * T * B * N);
   w.st_probe = take(sizeof(float2) * B * M * N);
   w.st_nprobe = take(sizeof(float) * B * N);
-  w.scratch_f = take(T == 1 || keep_farfield ? sizeof(float2) * B * M * N : 0);
+  const bool mixed_ms = T > 1 && M > 1;
+  w.scratch_f = take(T == 1 || keep_farfield || mixed_ms ? sizeof(float2) * B * M * N : 0);
+  w.st_pm = take(mixed_ms ? sizeof(float2) * T * B * M * N : 0);
   w.pos_round = take(sizeof(int2) * B);
   w.err = take(sizeof(float) * B);
   w.obj_grad = take(sizeof(float2) * T * P);
@@ -120,6 +120,7 @@ void bind_workspace(BatchArgs& a, void* base, const Workspace& w) {
   a.st_probe = reinterpret_cast<float2*>(p + w.st_probe);
   a.st_nprobe = reinterpret_cast<float*>(p + w.st_nprobe);
   a.scratch_f = reinterpret_cast<float2*>(p + w.scratch_f);
+  a.st_pm = reinterpret_cast<float2*>(p + w.st_pm);
   a.pos_round = reinterpret_cast<int2*>(p + w.pos_round);
   a.err = reinterpret_cast<float*>(p + w.err);
   a.obj_grad = reinterpret_cast<float2*>(p + w.obj_grad);
@@ -248,6 +249,8 @@ int ptycho_gd_batch(const ptycho_geometry* g, void* object, void* probe,
   a.fix_probe = fix_probe ? 1 : 0;
   a.mixed_formula = (g->num_probes > 1 || (g->flags & PTYCHO_FLAG_MIXED_STATE)) ? 1 : 0;
   a.keep_farfield = (g->flags & PTYCHO_FLAG_KEEP_FARFIELD) ? 1 : 0;
+  if (a.keep_farfield && g->num_slices > 1 && g->num_probes > 1)
+    return fail(PTYCHO_ERR_UNSUPPORTED, "PTYCHO_FLAG_KEEP_FARFIELD for mixed-state multislice");
   return run_batch(g, object, probe, amplitudes, amplitude_rows, positions_px, position_rows,
                    batch, detector_mask, propagators, error_accum, workspace, workspace_bytes,
                    stream, a);
@@ -268,6 +271,8 @@ int ptycho_projection_batch(const ptycho_geometry* g, void* object, void* probe,
   if (g->flags & PTYCHO_FLAG_KEEP_FARFIELD)
     return fail(PTYCHO_ERR_UNSUPPORTED, "PTYCHO_FLAG_KEEP_FARFIELD applies to gradient-descent "
                                         "batches only");
+  if (g->num_slices > 1 && g->num_probes > 1)
+    return fail(PTYCHO_ERR_UNSUPPORTED, "projection sets for mixed-state multislice");
   a.projection = 1;
   a.pa = projection_a;
   a.pb = projection_b;
@@ -295,6 +300,8 @@ int ptycho_position_correction(const ptycho_geometry* g, const void* object,
   if (!(g->flags & PTYCHO_FLAG_KEEP_FARFIELD))
     return fail(PTYCHO_ERR_INVALID_ARGUMENT, "position correction needs the far fields of a "
                                              "batch run with PTYCHO_FLAG_KEEP_FARFIELD");
+  if (g->num_slices > 1 && g->num_probes > 1)
+    return fail(PTYCHO_ERR_UNSUPPORTED, "position correction for mixed-state multislice");
   if (!object || !amplitudes || !positions_px || !positions_initial)
     return fail(PTYCHO_ERR_INVALID_ARGUMENT, "object, amplitudes, positions_px and "
                                              "positions_initial must be non-null");
@@ -365,6 +372,8 @@ int ptycho_gd_gradient(const ptycho_geometry* g, const void* object, const void*
                                              "and loss must be non-null");
   if (g->num_slices > 1 && !propagators)
     return fail(PTYCHO_ERR_INVALID_ARGUMENT, "multislice needs propagators");
+  if (g->num_slices > 1 && g->num_probes > 1)
+    return fail(PTYCHO_ERR_UNSUPPORTED, "gradients of mixed-state multislice models");
   a.mixed_formula = (g->num_probes > 1 || (g->flags & PTYCHO_FLAG_MIXED_STATE)) ? 1 : 0;
   a.object = const_cast<void*>(object);
   a.probe = static_cast<float2*>(const_cast<void*>(probe));

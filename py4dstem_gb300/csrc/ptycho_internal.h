@@ -57,6 +57,7 @@ struct BatchArgs {
   float2* st_probe;     // (B,M,N)
   float* st_nprobe;     // (B,N)
   float2* scratch_f;    // (B,M,N) far fields FFT2(psi_m): single slice, or kept for A16
+  float2* st_pm;        // (T,B,M,N) probe of each slice and mode (mixed-state multislice)
   int2* pos_round;      // (B)
   float* err;           // (B)
   float2* obj_grad;     // (T,P)
@@ -74,7 +75,7 @@ struct BatchArgs {
 };
 
 struct Workspace {
-  size_t probe_spec, tw, st_obj, st_nobj, st_probe, st_nprobe, scratch_f, pos_round, err,
+  size_t probe_spec, tw, st_obj, st_nobj, st_probe, st_nprobe, scratch_f, st_pm, pos_round, err,
       obj_grad, obj_nrm, tile_max, obj_part, obj_npart, probe_part, probe_npart, probe_bmax, probe_grad,
       probe_nrm, com, red, total;
 };

@@ -103,12 +103,14 @@ __global__ void __launch_bounds__(NT, 1) probe_spectrum_kernel(BatchArgs a) {
 // Everything of one scan position b (see the file header); the block's shared
 // memory holds the wave, the tables and the ramps. `red` is the block-sum scratch.
 // kMode fixes at compile time what the batch is (fewer live registers, fewer
-// spills): 0 any, 1 single slice / single probe, 2 single-slice mixed state,
-// 3 multislice / single probe; modes 1-3 are gradient descent with no
-// projection sets, forward-only pass, kept far fields or exact probe gradient.
+// spills): 0 any single slice or single-probe multislice, 1 single slice /
+// single probe, 2 single-slice mixed state, 3 multislice / single probe, 4
+// mixed-state multislice; modes 1-3 are gradient descent with no projection
+// sets, forward-only pass, kept far fields or exact probe gradient; mode 4 is
+// gradient descent or the forward-only pass.
 template <int SX, int SY, int NT, int kMode>
 __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, float* red) {
-  constexpr bool kPlain = kMode != 0;
+  constexpr bool kPlain = kMode >= 1 && kMode <= 3;
   constexpr bool kT1 = kMode == 1 || kMode == 2;
   constexpr bool kM1 = kMode == 1 || kMode == 3;
   using L = Layout<SX, SY>;
@@ -136,7 +138,7 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
   const int x0 = (int)rx;
   const int y0 = (int)ry;
   const float invN = 1.0f / (float)N;
-  const bool ps = !kPlain && a.projection != 0;
+  const bool ps = !kPlain && kMode != 4 && a.projection != 0;
   const bool fwd = !kPlain && a.forward_only != 0;  // per-position error only (block-uniform)
   const float* amp = a.amplitudes + (size_t)arow * N;
 
@@ -198,7 +200,7 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
   // S_b^H (conj(O) chi) = IFFT2(conj(ramp) FFT2(conj(O) chi)). The reference's
   // update omits S_b^H; here the FFT2 and the conj(ramp) are applied per position
   // and the IFFT2 once to the batch sum. buf holds conj(O) chi on entry.
-  const bool exact = !kPlain && a.exact_probe_grad != 0;
+  const bool exact = !kPlain && kMode != 4 && a.exact_probe_grad != 0;
   auto unshift_probe_term = [&](float2* dst) {
     fft2d<SX, SY, NT, -1>(buf, twx, twy);
     for (int e = tid; e < N; e += NT) {
@@ -213,6 +215,111 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
   const float px_ = 1.0f - a.pa - a.pb;  // projection x
   const float py_ = 1.0f - a.pc;          // projection y
 
+  if constexpr (kMode == 4) {
+    // ------------------------------------------ mixed-state multislice (GD)
+    // (ptychographic_methods.py:3102-3160 forward, 2742-2804 projection,
+    // 3162-3258 adjoint). Every mode runs through the slices on its own:
+    // P_{s+1,m} = IFFT2(FFT2(O_s P_{s,m}) H_s), with each P_{s,m} stashed; the far
+    // fields F_m share the ratio A / sqrt(sum_m |F_m|^2); the adjoint of each mode
+    // walks back through the slices, adding conj(P_{s,m}) chi_{s,m} and |P_{s,m}|^2
+    // into slice s's staged terms.
+    for (int m = 0; m < M; ++m) {
+      shifted_probe(m);
+      for (int s = 0; s < T; ++s) {
+        float2* pst = a.st_pm + (((size_t)s * a.B + b) * M + m) * N;
+        for (int e = tid; e < N; e += NT) {
+          const int x = e / SY, y = e % SY;
+          const float2 p = c_scale(buf[x * LD + y], invN);
+          pst[e] = p;
+          buf[x * LD + y] = c_mul(load_object(a, s, obj_x(x), obj_y(y)), p);
+        }
+        __syncthreads();
+        if (s + 1 < T) {
+          fft2d<SX, SY, NT, -1>(buf, twx, twy);
+          const float2* h = a.props + (size_t)s * N;
+          for (int e = tid; e < N; e += NT) {
+            const int idx = (e / SY) * LD + e % SY;
+            buf[idx] = c_mul(buf[idx], h[e]);
+          }
+          __syncthreads();
+          fft2d<SX, SY, NT, +1>(buf, twx, twy);
+        }
+      }
+      fft2d<SX, SY, NT, -1>(buf, twx, twy);
+      float2* f = a.scratch_f + ((size_t)b * M + m) * N;
+      for (int e = tid; e < N; e += NT) {
+        const float2 v = buf[(e / SY) * LD + e % SY];
+        f[e] = v;
+        const float av = hypotf(v.x, v.y);  // |F_m|^2 as numpy forms it
+        itot[e] = (m == 0 ? 0.0f : itot[e]) + av * av;
+      }
+      __syncthreads();
+    }
+    for (int e = tid; e < N; e += NT) {
+      const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
+      float tot = sqrtf(itot[e]);
+      if (a.det_mask) tot = sqrtf(itot[e] * mk * mk);
+      const float A = amp[e];
+      const float d = A - tot;
+      err += d * d;
+      itot[e] = tot == 0.0f ? 0.0f : A / tot;
+    }
+    __syncthreads();
+    if (fwd) goto done;
+    for (int m = 0; m < M; ++m) {
+      const float2* f = a.scratch_f + ((size_t)b * M + m) * N;
+      for (int e = tid; e < N; e += NT) {
+        const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
+        float2 fv = f[e];
+        if (a.det_mask) fv = c_scale(fv, mk);
+        float2 r = c_sub(c_scale(fv, itot[e]), fv);
+        if (a.det_mask) r = c_scale(r, mk);
+        buf[(e / SY) * LD + e % SY] = r;
+      }
+      __syncthreads();
+      fft2d<SX, SY, NT, +1>(buf, twx, twy);
+      for (int s = T - 1; s >= 0; --s) {
+        const float2* pst = a.st_pm + (((size_t)s * a.B + b) * M + m) * N;
+        float2* gobj = a.st_obj + ((size_t)s * a.B + b) * N;
+        float* nobj = a.st_nobj + ((size_t)s * a.B + b) * N;
+        for (int e = tid; e < N; e += NT) {
+          const int x = e / SY, y = e % SY;
+          const int idx = x * LD + y;
+          const float2 chi = c_scale(buf[idx], invN);
+          const float2 p = pst[e];
+          const float2 o = load_object(a, s, obj_x(x), obj_y(y));
+          const float2 g = object_term(a.potential, o, p, chi);
+          const float pn = c_abs2(p);
+          if (m == 0) {
+            gobj[e] = g;
+            nobj[e] = pn;
+          } else {
+            gobj[e] = c_add(gobj[e], g);
+            nobj[e] = nobj[e] + pn;
+          }
+          const float2 bt = c_mul(chi, make_float2(o.x, -o.y));  // chi * conj(O_s)
+          if (s > 0) {
+            buf[idx] = bt;
+          } else {
+            a.st_probe[((size_t)b * M + m) * N + e] = bt;
+            if (m == 0) a.st_nprobe[(size_t)b * N + e] = c_abs2(o);
+          }
+        }
+        __syncthreads();
+        if (s > 0) {
+          fft2d<SX, SY, NT, -1>(buf, twx, twy);
+          const float2* h = a.props + (size_t)(s - 1) * N;
+          for (int e = tid; e < N; e += NT) {
+            const int idx = (e / SY) * LD + e % SY;
+            const float2 hv = h[e];
+            buf[idx] = c_mul(buf[idx], make_float2(hv.x, -hv.y));
+          }
+          __syncthreads();
+          fft2d<SX, SY, NT, +1>(buf, twx, twy);
+        }
+      }
+    }
+  } else {
   if (T == 1) {
     // ------------------------------------------------------------ single slice
     const bool mixed = kMode == 2 || (kMode == 0 && (M > 1 || a.mixed_formula));
@@ -473,6 +580,8 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
       }
     }
   }
+
+  }  // kMode != 4
 
 done:
   const float tot = block_sum<NT>(err, red);
@@ -820,7 +929,8 @@ cudaError_t launch_spectrum_t(const BatchArgs& a, cudaStream_t s) {
 
 template <int SX, int SY, int NT>
 cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
-  const bool mixed = a.T == 1 && (a.M > 1 || a.mixed_formula);
+  const bool mixed_ms = a.T > 1 && a.M > 1;
+  const bool mixed = (a.T == 1 && (a.M > 1 || a.mixed_formula)) || mixed_ms;
   const size_t smem = Layout<SX, SY>::smem_bytes(mixed);
   static bool configured = false;
   if (!configured) {
@@ -830,20 +940,25 @@ cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(position_kernel<SX, SY, NT, 1>, attr, bytes);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(position_kernel<SX, SY, NT, 2>, attr, bytes);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(position_kernel<SX, SY, NT, 3>, attr, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(position_kernel<SX, SY, NT, 4>, attr, bytes);
     if (e != cudaSuccess) return e;
     configured = true;
   }
   // plain gradient-descent batches run an instantiation with the other modes
-  // compiled out (see position_one)
+  // compiled out (see position_one); mixed-state multislice has its own
+  if (mixed_ms && (a.projection || a.keep_farfield || a.exact_probe_grad))
+    return cudaErrorNotSupported;
   const bool plain = !a.projection && !a.forward_only && !a.keep_farfield && !a.exact_probe_grad;
-  const int mode = !plain ? 0
+  const int mode = mixed_ms ? 4
+                   : !plain ? 0
                    : a.T == 1 ? (a.M == 1 && !a.mixed_formula ? 1 : 2)
-                   : (a.M == 1 ? 3 : 0);
+                   : 3;
   timing_before(s);
   switch (mode) {
     case 1: position_kernel<SX, SY, NT, 1><<<a.B, NT, smem, s>>>(a); break;
     case 2: position_kernel<SX, SY, NT, 2><<<a.B, NT, smem, s>>>(a); break;
     case 3: position_kernel<SX, SY, NT, 3><<<a.B, NT, smem, s>>>(a); break;
+    case 4: position_kernel<SX, SY, NT, 4><<<a.B, NT, smem, s>>>(a); break;
     default: position_kernel<SX, SY, NT, 0><<<a.B, NT, smem, s>>>(a); break;
   }
   cudaError_t e = cudaGetLastError();

@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(NT) object_update_kernel(BatchArgs a, int ntil
   const size_t o = (size_t)s * P + i;
   const float nrm = normaliser(a.obj_nrm[o], smax, a.norm_min);
   const float2 g = a.obj_grad[o];
-  const bool mixed_order = a.T == 1 && (a.M > 1 || a.mixed_formula);
+  const bool mixed_order = a.M > 1 || a.mixed_formula;
   if (a.potential) {
     float* obj = reinterpret_cast<float*>(a.object);
     if (a.projection) {

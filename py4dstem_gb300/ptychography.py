@@ -455,6 +455,10 @@ class _PtychographyBase(PreprocessMixin):
         if correct_positions and use_projection:
             raise NotImplementedError(
                 "position correction (fix_positions=False) runs with gradient descent only")
+        if self._multislice and self._mixed and (use_projection or correct_positions):
+            raise NotImplementedError(
+                "mixed-state multislice runs gradient descent with fixed positions only "
+                "(projection sets and position correction are not implemented for it)")
 
         J = self._num_diffraction_patterns
         shuffled = np.arange(J)
@@ -1008,6 +1012,176 @@ class MultislicePtychography(_PtychographyBase):
             detector_fourier_mask=detector_fourier_mask, store_iterations=store_iterations,
             reset=reset, device=device, clear_fft_cache=clear_fft_cache,
             object_type=object_type,
+            unsupported=dict(
+                global_affine_transformation=global_affine_transformation and not fix_positions,
+                fix_probe_aperture=fix_probe_aperture and not fix_probe,
+                constrain_probe_amplitude=constrain_probe_amplitude and not fix_probe,
+                constrain_probe_fourier_amplitude=constrain_probe_fourier_amplitude
+                and not fix_probe,
+                fit_probe_aberrations=fit_probe_aberrations and not fix_probe,
+                gaussian_filter=gaussian_filter and gaussian_filter_sigma is not None,
+                butterworth_filter=butterworth_filter
+                and (q_lowpass is not None or q_highpass is not None),
+                kz_regularization_filter=kz_regularization_filter
+                and kz_regularization_gamma is not None,
+                identical_slices=identical_slices,
+                tv_denoise=tv_denoise and tv_denoise_weights is not None,
+                tv_denoise_chambolle=tv_denoise_chambolle
+                and tv_denoise_weight_chambolle is not None,
+            ))
+
+
+class MixedstateMultislicePtychography(_PtychographyBase):
+    """Mixed-state multislice ptychography: object (T,Px,Py), probe (M,Sx,Sy)
+    incoherent modes, each propagated through the slices
+    (mixedstate_multislice_ptychography.py; operators
+    ptychographic_methods.py:3096-3258). Gradient descent with fixed positions."""
+
+    _multislice = True
+    _mixed = True
+
+    def __init__(
+        self,
+        energy: float,
+        num_slices: int,
+        slice_thicknesses: Union[float, Sequence[float]],
+        num_probes: int = None,
+        datacube=None,
+        semiangle_cutoff: float = None,
+        semiangle_cutoff_pixels: float = None,
+        rolloff: float = 2.0,
+        vacuum_probe_intensity: np.ndarray = None,
+        polar_parameters: Mapping[str, float] = None,
+        object_padding_px: Tuple[int, int] = None,
+        initial_object_guess: np.ndarray = None,
+        initial_probe_guess: np.ndarray = None,
+        initial_scan_positions: np.ndarray = None,
+        object_fov_ang: Tuple[float, float] = None,
+        positions_offset_ang: np.ndarray = None,
+        theta_x: float = 0,
+        theta_y: float = 0,
+        middle_focus: bool = False,
+        object_type: str = "complex",
+        positions_mask: np.ndarray = None,
+        verbose: bool = True,
+        device: str = "gpu",
+        storage: str = None,
+        clear_fft_cache: bool = True,
+        name: str = "multi-slice_ptychographic_reconstruction",
+        **kwargs,
+    ):
+        if initial_probe_guess is None or isinstance(initial_probe_guess, ComplexProbe):
+            if num_probes is None:
+                raise ValueError(
+                    "If initial_probe_guess is None, or a ComplexProbe object, "
+                    "num_probes must be specified.")
+        else:
+            if len(initial_probe_guess.shape) != 3:
+                raise ValueError("Specified initial_probe_guess must have dimensions (N,Sx,Sy).")
+            num_probes = initial_probe_guess.shape[0]
+        slice_thicknesses = np.array(slice_thicknesses)
+        if slice_thicknesses.shape == ():
+            slice_thicknesses = np.tile(slice_thicknesses, num_slices - 1)
+        elif slice_thicknesses.shape[0] != (num_slices - 1):
+            raise ValueError(
+                f"slice_thicknesses must have length {num_slices - 1}, "
+                f"not {slice_thicknesses.shape[0]}.")
+        self._common_init(energy, datacube, semiangle_cutoff, semiangle_cutoff_pixels, rolloff,
+                          vacuum_probe_intensity, polar_parameters, initial_object_guess,
+                          initial_probe_guess, initial_scan_positions, object_fov_ang,
+                          positions_offset_ang, object_padding_px, object_type, positions_mask,
+                          verbose, device, storage, clear_fft_cache, name, kwargs)
+        if middle_focus:
+            half = slice_thicknesses.mean() * num_slices / 2
+            self._polar_parameters["C10"] -= half
+        self._num_probes = num_probes
+        self._num_slices = num_slices
+        self._slice_thicknesses = slice_thicknesses
+        self._theta_x = theta_x
+        self._theta_y = theta_y
+
+    preprocess = SingleslicePtychography.preprocess
+
+    def reconstruct(
+        self,
+        num_iter: int = 8,
+        reconstruction_method: str = "gradient-descent",
+        reconstruction_parameter: float = 1.0,
+        reconstruction_parameter_a: float = None,
+        reconstruction_parameter_b: float = None,
+        reconstruction_parameter_c: float = None,
+        max_batch_size: int = None,
+        seed_random: int = None,
+        step_size: float = 0.5,
+        normalization_min: float = 1,
+        positions_step_size: float = 0.9,
+        fix_probe_com: bool = True,
+        orthogonalize_probe: bool = True,
+        fix_probe: bool = False,
+        fix_probe_aperture: bool = False,
+        constrain_probe_amplitude: bool = False,
+        constrain_probe_amplitude_relative_radius: float = 0.5,
+        constrain_probe_amplitude_relative_width: float = 0.05,
+        constrain_probe_fourier_amplitude: bool = False,
+        constrain_probe_fourier_amplitude_max_width_pixels: float = 3.0,
+        constrain_probe_fourier_amplitude_constant_intensity: bool = False,
+        fix_positions: bool = True,
+        fix_positions_com: bool = True,
+        max_position_update_distance: float = None,
+        max_position_total_distance: float = None,
+        global_affine_transformation: bool = False,
+        gaussian_filter_sigma: float = None,
+        gaussian_filter: bool = True,
+        fit_probe_aberrations: bool = False,
+        fit_probe_aberrations_max_angular_order: int = 4,
+        fit_probe_aberrations_max_radial_order: int = 4,
+        fit_probe_aberrations_remove_initial: bool = False,
+        fit_probe_aberrations_using_scikit_image: bool = True,
+        num_probes_fit_aberrations: int = np.inf,
+        butterworth_filter: bool = True,
+        q_lowpass: float = None,
+        q_highpass: float = None,
+        butterworth_order: float = 2,
+        kz_regularization_filter: bool = True,
+        kz_regularization_gamma: Union[float, np.ndarray] = None,
+        identical_slices: bool = False,
+        object_positivity: bool = True,
+        shrinkage_rad: float = 0.0,
+        fix_potential_baseline: bool = True,
+        detector_fourier_mask: np.ndarray = None,
+        pure_phase_object: bool = False,
+        tv_denoise_chambolle: bool = True,
+        tv_denoise_weight_chambolle=None,
+        tv_denoise_pad_chambolle=1,
+        tv_denoise: bool = True,
+        tv_denoise_weights=None,
+        tv_denoise_inner_iter=40,
+        store_iterations: bool = False,
+        progress_bar: bool = True,
+        reset: bool = None,
+        device: str = None,
+        clear_fft_cache: bool = None,
+        object_type: str = None,
+    ):
+        """Run `num_iter` mixed-state multislice iterations on the GPU
+        (mixedstate_multislice_ptychography.py:723-1146)."""
+        return self._reconstruct_impl(
+            num_iter=num_iter, reconstruction_method=reconstruction_method,
+            reconstruction_parameter=reconstruction_parameter,
+            reconstruction_parameter_a=reconstruction_parameter_a,
+            reconstruction_parameter_b=reconstruction_parameter_b,
+            reconstruction_parameter_c=reconstruction_parameter_c,
+            max_batch_size=max_batch_size, seed_random=seed_random, step_size=step_size,
+            normalization_min=normalization_min, fix_probe_com=fix_probe_com,
+            fix_probe=fix_probe, fix_positions=fix_positions,
+            fix_positions_com=fix_positions_com, positions_step_size=positions_step_size,
+            max_position_update_distance=max_position_update_distance,
+            max_position_total_distance=max_position_total_distance,
+            pure_phase_object=pure_phase_object, object_positivity=object_positivity,
+            shrinkage_rad=shrinkage_rad, fix_potential_baseline=fix_potential_baseline,
+            detector_fourier_mask=detector_fourier_mask, store_iterations=store_iterations,
+            reset=reset, device=device, clear_fft_cache=clear_fft_cache,
+            object_type=object_type, orthogonalize_probe=orthogonalize_probe,
             unsupported=dict(
                 global_affine_transformation=global_affine_transformation and not fix_positions,
                 fix_probe_aperture=fix_probe_aperture and not fix_probe,

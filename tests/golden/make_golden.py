@@ -95,6 +95,15 @@ CASES = {
         cls="single", ctor=dict(object_fov_ang=(32.0, 32.0)), guess=(128, 128),
         mask_seed=5,
         rec=dict(num_iter=4, max_batch_size=16, step_size=0.5, seed_random=8)),
+    # mixed-state multislice: two modes through three slices
+    "mms_gd_T3M2": dict(
+        gen=dict(name="mms", seed=24, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=96, num_slices=3, slice_thickness=20.0, num_modes=2,
+                 mode_weights=(0.8, 0.2)),
+        cls="mixed_multi", ctor=dict(object_fov_ang=(24.0, 24.0), num_slices=3,
+                                     slice_thicknesses=20.0, num_probes=2),
+        global_seed=9, guess=(3, 96, 96),
+        rec=dict(num_iter=5, max_batch_size=25, step_size=0.5, seed_random=10)),
     "mixed_gd_M3": dict(
         gen=dict(name="mx", seed=14, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
                  detector=64, object_px=96, num_modes=3, mode_weights=(0.7, 0.2, 0.1)),
@@ -207,7 +216,8 @@ def make_case(ref, name, spec):
                       q_pixel_units="mrad")
     ctor = dict(energy=300e3, semiangle_cutoff=20.0, defocus=100.0, **spec["ctor"])
     cls = {"single": ref.SingleslicePtychography, "multi": ref.MultislicePtychography,
-           "mixed": ref.MixedstatePtychography}[spec["cls"]]
+           "mixed": ref.MixedstatePtychography,
+           "mixed_multi": ref.MixedstateMultislicePtychography}[spec["cls"]]
     extra = {}
     guess = None
     if "guess" in spec:

@@ -120,7 +120,8 @@ class Golden:
         if "object_fov_ang" in ctor:
             ctor["object_fov_ang"] = tuple(ctor["object_fov_ang"])
         cls = {"single": api.SingleslicePtychography, "multi": api.MultislicePtychography,
-               "mixed": api.MixedstatePtychography}[m["cls"]]
+               "mixed": api.MixedstatePtychography,
+               "mixed_multi": api.MixedstateMultislicePtychography}[m["cls"]]
         if self.guess is not None:
             ctor["initial_object_guess"] = self.guess.copy()
         if m.get("global_seed") is not None:
@@ -139,8 +140,9 @@ class Golden:
             mean_intensity=p._mean_diffraction_intensity,
             fov_mask_inverse=p._object_fov_mask_inverse, object_type=p._object_type,
             num_slices=m["ctor"].get("num_slices", 1), num_probes=m["ctor"].get("num_probes", 1),
-            mixed=m["cls"] == "mixed",
-            propagators=getattr(p, "_propagator_arrays", None) if m["cls"] == "multi" else None,
+            mixed=m["cls"] in ("mixed", "mixed_multi"),
+            propagators=(getattr(p, "_propagator_arrays", None)
+                         if m["cls"] in ("multi", "mixed_multi") else None),
             sampling=tuple(p.sampling))
 
     def oracle_kwargs(self):

@@ -92,6 +92,36 @@ def test_multislice(cuda, slices, potential):
     compare(st, 2e-5, 2e-5, 2e-5, num_iter=1, max_batch_size=8, seed_random=4, **OFF)
 
 
+@pytest.mark.parametrize("S,slices,modes,potential", [(64, 2, 2, False), (32, 3, 3, False),
+                                                      (64, 2, 2, True), (128, 2, 2, False),
+                                                      (96, 3, 2, False)])
+def test_mixed_state_multislice(cuda, S, slices, modes, potential):
+    """Every probe mode through every slice (kernel mode 4), two iterations."""
+    st = make_state(S=S, J=16, slices=slices, modes=modes, potential=potential,
+                    seed=40 + S + slices + modes)
+    compare(st, 2e-5, 2e-5, 2e-5, num_iter=2, max_batch_size=8, seed_random=5, **OFF)
+
+
+def test_mixed_state_multislice_mask_fix_probe_constraints(cuda):
+    st = make_state(S=64, J=16, slices=2, modes=2, seed=47)
+    mask = (np.random.default_rng(3).uniform(size=(64, 64)) > 0.05).astype(np.float32)
+    compare(st, 2e-5, 2e-5, 2e-5, num_iter=2, max_batch_size=8, seed_random=6,
+            detector_fourier_mask=mask, fix_probe=True, **OFF)
+    # with the per-iteration constraints (mode orthogonalisation amplifies rounding
+    # in the weak modes) the bar of test_constraints_several_iterations
+    st = make_state(S=64, J=16, slices=2, modes=3, seed=48)
+    compare(st, 1e-4, 1e-4, 2e-5, num_iter=3, max_batch_size=8, seed_random=7,
+            fix_probe_com=True, fix_potential_baseline=True, orthogonalize_probe=True)
+
+
+def test_mixed_state_multislice_rejects_projection_sets(cuda):
+    from py4dstem_gb300 import _native
+
+    st = make_state(S=32, J=9, slices=2, modes=2, seed=49)
+    with pytest.raises(_native.PtychoError):
+        gpu_reconstruct(st, num_iter=1, method="PS", a=0.0, b=0.5, c=2.0)
+
+
 @pytest.mark.parametrize("method,abc", [("DM", (-1.0, 1.0, 2.0)), ("RAAR", (0.0, 0.5, 2.0)),
                                         ("RRR", (-1.0, 1.0, 2.0)), ("SUPERFLIP", (0.0, 1.0, 2.0)),
                                         ("GP", (0.3, 0.6, 1.4))])
