@@ -10,6 +10,7 @@ include/ptycho_gb300.h).
 
 from .datacube import Calibration, DataCube
 from .optics import ComplexProbe, electron_wavelength_angstrom
+from .io import read, save
 from .ptychography import (MixedstateMultislicePtychography, MixedstatePtychography,
                            MultislicePtychography, SingleslicePtychography)
 
@@ -22,6 +23,8 @@ __all__ = [
     "MultislicePtychography",
     "SingleslicePtychography",
     "electron_wavelength_angstrom",
+    "read",
+    "save",
 ]
 
 __version__ = "0.1.0"

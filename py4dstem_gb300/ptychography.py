@@ -179,6 +179,12 @@ class _PtychographyBase(PreprocessMixin):
         self._storage = storage
         return self
 
+    def save(self, path):
+        """Write this reconstruction to `path` (.npz; see py4dstem_gb300.io)."""
+        from . import io
+
+        io.save(path, self)
+
     def set_save_defaults(self, save_datacube=False, save_exit_waves=False,
                           save_iterations=True, save_iterations_frequency=1):
         self._save_datacube = save_datacube

@@ -146,3 +146,24 @@ def test_graph_replay_matches_eager(cuda, name):
     np.testing.assert_array_equal(out[0][0], out[1][0])
     np.testing.assert_array_equal(out[0][1], out[1][1])
     assert out[0][2] == out[1][2]
+
+
+def test_save_read_continue(cuda, tmp_path):
+    """A reconstruction saved, read back and preprocessed again continues from
+    the saved object and probe."""
+    import py4dstem_gb300 as pg
+
+    g = Golden("ss_gd_det128")
+    p = g.build()
+    kw = g.rec_kwargs()
+    kw["num_iter"] = 2
+    p.reconstruct(**kw)
+    p.set_save_defaults(save_datacube=True)
+    p.save(tmp_path / "r.npz")
+    q = pg.read(tmp_path / "r.npz")
+    np.testing.assert_array_equal(q.object, p.object)
+    np.testing.assert_array_equal(q.probe, p.probe)
+    q.preprocess(**g.meta["preprocess"])
+    np.testing.assert_array_equal(q._object, p._object)
+    q.reconstruct(**dict(kw, num_iter=1))
+    assert np.isfinite(q.error) and q.error < p.error_iterations[0]
