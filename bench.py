@@ -66,7 +66,8 @@ def parse_args(argv=None):
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
     ap.add_argument("--ref-cores", type=int, default=0,
                     help="reference arm: limit the worker processes (0 = all host cores)")
-    ap.add_argument("--workload", choices=["gd128", "multiscan", "multislice"], default="gd128",
+    ap.add_argument("--workload", choices=["gd128", "multiscan", "multislice", "projection",
+                                           "poscorr", "mixed-multislice"], default="gd128",
                     help="gd128: the single-slice 128^2-detector workload (default); multiscan: "
                          "16 mixed-state scans of uneven sizes in one graph-captured launch")
     ap.add_argument("--scans", type=int, default=16, help="multiscan: number of scans")
@@ -718,6 +719,104 @@ def run_multislice(args):
     return 0
 
 
+def run_variant(args):
+    """The benchmark scan (128x128 positions, 128^2 detector, 512^2 object) with
+    one of the options the reference runs at scale:
+      projection        DM_AP (a=-1, b=1, c=2) on whole-scan batches (the
+                        reference allows no mini-batches with projection sets),
+                        2 GiB of persistent exit waves;
+      poscorr           gradient descent, batch 1024, position correction with
+                        both distance limits and the positions CoM constraint;
+      mixed-multislice  a 64x64 scan through 4 slices with 2 probe modes, batch 256.
+    value = position updates/s over K full iterations (device-resident amplitudes)."""
+    rank, world, local = dist_env()
+    if world > 1:
+        print(json.dumps({"workload": args.workload, "unavailable": "single-GPU workload"}))
+        return 0
+    import torch
+
+    torch.cuda.set_device(local)
+    from py4dstem_gb300 import engine, roofline, synthetic
+    from py4dstem_gb300.ptychography import method_parameters
+
+    w = args.workload
+    n = 128 * 128
+    if w == "mixed-multislice":
+        from py4dstem_gb300 import MixedstateMultislicePtychography
+
+        case = synthetic.make_scan("mms", 5, (64, 64), 0.4, 0.05, 128, 256, dose=1e5,
+                                   num_slices=4, slice_thickness=20.0, num_modes=2,
+                                   mode_weights=(0.8, 0.2), backend="torch",
+                                   device=f"cuda:{local}")
+        p = MixedstateMultislicePtychography(datacube=case.datacube, verbose=False,
+                                             device="gpu", **case.ctor_kwargs)
+        p.preprocess(max_batch_size=256, **case.preprocess_kwargs)
+        B, T, M = 256, 4, 2
+    else:
+        case = build_case(128, 1234, f"cuda:{local}")
+        p = preprocess(case, storage="gpu")
+        B = p._num_diffraction_patterns if w == "projection" else 1024
+        T, M = 1, 1
+    J = p._num_diffraction_patterns
+    projection = w == "projection"
+    use_projection, pa, pb, pc, _, step = method_parameters(
+        "DM_AP" if projection else "GD", 1.0, None, None, None, 0.5)
+    poscorr = w == "poscorr"
+    st = engine.create_state(
+        roi_shape=tuple(p._region_of_interest_shape), object_array=np.asarray(p._object),
+        probe_array=p._probe, amplitudes=p._amplitudes_for_state(),
+        positions_px=p._positions_px, num_slices=T, num_probes=M, potential=False,
+        max_batch=B, storage="gpu",
+        propagators=p._propagator_arrays if T > 1 else None,
+        fov_mask_inverse=p._object_fov_mask_inverse, projection=projection,
+        mixed_state=M > 1, positions_initial=p._positions_px_initial if poscorr else None)
+    drv = engine.IterationDriver(
+        st, max_batch=B, projection=projection, projection_abc=(pa or 0, pb or 0, pc or 0),
+        step_size=step, normalization_min=1.0,
+        use_mask=bool(p._object_fov_mask_inverse.sum() > 0), orthogonalize_probe=M > 1,
+        mean_intensity=p._mean_diffraction_intensity, graph=not poscorr,
+        position_correction=(dict(step_size=0.9, max_update_px=0.5, max_total_px=2.0,
+                                  center_of_mass=True) if poscorr else None))
+    rng = np.random.RandomState(3)
+    order = np.arange(J)
+
+    def step_fn():
+        if not projection:
+            rng.shuffle(order)
+        drv.iterate(order)
+        drv.error()
+
+    for _ in range(max(args.warmup, 2)):
+        step_fn()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        ev0.record()
+        for _ in range(args.steps):
+            step_fn()
+        ev1.record()
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    fl = roofline.flops_per_position(n, num_slices=T, num_probes=M)
+    line = {
+        "metric": f"position updates/s ({w}, 128^2 det)",
+        "value": J * args.steps / (ms * 1e-3), "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": max(args.warmup, 2), "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": w, "positions": J, "batch": B, "slices": T, "modes": M,
+                   "detector": 128, "object": list(np.shape(p._object)),
+                   "method": "DM_AP" if projection else "GD",
+                   "position_correction": poscorr},
+        "flops_per_position": fl,
+        "achieved_tflops": fl * J * args.steps / (ms * 1e-3) / 1e12,
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main(argv=None):
     args = parse_args(argv)
     if args.impl == "reference":
@@ -726,6 +825,8 @@ def main(argv=None):
         return run_multiscan(args)
     if args.workload == "multislice":
         return run_multislice(args)
+    if args.workload in ("projection", "poscorr", "mixed-multislice"):
+        return run_variant(args)
     return run_ours(args)
 
 

@@ -15,6 +15,8 @@ Operators counted (reference, py4DSTEM/process/phase/):
       far-field FFT and IFFT, T-1 back propagations), 50 + 24 (T - 1) flops/pixel
   mixed state   ptychographic_methods.py:2696-3000
       3 FFTs per mode, 20 + 30 M flops/pixel
+  mixed-state multislice  ptychographic_methods.py:3102-3258
+      the multislice count for every mode
 """
 
 from __future__ import annotations
@@ -28,6 +30,10 @@ def fft_flops(n_pixels: int) -> float:
 
 def flops_per_position(n_pixels: int, num_slices: int = 1, num_probes: int = 1) -> float:
     f = fft_flops(n_pixels)
+    if num_slices > 1 and num_probes > 1:
+        # every mode through every slice and back: (4T - 1) transforms per mode
+        t, m = num_slices, num_probes
+        return m * ((4 * t - 1) * f + (50 + 24 * (t - 1)) * n_pixels)
     if num_slices > 1:
         t = num_slices
         return (4 * t - 1) * f + (50 + 24 * (t - 1)) * n_pixels
