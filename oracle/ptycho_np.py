@@ -171,7 +171,9 @@ class Oracle:
             patches = self.object[:, rows, cols]
             if self.object_type == "potential":
                 patches = np.exp(1j * patches)
-            probes = np.empty((self.num_slices,) + shifted.shape, dtype=patches.dtype)
+            # (T, B, M, Sx, Sy); an unshifted (M, Sx, Sy) probe broadcasts over B
+            shape = (self.num_slices, patches.shape[1], self.num_probes) + patches.shape[-2:]
+            probes = np.empty(shape, dtype=patches.dtype)
             probes[0] = shifted
             for s in range(self.num_slices):
                 ov = np.expand_dims(patches[s], axis=1) * probes[s]

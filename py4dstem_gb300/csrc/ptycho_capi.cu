@@ -249,8 +249,6 @@ int ptycho_gd_batch(const ptycho_geometry* g, void* object, void* probe,
   a.fix_probe = fix_probe ? 1 : 0;
   a.mixed_formula = (g->num_probes > 1 || (g->flags & PTYCHO_FLAG_MIXED_STATE)) ? 1 : 0;
   a.keep_farfield = (g->flags & PTYCHO_FLAG_KEEP_FARFIELD) ? 1 : 0;
-  if (a.keep_farfield && g->num_slices > 1 && g->num_probes > 1)
-    return fail(PTYCHO_ERR_UNSUPPORTED, "PTYCHO_FLAG_KEEP_FARFIELD for mixed-state multislice");
   return run_batch(g, object, probe, amplitudes, amplitude_rows, positions_px, position_rows,
                    batch, detector_mask, propagators, error_accum, workspace, workspace_bytes,
                    stream, a);
@@ -271,8 +269,6 @@ int ptycho_projection_batch(const ptycho_geometry* g, void* object, void* probe,
   if (g->flags & PTYCHO_FLAG_KEEP_FARFIELD)
     return fail(PTYCHO_ERR_UNSUPPORTED, "PTYCHO_FLAG_KEEP_FARFIELD applies to gradient-descent "
                                         "batches only");
-  if (g->num_slices > 1 && g->num_probes > 1)
-    return fail(PTYCHO_ERR_UNSUPPORTED, "projection sets for mixed-state multislice");
   a.projection = 1;
   a.pa = projection_a;
   a.pb = projection_b;
@@ -300,8 +296,7 @@ int ptycho_position_correction(const ptycho_geometry* g, const void* object,
   if (!(g->flags & PTYCHO_FLAG_KEEP_FARFIELD))
     return fail(PTYCHO_ERR_INVALID_ARGUMENT, "position correction needs the far fields of a "
                                              "batch run with PTYCHO_FLAG_KEEP_FARFIELD");
-  if (g->num_slices > 1 && g->num_probes > 1)
-    return fail(PTYCHO_ERR_UNSUPPORTED, "position correction for mixed-state multislice");
+
   if (!object || !amplitudes || !positions_px || !positions_initial)
     return fail(PTYCHO_ERR_INVALID_ARGUMENT, "object, amplitudes, positions_px and "
                                              "positions_initial must be non-null");

@@ -106,8 +106,9 @@ __global__ void __launch_bounds__(NT, 1) probe_spectrum_kernel(BatchArgs a) {
 // spills): 0 any single slice or single-probe multislice, 1 single slice /
 // single probe, 2 single-slice mixed state, 3 multislice / single probe, 4
 // mixed-state multislice; modes 1-3 are gradient descent with no projection
-// sets, forward-only pass, kept far fields or exact probe gradient; mode 4 is
-// gradient descent or the forward-only pass.
+// sets, forward-only pass, kept far fields or exact probe gradient; mode 4 runs
+// gradient descent, projection sets or the forward-only pass (its far fields
+// always stay in scratch_f).
 template <int SX, int SY, int NT, int kMode>
 __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, float* red) {
   constexpr bool kPlain = kMode >= 1 && kMode <= 3;
@@ -138,7 +139,7 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
   const int x0 = (int)rx;
   const int y0 = (int)ry;
   const float invN = 1.0f / (float)N;
-  const bool ps = !kPlain && kMode != 4 && a.projection != 0;
+  const bool ps = !kPlain && a.projection != 0;
   const bool fwd = !kPlain && a.forward_only != 0;  // per-position error only (block-uniform)
   const float* amp = a.amplitudes + (size_t)arow * N;
 
@@ -216,9 +217,9 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
   const float py_ = 1.0f - a.pc;          // projection y
 
   if constexpr (kMode == 4) {
-    // ------------------------------------------ mixed-state multislice (GD)
-    // (ptychographic_methods.py:3102-3160 forward, 2742-2804 projection,
-    // 3162-3258 adjoint). Every mode runs through the slices on its own:
+    // ------------------------------- mixed-state multislice (GD or projection sets)
+    // (ptychographic_methods.py:3102-3160 forward, 2742-2904 projections,
+    // 3162-3400 adjoints). Every mode runs through the slices on its own:
     // P_{s+1,m} = IFFT2(FFT2(O_s P_{s,m}) H_s), with each P_{s,m} stashed; the far
     // fields F_m share the ratio A / sqrt(sum_m |F_m|^2); the adjoint of each mode
     // walks back through the slices, adding conj(P_{s,m}) chi_{s,m} and |P_{s,m}|^2
@@ -244,6 +245,17 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
           __syncthreads();
           fft2d<SX, SY, NT, +1>(buf, twx, twy);
         }
+      }
+      if (ps) {
+        // projection sets: the factor c psi + (1 - c) exit wave is projected
+        const float2* ew = a.exit_waves + ((size_t)prow * M + m) * N;
+        for (int e = tid; e < N; e += NT) {
+          const int idx = (e / SY) * LD + e % SY;
+          const float2 psi = buf[idx];
+          const float2 w = a.ew_valid ? ew[e] : psi;
+          buf[idx] = c_add(c_scale(psi, a.pc), c_scale(w, py_));
+        }
+        __syncthreads();
       }
       fft2d<SX, SY, NT, -1>(buf, twx, twy);
       float2* f = a.scratch_f + ((size_t)b * M + m) * N;
@@ -272,12 +284,30 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
         const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
         float2 fv = f[e];
         if (a.det_mask) fv = c_scale(fv, mk);
-        float2 r = c_sub(c_scale(fv, itot[e]), fv);
-        if (a.det_mask) r = c_scale(r, mk);
+        float2 r = c_scale(fv, itot[e]);
+        if (!ps) {
+          r = c_sub(r, fv);
+          if (a.det_mask) r = c_scale(r, mk);
+        }
         buf[(e / SY) * LD + e % SY] = r;
       }
       __syncthreads();
       fft2d<SX, SY, NT, +1>(buf, twx, twy);
+      if (ps) {
+        // new exit wave x w + a psi + b projected; psi recomputed from the stash
+        float2* ew = a.exit_waves + ((size_t)prow * M + m) * N;
+        const float2* plast = a.st_pm + (((size_t)(T - 1) * a.B + b) * M + m) * N;
+        for (int e = tid; e < N; e += NT) {
+          const int x = e / SY, y = e % SY;
+          const float2 proj = c_scale(buf[x * LD + y], invN);
+          const float2 psi = c_mul(load_object(a, T - 1, obj_x(x), obj_y(y)), plast[e]);
+          const float2 w = a.ew_valid ? ew[e] : psi;
+          const float2 nw = c_add(c_add(c_scale(w, px_), c_scale(psi, a.pa)), c_scale(proj, a.pb));
+          ew[e] = nw;
+          buf[x * LD + y] = c_scale(nw, (float)N);  // keep buf in unscaled units
+        }
+        __syncthreads();
+      }
       for (int s = T - 1; s >= 0; --s) {
         const float2* pst = a.st_pm + (((size_t)s * a.B + b) * M + m) * N;
         float2* gobj = a.st_obj + ((size_t)s * a.B + b) * N;
@@ -716,7 +746,7 @@ __global__ void __launch_bounds__(NT, 1) position_correction_kernel(BatchArgs a)
             const int x = e / SY, y = e % SY;
             int ox, oy;
             moved(dir, x, y, ox, oy);
-            const float2 p = s == 0 ? a.probe[e] : c_scale(buf[x * LD + y], invN);
+            const float2 p = s == 0 ? a.probe[(size_t)m * N + e] : c_scale(buf[x * LD + y], invN);
             buf[x * LD + y] = c_mul(load_object(a, s, ox, oy), p);
           }
           __syncthreads();
@@ -946,8 +976,7 @@ cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
   }
   // plain gradient-descent batches run an instantiation with the other modes
   // compiled out (see position_one); mixed-state multislice has its own
-  if (mixed_ms && (a.projection || a.keep_farfield || a.exact_probe_grad))
-    return cudaErrorNotSupported;
+  if (mixed_ms && a.exact_probe_grad) return cudaErrorNotSupported;
   const bool plain = !a.projection && !a.forward_only && !a.keep_farfield && !a.exact_probe_grad;
   const int mode = mixed_ms ? 4
                    : !plain ? 0

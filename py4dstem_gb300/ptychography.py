@@ -461,10 +461,6 @@ class _PtychographyBase(PreprocessMixin):
         if correct_positions and use_projection:
             raise NotImplementedError(
                 "position correction (fix_positions=False) runs with gradient descent only")
-        if self._multislice and self._mixed and (use_projection or correct_positions):
-            raise NotImplementedError(
-                "mixed-state multislice runs gradient descent with fixed positions only "
-                "(projection sets and position correction are not implemented for it)")
 
         J = self._num_diffraction_patterns
         shuffled = np.arange(J)
@@ -1041,7 +1037,7 @@ class MixedstateMultislicePtychography(_PtychographyBase):
     """Mixed-state multislice ptychography: object (T,Px,Py), probe (M,Sx,Sy)
     incoherent modes, each propagated through the slices
     (mixedstate_multislice_ptychography.py; operators
-    ptychographic_methods.py:3096-3258). Gradient descent with fixed positions."""
+    ptychographic_methods.py:3096-3400)."""
 
     _multislice = True
     _mixed = True

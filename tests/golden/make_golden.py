@@ -104,6 +104,24 @@ CASES = {
                                      slice_thicknesses=20.0, num_probes=2),
         global_seed=9, guess=(3, 96, 96),
         rec=dict(num_iter=5, max_batch_size=25, step_size=0.5, seed_random=10)),
+    "mms_ap": dict(
+        gen=dict(name="msa", seed=25, scan_shape=(8, 8), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=96, num_slices=2, slice_thickness=20.0, num_modes=2,
+                 mode_weights=(0.8, 0.2)),
+        cls="mixed_multi", ctor=dict(object_fov_ang=(24.0, 24.0), num_slices=2,
+                                     slice_thicknesses=20.0, num_probes=2),
+        global_seed=11, guess=(2, 96, 96),
+        rec=dict(num_iter=4, reconstruction_method="RAAR", reconstruction_parameter=0.8)),
+    "mms_gd_poscorr": dict(
+        gen=dict(name="msp", seed=26, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=96, num_slices=2, slice_thickness=20.0, num_modes=2,
+                 mode_weights=(0.8, 0.2)),
+        cls="mixed_multi", ctor=dict(object_fov_ang=(24.0, 24.0), num_slices=2,
+                                     slice_thicknesses=20.0, num_probes=2),
+        global_seed=12, guess=(2, 96, 96), perturb_ang=0.15,
+        rec=dict(num_iter=4, max_batch_size=25, step_size=0.5, seed_random=11,
+                 fix_positions=False, positions_step_size=0.5,
+                 max_position_update_distance=0.1, max_position_total_distance=0.5)),
     "mixed_gd_M3": dict(
         gen=dict(name="mx", seed=14, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
                  detector=64, object_px=96, num_modes=3, mode_weights=(0.7, 0.2, 0.1)),

@@ -114,12 +114,12 @@ def test_mixed_state_multislice_mask_fix_probe_constraints(cuda):
             fix_probe_com=True, fix_potential_baseline=True, orthogonalize_probe=True)
 
 
-def test_mixed_state_multislice_rejects_projection_sets(cuda):
-    from py4dstem_gb300 import _native
-
-    st = make_state(S=32, J=9, slices=2, modes=2, seed=49)
-    with pytest.raises(_native.PtychoError):
-        gpu_reconstruct(st, num_iter=1, method="PS", a=0.0, b=0.5, c=2.0)
+@pytest.mark.parametrize("abc", [(-1.0, 1.0, 2.0), (0.0, 0.5, 2.0), (0.3, 0.6, 1.4)])
+def test_mixed_state_multislice_projection_sets(cuda, abc):
+    """Projection sets through kernel mode 4: per-mode exit waves at the last slice."""
+    st = make_state(S=32, J=16, slices=2, modes=2, seed=49)
+    a, b, c = abc
+    compare(st, 5e-5, 5e-5, 5e-5, num_iter=2, method="PS", a=a, b=b, c=c, **OFF)
 
 
 @pytest.mark.parametrize("method,abc", [("DM", (-1.0, 1.0, 2.0)), ("RAAR", (0.0, 0.5, 2.0)),

@@ -80,22 +80,14 @@ def test_rejects_object_smaller_than_roi(lib):
 
 
 def test_mixed_multislice_geometry(lib):
-    """Gradient descent takes mixed-state multislice geometries (the call gets
-    as far as the workspace check here); projection sets and kept far fields
-    (position correction) refuse them before any launch."""
+    """Mixed-state multislice geometries are accepted (the calls get as far as the
+    workspace check here); the workspace holds every slice's probe per mode."""
     g = geometry(T=2, M=2)
     assert _gd(lib, g) == 3  # null workspace: the geometry itself was accepted
     need = lib.ptycho_workspace_bytes(ctypes.byref(g), 4)
-    assert need > lib.ptycho_workspace_bytes(ctypes.byref(geometry(T=2, M=1)), 4)
-    ws = ctypes.c_void_p(0x100000)
-    dummy = ctypes.c_void_p(0x1000)
-    st = lib.ptycho_projection_batch(ctypes.byref(g), dummy, dummy, dummy, None, dummy, None, 4,
-                                     0.0, 0.5, 2.0, 1.0, 0, dummy, 0, dummy, dummy, ws, need,
-                                     None)
-    assert st == 2 and b"mixed-state multislice" in lib.ptycho_last_error()
-    gk = _native.Geometry(64, 64, 128, 128, 2, 2, 0, _native.FLAG_KEEP_FARFIELD)
-    need = lib.ptycho_workspace_bytes(ctypes.byref(gk), 4)
-    assert _gd(lib, gk, ws=ws, wsb=need) == 2
+    # + T B M N c64 stash + B M N c64 far fields over the single-probe multislice
+    base = lib.ptycho_workspace_bytes(ctypes.byref(geometry(T=2, M=1)), 4)
+    assert need >= base + (2 * 4 * 2 + 4 * 2) * 64 * 64 * 8 - 4 * 64 * 64 * 8
 
 
 def test_rejects_bad_batch_and_workspace(lib):
