@@ -1,6 +1,7 @@
 // extern "C" entry points of libptycho_gb300.so (declared in include/ptycho_gb300.h).
 // Validates arguments, carves the caller's workspace and launches the kernels of
-// ptycho_position.cu and ptycho_reduce.cu on the caller's stream.
+// ptycho_position.cuh (instantiated per region-of-interest size) and ptycho_reduce.cu
+// on the caller's stream.
 #include <cuda_runtime.h>
 
 #include <cstdarg>
