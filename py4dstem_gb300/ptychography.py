@@ -167,11 +167,23 @@ class _PtychographyBase(PreprocessMixin):
 
     def _amplitudes_for_state(self):
         """The amplitudes as create_state takes them: the device tensor when the
-        preprocessing left one and storage is "gpu", else the host array."""
+        preprocessing left one and storage is "gpu", else the host array. With
+        storage "cpu" a pageable host array is moved once into page-locked memory
+        (kept for later calls), so the batch kernels read it in place instead of
+        staging every batch through a host-side gather."""
         dev = self.__dict__.get("_amplitudes_device")
         if dev is not None and self._storage == "gpu":
             return dev
-        return self._amplitudes
+        host = self._amplitudes
+        if self._storage == "cpu" and self._device == "gpu" and host is not None \
+                and engine.mapped_host_address(np.ascontiguousarray(host)) is None:
+            import torch
+
+            pinned = torch.empty(tuple(host.shape), dtype=torch.float32, pin_memory=True)
+            pinned.numpy()[...] = host
+            host = pinned.numpy()
+            self.__dict__["_amplitudes_host"] = host
+        return host
 
     def set_storage(self, storage):
         if storage not in ("cpu", "gpu"):
