@@ -160,6 +160,28 @@ def create_state(*, roi_shape, object_array, probe_array, amplitudes, positions_
     return st
 
 
+def refresh_state(st: DeviceState, *, object_array, probe_array, positions_px,
+                  detector_mask=None, fov_mask_inverse=None, positions_initial=None) -> None:
+    """Copy new values of the per-call inputs into an existing state's buffers
+    (same shapes), so that kernels and captured graphs that hold its pointers run
+    on them."""
+    torch = _torch()
+
+    def put(dst, arr, dtype):
+        src = torch.from_numpy(np.ascontiguousarray(arr, dtype=dtype).reshape(tuple(dst.shape)))
+        dst.copy_(src)
+
+    put(st.object, object_array, np.asarray(object_array).dtype)
+    put(st.probe, probe_array, np.complex64)
+    put(st.positions, positions_px, np.float32)
+    if detector_mask is not None:
+        put(st.det_mask, np.asarray(detector_mask), np.float32)
+    if fov_mask_inverse is not None:
+        put(st.fov_mask_inverse, fov_mask_inverse, np.uint8)
+    if positions_initial is not None:
+        put(st.positions_initial, positions_initial, np.float32)
+
+
 def _ws_ptr(st: DeviceState):
     base = st.workspace.data_ptr()
     aligned = (base + 255) & ~255

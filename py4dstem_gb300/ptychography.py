@@ -484,27 +484,9 @@ class _PtychographyBase(PreprocessMixin):
         potential = self._object_type == "potential"
         obj = np.asarray(self._object, dtype=np.float32 if potential else np.complex64)
         use_mask = bool(fix_potential_baseline and self._object_fov_mask_inverse.sum() > 0)
-        st = engine.create_state(
-            roi_shape=tuple(self._region_of_interest_shape), object_array=obj,
-            probe_array=self._probe, amplitudes=self._amplitudes_for_state(),
-            positions_px=self._positions_px, num_slices=self._num_slices,
-            num_probes=self._num_probes, potential=potential, max_batch=int(max_batch_size),
-            storage=self._storage,
-            propagators=getattr(self, "_propagator_arrays", None) if self._multislice else None,
-            detector_mask=detector_fourier_mask,
-            fov_mask_inverse=self._object_fov_mask_inverse if use_mask else None,
-            projection=use_projection, mixed_state=self._mixed,
-            positions_initial=self._positions_px_initial if correct_positions else None)
-        if use_projection and self._exit_waves is not None:
-            import torch
-
-            st.exit_waves.copy_(torch.from_numpy(
-                np.asarray(self._exit_waves, dtype=np.complex64).reshape(st.exit_waves.shape)))
-            st.exit_waves_valid = True
-        self._device_state = st
-
-        driver = engine.IterationDriver(
-            st, max_batch=int(max_batch_size), projection=use_projection, step_size=step_size,
+        amplitudes = self._amplitudes_for_state()
+        driver_kw = dict(
+            max_batch=int(max_batch_size), projection=use_projection, step_size=step_size,
             normalization_min=normalization_min, fix_probe=fix_probe,
             projection_abc=(pa, pb, pc), shrinkage_rad=shrinkage_rad, use_mask=use_mask,
             pure_phase=pure_phase_object and self._object_type == "complex",
@@ -518,6 +500,48 @@ class _PtychographyBase(PreprocessMixin):
                 # the reference passes fix_positions_com and not fix_positions on
                 # (singleslice_ptychography.py:956, ptychographic_constraints.py:1355-1377)
                 center_of_mass=not fix_positions_com) if correct_positions else None))
+        # Device state and iteration driver are kept between calls with the same
+        # arrays and settings: a later call copies the current object, probe and
+        # positions into the same buffers and replays the iteration graph captured
+        # before (the reference rebuilds nothing on the device either).
+        key = (self._storage, obj.shape, obj.dtype.str, np.shape(self._probe),
+               self._num_slices, self._num_probes, potential, self._mixed, correct_positions,
+               detector_fourier_mask is not None,
+               repr(sorted((k, repr(v)) for k, v in driver_kw.items())))
+        cached = self.__dict__.get("_state_cache")
+        if cached is not None and cached[0] == key and cached[1] is amplitudes:
+            st, driver = cached[2], cached[3]
+            engine.refresh_state(
+                st, object_array=obj, probe_array=self._probe, positions_px=self._positions_px,
+                detector_mask=detector_fourier_mask,
+                fov_mask_inverse=self._object_fov_mask_inverse if use_mask else None,
+                positions_initial=self._positions_px_initial if correct_positions else None)
+        else:
+            self.__dict__["_state_cache"] = None  # release the previous buffers first
+            st = engine.create_state(
+                roi_shape=tuple(self._region_of_interest_shape), object_array=obj,
+                probe_array=self._probe, amplitudes=amplitudes,
+                positions_px=self._positions_px, num_slices=self._num_slices,
+                num_probes=self._num_probes, potential=potential,
+                max_batch=int(max_batch_size), storage=self._storage,
+                propagators=(getattr(self, "_propagator_arrays", None)
+                             if self._multislice else None),
+                detector_mask=detector_fourier_mask,
+                fov_mask_inverse=self._object_fov_mask_inverse if use_mask else None,
+                projection=use_projection, mixed_state=self._mixed,
+                positions_initial=self._positions_px_initial if correct_positions else None)
+            driver = engine.IterationDriver(st, **driver_kw)
+            self.__dict__["_state_cache"] = (key, amplitudes, st, driver)
+        if use_projection:
+            if self._exit_waves is not None:
+                import torch
+
+                st.exit_waves.copy_(torch.from_numpy(np.asarray(
+                    self._exit_waves, dtype=np.complex64).reshape(st.exit_waves.shape)))
+                st.exit_waves_valid = True
+            else:
+                st.exit_waves_valid = False
+        self._device_state = st
         error = np.float32(0.0)
         if num_iter > 0 and not use_projection:
             np.random.shuffle(shuffled)

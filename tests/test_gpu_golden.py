@@ -167,3 +167,27 @@ def test_save_read_continue(cuda, tmp_path):
     np.testing.assert_array_equal(q._object, p._object)
     q.reconstruct(**dict(kw, num_iter=1))
     assert np.isfinite(q.error) and q.error < p.error_iterations[0]
+
+
+def test_repeated_calls_reuse_state_and_match(cuda):
+    """Consecutive reconstruct() calls with the same settings reuse the device
+    state and the captured iteration graph, with the same bits as calls that
+    build a new state each time; a change of settings builds a new state."""
+    g = Golden("ss_gd_det128")
+    kw = g.rec_kwargs()
+    n = kw.pop("num_iter")
+    b = g.build()
+    c = g.build()
+    states = set()
+    for _ in range(n):
+        b.reconstruct(num_iter=1, **kw)
+        states.add(id(b._device_state))
+        c.__dict__["_state_cache"] = None
+        c.reconstruct(num_iter=1, **kw)
+    assert len(states) == 1
+    assert b.error_iterations == c.error_iterations
+    np.testing.assert_array_equal(b.object, c.object)
+    np.testing.assert_array_equal(b.probe, c.probe)
+    st = b._device_state
+    b.reconstruct(num_iter=1, **dict(kw, step_size=0.25))
+    assert b._device_state is not st

@@ -167,3 +167,12 @@ def test_deterministic_and_storage_independent(cuda):
         np.testing.assert_array_equal(x[0], y[0])
         np.testing.assert_array_equal(x[1], y[1])
         assert x[2] == y[2]
+
+
+@pytest.mark.parametrize("J,B", [(1, 1), (7, 3), (2100, 2100), (2100, 700)])
+def test_batch_edges(cuda, J, B):
+    """A single position; ragged batches; a batch longer than the object
+    reduction's 2048-position list window (two windows per tile)."""
+    st = make_state(S=32, J=J, seed=60 + J % 7, obj_px=None if J < 100 else 192)
+    tol = 2e-5 if J < 100 else 5e-5
+    compare(st, tol, tol, tol, num_iter=2, max_batch_size=B, seed_random=3, **OFF)
