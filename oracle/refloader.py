@@ -124,6 +124,38 @@ class DataCube:
     def Rshape(self):
         return self.data.shape[:2]
 
+    # the diffraction-space reshaping the phase classes call in preprocess()
+    # (phase_base_class.py:280-420) runs the reference's own functions
+    # (py4DSTEM/preprocess/preprocess.py) on this object
+    R_Nx = property(lambda self: self.data.shape[0])
+    R_Ny = property(lambda self: self.data.shape[1])
+    Q_Nx = property(lambda self: self.data.shape[2])
+    Q_Ny = property(lambda self: self.data.shape[3])
+
+    def set_dim(self, *args, **kwargs):
+        pass
+
+    def calibrate(self):
+        pass
+
+    def bin_Q(self, N, dtype=None):
+        from py4DSTEM.preprocess.preprocess import bin_data_diffraction
+
+        return bin_data_diffraction(self, N, dtype)
+
+    def pad_Q(self, N=None, output_size=None):
+        from py4DSTEM.preprocess.preprocess import pad_data_diffraction
+
+        return pad_data_diffraction(self, pad_factor=N, output_size=output_size)
+
+    def resample_Q(self, N=None, output_size=None, method="bilinear",
+                   conserve_array_sums=False):
+        from py4DSTEM.preprocess.preprocess import resample_data_diffraction
+
+        return resample_data_diffraction(self, resampling_factor=N, output_size=output_size,
+                                         method=method,
+                                         conserve_array_sums=conserve_array_sums)
+
 
 class _Calibration:
     def __init__(self, r_size, r_units, q_size, q_units):
@@ -141,6 +173,9 @@ class _Calibration:
 
     def get_Q_pixel_units(self):
         return self._q[1]
+
+    def set_Q_pixel_size(self, size):
+        self._q = (size, self._q[1])
 
 
 def _package(name, path):

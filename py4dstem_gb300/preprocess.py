@@ -83,6 +83,57 @@ def shift_bilinear(ar, xshift, yshift):
     )
 
 
+def _corner_slices(n_in, n_out):
+    """(source, destination) index slices of the two corners of a spectrum axis
+    that a Fourier resize keeps: the first ceil(m/2) and the last floor(m/2)
+    frequencies, m = min(n_in, n_out); the whole axis when the sizes agree."""
+    if n_in == n_out:
+        return (slice(None), slice(None)), (slice(None), slice(None))
+    m = min(n_in, n_out)
+    lo, hi = (m + 1) // 2, m // 2
+    return (slice(0, lo), slice(0, lo)), (slice(n_in - hi, n_in), slice(n_out - hi, n_out))
+
+
+def fourier_resample(array, output_size, force_nonnegative=False, conserve_array_sums=True,
+                     chunk=256):
+    """Fourier interpolation of the last two axes of a 2D or 4D array to
+    `output_size` (process/utils/utils.py:412-640): the kept corners of each
+    pattern's complex64 spectrum are copied into a zero spectrum of the new
+    size, inverse transformed, and the real part taken as float32; negative
+    values clipped when force_nonnegative; multiplied by the size ratio unless
+    conserve_array_sums."""
+    array = np.asarray(array)
+    n_in = array.shape[-2:]
+    output_size = tuple(int(v) for v in output_size)
+    (xa, xb), (xc, xd) = _corner_slices(n_in[0], output_size[0])
+    (ya, yb), (yc, yd) = _corner_slices(n_in[1], output_size[1])
+    corners = [((xa, ya), (xb, yb)), ((xc, ya), (xd, yb)), ((xa, yc), (xb, yd)),
+               ((xc, yc), (xd, yd))]
+
+    def resize(block):
+        spec = np.fft.fft2(block)
+        out = np.zeros(block.shape[:-2] + output_size, dtype=np.complex64)
+        for (sx_, sy_), (dx_, dy_) in corners:
+            out[..., dx_, dy_] = spec[..., sx_, sy_]
+        return np.real(np.fft.ifft2(out)).astype(np.float32)
+
+    if array.ndim == 2:
+        result = resize(array)
+    elif array.ndim == 4:
+        result = np.zeros(array.shape[:2] + output_size, dtype=np.float32)
+        flat_in = array.reshape((-1,) + n_in)
+        flat_out = result.reshape((-1,) + output_size)
+        for start in range(0, flat_in.shape[0], chunk):
+            flat_out[start:start + chunk] = resize(flat_in[start:start + chunk])
+    else:
+        raise ValueError(f"fourier_resample takes 2D or 4D arrays, not {array.ndim}D")
+    if force_nonnegative:
+        result = np.maximum(result, 0)
+    if not conserve_array_sums:
+        result = result * (np.prod(output_size) / np.prod(n_in))
+    return result
+
+
 def _plane(xy, mx, my, b):
     return mx * xy[0] + my * xy[1] + b
 
@@ -173,27 +224,61 @@ class PreprocessMixin:
             factor_x, factor_y = sx / qx, sy / qy
             if factor_x != factor_y:
                 raise ValueError("Datacube calibration can only handle uniform Q-sampling.")
-            if reshaping_method != "bin":
-                raise NotImplementedError(
-                    "only reshaping_method='bin' is implemented for diffraction resampling")
+            if reshaping_method not in ("bin", "fourier", "bilinear"):
+                raise ValueError(
+                    "reshaping_method needs to be one of 'bilinear', 'fourier', or 'bin', "
+                    f"not {reshaping_method}.")
             if com_shifts is not None:
                 com_shifts = (com_shifts[0] * factor_x, com_shifts[1] * factor_x)
             if com_measured is not None:
                 com_measured = (com_measured[0] * factor_x, com_measured[1] * factor_x)
-            binf = int(1 / factor_x)
-            if binf < 1:
-                raise ValueError(f"Calculated binning factor {binf} is less than 1.")
-            nx, ny = qx // binf, qy // binf
-            data = data[..., : nx * binf, : ny * binf].reshape(
-                rshape + (nx, binf, ny, binf)).sum(axis=(-3, -1))
-            q = datacube.calibration.get_Q_pixel_size() * binf
-            datacube = _RebinnedCube(data, datacube.calibration, q)
-            if vacuum_probe_intensity is not None:
-                v = vacuum_probe_intensity[: nx * binf, : ny * binf]
-                vacuum_probe_intensity = v.reshape(nx, binf, ny, binf).sum(axis=(1, 3))
-            if dp_mask is not None:
-                v = dp_mask[: nx * binf, : ny * binf]
-                dp_mask = v.reshape(nx, binf, ny, binf).sum(axis=(1, 3))
+            q0 = datacube.calibration.get_Q_pixel_size()
+            if reshaping_method == "bin":
+                binf = int(1 / factor_x)
+                if binf < 1:
+                    raise ValueError(f"Calculated binning factor {binf} is less than 1.")
+                nx, ny = qx // binf, qy // binf
+                data = data[..., : nx * binf, : ny * binf].reshape(
+                    rshape + (nx, binf, ny, binf)).sum(axis=(-3, -1))
+                datacube = _RebinnedCube(data, datacube.calibration, q0 * binf)
+                if vacuum_probe_intensity is not None:
+                    v = vacuum_probe_intensity[: nx * binf, : ny * binf]
+                    vacuum_probe_intensity = v.reshape(nx, binf, ny, binf).sum(axis=(1, 3))
+                if dp_mask is not None:
+                    v = dp_mask[: nx * binf, : ny * binf]
+                    dp_mask = v.reshape(nx, binf, ny, binf).sum(axis=(1, 3))
+            elif reshaping_method == "fourier":
+                # preprocess/preprocess.py:636-663 (scale given, sums not rescaled)
+                out = (np.asarray((qx, qy)) * np.asarray(factor_x)).astype("intp")
+                data = fourier_resample(data, tuple(out))
+                datacube = _RebinnedCube(data, datacube.calibration, q0 / factor_x)
+                if vacuum_probe_intensity is not None:
+                    vacuum_probe_intensity = fourier_resample(
+                        vacuum_probe_intensity, (sx, sy), force_nonnegative=True)
+                if dp_mask is not None:
+                    dp_mask = fourier_resample(dp_mask, (sx, sy), force_nonnegative=True,
+                                               conserve_array_sums=False)
+            else:
+                # preprocess/preprocess.py:665-717: per-pattern linear zoom into a
+                # float64 cube, divided by the area factor
+                from scipy.ndimage import zoom
+
+                f = np.tile(np.asarray(factor_x), 2)
+                out = np.round(f * np.array((qx, qy))).astype("int")
+                resized = np.zeros(rshape + tuple(out))
+                for rx in range(rshape[0]):
+                    for ry in range(rshape[1]):
+                        resized[rx, ry] = zoom(np.asarray(data[rx, ry], dtype=np.float32), f,
+                                               order=1, mode="nearest", grid_mode=True)
+                data = resized / f.prod()
+                datacube = _RebinnedCube(data, datacube.calibration, q0 / f[0])
+                if vacuum_probe_intensity is not None:
+                    vacuum_probe_intensity = zoom(vacuum_probe_intensity, (factor_x, factor_x),
+                                                  order=1, mode="grid-wrap", grid_mode=True)
+                    vacuum_probe_intensity = vacuum_probe_intensity / factor_x ** 2
+                if dp_mask is not None:
+                    dp_mask = zoom(dp_mask, (factor_x, factor_x), order=1, mode="grid-wrap",
+                                   grid_mode=True)
 
         if padded_diffraction_intensities_shape is not None:
             qx, qy = data.shape[-2:]

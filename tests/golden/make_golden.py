@@ -156,6 +156,24 @@ PRE_CASES = {
         pre=dict(plot_center_of_mass=False, plot_rotation=False, plot_probe_overlaps=False,
                  force_com_transpose=True, crop_patterns=True, force_com_shifts=[24.6, 24.6],
                  vectorized_com_calculation=False)),
+    # diffraction resampling (the reference's default 'bilinear' and 'fourier') and
+    # padding of a 128^2 detector, with a vacuum probe and a detector mask
+    "prep_fourier_vacuum": dict(
+        gen=dict(name="prf", seed=27, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
+                 detector=128, object_px=160),
+        ctor=dict(object_fov_ang=(40.0, 40.0)), scan_positions=True, vacuum=True,
+        dp_mask_radius=50,
+        pre=dict(plot_center_of_mass=False, plot_rotation=False, plot_probe_overlaps=False,
+                 force_com_rotation=0.0, force_com_transpose=False,
+                 diffraction_intensities_shape=[64, 64], reshaping_method="fourier")),
+    "prep_bilinear_pad": dict(
+        gen=dict(name="prb", seed=28, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
+                 detector=128, object_px=160),
+        ctor=dict(object_fov_ang=(40.0, 40.0)), scan_positions=True,
+        pre=dict(plot_center_of_mass=False, plot_rotation=False, plot_probe_overlaps=False,
+                 force_com_rotation=0.0, force_com_transpose=False,
+                 diffraction_intensities_shape=[48, 48],
+                 padded_diffraction_intensities_shape=[64, 64])),
 }
 
 
@@ -172,6 +190,16 @@ def make_pre_case(ref, name, spec):
     kw = {}
     if spec["scan_positions"]:
         kw["initial_scan_positions"] = case.scan_positions_ang
+    if spec.get("vacuum"):
+        # the probe's own aperture intensity, detector-centred, as the vacuum probe
+        from py4dstem_gb300.optics import ComplexProbe
+
+        det = spec["gen"]["detector"]
+        pr = ComplexProbe(energy=300e3, gpts=(det, det), sampling=(0.25, 0.25),
+                          semiangle_cutoff=20.0, rolloff=2.0).build()._array
+        vpi = np.fft.fftshift(np.abs(np.fft.fft2(pr)) ** 2).astype(np.float64)
+        arrays["vacuum_probe_intensity"] = vpi
+        kw["vacuum_probe_intensity"] = vpi.copy()
     if "positions_mask_seed" in spec:
         mrng = np.random.default_rng(spec["positions_mask_seed"])
         pmask = mrng.random(data.shape[:2]) > 0.1

@@ -40,6 +40,8 @@ class PrepGolden:
         self.scan_positions_ang = z["scan_positions_ang"]
         self.positions_mask = z["positions_mask"] if "positions_mask" in z.files else None
         self.dp_mask = z["dp_mask"] if "dp_mask" in z.files else None
+        self.vacuum = (z["vacuum_probe_intensity"] if "vacuum_probe_intensity" in z.files
+                       else None)
         self.pre = {k[4:]: z[k] for k in z.files if k.startswith("pre_")}
 
     def build(self, device="gpu", storage=None):
@@ -52,6 +54,8 @@ class PrepGolden:
             kw["initial_scan_positions"] = self.scan_positions_ang.copy()
         if self.positions_mask is not None:
             kw["positions_mask"] = self.positions_mask.copy()
+        if self.vacuum is not None:
+            kw["vacuum_probe_intensity"] = self.vacuum.copy()
         dc = DataCube(self.datacube_counts.copy(), r_pixel_size=m["r_pixel_size"],
                       r_pixel_units="A", q_pixel_size=m["q_pixel_size"], q_pixel_units="mrad")
         p = api.SingleslicePtychography(datacube=dc, verbose=False, device=device,
