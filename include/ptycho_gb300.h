@@ -247,27 +247,37 @@ int ptycho_probe_orthogonalize(const ptycho_geometry* geometry, void* probe, voi
 /*
  * Intensity centre of mass of each (qx, qy) pattern of `intensities`
  * (num_patterns, qx, qy) float32: com_x = sum(I kx)/sum(I), com_y = sum(I ky)/sum(I)
- * with kx, ky the pixel indices and I = pattern * mask (mask (qx, qy) float32
- * or NULL). Replaces the vectorised centre of mass of
- * _calculate_intensities_center_of_mass (phase_base_class.py:613-700).
- * qx * qy <= 40000.
+ * with kx, ky the pixel indices and I = pattern * mask, in NumPy's types for
+ * that product (mask (qx, qy)):
+ *   mask_mode 0  no mask (mask NULL); float32 results;
+ *   mask_mode 1  float32 mask (a boolean mask as 0/1); float32 results;
+ *   mask_mode 2  float64 mask, vectorised form: float64 products, sums and
+ *                results (com_x, com_y are double arrays);
+ *   mask_mode 3  float64 mask, per-pattern form (the product rounded to float32
+ *                in place); float32 results.
+ * Replaces the centre of mass of _calculate_intensities_center_of_mass
+ * (phase_base_class.py:613-700). Patterns up to 128 x 128 (any shape whose
+ * summation tree fits one block's shared memory otherwise).
  */
 int ptycho_pattern_com(const float* intensities, int32_t num_patterns, int32_t qx, int32_t qy,
-                       const float* mask, float* com_x, float* com_y, void* stream);
+                       const void* mask, int32_t mask_mode, void* com_x, void* com_y,
+                       void* stream);
 
 /*
  * Rotation search of the real/reciprocal-space rotation: for every angle a
  * (cos_angles[a], sin_angles[a], float32) and t = 0 (as is) / 1 (x and y
  * exchanged), values[t * num_angles + a] = the mean over the scan interior of
  * |curl| (or |div| when maximize_divergence) of the centre-of-mass field
- * (com_x, com_y) (scan_x, scan_y) rotated by that angle. The caller takes the
- * arg-min (arg-max) exactly as _solve_for_center_of_mass_relative_rotation
+ * (com_x, com_y) (scan_x, scan_y) rotated by that angle, in float32, or in
+ * float64 when com_is_double (com_x, com_y and values are then double arrays,
+ * the angles' float32 cos / sin promoted). The caller takes the arg-min
+ * (arg-max) exactly as _solve_for_center_of_mass_relative_rotation
  * (phase_base_class.py:1086-1182) does.
  */
-int ptycho_rotation_search(const float* com_x, const float* com_y, int32_t scan_x,
-                           int32_t scan_y, const float* cos_angles, const float* sin_angles,
-                           int32_t num_angles, int32_t maximize_divergence, float* values,
-                           void* stream);
+int ptycho_rotation_search(const void* com_x, const void* com_y, int32_t com_is_double,
+                           int32_t scan_x, int32_t scan_y, const float* cos_angles,
+                           const float* sin_angles, int32_t num_angles,
+                           int32_t maximize_divergence, void* values, void* stream);
 
 /*
  * Corner-centring and square root: output pattern o takes source pattern

@@ -97,9 +97,9 @@ _SIGNATURES = {
         [ctypes.POINTER(Geometry), _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _sz, _vp],
         ctypes.c_int,
     ),
-    "ptycho_pattern_com": ([_vp, _i32, _i32, _i32, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "ptycho_pattern_com": ([_vp, _i32, _i32, _i32, _vp, _i32, _vp, _vp, _vp], ctypes.c_int),
     "ptycho_rotation_search": (
-        [_vp, _vp, _i32, _i32, _vp, _vp, _i32, _i32, _vp, _vp], ctypes.c_int),
+        [_vp, _vp, _i32, _i32, _i32, _vp, _vp, _i32, _i32, _vp, _vp], ctypes.c_int),
     "ptycho_normalize_patterns": (
         [_vp, _i32, _i32, _vp, _i32, _vp, _vp, _i32, _vp, _vp, _vp], ctypes.c_int),
     "ptycho_probe_overlap": (

@@ -543,15 +543,19 @@ int ptycho_probe_mix(const ptycho_geometry* g, const void* probe_in, const void*
 
 // ----------------------------------------------------------------- preprocess
 int ptycho_pattern_com(const float* intensities, int32_t num_patterns, int32_t qx, int32_t qy,
-                       const float* mask, float* com_x, float* com_y, void* stream) {
+                       const void* mask, int32_t mask_mode, void* com_x, void* com_y,
+                       void* stream) {
   if (!intensities || !com_x || !com_y)
     return fail(PTYCHO_ERR_INVALID_ARGUMENT, "intensities, com_x and com_y must be non-null");
   if (num_patterns < 0 || qx < 1 || qy < 1)
     return fail(PTYCHO_ERR_INVALID_ARGUMENT, "bad pattern count or shape (%d, %d x %d)",
                 num_patterns, qx, qy);
+  if (mask_mode < 0 || mask_mode > 3 || (mask_mode != 0 && !mask))
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "mask_mode %d needs %s", mask_mode,
+                mask_mode < 0 || mask_mode > 3 ? "a value in 0..3" : "a mask");
   if (num_patterns == 0) return PTYCHO_OK;
-  cudaError_t e = launch_pattern_com(intensities, num_patterns, qx, qy, mask, com_x, com_y,
-                                     static_cast<cudaStream_t>(stream));
+  cudaError_t e = launch_pattern_com(intensities, num_patterns, qx, qy, mask, mask_mode, com_x,
+                                     com_y, static_cast<cudaStream_t>(stream));
   if (e == cudaErrorInvalidValue)
     return fail(PTYCHO_ERR_UNSUPPORTED, "%d x %d patterns do not fit one block's shared memory",
                 qx, qy);
@@ -559,10 +563,10 @@ int ptycho_pattern_com(const float* intensities, int32_t num_patterns, int32_t q
   return PTYCHO_OK;
 }
 
-int ptycho_rotation_search(const float* com_x, const float* com_y, int32_t scan_x,
-                           int32_t scan_y, const float* cos_angles, const float* sin_angles,
-                           int32_t num_angles, int32_t maximize_divergence, float* values,
-                           void* stream) {
+int ptycho_rotation_search(const void* com_x, const void* com_y, int32_t com_is_double,
+                           int32_t scan_x, int32_t scan_y, const float* cos_angles,
+                           const float* sin_angles, int32_t num_angles,
+                           int32_t maximize_divergence, void* values, void* stream) {
   if (!com_x || !com_y || !cos_angles || !sin_angles || !values)
     return fail(PTYCHO_ERR_INVALID_ARGUMENT, "null pointer argument");
   if (scan_x < 3 || scan_y < 3 || num_angles < 1)
@@ -570,7 +574,8 @@ int ptycho_rotation_search(const float* com_x, const float* com_y, int32_t scan_
                 "the rotation search needs a scan of at least 3 x 3 and one angle "
                 "(got %d x %d, %d angles)", scan_x, scan_y, num_angles);
   cudaError_t e = launch_rotation_search(com_x, com_y, scan_x, scan_y, cos_angles, sin_angles,
-                                         num_angles, maximize_divergence ? 1 : 0, values,
+                                         num_angles, maximize_divergence ? 1 : 0,
+                                         com_is_double ? 1 : 0, values,
                                          static_cast<cudaStream_t>(stream));
   if (e == cudaErrorInvalidValue)
     return fail(PTYCHO_ERR_UNSUPPORTED, "a %d x %d scan is too large for the rotation search",

@@ -126,11 +126,11 @@ cudaError_t launch_probe_mix(const BatchArgs& a, const float2* in, const float2*
                              float2* out, cudaStream_t s);
 
 // Preprocessing kernels (ptycho_preprocess.cu).
-cudaError_t launch_pattern_com(const float* in, int num, int Qx, int Qy, const float* mask,
-                               float* cx, float* cy, cudaStream_t s);
-cudaError_t launch_rotation_search(const float* nx, const float* ny, int R0, int R1,
+cudaError_t launch_pattern_com(const float* in, int num, int Qx, int Qy, const void* mask,
+                               int mask_mode, void* cx, void* cy, cudaStream_t s);
+cudaError_t launch_rotation_search(const void* nx, const void* ny, int R0, int R1,
                                    const float* cos_a, const float* sin_a, int A, int div,
-                                   float* vals, cudaStream_t s);
+                                   int is_double, void* vals, cudaStream_t s);
 cudaError_t launch_pattern_normalize(const float* in, int Qx, int Qy, const int32_t* rows,
                                      int num_out, const float* cfx, const float* cfy,
                                      int crop_w, float* amps, float* sums, cudaStream_t s);

@@ -24,6 +24,8 @@
 // kernels, in which one thread walks the tree.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "ptycho_internal.h"
 
 namespace pty {
@@ -36,6 +38,15 @@ __host__ __device__ __forceinline__ int pw_half(int n) {
   int h = n / 2;
   return h - h % 8;
 }
+
+// Single-rounding add / multiply / divide in the accumulation type (float32
+// for float32 NumPy arrays, float64 where NumPy promotes to float64).
+__device__ __forceinline__ float acc_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double acc_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float acc_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double acc_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float acc_div(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double acc_div(double a, double b) { return __ddiv_rn(a, b); }
 
 // Leaves of the pairwise tree over n values, left to right (one thread).
 __device__ int pairwise_leaves(int n, int* lo, int* len) {
@@ -65,33 +76,34 @@ __device__ int pairwise_leaves(int n, int* lo, int* len) {
 }
 
 // Sum of one leaf [l, l + m) of values f(i).
-template <typename F>
-__device__ __forceinline__ float leaf_sum(const F& f, int l, int m) {
+template <typename Acc, typename F>
+__device__ __forceinline__ Acc leaf_sum(const F& f, int l, int m) {
   if (m < 8) {
-    float r = 0.0f;
-    for (int i = 0; i < m; ++i) r = __fadd_rn(r, f(l + i));
+    Acc r = 0;
+    for (int i = 0; i < m; ++i) r = acc_add(r, (Acc)f(l + i));
     return r;
   }
-  float r[8];
+  Acc r[8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) r[j] = f(l + j);
   int i = 8;
   for (; i < m - (m % 8); i += 8) {
 #pragma unroll
-    for (int j = 0; j < 8; ++j) r[j] = __fadd_rn(r[j], f(l + i + j));
+    for (int j = 0; j < 8; ++j) r[j] = acc_add(r[j], (Acc)f(l + i + j));
   }
-  float res = __fadd_rn(__fadd_rn(__fadd_rn(r[0], r[1]), __fadd_rn(r[2], r[3])),
-                        __fadd_rn(__fadd_rn(r[4], r[5]), __fadd_rn(r[6], r[7])));
-  for (; i < m; ++i) res = __fadd_rn(res, f(l + i));
+  Acc res = acc_add(acc_add(acc_add(r[0], r[1]), acc_add(r[2], r[3])),
+                    acc_add(acc_add(r[4], r[5]), acc_add(r[6], r[7])));
+  for (; i < m; ++i) res = acc_add(res, (Acc)f(l + i));
   return res;
 }
 
 // Combines the leaf sums of the tree over n values in tree order (one thread).
 // Post-order walk with an explicit stack: each frame is a node still waiting for
 // its right half.
-__device__ float pairwise_combine(int n, const float* leaf) {
+template <typename Acc>
+__device__ Acc pairwise_combine(int n, const Acc* leaf) {
   int fn[40];      // size of the node's right half
-  float fv[40];    // value of its left half
+  Acc fv[40];      // value of its left half
   int sp = 0, k = 0;
   int m = n;
   for (;;) {
@@ -99,11 +111,11 @@ __device__ float pairwise_combine(int n, const float* leaf) {
     while (m > kPwBlock) {
       const int h = pw_half(m);
       fn[sp] = m - h;
-      fv[sp] = 0.0f;
+      fv[sp] = 0;
       ++sp;
       m = h;
     }
-    float v = leaf[k++];
+    Acc v = leaf[k++];
     // climb: a finished left half starts its right sibling; a finished right
     // half completes its parent
     for (;;) {
@@ -115,7 +127,7 @@ __device__ float pairwise_combine(int n, const float* leaf) {
         break;
       }
       --sp;  // v is a right half
-      v = __fadd_rn(fv[sp], v);
+      v = acc_add(fv[sp], v);
     }
   }
 }
@@ -127,45 +139,67 @@ __device__ __forceinline__ int pmod(int v, int m) {
 
 // ------------------------------------------------------------ centre of mass
 // cx[p] = sum(I kx) / sum(I), cy[p] = sum(I ky) / sum(I) with I = pattern * mask
-// (phase_base_class.py:646-672): kx, ky are the pixel indices along x and y.
+// (phase_base_class.py:646-688): kx, ky are the pixel indices along x and y.
+// Mask modes follow NumPy's promotion of pattern (float32) * mask:
+//   0  no mask;
+//   1  boolean or float32 mask: float32 products and sums;
+//   2  float64 mask, vectorised form: the float64 array, float64 sums;
+//   3  float64 mask, per-pattern loop (mi *= mask in place): the float64 product
+//      rounded to float32, float32 sums.
+template <int kMask>
+struct MaskedPixel {
+  using Acc = typename std::conditional<kMask == 2, double, float>::type;
+  const float* src;
+  const void* mask;
+  __device__ __forceinline__ Acc operator()(int e) const {
+    const float v = __ldg(src + e);
+    if constexpr (kMask == 0) {
+      return v;
+    } else if constexpr (kMask == 1) {
+      return __fmul_rn(v, __ldg(static_cast<const float*>(mask) + e));
+    } else if constexpr (kMask == 2) {
+      return __dmul_rn((double)v, __ldg(static_cast<const double*>(mask) + e));
+    } else {
+      return __double2float_rn(__dmul_rn((double)v, __ldg(static_cast<const double*>(mask) + e)));
+    }
+  }
+};
+
+template <int kMask>
 __global__ void __launch_bounds__(kPreThreads) pattern_com_general_kernel(
-    const float* __restrict__ in, int Qx, int Qy, const float* __restrict__ mask,
-    int max_leaves, float* __restrict__ cx, float* __restrict__ cy) {
+    const float* __restrict__ in, int Qx, int Qy, const void* __restrict__ mask,
+    int max_leaves, void* cx_out, void* cy_out) {
+  using Px = MaskedPixel<kMask>;
+  using Acc = typename Px::Acc;
   extern __shared__ float4 smem4[];
   const int N = Qx * Qy;
-  float* pat = reinterpret_cast<float*>(smem4);
-  float* leaf = pat + N;                                        // 3 * max_leaves
-  int* llo = reinterpret_cast<int*>(leaf + 3 * max_leaves);     // max_leaves
-  int* llen = llo + max_leaves;                                 // max_leaves
+  Acc* leaf = reinterpret_cast<Acc*>(smem4);                       // 3 * max_leaves
+  int* llo = reinterpret_cast<int*>(leaf + 3 * max_leaves);        // max_leaves
+  int* llen = llo + max_leaves;                                    // max_leaves
   __shared__ int nleaves;
-  const float* src = in + (size_t)blockIdx.x * N;
-  for (int e = threadIdx.x; e < N; e += kPreThreads) {
-    float v = src[e];
-    if (mask) v = __fmul_rn(v, mask[e]);
-    pat[e] = v;
-  }
+  const Px px{in + (size_t)blockIdx.x * N, mask};
   if (threadIdx.x == 0) nleaves = pairwise_leaves(N, llo, llen);
   __syncthreads();
   const int L = nleaves;
   for (int t = threadIdx.x; t < 3 * L; t += kPreThreads) {
     const int q = t / L, j = t - q * L;
-    float s;
+    Acc s;
     if (q == 0) {
-      s = leaf_sum([&](int e) { return pat[e]; }, llo[j], llen[j]);
+      s = leaf_sum<Acc>(px, llo[j], llen[j]);
     } else if (q == 1) {
-      s = leaf_sum([&](int e) { return __fmul_rn(pat[e], (float)(e / Qy)); }, llo[j], llen[j]);
+      s = leaf_sum<Acc>([&](int e) { return acc_mul(px(e), (Acc)(e / Qy)); }, llo[j], llen[j]);
     } else {
-      s = leaf_sum([&](int e) { return __fmul_rn(pat[e], (float)(e % Qy)); }, llo[j], llen[j]);
+      s = leaf_sum<Acc>([&](int e) { return acc_mul(px(e), (Acc)(e % Qy)); }, llo[j], llen[j]);
     }
     leaf[q * max_leaves + j] = s;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    const float s0 = __fadd_rn(0.0f, pairwise_combine(N, leaf));
-    const float s1 = __fadd_rn(0.0f, pairwise_combine(N, leaf + max_leaves));
-    const float s2 = __fadd_rn(0.0f, pairwise_combine(N, leaf + 2 * max_leaves));
-    cx[blockIdx.x] = __fdiv_rn(s1, s0);
-    cy[blockIdx.x] = __fdiv_rn(s2, s0);
+    const Acc s0 = acc_add((Acc)0, pairwise_combine<Acc>(N, leaf));
+    const Acc s1 = acc_add((Acc)0, pairwise_combine<Acc>(N, leaf + max_leaves));
+    const Acc s2 = acc_add((Acc)0, pairwise_combine<Acc>(N, leaf + 2 * max_leaves));
+    static_cast<Acc*>(cx_out)[blockIdx.x] = acc_div(s1, s0);
+    static_cast<Acc*>(cy_out)[blockIdx.x] = acc_div(s2, s0);
   }
 }
 
@@ -174,48 +208,49 @@ __global__ void __launch_bounds__(kPreThreads) pattern_com_general_kernel(
 // |d cx/dx + d cy/dy| (divergence, `div` != 0) of the CoM field rotated by angle
 // a (cos_a, sin_a) and, for t = 1, with x and y exchanged
 // (phase_base_class.py:1086-1182; central differences over two pixels).
+// T is the type of the CoM field (float64 when the centre of mass was formed in
+// float64); the float32 cos / sin of the angles are promoted to it, as NumPy does.
+template <typename T>
 __global__ void __launch_bounds__(kPreThreads) rotation_search_kernel(
-    const float* __restrict__ nx, const float* __restrict__ ny, int R0, int R1,
+    const T* __restrict__ nx, const T* __restrict__ ny, int R0, int R1,
     const float* __restrict__ cos_a, const float* __restrict__ sin_a, int A, int div,
-    int max_leaves, float* __restrict__ vals) {
+    int max_leaves, T* __restrict__ vals) {
   extern __shared__ float4 smem4[];
-  float* leaf = reinterpret_cast<float*>(smem4);
+  T* leaf = reinterpret_cast<T*>(smem4);
   int* llo = reinterpret_cast<int*>(leaf + max_leaves);
   int* llen = llo + max_leaves;
   __shared__ int nleaves;
   const int a = blockIdx.x % A;
   const int t = blockIdx.x / A;
-  const float c = cos_a[a], s = sin_a[a];
+  const T c = cos_a[a], s = sin_a[a];
   const int W = R1 - 2;
   const int n = (R0 - 2) * W;
   auto rx = [&](int i, int j) {
-    const float X = nx[i * R1 + j], Y = ny[i * R1 + j];
-    return t ? __fsub_rn(__fmul_rn(c, Y), __fmul_rn(s, X))
-             : __fsub_rn(__fmul_rn(c, X), __fmul_rn(s, Y));
+    const T X = nx[i * R1 + j], Y = ny[i * R1 + j];
+    return t ? acc_add(acc_mul(c, Y), -acc_mul(s, X)) : acc_add(acc_mul(c, X), -acc_mul(s, Y));
   };
   auto ry = [&](int i, int j) {
-    const float X = nx[i * R1 + j], Y = ny[i * R1 + j];
-    return t ? __fadd_rn(__fmul_rn(s, Y), __fmul_rn(c, X))
-             : __fadd_rn(__fmul_rn(s, X), __fmul_rn(c, Y));
+    const T X = nx[i * R1 + j], Y = ny[i * R1 + j];
+    return t ? acc_add(acc_mul(s, Y), acc_mul(c, X)) : acc_add(acc_mul(s, X), acc_mul(c, Y));
   };
   auto value = [&](int e) {
     const int i = e / W, j = e - (e / W) * W;
     if (div) {
-      const float gxx = __fsub_rn(rx(i + 2, j + 1), rx(i, j + 1));
-      const float gyy = __fsub_rn(ry(i + 1, j + 2), ry(i + 1, j));
-      return fabsf(__fadd_rn(gxx, gyy));
+      const T gxx = acc_add(rx(i + 2, j + 1), -rx(i, j + 1));
+      const T gyy = acc_add(ry(i + 1, j + 2), -ry(i + 1, j));
+      return abs(acc_add(gxx, gyy));
     }
-    const float gxy = __fsub_rn(rx(i + 1, j + 2), rx(i + 1, j));
-    const float gyx = __fsub_rn(ry(i + 2, j + 1), ry(i, j + 1));
-    return fabsf(__fsub_rn(gyx, gxy));
+    const T gxy = acc_add(rx(i + 1, j + 2), -rx(i + 1, j));
+    const T gyx = acc_add(ry(i + 2, j + 1), -ry(i, j + 1));
+    return abs(acc_add(gyx, -gxy));
   };
   if (threadIdx.x == 0) nleaves = pairwise_leaves(n, llo, llen);
   __syncthreads();
-  for (int j = threadIdx.x; j < nleaves; j += kPreThreads) leaf[j] = leaf_sum(value, llo[j], llen[j]);
+  for (int j = threadIdx.x; j < nleaves; j += kPreThreads) leaf[j] = leaf_sum<T>(value, llo[j], llen[j]);
   __syncthreads();
   if (threadIdx.x == 0) {
-    const float sum = __fadd_rn(0.0f, pairwise_combine(n, leaf));
-    vals[blockIdx.x] = __fdiv_rn(sum, (float)n);
+    const T sum = acc_add((T)0, pairwise_combine<T>(n, leaf));
+    vals[blockIdx.x] = acc_div(sum, (T)n);
   }
 }
 
@@ -264,7 +299,7 @@ __global__ void __launch_bounds__(kPreThreads) pattern_normalize_general_kernel(
   }
   __syncthreads();
   for (int j = threadIdx.x; j < nleaves; j += kPreThreads)
-    leaf[j] = leaf_sum([&](int e) { return sh[e]; }, llo[j], llen[j]);
+    leaf[j] = leaf_sum<float>([&](int e) { return sh[e]; }, llo[j], llen[j]);
   // amplitudes (numpy.maximum keeps its first argument unless it is below the second)
   const int Cx = crop_w > 0 ? 2 * crop_w : Qx;
   const int Cy = crop_w > 0 ? 2 * crop_w : Qy;
@@ -278,7 +313,7 @@ __global__ void __launch_bounds__(kPreThreads) pattern_normalize_general_kernel(
     dst[e] = __fsqrt_rn(v);
   }
   __syncthreads();
-  if (threadIdx.x == 0) sums[o] = __fadd_rn(0.0f, pairwise_combine(N, leaf));
+  if (threadIdx.x == 0) sums[o] = __fadd_rn(0.0f, pairwise_combine<float>(N, leaf));
 }
 
 
@@ -287,20 +322,20 @@ __global__ void __launch_bounds__(kPreThreads) pattern_normalize_general_kernel(
 // then r += a[lo + j + 8 k] for k = 1 .. l/8 - 1 (values from `val`). Lane j of
 // an 8-lane group holds chain j; the group's lane 0 gets the leaf sum
 // ((r0 + r1) + (r2 + r3)) + ((r4 + r5) + (r6 + r7)) plus the l % 8 tail in order.
-template <typename V>
-__device__ __forceinline__ float leaf_chain_sum(const V& val, int lo, int l) {
+template <typename Acc, typename V>
+__device__ __forceinline__ Acc leaf_chain_sum(const V& val, int lo, int l) {
   const int j = threadIdx.x & 7;
   const int groups = l >> 3;
-  float r = val(lo + j);
-  for (int k = 1; k < groups; ++k) r = __fadd_rn(r, val(lo + j + 8 * k));
-  float o = __shfl_down_sync(0xffffffffu, r, 1, 8);
-  if ((j & 1) == 0) r = __fadd_rn(r, o);
+  Acc r = val(lo + j);
+  for (int k = 1; k < groups; ++k) r = acc_add(r, (Acc)val(lo + j + 8 * k));
+  Acc o = __shfl_down_sync(0xffffffffu, r, 1, 8);
+  if ((j & 1) == 0) r = acc_add(r, o);
   o = __shfl_down_sync(0xffffffffu, r, 2, 8);
-  if ((j & 3) == 0) r = __fadd_rn(r, o);
+  if ((j & 3) == 0) r = acc_add(r, o);
   o = __shfl_down_sync(0xffffffffu, r, 4, 8);
   if (j == 0) {
-    r = __fadd_rn(r, o);
-    for (int i = groups * 8; i < l; ++i) r = __fadd_rn(r, val(lo + i));
+    r = acc_add(r, o);
+    for (int i = groups * 8; i < l; ++i) r = acc_add(r, (Acc)val(lo + i));
   }
   return r;
 }
@@ -308,13 +343,14 @@ __device__ __forceinline__ float leaf_chain_sum(const V& val, int lo, int l) {
 // In-place pairwise sum of q arrays of L = 2^levels leaf sums each (arrays at
 // vals + q * L): level by level, vals[j] += vals[j + s]; the totals land in
 // vals[q * L]. Called by all threads of the block.
-__device__ __forceinline__ void tree_add(float* vals, int q, int L) {
+template <typename Acc>
+__device__ __forceinline__ void tree_add(Acc* vals, int q, int L) {
   for (int s = 1; s < L; s <<= 1) {
     const int pairs = L / (2 * s);
     for (int t = threadIdx.x; t < q * pairs; t += blockDim.x) {
       const int a = t / pairs, k = t - (t / pairs) * pairs;
-      float* v = vals + a * L + 2 * s * k;
-      v[0] = __fadd_rn(v[0], v[s]);
+      Acc* v = vals + a * L + 2 * s * k;
+      v[0] = acc_add(v[0], v[s]);
     }
     __syncthreads();
   }
@@ -323,37 +359,36 @@ __device__ __forceinline__ void tree_add(float* vals, int q, int L) {
 // Centre of mass, perfect tree: block = 8 L threads (at least one warp), one
 // pattern per block, lane group g sums leaf g of the three quantities straight
 // from global memory (each warp load covers four 32-byte runs).
+template <int kMask>
 __global__ void __launch_bounds__(1024) pattern_com_kernel(
-    const float* __restrict__ in, int Qx, int Qy, const float* __restrict__ mask, int leaf,
-    int L, float* __restrict__ cx, float* __restrict__ cy) {
-  __shared__ float vals[3 * 128];
+    const float* __restrict__ in, int Qx, int Qy, const void* __restrict__ mask, int leaf,
+    int L, void* cx_out, void* cy_out) {
+  using Px = MaskedPixel<kMask>;
+  using Acc = typename Px::Acc;
+  __shared__ Acc vals[3 * 128];
   const int N = Qx * Qy;
   const int g = threadIdx.x >> 3;
-  const float* src = in + (size_t)blockIdx.x * N;
+  const Px px{in + (size_t)blockIdx.x * N, mask};
   // lanes past the last leaf (blocks of one warp) sum elements 0..7 and drop
   // the result: every lane of a warp takes part in the shuffles
   const int lo = g < L ? g * leaf : 0;
   const int len = g < L ? leaf : 8;
-  auto inten = [&](int e) {
-    const float v = __ldg(src + e);
-    return mask ? __fmul_rn(v, __ldg(mask + e)) : v;
-  };
-  const float s0 = leaf_chain_sum(inten, lo, len);
-  const float s1 = leaf_chain_sum(
-      [&](int e) { return __fmul_rn(inten(e), (float)(e / Qy)); }, lo, len);
-  const float s2 = leaf_chain_sum(
-      [&](int e) { return __fmul_rn(inten(e), (float)(e - (e / Qy) * Qy)); }, lo, len);
+  const Acc s0 = leaf_chain_sum<Acc>(px, lo, len);
+  const Acc s1 = leaf_chain_sum<Acc>(
+      [&](int e) { return acc_mul(px(e), (Acc)(e / Qy)); }, lo, len);
+  const Acc s2 = leaf_chain_sum<Acc>(
+      [&](int e) { return acc_mul(px(e), (Acc)(e - (e / Qy) * Qy)); }, lo, len);
   if (g < L && (threadIdx.x & 7) == 0) {
     vals[g] = s0;
     vals[L + g] = s1;
     vals[2 * L + g] = s2;
   }
   __syncthreads();
-  tree_add(vals, 3, L);
+  tree_add<Acc>(vals, 3, L);
   if (threadIdx.x == 0) {
-    const float t0 = __fadd_rn(0.0f, vals[0]);
-    cx[blockIdx.x] = __fdiv_rn(__fadd_rn(0.0f, vals[L]), t0);
-    cy[blockIdx.x] = __fdiv_rn(__fadd_rn(0.0f, vals[2 * L]), t0);
+    const Acc t0 = acc_add((Acc)0, vals[0]);
+    static_cast<Acc*>(cx_out)[blockIdx.x] = acc_div(acc_add((Acc)0, vals[L]), t0);
+    static_cast<Acc*>(cy_out)[blockIdx.x] = acc_div(acc_add((Acc)0, vals[2 * L]), t0);
   }
 }
 
@@ -430,7 +465,7 @@ __global__ void __launch_bounds__(1024) pattern_normalize_kernel(
   __syncthreads();
 
   const int g = tid >> 3;
-  const float ls = leaf_chain_sum([&](int e) { return pat[e]; }, g < L ? g * leaf : 0,
+  const float ls = leaf_chain_sum<float>([&](int e) { return pat[e]; }, g < L ? g * leaf : 0,
                                   g < L ? leaf : 8);
   if (g < L && (tid & 7) == 0) vals[g] = ls;
 
@@ -449,7 +484,7 @@ __global__ void __launch_bounds__(1024) pattern_normalize_kernel(
     dst[e] = __fsqrt_rn(a);
   }
   __syncthreads();
-  tree_add(vals, 1, L);
+  tree_add<float>(vals, 1, L);
   if (tid == 0) sums[o] = __fadd_rn(0.0f, vals[0]);
 }
 
@@ -483,37 +518,59 @@ cudaError_t set_smem(const void* fn, size_t bytes) {
 
 size_t preprocess_smem_limit() { return 227 * 1024; }
 
-cudaError_t launch_pattern_com(const float* in, int num, int Qx, int Qy, const float* mask,
-                               float* cx, float* cy, cudaStream_t s) {
+template <int kMask>
+cudaError_t launch_pattern_com_t(const float* in, int num, int Qx, int Qy, const void* mask,
+                                 void* cx, void* cy, cudaStream_t s) {
+  using Acc = typename MaskedPixel<kMask>::Acc;
   const int N = Qx * Qy;
   int leaf = 0, levels = 0;
   if (pairwise_perfect(N, leaf, levels)) {
     const int L = 1 << levels;
     const int threads = 8 * L < 32 ? 32 : 8 * L;
-    pattern_com_kernel<<<num, threads, 0, s>>>(in, Qx, Qy, mask, leaf, L, cx, cy);
+    pattern_com_kernel<kMask><<<num, threads, 0, s>>>(in, Qx, Qy, mask, leaf, L, cx, cy);
     return cudaGetLastError();
   }
   const int L = pairwise_leaf_count(N);
-  const size_t smem = sizeof(float) * ((size_t)N + 3 * L) + sizeof(int) * 2 * L;
+  const size_t smem = sizeof(Acc) * 3 * (size_t)L + sizeof(int) * 2 * L;
   if (smem > preprocess_smem_limit()) return cudaErrorInvalidValue;
-  cudaError_t e = set_smem((const void*)pattern_com_general_kernel, smem);
+  cudaError_t e = set_smem((const void*)pattern_com_general_kernel<kMask>, smem);
   if (e != cudaSuccess) return e;
-  pattern_com_general_kernel<<<num, kPreThreads, smem, s>>>(in, Qx, Qy, mask, L, cx, cy);
+  pattern_com_general_kernel<kMask><<<num, kPreThreads, smem, s>>>(in, Qx, Qy, mask, L, cx, cy);
   return cudaGetLastError();
 }
 
-cudaError_t launch_rotation_search(const float* nx, const float* ny, int R0, int R1,
-                                   const float* cos_a, const float* sin_a, int A, int div,
-                                   float* vals, cudaStream_t s) {
+cudaError_t launch_pattern_com(const float* in, int num, int Qx, int Qy, const void* mask,
+                               int mask_mode, void* cx, void* cy, cudaStream_t s) {
+  switch (mask_mode) {
+    case 0: return launch_pattern_com_t<0>(in, num, Qx, Qy, nullptr, cx, cy, s);
+    case 1: return launch_pattern_com_t<1>(in, num, Qx, Qy, mask, cx, cy, s);
+    case 2: return launch_pattern_com_t<2>(in, num, Qx, Qy, mask, cx, cy, s);
+    case 3: return launch_pattern_com_t<3>(in, num, Qx, Qy, mask, cx, cy, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <typename T>
+cudaError_t launch_rotation_search_t(const void* nx, const void* ny, int R0, int R1,
+                                     const float* cos_a, const float* sin_a, int A, int div,
+                                     void* vals, cudaStream_t s) {
   const int n = (R0 - 2) * (R1 - 2);
   const int L = pairwise_leaf_count(n);
-  const size_t smem = sizeof(float) * L + sizeof(int) * 2 * (size_t)L;
+  const size_t smem = sizeof(T) * L + sizeof(int) * 2 * (size_t)L;
   if (smem > preprocess_smem_limit()) return cudaErrorInvalidValue;
-  cudaError_t e = set_smem((const void*)rotation_search_kernel, smem);
+  cudaError_t e = set_smem((const void*)rotation_search_kernel<T>, smem);
   if (e != cudaSuccess) return e;
-  rotation_search_kernel<<<2 * A, kPreThreads, smem, s>>>(nx, ny, R0, R1, cos_a, sin_a, A, div,
-                                                          L, vals);
+  rotation_search_kernel<T><<<2 * A, kPreThreads, smem, s>>>(
+      static_cast<const T*>(nx), static_cast<const T*>(ny), R0, R1, cos_a, sin_a, A, div, L,
+      static_cast<T*>(vals));
   return cudaGetLastError();
+}
+
+cudaError_t launch_rotation_search(const void* nx, const void* ny, int R0, int R1,
+                                   const float* cos_a, const float* sin_a, int A, int div,
+                                   int is_double, void* vals, cudaStream_t s) {
+  return is_double ? launch_rotation_search_t<double>(nx, ny, R0, R1, cos_a, sin_a, A, div, vals, s)
+                   : launch_rotation_search_t<float>(nx, ny, R0, R1, cos_a, sin_a, A, div, vals, s);
 }
 
 cudaError_t launch_pattern_normalize(const float* in, int Qx, int Qy, const int32_t* rows,

@@ -49,40 +49,56 @@ def upload_intensities(intensities: np.ndarray):
     return torch.from_numpy(arr.reshape((-1, qx, qy))).to("cuda")
 
 
-def pattern_com(intensities_dev, mask=None):
-    """(com_x, com_y) float32 host arrays, one value per pattern."""
+def pattern_com(intensities_dev, mask=None, vectorized=True):
+    """(com_x, com_y) host arrays, one value per pattern, in the type NumPy gives
+    pattern * mask: float32 without a mask or with a boolean / float32 / small
+    integer mask; float64 for any other mask in the vectorised form; float32 with
+    the float64 product rounded in place in the per-pattern form."""
     torch = _torch()
     J, qx, qy = intensities_dev.shape
-    cx = torch.empty(J, dtype=torch.float32, device=intensities_dev.device)
-    cy = torch.empty_like(cx)
-    mask_dev = None
+    dev = intensities_dev.device
+    mode, mask_dev = 0, None
     if mask is not None:
-        mask_dev = torch.from_numpy(np.ascontiguousarray(mask, dtype=np.float32)).to(cx.device)
+        m = np.asarray(mask)
+        if np.result_type(np.float32, m.dtype) == np.float32:
+            mode = 1
+            mask_dev = torch.from_numpy(np.ascontiguousarray(m, dtype=np.float32)).to(dev)
+        else:
+            mode = 2 if vectorized else 3
+            mask_dev = torch.from_numpy(np.ascontiguousarray(m, dtype=np.float64)).to(dev)
+    out_t = torch.float64 if mode == 2 else torch.float32
+    cx = torch.empty(J, dtype=out_t, device=dev)
+    cy = torch.empty_like(cx)
     _native.check(_native.lib().ptycho_pattern_com(
         _ptr(intensities_dev), int(J), int(qx), int(qy),
-        None if mask_dev is None else _ptr(mask_dev), _ptr(cx), _ptr(cy), _stream()))
+        None if mask_dev is None else _ptr(mask_dev), mode, _ptr(cx), _ptr(cy), _stream()))
     return cx.cpu().numpy(), cy.cpu().numpy()
 
 
 def rotation_values(com_x: np.ndarray, com_y: np.ndarray, cos_a: np.ndarray, sin_a: np.ndarray,
                     maximize_divergence: bool) -> np.ndarray:
-    """(2, A) float32: the mean |curl| (|div|) per angle, untransposed then transposed."""
+    """(2, A): the mean |curl| (|div|) per angle, untransposed then transposed, in
+    the type of the CoM field (float32, or float64 when the centre of mass was
+    formed in float64)."""
     torch = _torch()
     r0, r1 = com_x.shape
+    dbl = np.result_type(com_x.dtype, com_y.dtype, np.float32) == np.float64
     if r0 < 3 or r1 < 3:
         raise ValueError(
             f"the rotation search needs a scan of at least 3 x 3 positions (got {r0} x {r1}); "
             "pass force_com_rotation")
     dev = torch.device("cuda", torch.cuda.current_device())
 
-    def up(a):
-        return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(dev)
+    def up(a, dtype):
+        return torch.from_numpy(np.ascontiguousarray(a, dtype=dtype)).to(dev)
 
-    nx, ny, c, s = up(com_x), up(com_y), up(np.ravel(cos_a)), up(np.ravel(sin_a))
+    ft = np.float64 if dbl else np.float32
+    nx, ny = up(com_x, ft), up(com_y, ft)
+    c, s = up(np.ravel(cos_a), np.float32), up(np.ravel(sin_a), np.float32)
     A = int(c.numel())
-    vals = torch.empty(2 * A, dtype=torch.float32, device=dev)
+    vals = torch.empty(2 * A, dtype=torch.float64 if dbl else torch.float32, device=dev)
     _native.check(_native.lib().ptycho_rotation_search(
-        _ptr(nx), _ptr(ny), int(r0), int(r1), _ptr(c), _ptr(s), A,
+        _ptr(nx), _ptr(ny), 1 if dbl else 0, int(r0), int(r1), _ptr(c), _ptr(s), A,
         1 if maximize_divergence else 0, _ptr(vals), _stream()))
     return vals.cpu().numpy().reshape(2, A)
 

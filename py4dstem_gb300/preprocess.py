@@ -366,10 +366,10 @@ class PreprocessMixin:
             ky = np.arange(intensities.shape[-1], dtype=np.float32)
             kya, kxa = np.meshgrid(ky, kx)
             if intensities_dev is not None:
-                # both branches below give these bits for a 0/1 mask
+                # the bits of the branch below that `vectorized` selects
                 from . import device_preprocess
 
-                cx, cy = device_preprocess.pattern_com(intensities_dev, dp_mask)
+                cx, cy = device_preprocess.pattern_com(intensities_dev, dp_mask, vectorized)
                 cmx = cx.reshape(intensities.shape[:2])
                 cmy = cy.reshape(intensities.shape[:2])
             elif vectorized:
@@ -433,8 +433,7 @@ class PreprocessMixin:
             from . import device_preprocess
 
             vals = device_preprocess.rotation_values(
-                np.asarray(cnx, dtype=np.float32), np.asarray(cny, dtype=np.float32),
-                np.cos(rad), np.sin(rad), maximize_divergence)
+                np.asarray(cnx), np.asarray(cny), np.cos(rad), np.sin(rad), maximize_divergence)
             return vals[0], vals[1]
         return tuple(self._curl_or_div(*self._rotated(cnx[None], cny[None], rad, t),
                                        maximize_divergence, axis=(-2, -1)) for t in (False, True))

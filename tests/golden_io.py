@@ -66,6 +66,20 @@ class PrepGolden:
         p.preprocess(**pre)
         return p
 
+    @staticmethod
+    def same_state(p, q):
+        """Assert that two preprocessed objects hold the same bits."""
+        for key in ("com_measured_x", "com_measured_y", "com_fitted_x", "com_fitted_y",
+                    "com_normalized_x", "com_normalized_y", "positions_px", "probe",
+                    "object_fov_mask"):
+            a, b = np.asarray(getattr(p, "_" + key)), np.asarray(getattr(q, "_" + key))
+            assert a.dtype == b.dtype, key
+            np.testing.assert_array_equal(a, b, err_msg=key)
+        assert p._rotation_best_rad == q._rotation_best_rad
+        assert p._rotation_best_transpose == q._rotation_best_transpose
+        assert np.float32(p._mean_diffraction_intensity) == np.float32(q._mean_diffraction_intensity)
+        np.testing.assert_array_equal(p._amplitudes, q._amplitudes)
+
     def check(self, p, fov_mask=True, probe_exact=True):
         """Assert that a preprocessed object holds the reference's bits. The
         initial probe is NumPy FFT work on the host, whose float32 bits may differ
