@@ -238,6 +238,33 @@ int ptycho_probe_orthogonalize(const ptycho_geometry* geometry, void* probe, voi
                                size_t workspace_bytes, void* stream);
 
 /*
+ * Optional per-iteration constraints (off by default in the reference).
+ *
+ * Identical slices: every slice of the (T, Px, Py) object becomes the mean over
+ * slices. Replaces _object_identical_slices_constraint
+ * (ptychographic_constraints.py:630-647).
+ */
+int ptycho_object_identical_slices(const ptycho_geometry* geometry, void* object, void* stream);
+
+/*
+ * Probe aperture: probe mode 0 <- IFFT2(exp(i angle(FFT2(probe))) aperture), scaled
+ * back to its power sum |probe|^2; aperture (Sx, Sy) float32 is the Fourier
+ * amplitude of the initial probe. Replaces _probe_aperture_constraint
+ * (ptychographic_constraints.py:1004-1040; mode 0 for mixed states, :1243-1247).
+ */
+int ptycho_probe_aperture_constraint(const ptycho_geometry* geometry, void* probe,
+                                     const float* aperture, void* stream);
+
+/*
+ * Probe amplitude: every probe mode times the real-space mask (Sx, Sy) float32,
+ * scaled back to its power sum. Replaces _probe_amplitude_constraint
+ * (ptychographic_constraints.py:920-957); the soft top-hat mask
+ * 0.5 (1 - erf(sigma r / (1 - r^2))) is formed by the caller.
+ */
+int ptycho_probe_amplitude_constraint(const ptycho_geometry* geometry, void* probe,
+                                      const float* mask, void* stream);
+
+/*
  * Preprocessing (one-time, before the reconstruction loop). Sums follow the
  * order of NumPy's float32 pairwise add.reduce over each contiguous run, and
  * products and quotients are rounded once each, so the results carry the bits

@@ -84,6 +84,8 @@ class Oracle:
         self.J = self.amplitudes.shape[0]
         self.exit_waves = None
         self.error_iterations = []
+        # Fourier amplitude of the initial probe (preprocess, store_initial_arrays)
+        self.probe_initial_aperture = np.abs(np.fft.fft2(self.probe))
 
     def fft2(self, a):
         if self.fft_round_trip:
@@ -432,6 +434,46 @@ class Oracle:
         x0, y0 = self.center_of_mass(inten)
         self.probe = self.fft_shift(self.probe, -np.array([x0, y0]))
 
+    def object_identical_slices(self):
+        """ptychographic_constraints.py:630-647."""
+        self.object[:] = self.object.mean(0, keepdims=True)
+
+    @staticmethod
+    def _probe_aperture(p, aperture):
+        """ptychographic_constraints.py:1004-1040."""
+        s0 = np.sum(np.abs(p) ** 2)
+        phase = np.angle(np.fft.fft2(p))
+        u = np.fft.ifft2(np.exp(1j * phase) * aperture)
+        return u * np.sqrt(s0 / np.sum(np.abs(u) ** 2))
+
+    @staticmethod
+    def _probe_amplitude(p, relative_radius, relative_width):
+        """ptychographic_constraints.py:920-957."""
+        from scipy.special import erf
+
+        s0 = np.sum(np.abs(p) ** 2)
+        X = np.fft.fftfreq(p.shape[0])[:, None]
+        Y = np.fft.fftfreq(p.shape[1])[None]
+        r = np.hypot(X, Y) - relative_radius
+        sigma = np.sqrt(np.pi) / relative_width
+        u = p * (0.5 * (1 - erf(sigma * r / (1 - r ** 2))))
+        return u * np.sqrt(s0 / np.sum(np.abs(u) ** 2))
+
+    def probe_optional_constraints(self, aperture, amplitude, radius, width):
+        """ptychographic_constraints.py:1091-1148 (single probe), 1218-1285 (mixed)."""
+        if aperture:
+            if self.mixed:
+                self.probe[0] = self._probe_aperture(self.probe[0],
+                                                     self.probe_initial_aperture[0])
+            else:
+                self.probe = self._probe_aperture(self.probe, self.probe_initial_aperture)
+        if amplitude:
+            if self.mixed:
+                for i in range(self.num_probes):
+                    self.probe[i] = self._probe_amplitude(self.probe[i], radius, width)
+            else:
+                self.probe = self._probe_amplitude(self.probe, radius, width)
+
     def probe_orthogonalization(self):
         """ptychographic_constraints.py:1181-1216."""
         n = self.num_probes
@@ -452,7 +494,10 @@ class Oracle:
                     fix_potential_baseline=True, pure_phase_object=False,
                     object_positivity=True, detector_fourier_mask=None, fix_positions=True,
                     fix_positions_com=True, positions_step_size=0.5,
-                    max_position_update_distance=None, max_position_total_distance=None):
+                    max_position_update_distance=None, max_position_total_distance=None,
+                    fix_probe_aperture=False, constrain_probe_amplitude=False,
+                    constrain_probe_amplitude_relative_radius=0.5,
+                    constrain_probe_amplitude_relative_width=0.05, identical_slices=False):
         """singleslice_ptychography.py:606-996 (and the multislice / mixed-state twins)."""
         projection = method != "GD"
         J = self.J
@@ -493,11 +538,16 @@ class Oracle:
                         max_position_total_distance)
                 error += be
             error /= self.mean_intensity * J
+            if identical_slices and self.num_slices > 1:
+                self.object_identical_slices()
             self.object_constraints(shrinkage_rad, mask,
                                     pure_phase_object and self.object_type == "complex",
                                     object_positivity)
             if fix_probe_com and not fix_probe:
                 self.probe_com_constraint()
+            self.probe_optional_constraints(
+                fix_probe_aperture and not fix_probe, constrain_probe_amplitude and not fix_probe,
+                constrain_probe_amplitude_relative_radius, constrain_probe_amplitude_relative_width)
             if self.mixed and orthogonalize_probe:
                 self.probe_orthogonalization()
             # phase_base_class.py:2179-2195 passes fix_positions_com and not fix_positions

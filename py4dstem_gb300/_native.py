@@ -97,6 +97,11 @@ _SIGNATURES = {
         [ctypes.POINTER(Geometry), _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _sz, _vp],
         ctypes.c_int,
     ),
+    "ptycho_object_identical_slices": ([ctypes.POINTER(Geometry), _vp, _vp], ctypes.c_int),
+    "ptycho_probe_aperture_constraint": (
+        [ctypes.POINTER(Geometry), _vp, _vp, _vp], ctypes.c_int),
+    "ptycho_probe_amplitude_constraint": (
+        [ctypes.POINTER(Geometry), _vp, _vp, _vp], ctypes.c_int),
     "ptycho_pattern_com": ([_vp, _i32, _i32, _i32, _vp, _i32, _vp, _vp, _vp], ctypes.c_int),
     "ptycho_rotation_search": (
         [_vp, _vp, _i32, _i32, _i32, _vp, _vp, _i32, _i32, _vp, _vp], ctypes.c_int),

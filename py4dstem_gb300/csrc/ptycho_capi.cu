@@ -541,6 +541,57 @@ int ptycho_probe_mix(const ptycho_geometry* g, const void* probe_in, const void*
   return PTYCHO_OK;
 }
 
+// ------------------------------------------------------- optional constraints
+int ptycho_object_identical_slices(const ptycho_geometry* g, void* object, void* stream) {
+  int st = check_geometry(g);
+  if (st != PTYCHO_OK) return st;
+  if (!object) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "object must be non-null");
+  BatchArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.Px = g->object_x;
+  a.Py = g->object_y;
+  a.T = g->num_slices;
+  a.potential = g->object_is_potential;
+  a.object = object;
+  cudaError_t e = launch_identical_slices(a, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "identical-slices kernel");
+  return PTYCHO_OK;
+}
+
+int ptycho_probe_aperture_constraint(const ptycho_geometry* g, void* probe,
+                                     const float* aperture, void* stream) {
+  int st = check_geometry(g);
+  if (st != PTYCHO_OK) return st;
+  if (!probe || !aperture)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "probe and aperture must be non-null");
+  BatchArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.Sx = g->roi_x;
+  a.Sy = g->roi_y;
+  a.M = g->num_probes;
+  a.probe = static_cast<float2*>(probe);
+  a.aperture = aperture;
+  cudaError_t e = launch_probe_aperture(a, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "probe aperture kernel");
+  return PTYCHO_OK;
+}
+
+int ptycho_probe_amplitude_constraint(const ptycho_geometry* g, void* probe, const float* mask,
+                                      void* stream) {
+  int st = check_geometry(g);
+  if (st != PTYCHO_OK) return st;
+  if (!probe || !mask) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "probe and mask must be non-null");
+  BatchArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.Sx = g->roi_x;
+  a.Sy = g->roi_y;
+  a.M = g->num_probes;
+  a.probe = static_cast<float2*>(probe);
+  cudaError_t e = launch_probe_amplitude(a, mask, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "probe amplitude kernel");
+  return PTYCHO_OK;
+}
+
 // ----------------------------------------------------------------- preprocess
 int ptycho_pattern_com(const float* intensities, int32_t num_patterns, int32_t qx, int32_t qy,
                        const void* mask, int32_t mask_mode, void* com_x, void* com_y,

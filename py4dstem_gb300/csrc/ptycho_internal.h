@@ -29,6 +29,7 @@ struct BatchArgs {
   int exact_probe_grad;    // probe term through the adjoint of the sub-pixel shift
   int prepare_spectrum;    // after the probe update, the next batch's probe spectrum
   int nobj_only;           // object reduction of the |P|^2 terms alone (probe overlap)
+  const float* aperture;   // (N) Fourier amplitude of the initial probe (aperture constraint)
 
   void* object;                 // (T,Px,Py) float2 or float
   float2* probe;                // (M,N)
@@ -97,6 +98,12 @@ cudaError_t launch_position_correction(const BatchArgs& a, cudaStream_t s);
 cudaError_t launch_probe_inverse(const BatchArgs& a, cudaStream_t s);
 // |P_b|^2 of the shifted probe (mode 0) of every batch position into st_nobj.
 cudaError_t launch_probe_intensity(const BatchArgs& a, cudaStream_t s);
+// Probe mode 0 with its Fourier amplitude replaced by a.aperture, power kept.
+cudaError_t launch_probe_aperture(const BatchArgs& a, cudaStream_t s);
+// Every probe mode times a real-space mask, power of each mode kept.
+cudaError_t launch_probe_amplitude(const BatchArgs& a, const float* mask, cudaStream_t s);
+// Every slice of the object set to the mean over slices.
+cudaError_t launch_identical_slices(const BatchArgs& a, cudaStream_t s);
 // overlap += sum over the batch of the staged |P_b|^2, scattered into the object grid.
 cudaError_t launch_overlap_accumulate(const BatchArgs& a, float* overlap, cudaStream_t s);
 // Register-resident 128 x 128 single-slice GD kernel (ptycho_gd128.cu).

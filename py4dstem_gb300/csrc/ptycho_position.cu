@@ -12,7 +12,8 @@ namespace pty {
   cudaError_t launch_position_kernel_##S(const BatchArgs& a, cudaStream_t s);       \
   cudaError_t launch_position_correction_##S(const BatchArgs& a, cudaStream_t s);   \
   cudaError_t launch_probe_inverse_##S(const BatchArgs& a, cudaStream_t s);         \
-  cudaError_t launch_probe_intensity_##S(const BatchArgs& a, cudaStream_t s);
+  cudaError_t launch_probe_intensity_##S(const BatchArgs& a, cudaStream_t s);        \
+  cudaError_t launch_probe_aperture_##S(const BatchArgs& a, cudaStream_t s);
 
 PTY_DECLARE_SIZE(32)
 PTY_DECLARE_SIZE(48)
@@ -62,6 +63,10 @@ cudaError_t launch_probe_inverse(const BatchArgs& a, cudaStream_t s) {
 
 cudaError_t launch_probe_intensity(const BatchArgs& a, cudaStream_t s) {
   PTY_DISPATCH(launch_probe_intensity, a, s)
+}
+
+cudaError_t launch_probe_aperture(const BatchArgs& a, cudaStream_t s) {
+  PTY_DISPATCH(launch_probe_aperture, a, s)
 }
 
 }  // namespace pty

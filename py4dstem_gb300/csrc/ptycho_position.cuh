@@ -934,6 +934,80 @@ cudaError_t launch_probe_intensity_t(const BatchArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// Power of a block's values: sum over the block in a fixed order (thread
+// partials, then warp order), broadcast to every thread.
+template <int NT>
+__device__ __forceinline__ float block_sum_all_f(float v, float* red) {
+  const float t = block_sum<NT>(v, red);
+  __syncthreads();
+  if (threadIdx.x == 0) red[0] = t;
+  __syncthreads();
+  const float r = red[0];
+  __syncthreads();
+  return r;
+}
+
+// Probe aperture constraint on probe mode 0 (ptychographic_constraints.py:1004-1040,
+// mode 0 only for mixed states :1243-1247): P <- IFFT2(exp(i angle FFT2(P)) A),
+// rescaled to the power sum |P|^2 it had before.
+template <int SX, int SY, int NT>
+__global__ void __launch_bounds__(NT, 1) probe_aperture_kernel(BatchArgs a) {
+  using L = Layout<SX, SY>;
+  constexpr int N = L::N;
+  constexpr int LD = L::LD;
+  extern __shared__ float4 smem4[];
+  float2* buf = reinterpret_cast<float2*>(smem4);
+  float2* twx = buf + SX * LD;
+  float2* twy = twx + SX;
+  __shared__ float red[NT / 32];
+  fill_twiddles<SX, NT>(twx);
+  fill_twiddles<SY, NT>(twy);
+  float part = 0.0f;
+  for (int e = threadIdx.x; e < N; e += NT) {
+    const float2 p = a.probe[e];
+    const float av = hypotf(p.x, p.y);
+    part += av * av;
+    buf[(e / SY) * LD + e % SY] = p;
+  }
+  const float s0 = block_sum_all_f<NT>(part, red);
+  fft2d<SX, SY, NT, -1>(buf, twx, twy);
+  for (int e = threadIdx.x; e < N; e += NT) {
+    const int idx = (e / SY) * LD + e % SY;
+    const float2 f = buf[idx];
+    float sn, cs;
+    sincosf(atan2f(f.y, f.x), &sn, &cs);
+    const float ap = a.aperture[e];
+    buf[idx] = make_float2(cs * ap, sn * ap);
+  }
+  __syncthreads();
+  fft2d<SX, SY, NT, +1>(buf, twx, twy);
+  const float invN = 1.0f / (float)N;
+  part = 0.0f;
+  for (int e = threadIdx.x; e < N; e += NT) {
+    const float2 u = c_scale(buf[(e / SY) * LD + e % SY], invN);
+    const float av = hypotf(u.x, u.y);
+    part += av * av;
+  }
+  const float s1 = block_sum_all_f<NT>(part, red);
+  const float k = sqrtf(s0 / s1);
+  for (int e = threadIdx.x; e < N; e += NT)
+    a.probe[e] = c_scale(c_scale(buf[(e / SY) * LD + e % SY], invN), k);
+}
+
+template <int SX, int SY, int NT>
+cudaError_t launch_probe_aperture_t(const BatchArgs& a, cudaStream_t s) {
+  const size_t smem = Layout<SX, SY>::smem_bytes(false);
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(probe_aperture_kernel<SX, SY, NT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  probe_aperture_kernel<SX, SY, NT><<<1, NT, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
 template <int SX, int SY, int NT>
 cudaError_t launch_probe_inverse_t(const BatchArgs& a, cudaStream_t s) {
   const size_t smem = Layout<SX, SY>::smem_bytes(false);
@@ -1022,5 +1096,8 @@ cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
   }                                                                                      \
   cudaError_t launch_probe_intensity_##S(const BatchArgs& a, cudaStream_t s) {           \
     return launch_probe_intensity_t<S, S, NT>(a, s);                                     \
+  }                                                                                      \
+  cudaError_t launch_probe_aperture_##S(const BatchArgs& a, cudaStream_t s) {            \
+    return launch_probe_aperture_t<S, S, NT>(a, s);                                      \
   }                                                                                      \
   }

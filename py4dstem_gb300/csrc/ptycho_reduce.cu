@@ -783,6 +783,66 @@ cudaError_t launch_reduce_and_update(const BatchArgs& a, cudaStream_t s) {
   return cudaSuccess;
 }
 
+// Probe amplitude constraint (ptychographic_constraints.py:920-957, every mode of a
+// mixed state :1256-1262): P_m <- P_m mask, rescaled to the power it had before.
+// One block per mode; the power sums in float64.
+__global__ void __launch_bounds__(NT) probe_amplitude_kernel(BatchArgs a, const float* mask) {
+  __shared__ double red[NT / 32];
+  const int N = a.Sx * a.Sy;
+  float2* p = a.probe + (size_t)blockIdx.x * N;
+  double s0 = 0.0, s1 = 0.0;
+  for (int e = threadIdx.x; e < N; e += NT) {
+    const float2 v = p[e];
+    const double m = mask[e];
+    s0 += (double)v.x * v.x + (double)v.y * v.y;
+    s1 += ((double)v.x * v.x + (double)v.y * v.y) * m * m;
+  }
+  const double t0 = block_sum_all(s0, red);
+  const double t1 = block_sum_all(s1, red);
+  const double k = sqrt(t0 / t1);
+  for (int e = threadIdx.x; e < N; e += NT) {
+    const float2 v = p[e];
+    const double f = (double)mask[e] * k;
+    p[e] = make_float2((float)(v.x * f), (float)(v.y * f));
+  }
+}
+
+// Identical-slices constraint (ptychographic_constraints.py:630-647): every slice
+// takes the mean over slices (sum in slice order, then / T).
+__global__ void __launch_bounds__(NT) identical_slices_kernel(BatchArgs a) {
+  const size_t P = (size_t)a.Px * a.Py;
+  const size_t i = (size_t)blockIdx.x * NT + threadIdx.x;
+  if (i >= P) return;
+  const float tf = (float)a.T;
+  if (a.potential) {
+    float* o = reinterpret_cast<float*>(a.object);
+    float m = o[i];
+    for (int s = 1; s < a.T; ++s) m = __fadd_rn(m, o[(size_t)s * P + i]);
+    m = __fdiv_rn(m, tf);
+    for (int s = 0; s < a.T; ++s) o[(size_t)s * P + i] = m;
+  } else {
+    float2* o = reinterpret_cast<float2*>(a.object);
+    float2 m = o[i];
+    for (int s = 1; s < a.T; ++s) {
+      const float2 v = o[(size_t)s * P + i];
+      m = make_float2(__fadd_rn(m.x, v.x), __fadd_rn(m.y, v.y));
+    }
+    m = make_float2(__fdiv_rn(m.x, tf), __fdiv_rn(m.y, tf));
+    for (int s = 0; s < a.T; ++s) o[(size_t)s * P + i] = m;
+  }
+}
+
+cudaError_t launch_probe_amplitude(const BatchArgs& a, const float* mask, cudaStream_t s) {
+  probe_amplitude_kernel<<<a.M, NT, 0, s>>>(a, mask);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_identical_slices(const BatchArgs& a, cudaStream_t s) {
+  const size_t P = (size_t)a.Px * a.Py;
+  identical_slices_kernel<<<(unsigned)((P + NT - 1) / NT), NT, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_overlap_accumulate(const BatchArgs& a, float* overlap, cudaStream_t s) {
   const int ntx = (a.Px + kTile - 1) / kTile;
   const int nty = (a.Py + kTile - 1) / kTile;

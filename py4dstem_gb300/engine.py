@@ -424,8 +424,23 @@ class IterationDriver:
                  shrinkage_rad=0.0, use_mask=False, pure_phase=False, positivity=True,
                  fix_probe_com=True, orthogonalize_probe=False, mean_intensity=1.0,
                  position_correction=None, device_orthogonalization=False,
-                 graph=False):
+                 graph=False, identical_slices=False, probe_aperture=None,
+                 probe_amplitude_mask=None):
+        """probe_aperture: (Sx, Sy) Fourier amplitude of the initial probe (mode 0)
+        for the aperture constraint; probe_amplitude_mask: (Sx, Sy) real-space mask
+        of the amplitude constraint; identical_slices: average the object slices."""
         self.st = st
+        torch = _torch()
+        dev = st.object.device
+
+        def dev_f32(a):
+            if a is None:
+                return None
+            return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(dev)
+
+        self.identical_slices = bool(identical_slices) and st.geometry.num_slices > 1
+        self.probe_aperture = dev_f32(probe_aperture)
+        self.probe_amplitude_mask = dev_f32(probe_amplitude_mask)
         self.device_orthogonalization = bool(device_orthogonalization)
         self.graph = None
         self.calls = 0
@@ -491,11 +506,28 @@ class IterationDriver:
         self._constraints()
 
     def _constraints(self) -> None:
+        # order of ptychographic_constraints.py:649-726 (objects) and 1091-1148,
+        # 1218-1285 (probes)
         st = self.st
+        lib = _native.lib()
+        if self.identical_slices:
+            _native.check(lib.ptycho_object_identical_slices(
+                ctypes.byref(st.geometry), _ptr(st.object), _stream()))
+            st.launches += 1
         object_constraints(st, shrinkage_rad=self.shrinkage_rad, use_mask=self.use_mask,
                            pure_phase=self.pure_phase, positivity=self.positivity)
         if self.fix_probe_com:
             probe_com_constraint(st)
+        if self.probe_aperture is not None:
+            _native.check(lib.ptycho_probe_aperture_constraint(
+                ctypes.byref(st.geometry), _ptr(st.probe), _ptr(self.probe_aperture),
+                _stream()))
+            st.launches += 1
+        if self.probe_amplitude_mask is not None:
+            _native.check(lib.ptycho_probe_amplitude_constraint(
+                ctypes.byref(st.geometry), _ptr(st.probe), _ptr(self.probe_amplitude_mask),
+                _stream()))
+            st.launches += 1
         if self.orthogonalize:
             probe_orthogonalization(st, on_device=self.device_orthogonalization)
         if self.positions_com:

@@ -455,7 +455,11 @@ class _PtychographyBase(PreprocessMixin):
                           max_position_total_distance, pure_phase_object, object_positivity, shrinkage_rad,
                           fix_potential_baseline, detector_fourier_mask, store_iterations,
                           reset, device, clear_fft_cache, object_type,
-                          orthogonalize_probe=False, unsupported=None):
+                          orthogonalize_probe=False, fix_probe_aperture=False,
+                          constrain_probe_amplitude=False,
+                          constrain_probe_amplitude_relative_radius=0.5,
+                          constrain_probe_amplitude_relative_width=0.05,
+                          identical_slices=False, unsupported=None):
         self.set_device(device, clear_fft_cache)
         self._require_gpu()
         self._reset_reconstruction(store_iterations, reset)
@@ -500,13 +504,33 @@ class _PtychographyBase(PreprocessMixin):
                 # the reference passes fix_positions_com and not fix_positions on
                 # (singleslice_ptychography.py:956, ptychographic_constraints.py:1355-1377)
                 center_of_mass=not fix_positions_com) if correct_positions else None))
+        # optional constraints: the initial probe's Fourier amplitude (mode 0) and the
+        # soft top-hat of the amplitude constraint (ptychographic_constraints.py:920-957)
+        aperture = amp_mask = None
+        if fix_probe_aperture:
+            if self._probe_initial_aperture is None:
+                raise ValueError("fix_probe_aperture needs preprocess(store_initial_arrays=True)")
+            aperture = np.asarray(self._probe_initial_aperture)
+            aperture = aperture[0] if aperture.ndim == 3 else aperture
+        if constrain_probe_amplitude:
+            from scipy.special import erf
+
+            sx, sy = (int(v) for v in self._region_of_interest_shape)
+            X = np.fft.fftfreq(sx)[:, None]
+            Y = np.fft.fftfreq(sy)[None]
+            r = np.hypot(X, Y) - constrain_probe_amplitude_relative_radius
+            sigma = np.sqrt(np.pi) / constrain_probe_amplitude_relative_width
+            amp_mask = 0.5 * (1 - erf(sigma * r / (1 - r ** 2)))
+        constraint_key = (fix_probe_aperture, id(self._probe_initial_aperture),
+                          constrain_probe_amplitude, constrain_probe_amplitude_relative_radius,
+                          constrain_probe_amplitude_relative_width, bool(identical_slices))
         # Device state and iteration driver are kept between calls with the same
         # arrays and settings: a later call copies the current object, probe and
         # positions into the same buffers and replays the iteration graph captured
         # before (the reference rebuilds nothing on the device either).
         key = (self._storage, obj.shape, obj.dtype.str, np.shape(self._probe),
                self._num_slices, self._num_probes, potential, self._mixed, correct_positions,
-               detector_fourier_mask is not None,
+               detector_fourier_mask is not None, constraint_key,
                repr(sorted((k, repr(v)) for k, v in driver_kw.items())))
         cached = self.__dict__.get("_state_cache")
         if cached is not None and cached[0] == key and cached[1] is amplitudes:
@@ -530,7 +554,9 @@ class _PtychographyBase(PreprocessMixin):
                 fov_mask_inverse=self._object_fov_mask_inverse if use_mask else None,
                 projection=use_projection, mixed_state=self._mixed,
                 positions_initial=self._positions_px_initial if correct_positions else None)
-            driver = engine.IterationDriver(st, **driver_kw)
+            driver = engine.IterationDriver(st, identical_slices=identical_slices,
+                                            probe_aperture=aperture,
+                                            probe_amplitude_mask=amp_mask, **driver_kw)
             self.__dict__["_state_cache"] = (key, amplitudes, st, driver)
         if use_projection:
             if self._exit_waves is not None:
@@ -768,10 +794,12 @@ class SingleslicePtychography(_PtychographyBase):
             detector_fourier_mask=detector_fourier_mask, store_iterations=store_iterations,
             reset=reset, device=device, clear_fft_cache=clear_fft_cache,
             object_type=object_type,
+            fix_probe_aperture=fix_probe_aperture and not fix_probe,
+            constrain_probe_amplitude=constrain_probe_amplitude and not fix_probe,
+            constrain_probe_amplitude_relative_radius=constrain_probe_amplitude_relative_radius,
+            constrain_probe_amplitude_relative_width=constrain_probe_amplitude_relative_width,
             unsupported=dict(
                 global_affine_transformation=global_affine_transformation and not fix_positions,
-                fix_probe_aperture=fix_probe_aperture and not fix_probe,
-                constrain_probe_amplitude=constrain_probe_amplitude and not fix_probe,
                 constrain_probe_fourier_amplitude=constrain_probe_fourier_amplitude
                 and not fix_probe,
                 fit_probe_aberrations=fit_probe_aberrations and not fix_probe,
@@ -903,10 +931,12 @@ class MixedstatePtychography(_PtychographyBase):
             detector_fourier_mask=detector_fourier_mask, store_iterations=store_iterations,
             reset=reset, device=device, clear_fft_cache=clear_fft_cache,
             object_type=object_type, orthogonalize_probe=orthogonalize_probe,
+            fix_probe_aperture=fix_probe_aperture and not fix_probe,
+            constrain_probe_amplitude=constrain_probe_amplitude and not fix_probe,
+            constrain_probe_amplitude_relative_radius=constrain_probe_amplitude_relative_radius,
+            constrain_probe_amplitude_relative_width=constrain_probe_amplitude_relative_width,
             unsupported=dict(
                 global_affine_transformation=global_affine_transformation and not fix_positions,
-                fix_probe_aperture=fix_probe_aperture and not fix_probe,
-                constrain_probe_amplitude=constrain_probe_amplitude and not fix_probe,
                 constrain_probe_fourier_amplitude=constrain_probe_fourier_amplitude
                 and not fix_probe,
                 fit_probe_aberrations=fit_probe_aberrations and not fix_probe,
@@ -1050,10 +1080,13 @@ class MultislicePtychography(_PtychographyBase):
             detector_fourier_mask=detector_fourier_mask, store_iterations=store_iterations,
             reset=reset, device=device, clear_fft_cache=clear_fft_cache,
             object_type=object_type,
+            fix_probe_aperture=fix_probe_aperture and not fix_probe,
+            constrain_probe_amplitude=constrain_probe_amplitude and not fix_probe,
+            constrain_probe_amplitude_relative_radius=constrain_probe_amplitude_relative_radius,
+            constrain_probe_amplitude_relative_width=constrain_probe_amplitude_relative_width,
+            identical_slices=identical_slices,
             unsupported=dict(
                 global_affine_transformation=global_affine_transformation and not fix_positions,
-                fix_probe_aperture=fix_probe_aperture and not fix_probe,
-                constrain_probe_amplitude=constrain_probe_amplitude and not fix_probe,
                 constrain_probe_fourier_amplitude=constrain_probe_fourier_amplitude
                 and not fix_probe,
                 fit_probe_aberrations=fit_probe_aberrations and not fix_probe,
@@ -1062,7 +1095,6 @@ class MultislicePtychography(_PtychographyBase):
                 and (q_lowpass is not None or q_highpass is not None),
                 kz_regularization_filter=kz_regularization_filter
                 and kz_regularization_gamma is not None,
-                identical_slices=identical_slices,
                 tv_denoise=tv_denoise and tv_denoise_weights is not None,
                 tv_denoise_chambolle=tv_denoise_chambolle
                 and tv_denoise_weight_chambolle is not None,
@@ -1220,10 +1252,13 @@ class MixedstateMultislicePtychography(_PtychographyBase):
             detector_fourier_mask=detector_fourier_mask, store_iterations=store_iterations,
             reset=reset, device=device, clear_fft_cache=clear_fft_cache,
             object_type=object_type, orthogonalize_probe=orthogonalize_probe,
+            fix_probe_aperture=fix_probe_aperture and not fix_probe,
+            constrain_probe_amplitude=constrain_probe_amplitude and not fix_probe,
+            constrain_probe_amplitude_relative_radius=constrain_probe_amplitude_relative_radius,
+            constrain_probe_amplitude_relative_width=constrain_probe_amplitude_relative_width,
+            identical_slices=identical_slices,
             unsupported=dict(
                 global_affine_transformation=global_affine_transformation and not fix_positions,
-                fix_probe_aperture=fix_probe_aperture and not fix_probe,
-                constrain_probe_amplitude=constrain_probe_amplitude and not fix_probe,
                 constrain_probe_fourier_amplitude=constrain_probe_fourier_amplitude
                 and not fix_probe,
                 fit_probe_aberrations=fit_probe_aberrations and not fix_probe,
@@ -1232,7 +1267,6 @@ class MixedstateMultislicePtychography(_PtychographyBase):
                 and (q_lowpass is not None or q_highpass is not None),
                 kz_regularization_filter=kz_regularization_filter
                 and kz_regularization_gamma is not None,
-                identical_slices=identical_slices,
                 tv_denoise=tv_denoise and tv_denoise_weights is not None,
                 tv_denoise_chambolle=tv_denoise_chambolle
                 and tv_denoise_weight_chambolle is not None,

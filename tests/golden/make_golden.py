@@ -122,6 +122,29 @@ CASES = {
         rec=dict(num_iter=4, max_batch_size=25, step_size=0.5, seed_random=11,
                  fix_positions=False, positions_step_size=0.5,
                  max_position_update_distance=0.1, max_position_total_distance=0.5)),
+    # optional constraints: probe aperture and amplitude, identical slices
+    "ss_gd_probe_constraints": dict(
+        gen=dict(name="spc", seed=29, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=96),
+        cls="single", ctor=dict(object_fov_ang=(24.0, 24.0)), guess=(96, 96),
+        rec=dict(num_iter=4, max_batch_size=25, step_size=0.5, seed_random=12,
+                 fix_probe_aperture=True, constrain_probe_amplitude=True,
+                 constrain_probe_amplitude_relative_radius=0.4,
+                 constrain_probe_amplitude_relative_width=0.08)),
+    "mixed_gd_probe_constraints": dict(
+        gen=dict(name="mpc", seed=30, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=96, num_modes=2, mode_weights=(0.8, 0.2)),
+        cls="mixed", ctor=dict(object_fov_ang=(24.0, 24.0), num_probes=2), global_seed=13,
+        guess=(96, 96),
+        rec=dict(num_iter=4, max_batch_size=25, step_size=0.5, seed_random=13,
+                 fix_probe_aperture=True, constrain_probe_amplitude=True)),
+    "ms_gd_identical_slices": dict(
+        gen=dict(name="mis", seed=31, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=96, num_slices=3, slice_thickness=20.0),
+        cls="multi", ctor=dict(object_fov_ang=(24.0, 24.0), num_slices=3, slice_thicknesses=20.0),
+        guess=(3, 96, 96),
+        rec=dict(num_iter=4, max_batch_size=25, step_size=0.5, seed_random=14,
+                 identical_slices=True)),
     "mixed_gd_M3": dict(
         gen=dict(name="mx", seed=14, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
                  detector=64, object_px=96, num_modes=3, mode_weights=(0.7, 0.2, 0.1)),
