@@ -247,6 +247,18 @@ int ptycho_probe_orthogonalize(const ptycho_geometry* geometry, void* probe, voi
 int ptycho_object_identical_slices(const ptycho_geometry* geometry, void* object, void* stream);
 
 /*
+ * Gaussian object constraint: the object (all axes of the (T, Px, Py) array, the
+ * real and imaginary parts separately; the phase alone with pure_phase) blurred
+ * with weights[0 .. 2 radius] (float64, the normalised Gaussian) and reflecting
+ * boundaries, one axis after the other, each pass in float64 and stored as
+ * float32. scratch: 4 T Px Py floats. Replaces _object_gaussian_constraint
+ * (ptychographic_constraints.py:119-151, scipy.ndimage.gaussian_filter).
+ */
+int ptycho_object_gaussian_constraint(const ptycho_geometry* geometry, void* object,
+                                      const double* weights, int32_t radius,
+                                      int32_t pure_phase, void* scratch, void* stream);
+
+/*
  * Probe aperture: probe mode 0 <- IFFT2(exp(i angle(FFT2(probe))) aperture), scaled
  * back to its power sum |probe|^2; aperture (Sx, Sy) float32 is the Fourier
  * amplitude of the initial probe. Replaces _probe_aperture_constraint

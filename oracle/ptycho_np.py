@@ -434,6 +434,16 @@ class Oracle:
         x0, y0 = self.center_of_mass(inten)
         self.probe = self.fft_shift(self.probe, -np.array([x0, y0]))
 
+    def object_gaussian(self, sigma_px, pure_phase):
+        """ptychographic_constraints.py:119-151."""
+        from scipy.ndimage import gaussian_filter
+
+        if not pure_phase or self.object_type == "potential":
+            self.object = gaussian_filter(self.object, sigma_px)
+        else:
+            phase = gaussian_filter(np.angle(self.object), sigma_px)
+            self.object = np.exp(1.0j * phase)
+
     def object_identical_slices(self):
         """ptychographic_constraints.py:630-647."""
         self.object[:] = self.object.mean(0, keepdims=True)
@@ -497,7 +507,8 @@ class Oracle:
                     max_position_update_distance=None, max_position_total_distance=None,
                     fix_probe_aperture=False, constrain_probe_amplitude=False,
                     constrain_probe_amplitude_relative_radius=0.5,
-                    constrain_probe_amplitude_relative_width=0.05, identical_slices=False):
+                    constrain_probe_amplitude_relative_width=0.05, identical_slices=False,
+                    gaussian_filter_sigma=None, gaussian_filter=True):
         """singleslice_ptychography.py:606-996 (and the multislice / mixed-state twins)."""
         projection = method != "GD"
         J = self.J
@@ -538,6 +549,9 @@ class Oracle:
                         max_position_total_distance)
                 error += be
             error /= self.mean_intensity * J
+            if gaussian_filter and gaussian_filter_sigma is not None:
+                self.object_gaussian(gaussian_filter_sigma / self.sampling[0],
+                                     pure_phase_object and self.object_type == "complex")
             if identical_slices and self.num_slices > 1:
                 self.object_identical_slices()
             self.object_constraints(shrinkage_rad, mask,

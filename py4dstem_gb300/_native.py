@@ -98,6 +98,8 @@ _SIGNATURES = {
         ctypes.c_int,
     ),
     "ptycho_object_identical_slices": ([ctypes.POINTER(Geometry), _vp, _vp], ctypes.c_int),
+    "ptycho_object_gaussian_constraint": (
+        [ctypes.POINTER(Geometry), _vp, _vp, _i32, _i32, _vp, _vp], ctypes.c_int),
     "ptycho_probe_aperture_constraint": (
         [ctypes.POINTER(Geometry), _vp, _vp, _vp], ctypes.c_int),
     "ptycho_probe_amplitude_constraint": (

@@ -558,6 +558,28 @@ int ptycho_object_identical_slices(const ptycho_geometry* g, void* object, void*
   return PTYCHO_OK;
 }
 
+int ptycho_object_gaussian_constraint(const ptycho_geometry* g, void* object,
+                                      const double* weights, int32_t radius,
+                                      int32_t pure_phase, void* scratch, void* stream) {
+  int st = check_geometry(g);
+  if (st != PTYCHO_OK) return st;
+  if (!object || !weights || !scratch)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "object, weights and scratch must be non-null");
+  if (radius < 0) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "radius must be >= 0");
+  BatchArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.Px = g->object_x;
+  a.Py = g->object_y;
+  a.T = g->num_slices;
+  a.potential = g->object_is_potential;
+  a.object = object;
+  cudaError_t e = launch_object_gaussian(a, weights, radius, pure_phase ? 1 : 0,
+                                         static_cast<float*>(scratch),
+                                         static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "object Gaussian kernels");
+  return PTYCHO_OK;
+}
+
 int ptycho_probe_aperture_constraint(const ptycho_geometry* g, void* probe,
                                      const float* aperture, void* stream) {
   int st = check_geometry(g);

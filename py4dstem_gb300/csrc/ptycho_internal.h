@@ -104,6 +104,10 @@ cudaError_t launch_probe_aperture(const BatchArgs& a, cudaStream_t s);
 cudaError_t launch_probe_amplitude(const BatchArgs& a, const float* mask, cudaStream_t s);
 // Every slice of the object set to the mean over slices.
 cudaError_t launch_identical_slices(const BatchArgs& a, cudaStream_t s);
+// Gaussian blur of the object (weights w[0 .. 2R], reflect boundaries), scratch of
+// 4 T Px Py floats.
+cudaError_t launch_object_gaussian(const BatchArgs& a, const double* w, int R, int pure_phase,
+                                   float* scratch, cudaStream_t s);
 // overlap += sum over the batch of the staged |P_b|^2, scattered into the object grid.
 cudaError_t launch_overlap_accumulate(const BatchArgs& a, float* overlap, cudaStream_t s);
 // Register-resident 128 x 128 single-slice GD kernel (ptycho_gd128.cu).

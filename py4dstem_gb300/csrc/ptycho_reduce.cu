@@ -832,6 +832,105 @@ __global__ void __launch_bounds__(NT) identical_slices_kernel(BatchArgs a) {
   }
 }
 
+// One axis of the object Gaussian constraint (ptychographic_constraints.py:119-151,
+// scipy.ndimage.gaussian_filter with mode "reflect"): out = sum_j w_j in[i + j]
+// over j in [-R, R] along `axis` of a (C, n0, n1, n2) float32 array (C = 2 for the
+// real and imaginary parts), in float64 as the centre term plus the symmetric
+// pairs from the outermost in, rounded once to float32 per pass.
+__global__ void __launch_bounds__(NT) gaussian_pass_kernel(const float* in, float* out, int n0,
+                                                           int n1, int n2, int axis,
+                                                           const double* w, int R, size_t total) {
+  const size_t i = (size_t)blockIdx.x * NT + threadIdx.x;
+  if (i >= total) return;
+  const size_t vol = (size_t)n0 * n1 * n2;
+  const size_t c = i / vol;
+  size_t r = i - c * vol;
+  const int i0 = (int)(r / ((size_t)n1 * n2));
+  r -= (size_t)i0 * n1 * n2;
+  const int i1 = (int)(r / n2);
+  const int i2 = (int)(r - (size_t)i1 * n2);
+  const int n = axis == 0 ? n0 : axis == 1 ? n1 : n2;
+  const int k = axis == 0 ? i0 : axis == 1 ? i1 : i2;
+  const size_t stride = axis == 0 ? (size_t)n1 * n2 : axis == 1 ? (size_t)n2 : 1;
+  const size_t base = i - (size_t)k * stride;
+  auto at = [&](int j) {  // reflect: d c b a | a b c d | d c b a
+    const int period = 2 * n;
+    int m = j % period;
+    if (m < 0) m += period;
+    if (m >= n) m = period - 1 - m;
+    return (double)in[base + (size_t)m * stride];
+  };
+  double acc = __dmul_rn(at(k), w[R]);
+  for (int j = R; j >= 1; --j) acc = __dadd_rn(acc, __dmul_rn(__dadd_rn(at(k - j), at(k + j)), w[R - j]));
+  out[i] = __double2float_rn(acc);
+}
+
+// Phase of a complex object into a float array, and back as exp(i phase).
+__global__ void __launch_bounds__(NT) object_phase_kernel(const float2* o, float* ph, size_t n) {
+  const size_t i = (size_t)blockIdx.x * NT + threadIdx.x;
+  if (i < n) ph[i] = atan2f(o[i].y, o[i].x);
+}
+__global__ void __launch_bounds__(NT) object_from_phase_kernel(const float* ph, float2* o, size_t n) {
+  const size_t i = (size_t)blockIdx.x * NT + threadIdx.x;
+  if (i < n) {
+    float sn, cs;
+    sincosf(ph[i], &sn, &cs);
+    o[i] = make_float2(cs, sn);
+  }
+}
+// Interleaved complex <-> planar (real plane, imaginary plane).
+__global__ void __launch_bounds__(NT) deinterleave_kernel(const float2* o, float* p, size_t n) {
+  const size_t i = (size_t)blockIdx.x * NT + threadIdx.x;
+  if (i < n) {
+    p[i] = o[i].x;
+    p[n + i] = o[i].y;
+  }
+}
+__global__ void __launch_bounds__(NT) interleave_kernel(const float* p, float2* o, size_t n) {
+  const size_t i = (size_t)blockIdx.x * NT + threadIdx.x;
+  if (i < n) o[i] = make_float2(p[i], p[n + i]);
+}
+
+cudaError_t launch_object_gaussian(const BatchArgs& a, const double* w, int R, int pure_phase,
+                                   float* scratch, cudaStream_t s) {
+  const size_t n = (size_t)a.T * a.Px * a.Py;
+  const unsigned gb = (unsigned)((n + NT - 1) / NT);
+  // planes: scratch[0 .. 2n) data, scratch[2n .. 4n) ping-pong
+  float* x = scratch;
+  float* y = scratch + 2 * n;
+  int C;
+  if (a.potential) {
+    cudaError_t e = cudaMemcpyAsync(x, a.object, sizeof(float) * n, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+    C = 1;
+  } else if (pure_phase) {
+    object_phase_kernel<<<gb, NT, 0, s>>>(static_cast<const float2*>(a.object), x, n);
+    C = 1;
+  } else {
+    deinterleave_kernel<<<gb, NT, 0, s>>>(static_cast<const float2*>(a.object), x, n);
+    C = 2;
+  }
+  // axes of the (T, Px, Py) array in order; a single slice is a 2D array
+  const int dims[3] = {a.T, a.Px, a.Py};
+  const size_t total = (size_t)C * n;
+  const unsigned gt = (unsigned)((total + NT - 1) / NT);
+  for (int ax = a.T > 1 ? 0 : 1; ax < 3; ++ax) {
+    gaussian_pass_kernel<<<gt, NT, 0, s>>>(x, y, dims[0], dims[1], dims[2], ax, w, R, total);
+    float* t = x;
+    x = y;
+    y = t;
+  }
+  if (a.potential) {
+    cudaError_t e = cudaMemcpyAsync(a.object, x, sizeof(float) * n, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+  } else if (pure_phase) {
+    object_from_phase_kernel<<<gb, NT, 0, s>>>(x, static_cast<float2*>(a.object), n);
+  } else {
+    interleave_kernel<<<gb, NT, 0, s>>>(x, static_cast<float2*>(a.object), n);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_probe_amplitude(const BatchArgs& a, const float* mask, cudaStream_t s) {
   probe_amplitude_kernel<<<a.M, NT, 0, s>>>(a, mask);
   return cudaGetLastError();

@@ -425,10 +425,11 @@ class IterationDriver:
                  fix_probe_com=True, orthogonalize_probe=False, mean_intensity=1.0,
                  position_correction=None, device_orthogonalization=False,
                  graph=False, identical_slices=False, probe_aperture=None,
-                 probe_amplitude_mask=None):
+                 probe_amplitude_mask=None, gaussian=None):
         """probe_aperture: (Sx, Sy) Fourier amplitude of the initial probe (mode 0)
         for the aperture constraint; probe_amplitude_mask: (Sx, Sy) real-space mask
-        of the amplitude constraint; identical_slices: average the object slices."""
+        of the amplitude constraint; identical_slices: average the object slices;
+        gaussian: (float64 weights of length 2 R + 1, pure_phase) of the object blur."""
         self.st = st
         torch = _torch()
         dev = st.object.device
@@ -441,6 +442,12 @@ class IterationDriver:
         self.identical_slices = bool(identical_slices) and st.geometry.num_slices > 1
         self.probe_aperture = dev_f32(probe_aperture)
         self.probe_amplitude_mask = dev_f32(probe_amplitude_mask)
+        self.gaussian = None
+        if gaussian is not None:
+            weights, pure = gaussian
+            w = torch.from_numpy(np.ascontiguousarray(weights, dtype=np.float64)).to(dev)
+            scratch = torch.empty(4 * st.object.numel(), dtype=torch.float32, device=dev)
+            self.gaussian = (w, (int(w.numel()) - 1) // 2, bool(pure), scratch)
         self.device_orthogonalization = bool(device_orthogonalization)
         self.graph = None
         self.calls = 0
@@ -510,6 +517,12 @@ class IterationDriver:
         # 1218-1285 (probes)
         st = self.st
         lib = _native.lib()
+        if self.gaussian is not None:
+            w, radius, pure, scratch = self.gaussian
+            _native.check(lib.ptycho_object_gaussian_constraint(
+                ctypes.byref(st.geometry), _ptr(st.object), _ptr(w), radius, 1 if pure else 0,
+                _ptr(scratch), _stream()))
+            st.launches += 2 + (3 if st.geometry.num_slices > 1 else 2)
         if self.identical_slices:
             _native.check(lib.ptycho_object_identical_slices(
                 ctypes.byref(st.geometry), _ptr(st.object), _stream()))

@@ -459,7 +459,8 @@ class _PtychographyBase(PreprocessMixin):
                           constrain_probe_amplitude=False,
                           constrain_probe_amplitude_relative_radius=0.5,
                           constrain_probe_amplitude_relative_width=0.05,
-                          identical_slices=False, unsupported=None):
+                          identical_slices=False, gaussian_filter_sigma=None,
+                          unsupported=None):
         self.set_device(device, clear_fft_cache)
         self._require_gpu()
         self._reset_reconstruction(store_iterations, reset)
@@ -521,7 +522,19 @@ class _PtychographyBase(PreprocessMixin):
             r = np.hypot(X, Y) - constrain_probe_amplitude_relative_radius
             sigma = np.sqrt(np.pi) / constrain_probe_amplitude_relative_width
             amp_mask = 0.5 * (1 - erf(sigma * r / (1 - r ** 2)))
-        constraint_key = (fix_probe_aperture, id(self._probe_initial_aperture),
+        gaussian = None
+        pure_phase = pure_phase_object and self._object_type == "complex"
+        if gaussian_filter_sigma is not None:
+            # scipy.ndimage.gaussian_filter's kernel (truncate 4) for the sigma in
+            # pixels (ptychographic_constraints.py:141)
+            sigma = gaussian_filter_sigma / self.sampling[0]
+            if sigma > 1e-15:
+                radius = int(4.0 * sigma + 0.5)
+                x = np.arange(-radius, radius + 1)
+                phi = np.exp(-0.5 / (sigma * sigma) * x ** 2)
+                gaussian = (phi / phi.sum(), pure_phase)
+        constraint_key = (None if gaussian is None else (gaussian_filter_sigma, pure_phase),
+                          fix_probe_aperture, id(self._probe_initial_aperture),
                           constrain_probe_amplitude, constrain_probe_amplitude_relative_radius,
                           constrain_probe_amplitude_relative_width, bool(identical_slices))
         # Device state and iteration driver are kept between calls with the same
@@ -556,7 +569,8 @@ class _PtychographyBase(PreprocessMixin):
                 positions_initial=self._positions_px_initial if correct_positions else None)
             driver = engine.IterationDriver(st, identical_slices=identical_slices,
                                             probe_aperture=aperture,
-                                            probe_amplitude_mask=amp_mask, **driver_kw)
+                                            probe_amplitude_mask=amp_mask, gaussian=gaussian,
+                                            **driver_kw)
             self.__dict__["_state_cache"] = (key, amplitudes, st, driver)
         if use_projection:
             if self._exit_waves is not None:
@@ -798,12 +812,12 @@ class SingleslicePtychography(_PtychographyBase):
             constrain_probe_amplitude=constrain_probe_amplitude and not fix_probe,
             constrain_probe_amplitude_relative_radius=constrain_probe_amplitude_relative_radius,
             constrain_probe_amplitude_relative_width=constrain_probe_amplitude_relative_width,
+            gaussian_filter_sigma=gaussian_filter_sigma if gaussian_filter else None,
             unsupported=dict(
                 global_affine_transformation=global_affine_transformation and not fix_positions,
                 constrain_probe_fourier_amplitude=constrain_probe_fourier_amplitude
                 and not fix_probe,
                 fit_probe_aberrations=fit_probe_aberrations and not fix_probe,
-                gaussian_filter=gaussian_filter and gaussian_filter_sigma is not None,
                 butterworth_filter=butterworth_filter
                 and (q_lowpass is not None or q_highpass is not None),
                 tv_denoise=tv_denoise and tv_denoise_weight is not None,
@@ -935,12 +949,12 @@ class MixedstatePtychography(_PtychographyBase):
             constrain_probe_amplitude=constrain_probe_amplitude and not fix_probe,
             constrain_probe_amplitude_relative_radius=constrain_probe_amplitude_relative_radius,
             constrain_probe_amplitude_relative_width=constrain_probe_amplitude_relative_width,
+            gaussian_filter_sigma=gaussian_filter_sigma if gaussian_filter else None,
             unsupported=dict(
                 global_affine_transformation=global_affine_transformation and not fix_positions,
                 constrain_probe_fourier_amplitude=constrain_probe_fourier_amplitude
                 and not fix_probe,
                 fit_probe_aberrations=fit_probe_aberrations and not fix_probe,
-                gaussian_filter=gaussian_filter and gaussian_filter_sigma is not None,
                 butterworth_filter=butterworth_filter
                 and (q_lowpass is not None or q_highpass is not None),
                 tv_denoise=tv_denoise and tv_denoise_weight is not None,
@@ -1084,13 +1098,13 @@ class MultislicePtychography(_PtychographyBase):
             constrain_probe_amplitude=constrain_probe_amplitude and not fix_probe,
             constrain_probe_amplitude_relative_radius=constrain_probe_amplitude_relative_radius,
             constrain_probe_amplitude_relative_width=constrain_probe_amplitude_relative_width,
+            gaussian_filter_sigma=gaussian_filter_sigma if gaussian_filter else None,
             identical_slices=identical_slices,
             unsupported=dict(
                 global_affine_transformation=global_affine_transformation and not fix_positions,
                 constrain_probe_fourier_amplitude=constrain_probe_fourier_amplitude
                 and not fix_probe,
                 fit_probe_aberrations=fit_probe_aberrations and not fix_probe,
-                gaussian_filter=gaussian_filter and gaussian_filter_sigma is not None,
                 butterworth_filter=butterworth_filter
                 and (q_lowpass is not None or q_highpass is not None),
                 kz_regularization_filter=kz_regularization_filter
@@ -1256,13 +1270,13 @@ class MixedstateMultislicePtychography(_PtychographyBase):
             constrain_probe_amplitude=constrain_probe_amplitude and not fix_probe,
             constrain_probe_amplitude_relative_radius=constrain_probe_amplitude_relative_radius,
             constrain_probe_amplitude_relative_width=constrain_probe_amplitude_relative_width,
+            gaussian_filter_sigma=gaussian_filter_sigma if gaussian_filter else None,
             identical_slices=identical_slices,
             unsupported=dict(
                 global_affine_transformation=global_affine_transformation and not fix_positions,
                 constrain_probe_fourier_amplitude=constrain_probe_fourier_amplitude
                 and not fix_probe,
                 fit_probe_aberrations=fit_probe_aberrations and not fix_probe,
-                gaussian_filter=gaussian_filter and gaussian_filter_sigma is not None,
                 butterworth_filter=butterworth_filter
                 and (q_lowpass is not None or q_highpass is not None),
                 kz_regularization_filter=kz_regularization_filter

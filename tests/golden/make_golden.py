@@ -145,6 +145,19 @@ CASES = {
         guess=(3, 96, 96),
         rec=dict(num_iter=4, max_batch_size=25, step_size=0.5, seed_random=14,
                  identical_slices=True)),
+    "ss_gd_gaussian": dict(
+        gen=dict(name="sgf", seed=32, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=96),
+        cls="single", ctor=dict(object_fov_ang=(24.0, 24.0)), guess=(96, 96),
+        rec=dict(num_iter=4, max_batch_size=25, step_size=0.5, seed_random=15,
+                 gaussian_filter_sigma=0.5)),
+    "ms_gd_gaussian_pure_phase": dict(
+        gen=dict(name="mgf", seed=33, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=96, num_slices=2, slice_thickness=20.0),
+        cls="multi", ctor=dict(object_fov_ang=(24.0, 24.0), num_slices=2, slice_thicknesses=20.0),
+        guess=(2, 96, 96),
+        rec=dict(num_iter=4, max_batch_size=25, step_size=0.5, seed_random=16,
+                 gaussian_filter_sigma=0.4, pure_phase_object=True)),
     "mixed_gd_M3": dict(
         gen=dict(name="mx", seed=14, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
                  detector=64, object_px=96, num_modes=3, mode_weights=(0.7, 0.2, 0.1)),

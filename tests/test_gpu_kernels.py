@@ -176,3 +176,42 @@ def test_batch_edges(cuda, J, B):
     st = make_state(S=32, J=J, seed=60 + J % 7, obj_px=None if J < 100 else 192)
     tol = 2e-5 if J < 100 else 5e-5
     compare(st, tol, tol, tol, num_iter=2, max_batch_size=B, seed_random=3, **OFF)
+
+
+@pytest.mark.parametrize("shape,potential,pure_phase,sigma", [
+    ((1, 96, 80), False, False, 1.7), ((3, 64, 64), True, False, 0.9),
+    ((2, 40, 56), False, True, 2.4), ((1, 48, 48), False, False, 20.0)])
+def test_object_gaussian_matches_scipy(cuda, shape, potential, pure_phase, sigma):
+    """The object blur against scipy.ndimage.gaussian_filter (reflecting edges,
+    every axis of the object array; a radius larger than the object too)."""
+    import ctypes
+
+    import torch
+    from scipy.ndimage import gaussian_filter
+
+    from py4dstem_gb300 import _native, engine
+
+    rng = np.random.default_rng(int(sigma * 10) + shape[0])
+    if potential:
+        obj = rng.normal(size=shape).astype(np.float32)
+    else:
+        obj = (np.exp(1j * rng.normal(size=shape)) * (1 + 0.1 * rng.normal(size=shape))
+               ).astype(np.complex64)
+    ref = obj[0] if shape[0] == 1 else obj
+    if pure_phase:
+        ref = np.exp(1.0j * gaussian_filter(np.angle(ref), sigma))
+    else:
+        ref = gaussian_filter(ref, sigma)
+    radius = int(4.0 * sigma + 0.5)
+    x = np.arange(-radius, radius + 1)
+    w = np.exp(-0.5 / (sigma * sigma) * x ** 2)
+    w = w / w.sum()
+    g = engine.make_geometry((32, 32), shape[1:], shape[0], 1, potential)
+    o = torch.from_numpy(obj).cuda()
+    wd = torch.from_numpy(w).cuda()
+    scratch = torch.empty(4 * o.numel(), dtype=torch.float32, device="cuda")
+    _native.check(_native.lib().ptycho_object_gaussian_constraint(
+        ctypes.byref(g), ctypes.c_void_p(o.data_ptr()), ctypes.c_void_p(wd.data_ptr()), radius,
+        1 if pure_phase else 0, ctypes.c_void_p(scratch.data_ptr()), None))
+    got = o.cpu().numpy().reshape(np.shape(ref))
+    assert np.max(np.abs(got - ref)) <= 2e-6 * np.max(np.abs(ref))

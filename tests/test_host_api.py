@@ -77,7 +77,7 @@ def test_unsupported_options_raise_before_gpu():
     with pytest.raises(NotImplementedError):
         p.reconstruct(fix_positions=False, reconstruction_method="DM_AP", **kw)
     with pytest.raises(NotImplementedError):
-        p.reconstruct(gaussian_filter_sigma=0.5, **kw)
+        p.reconstruct(q_lowpass=0.5, **kw)
 
     with pytest.raises(ValueError):
         p.reconstruct(reconstruction_method="DM_AP", max_batch_size=4, **kw)
