@@ -61,8 +61,10 @@ typedef struct ptycho_geometry {
  * mixedstate class) even when num_probes == 1. Implied when num_probes > 1. */
 #define PTYCHO_FLAG_MIXED_STATE 1
 
-/* Single slice, gradient descent: keep each position's far field FFT2(P_m O)
- * in the workspace for a following ptycho_position_correction() call. */
+/* Keep each position's far field FFT2(psi) of the forward pass (psi the exit
+ * wave of every probe mode) in the workspace for a following
+ * ptycho_position_correction() call. Gradient descent, any model; projection
+ * sets with a single probe (no mixed state). */
 #define PTYCHO_FLAG_KEEP_FARFIELD 2
 
 /* Batch chaining within one iteration (batch calls on one workspace and stream):

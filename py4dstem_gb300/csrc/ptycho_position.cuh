@@ -382,6 +382,9 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
           if (ps) {
             const float2 w = a.ew_valid ? ew[e] : psi;
             v = c_add(c_scale(psi, a.pc), c_scale(w, py_));
+            // position correction works on FFT2(psi), not on the projected factor;
+            // psi waits here and is transformed at the end (single probe only)
+            if (a.keep_farfield) a.scratch_f[(size_t)b * N + e] = psi;
           }
           buf[x * LD + y] = v;
         }
@@ -413,7 +416,7 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
         const int e = tid + (c0 + i) * NT;
         const int idx = (e / SY) * LD + e % SY;
         float2 f = buf[idx];
-        if (!kPlain && a.keep_farfield) a.scratch_f[(size_t)b * N + e] = f;  // unmasked, for A16
+        if (!kPlain && a.keep_farfield && !ps) a.scratch_f[(size_t)b * N + e] = f;  // unmasked, A16
         const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
         if (a.det_mask) f = c_scale(f, mk);
         const float af = c_abs(f);
@@ -542,6 +545,7 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
         const float2 psi = buf[idx];
         const float2 w = a.ew_valid ? ew_in[e] : psi;
         buf[idx] = c_add(c_scale(psi, a.pc), c_scale(w, py_));
+        if (a.keep_farfield) a.scratch_f[(size_t)b * N + e] = psi;  // see the single slice
       }
       __syncthreads();
     }
@@ -549,7 +553,7 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
     for (int e = tid; e < N; e += NT) {
       const int idx = (e / SY) * LD + e % SY;
       float2 f = buf[idx];
-      if (a.keep_farfield) a.scratch_f[(size_t)b * N + e] = f;  // unmasked, for A16
+      if (a.keep_farfield && !ps) a.scratch_f[(size_t)b * N + e] = f;  // unmasked, for A16
       const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
       if (a.det_mask) f = c_scale(f, mk);
       const float af = c_abs(f);
@@ -617,6 +621,15 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
     }
   }
 
+    if (ps && a.keep_farfield) {
+      // projection sets with position correction: the far field of psi
+      float2* f = a.scratch_f + (size_t)b * N;
+      __syncthreads();
+      for (int e = tid; e < N; e += NT) buf[(e / SY) * LD + e % SY] = f[e];
+      __syncthreads();
+      fft2d<SX, SY, NT, -1>(buf, twx, twy);
+      for (int e = tid; e < N; e += NT) f[e] = buf[(e / SY) * LD + e % SY];
+    }
   }  // kMode != 4
 
 done:

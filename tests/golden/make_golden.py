@@ -158,6 +158,21 @@ CASES = {
         guess=(2, 96, 96),
         rec=dict(num_iter=4, max_batch_size=25, step_size=0.5, seed_random=16,
                  gaussian_filter_sigma=0.4, pure_phase_object=True)),
+    # position correction with projection sets (whole-scan batches)
+    "ss_ap_poscorr": dict(
+        gen=dict(name="sap", seed=34, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=96),
+        cls="single", ctor=dict(object_fov_ang=(24.0, 24.0)), guess=(96, 96), perturb_ang=0.15,
+        rec=dict(num_iter=4, reconstruction_method="RAAR", reconstruction_parameter=0.9,
+                 fix_positions=False, positions_step_size=0.5,
+                 max_position_update_distance=0.1)),
+    "ms_ap_poscorr": dict(
+        gen=dict(name="map", seed=35, scan_shape=(8, 8), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=96, num_slices=2, slice_thickness=20.0),
+        cls="multi", ctor=dict(object_fov_ang=(24.0, 24.0), num_slices=2, slice_thicknesses=20.0),
+        guess=(2, 96, 96), perturb_ang=0.15,
+        rec=dict(num_iter=4, reconstruction_method="DM_AP", reconstruction_parameter=0.0,
+                 fix_positions=False, positions_step_size=0.5, max_position_total_distance=0.5)),
     "mixed_gd_M3": dict(
         gen=dict(name="mx", seed=14, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
                  detector=64, object_px=96, num_modes=3, mode_weights=(0.7, 0.2, 0.1)),
