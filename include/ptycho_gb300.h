@@ -63,8 +63,8 @@ typedef struct ptycho_geometry {
 
 /* Keep each position's far field FFT2(psi) of the forward pass (psi the exit
  * wave of every probe mode) in the workspace for a following
- * ptycho_position_correction() call. Gradient descent, any model; projection
- * sets with a single probe (no mixed state). */
+ * ptycho_position_correction() call. Gradient descent and projection sets, any
+ * model (projection sets transform psi once more per position and mode). */
 #define PTYCHO_FLAG_KEEP_FARFIELD 2
 
 /* Batch chaining within one iteration (batch calls on one workspace and stream):

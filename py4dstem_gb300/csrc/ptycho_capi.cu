@@ -267,10 +267,6 @@ int ptycho_projection_batch(const ptycho_geometry* g, void* object, void* probe,
   int st = prepare(g, batch, workspace, workspace_bytes, a);
   if (st != PTYCHO_OK) return st;
   if (!exit_waves) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "exit_waves must be non-null");
-  if ((g->flags & PTYCHO_FLAG_KEEP_FARFIELD) &&
-      (g->num_probes > 1 || (g->flags & PTYCHO_FLAG_MIXED_STATE)))
-    return fail(PTYCHO_ERR_UNSUPPORTED, "PTYCHO_FLAG_KEEP_FARFIELD with projection sets needs a "
-                                        "single probe (no mixed state)");
   a.projection = 1;
   a.keep_farfield = (g->flags & PTYCHO_FLAG_KEEP_FARFIELD) ? 1 : 0;
   a.pa = projection_a;

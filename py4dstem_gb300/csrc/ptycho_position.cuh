@@ -355,6 +355,22 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
         }
       }
     }
+    if (ps && a.keep_farfield) {
+      // projection sets with position correction: the far field of each mode's
+      // psi at the last slice, O_{T-1} P_{T-1,m} from the stash
+      for (int m = 0; m < M; ++m) {
+        const float2* plast = a.st_pm + (((size_t)(T - 1) * a.B + b) * M + m) * N;
+        __syncthreads();
+        for (int e = tid; e < N; e += NT) {
+          const int x = e / SY, y = e % SY;
+          buf[x * LD + y] = c_mul(load_object(a, T - 1, obj_x(x), obj_y(y)), plast[e]);
+        }
+        __syncthreads();
+        fft2d<SX, SY, NT, -1>(buf, twx, twy);
+        float2* f = a.scratch_f + ((size_t)b * M + m) * N;
+        for (int e = tid; e < N; e += NT) f[e] = buf[(e / SY) * LD + e % SY];
+      }
+    }
   } else {
   if (T == 1) {
     // ------------------------------------------------------------ single slice
@@ -383,8 +399,8 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
             const float2 w = a.ew_valid ? ew[e] : psi;
             v = c_add(c_scale(psi, a.pc), c_scale(w, py_));
             // position correction works on FFT2(psi), not on the projected factor;
-            // psi waits here and is transformed at the end (single probe only)
-            if (a.keep_farfield) a.scratch_f[(size_t)b * N + e] = psi;
+            // a single probe's psi waits here and is transformed at the end
+            if (a.keep_farfield && !mixed) a.scratch_f[(size_t)b * N + e] = psi;
           }
           buf[x * LD + y] = v;
         }
@@ -623,12 +639,30 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
 
     if (ps && a.keep_farfield) {
       // projection sets with position correction: the far field of psi
-      float2* f = a.scratch_f + (size_t)b * N;
-      __syncthreads();
-      for (int e = tid; e < N; e += NT) buf[(e / SY) * LD + e % SY] = f[e];
-      __syncthreads();
-      fft2d<SX, SY, NT, -1>(buf, twx, twy);
-      for (int e = tid; e < N; e += NT) f[e] = buf[(e / SY) * LD + e % SY];
+      if (T > 1 || !(M > 1 || a.mixed_formula)) {
+        float2* f = a.scratch_f + (size_t)b * N;
+        __syncthreads();
+        for (int e = tid; e < N; e += NT) buf[(e / SY) * LD + e % SY] = f[e];
+        __syncthreads();
+        fft2d<SX, SY, NT, -1>(buf, twx, twy);
+        for (int e = tid; e < N; e += NT) f[e] = buf[(e / SY) * LD + e % SY];
+      } else {
+        // mixed state: psi_m = P_m O again (the probe stash now holds the
+        // probe terms), then its far field, mode by mode
+        for (int m = 0; m < M; ++m) {
+          __syncthreads();
+          shifted_probe(m);
+          for (int e = tid; e < N; e += NT) {
+            const int x = e / SY, y = e % SY;
+            const float2 p = c_scale(buf[x * LD + y], invN);
+            buf[x * LD + y] = c_mul(p, load_object(a, 0, obj_x(x), obj_y(y)));
+          }
+          __syncthreads();
+          fft2d<SX, SY, NT, -1>(buf, twx, twy);
+          float2* f = a.scratch_f + ((size_t)b * M + m) * N;
+          for (int e = tid; e < N; e += NT) f[e] = buf[(e / SY) * LD + e % SY];
+        }
+      }
     }
   }  // kMode != 4
 

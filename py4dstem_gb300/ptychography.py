@@ -475,10 +475,6 @@ class _PtychographyBase(PreprocessMixin):
         if use_projection and detector_fourier_mask is not None:
             raise NotImplementedError()
         correct_positions = not fix_positions
-        if correct_positions and use_projection and self._mixed:
-            raise NotImplementedError(
-                "position correction (fix_positions=False) with projection sets needs a "
-                "single probe")
 
         J = self._num_diffraction_patterns
         shuffled = np.arange(J)

@@ -173,6 +173,14 @@ CASES = {
         guess=(2, 96, 96), perturb_ang=0.15,
         rec=dict(num_iter=4, reconstruction_method="DM_AP", reconstruction_parameter=0.0,
                  fix_positions=False, positions_step_size=0.5, max_position_total_distance=0.5)),
+    "mixed_ap_poscorr": dict(
+        gen=dict(name="xap", seed=36, scan_shape=(8, 8), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=96, num_modes=2, mode_weights=(0.8, 0.2)),
+        cls="mixed", ctor=dict(object_fov_ang=(24.0, 24.0), num_probes=2), global_seed=17,
+        guess=(96, 96), perturb_ang=0.15,
+        rec=dict(num_iter=3, reconstruction_method="RAAR", reconstruction_parameter=0.9,
+                 fix_positions=False, positions_step_size=0.5,
+                 max_position_update_distance=0.1, max_position_total_distance=0.4)),
     "mixed_gd_M3": dict(
         gen=dict(name="mx", seed=14, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
                  detector=64, object_px=96, num_modes=3, mode_weights=(0.7, 0.2, 0.1)),

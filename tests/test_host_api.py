@@ -75,9 +75,6 @@ def test_unsupported_options_raise_before_gpu():
     with pytest.raises(NotImplementedError):
         p.reconstruct(fix_positions=False, global_affine_transformation=True, **kw)
     with pytest.raises(NotImplementedError):
-        Golden("mixed_gd_M3").build(device="cpu").reconstruct(
-            fix_positions=False, reconstruction_method="DM_AP", **kw)
-    with pytest.raises(NotImplementedError):
         p.reconstruct(q_lowpass=0.5, **kw)
 
     with pytest.raises(ValueError):

@@ -106,16 +106,6 @@ def test_rejects_unknown_flags(lib):
     assert b"flags" in lib.ptycho_last_error()
 
 
-def test_keep_farfield_with_projection_sets_needs_single_probe(lib):
-    g = geometry(M=2)
-    g.flags = _native.FLAG_KEEP_FARFIELD
-    dummy = ctypes.c_void_p(0x1000)
-    st = lib.ptycho_projection_batch(ctypes.byref(g), dummy, dummy, dummy, None, dummy, None, 4,
-                                     0.0, 1.0, 1.0, 1.0, 0, dummy, 0, None, dummy,
-                                     ctypes.c_void_p(0x1000), 1 << 40, None)
-    assert st == 2 and b"single probe" in lib.ptycho_last_error()
-
-
 def _pc(lib, g, ws=ctypes.c_void_p(0x1000), wsb=1 << 40, initial=ctypes.c_void_p(0x1000)):
     dummy = ctypes.c_void_p(0x1000)
     return lib.ptycho_position_correction(ctypes.byref(g), dummy, None, None, dummy, None,
