@@ -16,7 +16,13 @@ each iteration).
          SingleslicePtychography with storage="cpu" whose amplitudes live in
          page-locked host memory; each call uploads object, probe and positions,
          its kernels read all amplitudes from host memory over the CPU-GPU link,
-         and it reads object, probe and error back.
+         and it reads object, probe and error back;
+  preprocess  preprocess() with the rotation search on the device for the whole
+         scan, against the host NumPy path on a sample of scan rows.
+
+Other workloads (--workload): multiscan (16 mixed-state scans in one graph
+launch per iteration), multislice (8 slices), projection (DM_AP on whole-scan
+batches), poscorr (position correction), mixed-multislice (4 slices, 2 modes).
 
 `--impl reference` times the reference algorithm (the float32 NumPy restatement
 in oracle/, which reproduces the reference CPU path bit for bit) on the host
