@@ -487,6 +487,9 @@ class _PtychographyBase(PreprocessMixin):
         obj = np.asarray(self._object, dtype=np.float32 if potential else np.complex64)
         use_mask = bool(fix_potential_baseline and self._object_fov_mask_inverse.sum() > 0)
         amplitudes = self._amplitudes_for_state()
+        if amplitudes is None:
+            raise ValueError("no diffraction amplitudes: call preprocess() with a datacube first "
+                             "(an object from py4dstem_gb300.read() keeps no amplitudes)")
         driver_kw = dict(
             max_batch=int(max_batch_size), projection=use_projection, step_size=step_size,
             normalization_min=normalization_min, fix_probe=fix_probe,

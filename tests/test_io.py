@@ -55,3 +55,12 @@ def test_save_requires_preprocess(tmp_path):
     p = pg.SingleslicePtychography(energy=300e3, device="cpu")
     with pytest.raises(ValueError):
         p.save(tmp_path / "x.npz")
+
+
+def test_read_without_preprocess_asks_for_it(tmp_path):
+    g = Golden("ss_gd_potential")
+    p = g.build(device="cpu")
+    p.save(tmp_path / "r.npz")
+    q = pg.read(tmp_path / "r.npz", device="cpu")
+    with pytest.raises(ValueError, match="GPU only"):
+        q.reconstruct(num_iter=1)
