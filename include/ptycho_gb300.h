@@ -160,7 +160,7 @@ int ptycho_position_correction(const ptycho_geometry* geometry, const void* obje
  * (float32 for potentials) and probe_grad (M,Sx,Sy) complex64 (NULL: skipped)
  * receive dloss/dRe + i dloss/dIm (for potentials dloss/dV). The object gradient
  * is -2N times the summed adjoint terms of _gradient_descent_adjoint
- * (ptychographic_methods.py:1818-1908, 2353-2458, 2906-3000) before their
+ * (ptychographic_methods.py:1818-1908, 2353-2458, 2906-3000, 3162-3400) before their
  * normalisation and step. The probe gradient is exact: each position's term
  * conj(O) chi goes back through the adjoint of its sub-pixel shift before the sum
  * (the reference's probe update sums the unshifted terms).

@@ -366,8 +366,6 @@ int ptycho_gd_gradient(const ptycho_geometry* g, const void* object, const void*
                                              "and loss must be non-null");
   if (g->num_slices > 1 && !propagators)
     return fail(PTYCHO_ERR_INVALID_ARGUMENT, "multislice needs propagators");
-  if (g->num_slices > 1 && g->num_probes > 1)
-    return fail(PTYCHO_ERR_UNSUPPORTED, "gradients of mixed-state multislice models");
   a.mixed_formula = (g->num_probes > 1 || (g->flags & PTYCHO_FLAG_MIXED_STATE)) ? 1 : 0;
   a.object = const_cast<void*>(object);
   a.probe = static_cast<float2*>(const_cast<void*>(probe));

@@ -113,8 +113,8 @@ __global__ void __launch_bounds__(NT, 1) probe_spectrum_kernel(BatchArgs a) {
 // single probe, 2 single-slice mixed state, 3 multislice / single probe, 4
 // mixed-state multislice; modes 1-3 are gradient descent with no projection
 // sets, forward-only pass, kept far fields or exact probe gradient; mode 4 runs
-// gradient descent, projection sets or the forward-only pass (its far fields
-// always stay in scratch_f).
+// every variant of the mixed-state multislice model (its far fields always stay
+// in scratch_f).
 template <int SX, int SY, int NT, int kMode>
 __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, float* red) {
   constexpr bool kPlain = kMode >= 1 && kMode <= 3;
@@ -207,7 +207,7 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
   // S_b^H (conj(O) chi) = IFFT2(conj(ramp) FFT2(conj(O) chi)). The reference's
   // update omits S_b^H; here the FFT2 and the conj(ramp) are applied per position
   // and the IFFT2 once to the batch sum. buf holds conj(O) chi on entry.
-  const bool exact = !kPlain && kMode != 4 && a.exact_probe_grad != 0;
+  const bool exact = !kPlain && a.exact_probe_grad != 0;
   auto unshift_probe_term = [&](float2* dst) {
     fft2d<SX, SY, NT, -1>(buf, twx, twy);
     for (int e = tid; e < N; e += NT) {
@@ -334,14 +334,15 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
             nobj[e] = nobj[e] + pn;
           }
           const float2 bt = c_mul(chi, make_float2(o.x, -o.y));  // chi * conj(O_s)
-          if (s > 0) {
+          if (s > 0 || exact) {
             buf[idx] = bt;
           } else {
             a.st_probe[((size_t)b * M + m) * N + e] = bt;
-            if (m == 0) a.st_nprobe[(size_t)b * N + e] = c_abs2(o);
           }
+          if (s == 0 && m == 0) a.st_nprobe[(size_t)b * N + e] = c_abs2(o);
         }
         __syncthreads();
+        if (s == 0 && exact) unshift_probe_term(a.st_probe + ((size_t)b * M + m) * N);
         if (s > 0) {
           fft2d<SX, SY, NT, -1>(buf, twx, twy);
           const float2* h = a.props + (size_t)(s - 1) * N;
@@ -1103,7 +1104,6 @@ cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
   }
   // plain gradient-descent batches run an instantiation with the other modes
   // compiled out (see position_one); mixed-state multislice has its own
-  if (mixed_ms && a.exact_probe_grad) return cudaErrorNotSupported;
   const bool plain = !a.projection && !a.forward_only && !a.keep_farfield && !a.exact_probe_grad;
   const int mode = mixed_ms ? 4
                    : !plain ? 0

@@ -2,8 +2,8 @@
 
 * Its backward (the hand-written adjoint kernel) agrees with central finite
   differences of the FP64 forward model (oracle) on 32 random object pixels and
-  32 random probe pixels, for single-slice (complex and potential), multislice
-  and mixed-state models.
+  32 random probe pixels, for single-slice (complex and potential), multislice,
+  mixed-state and mixed-state multislice models.
 * Its object gradient is -2N times the reference's summed adjoint term
   (the scatter of conj(P) chi, ptychographic_methods.py:1818-1908), evaluated by
   the float32 oracle; its probe gradient is the exact one (each term back
@@ -24,6 +24,7 @@ CASES = {
     "potential": dict(S=64, J=16, potential=True),
     "multislice": dict(S=64, J=16, slices=3),
     "mixed": dict(S=64, J=16, modes=2),
+    "mixed_multislice": dict(S=64, J=16, slices=2, modes=2),
 }
 
 
