@@ -367,6 +367,58 @@ int ptycho_mapped_host_pointer(const void* host, size_t bytes, void** device);
 int ptycho_prepare_stream(void* stream);
 
 /*
+ * Tomography (PtychographicTomography, ptychographic_tomography.py:991-1240).
+ * The object is a (n0, n1, n2) float32 potential volume (z, x, y).
+ *
+ * ptycho_volume_rotate: out = the volume resampled by the affine map
+ * input coordinate = offset + matrix . output coordinate, with cubic B-spline
+ * interpolation of mirror-extended spline coefficients and 0 where the input
+ * coordinate leaves [0, n - 1] on any axis: scipy.ndimage.affine_transform(order=3,
+ * mode="constant", prefilter=True) as _rotate_zxy_volume calls it
+ * (ptychographic_methods.py:849-868). Float64 arithmetic throughout. volume is
+ * float32 (volume_is_double 0) or float64 (1); out_mode 0 writes float32, 1
+ * writes float64, 2 adds into a float32 out (sum in float64, rounded once: the
+ * collective update of ptychographic_tomography.py:1121-1124). matrix (9, row
+ * major) and offset (3) are host arrays. scratch: n0*n1*n2 doubles. out may be
+ * the volume itself.
+ */
+int ptycho_volume_rotate(const void* volume, int32_t volume_is_double, void* out,
+                         int32_t out_mode, int32_t n0, int32_t n1, int32_t n2,
+                         const double* matrix, const double* offset, void* scratch,
+                         size_t scratch_bytes, void* stream);
+
+/*
+ * sliced (num_slices, n1, n2) = the volume summed over consecutive groups of
+ * ceil(n0 / num_slices) voxels along z, in voxel order, the last group padded
+ * with zeros (_project_sliced_object, ptychographic_methods.py:783-812).
+ */
+int ptycho_volume_project(const float* volume, int32_t n0, int32_t n1, int32_t n2,
+                          int32_t num_slices, float* sliced, void* stream);
+
+/*
+ * The voxels of slice t receive (sliced - sliced_old)[t] divided by the number
+ * of voxels the slice covers, in float64 (_expand_sliced_object,
+ * ptychographic_methods.py:814-847, applied to the slice update of
+ * ptychographic_tomography.py:1115-1119). out_mode 1 writes a float64 volume;
+ * 2 adds into a float32 volume (float64 sum rounded once).
+ */
+int ptycho_volume_expand_update(const float* sliced, const float* sliced_old,
+                                int32_t num_slices, int32_t n0, int32_t n1, int32_t n2,
+                                void* out, int32_t out_mode, void* stream);
+
+/* volume += addend / divisor, in float32 (ptychographic_tomography.py:1225-1226). */
+int ptycho_volume_add_scaled(float* volume, const float* addend, int64_t count, int32_t divisor,
+                             void* stream);
+
+/*
+ * Volume object constraints: v -= shrinkage (apply_shrinkage), then v = max(v, 0)
+ * (positivity), float32 (ptychographic_constraints.py:60-118 and 836-887 with no
+ * object mask).
+ */
+int ptycho_volume_constraints(float* volume, int64_t count, float shrinkage,
+                              int32_t apply_shrinkage, int32_t positivity, void* stream);
+
+/*
  * Instrumentation. When enabled, every launch of the fused per-position kernel
  * is bracketed by CUDA events recorded on its stream; ptycho_kernel_timing()
  * waits for the last one and returns the summed kernel time (ms) and the number

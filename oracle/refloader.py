@@ -131,6 +131,8 @@ class DataCube:
     R_Ny = property(lambda self: self.data.shape[1])
     Q_Nx = property(lambda self: self.data.shape[2])
     Q_Ny = property(lambda self: self.data.shape[3])
+    R_N = property(lambda self: self.data.shape[0] * self.data.shape[1])
+    Qshape = property(lambda self: self.data.shape[2:])
 
     def set_dim(self, *args, **kwargs):
         pass
@@ -203,7 +205,7 @@ def load_reference(root: str | None = None):
 
     Returns an object with attributes ``SingleslicePtychography``,
     ``MultislicePtychography``, ``MixedstatePtychography``,
-    ``MixedstateMultislicePtychography``, ``DataCube`` (the
+    ``MixedstateMultislicePtychography``, ``PtychographicTomography``, ``DataCube`` (the
     duck type above), ``utils`` (``process/phase/utils.py``) and ``root``.
     """
     root = root or os.environ.get("PY4DSTEM_REFERENCE", DEFAULT_REFERENCE_ROOT)
@@ -263,6 +265,7 @@ def load_reference(root: str | None = None):
     mixed = importlib.import_module("py4DSTEM.process.phase.mixedstate_ptychography")
     mixed_multi = importlib.import_module(
         "py4DSTEM.process.phase.mixedstate_multislice_ptychography")
+    tomo = importlib.import_module("py4DSTEM.process.phase.ptychographic_tomography")
     phase_utils = importlib.import_module("py4DSTEM.process.phase.utils")
 
     ns = types.SimpleNamespace(
@@ -270,6 +273,7 @@ def load_reference(root: str | None = None):
         MultislicePtychography=multi.MultislicePtychography,
         MixedstatePtychography=mixed.MixedstatePtychography,
         MixedstateMultislicePtychography=mixed_multi.MixedstateMultislicePtychography,
+        PtychographicTomography=tomo.PtychographicTomography,
         DataCube=DataCube,
         utils=phase_utils,
         root=root,

@@ -111,6 +111,13 @@ _SIGNATURES = {
         [_vp, _i32, _i32, _vp, _i32, _vp, _vp, _i32, _vp, _vp, _vp], ctypes.c_int),
     "ptycho_probe_overlap": (
         [ctypes.POINTER(Geometry), _vp, _vp, _i32, _i32, _vp, _vp, _sz, _vp], ctypes.c_int),
+    "ptycho_volume_rotate": (
+        [_vp, _i32, _vp, _i32, _i32, _i32, _i32, _vp, _vp, _vp, _sz, _vp], ctypes.c_int),
+    "ptycho_volume_project": ([_vp, _i32, _i32, _i32, _i32, _vp, _vp], ctypes.c_int),
+    "ptycho_volume_expand_update": (
+        [_vp, _vp, _i32, _i32, _i32, _i32, _vp, _i32, _vp], ctypes.c_int),
+    "ptycho_volume_add_scaled": ([_vp, _vp, ctypes.c_int64, _i32, _vp], ctypes.c_int),
+    "ptycho_volume_constraints": ([_vp, ctypes.c_int64, _f32, _i32, _i32, _vp], ctypes.c_int),
     "ptycho_gd_batch_noalloc": (
         [ctypes.POINTER(Geometry), _vp, _vp, _vp, _vp, _vp, _vp, _i32, _f32, _f32, _i32,
          _vp, _vp, _vp, _vp],

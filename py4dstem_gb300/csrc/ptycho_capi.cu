@@ -712,6 +712,89 @@ int ptycho_probe_overlap(const ptycho_geometry* g, const void* probe, const floa
   return PTYCHO_OK;
 }
 
+// ---- tomography volume operations (ptycho_volume.cu)
+
+int ptycho_volume_rotate(const void* volume, int32_t volume_is_double, void* out,
+                         int32_t out_mode, int32_t n0, int32_t n1, int32_t n2,
+                         const double* matrix, const double* offset, void* scratch,
+                         size_t scratch_bytes, void* stream) {
+  if (!volume || !out || !matrix || !offset || !scratch)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT,
+                "volume, out, matrix, offset and scratch must be non-null");
+  if (n0 < 1 || n1 < 1 || n2 < 1)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "bad volume shape (%d, %d, %d)", n0, n1, n2);
+  if (volume_is_double != 0 && volume_is_double != 1)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "volume_is_double must be 0 or 1");
+  if (out_mode < 0 || out_mode > 2)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "out_mode must be 0, 1 or 2 (got %d)", out_mode);
+  const size_t need = (size_t)n0 * n1 * n2 * sizeof(double);
+  if (scratch_bytes < need)
+    return fail(PTYCHO_ERR_WORKSPACE, "scratch of %zu bytes is smaller than the %zu needed",
+                scratch_bytes, need);
+  if (reinterpret_cast<uintptr_t>(scratch) % 8 != 0)
+    return fail(PTYCHO_ERR_WORKSPACE, "scratch must be 8-byte aligned");
+  cudaError_t e = launch_volume_rotate(volume, volume_is_double, out, out_mode, n0, n1, n2,
+                                       matrix, offset, static_cast<double*>(scratch),
+                                       static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "volume rotation kernels");
+  return PTYCHO_OK;
+}
+
+int ptycho_volume_project(const float* volume, int32_t n0, int32_t n1, int32_t n2,
+                          int32_t num_slices, float* sliced, void* stream) {
+  if (!volume || !sliced)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "volume and sliced must be non-null");
+  if (n0 < 1 || n1 < 1 || n2 < 1 || num_slices < 1)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "bad volume shape (%d, %d, %d) or slice count %d",
+                n0, n1, n2, num_slices);
+  cudaError_t e = launch_volume_project(volume, n0, (size_t)n1 * n2, num_slices, sliced,
+                                        static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "volume projection kernel");
+  return PTYCHO_OK;
+}
+
+int ptycho_volume_expand_update(const float* sliced, const float* sliced_old,
+                                int32_t num_slices, int32_t n0, int32_t n1, int32_t n2,
+                                void* out, int32_t out_mode, void* stream) {
+  if (!sliced || !sliced_old || !out)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "sliced, sliced_old and out must be non-null");
+  if (n0 < 1 || n1 < 1 || n2 < 1 || num_slices < 1)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "bad volume shape (%d, %d, %d) or slice count %d",
+                n0, n1, n2, num_slices);
+  if (out_mode != 1 && out_mode != 2)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "out_mode must be 1 or 2 (got %d)", out_mode);
+  cudaError_t e = launch_volume_expand(sliced, sliced_old, num_slices, n0, (size_t)n1 * n2, out,
+                                       out_mode, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "volume expansion kernel");
+  return PTYCHO_OK;
+}
+
+int ptycho_volume_add_scaled(float* volume, const float* addend, int64_t count, int32_t divisor,
+                             void* stream) {
+  if (!volume || !addend)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "volume and addend must be non-null");
+  if (count < 0 || divisor < 1)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "bad count %lld or divisor %d", (long long)count,
+                divisor);
+  if (count == 0) return PTYCHO_OK;
+  cudaError_t e = launch_volume_add_scaled(volume, addend, (size_t)count, divisor,
+                                           static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "volume add kernel");
+  return PTYCHO_OK;
+}
+
+int ptycho_volume_constraints(float* volume, int64_t count, float shrinkage,
+                              int32_t apply_shrinkage, int32_t positivity, void* stream) {
+  if (!volume) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "volume is null");
+  if (count < 0) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "bad count %lld", (long long)count);
+  if (count == 0 || (!apply_shrinkage && !positivity)) return PTYCHO_OK;
+  cudaError_t e = launch_volume_constraints(volume, (size_t)count, shrinkage,
+                                            apply_shrinkage ? 1 : 0, positivity ? 1 : 0,
+                                            static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "volume constraint kernel");
+  return PTYCHO_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------

@@ -146,4 +146,17 @@ cudaError_t launch_pattern_normalize(const float* in, int Qx, int Qy, const int3
                                      int num_out, const float* cfx, const float* cfy,
                                      int crop_w, float* amps, float* sums, cudaStream_t s);
 
+// ---- ptycho_volume.cu (tomography)
+cudaError_t launch_volume_rotate(const void* in, int in_is_double, void* out, int out_mode,
+                                 int n0, int n1, int n2, const double* matrix,
+                                 const double* offset, double* scratch, cudaStream_t s);
+cudaError_t launch_volume_project(const float* vol, int n0, size_t P, int T, float* sliced,
+                                  cudaStream_t s);
+cudaError_t launch_volume_expand(const float* sliced, const float* old, int T, int n0, size_t P,
+                                 void* out, int out_mode, cudaStream_t s);
+cudaError_t launch_volume_add_scaled(float* vol, const float* addend, size_t n, int divisor,
+                                     cudaStream_t s);
+cudaError_t launch_volume_constraints(float* vol, size_t n, float shrinkage, int apply_shrinkage,
+                                      int positivity, cudaStream_t s);
+
 }  // namespace pty

@@ -425,14 +425,17 @@ class IterationDriver:
                  fix_probe_com=True, orthogonalize_probe=False, mean_intensity=1.0,
                  position_correction=None, device_orthogonalization=False,
                  graph=False, identical_slices=False, probe_aperture=None,
-                 probe_amplitude_mask=None, gaussian=None):
+                 probe_amplitude_mask=None, gaussian=None, object_constraints=True):
         """probe_aperture: (Sx, Sy) Fourier amplitude of the initial probe (mode 0)
         for the aperture constraint; probe_amplitude_mask: (Sx, Sy) real-space mask
         of the amplitude constraint; identical_slices: average the object slices;
-        gaussian: (float64 weights of length 2 R + 1, pure_phase) of the object blur."""
+        gaussian: (float64 weights of length 2 R + 1, pure_phase) of the object blur;
+        object_constraints=False leaves the object constraints to the caller (the
+        tomography volume)."""
         self.st = st
         torch = _torch()
         dev = st.object.device
+        self.object_constraints = bool(object_constraints)
 
         def dev_f32(a):
             if a is None:
@@ -527,8 +530,9 @@ class IterationDriver:
             _native.check(lib.ptycho_object_identical_slices(
                 ctypes.byref(st.geometry), _ptr(st.object), _stream()))
             st.launches += 1
-        object_constraints(st, shrinkage_rad=self.shrinkage_rad, use_mask=self.use_mask,
-                           pure_phase=self.pure_phase, positivity=self.positivity)
+        if self.object_constraints:
+            object_constraints(st, shrinkage_rad=self.shrinkage_rad, use_mask=self.use_mask,
+                               pure_phase=self.pure_phase, positivity=self.positivity)
         if self.fix_probe_com:
             probe_com_constraint(st)
         if self.probe_aperture is not None:

@@ -386,6 +386,168 @@ def make_case(ref, name, spec):
     print(f"{name}: {os.path.getsize(path) / 1e6:.2f} MB, errors {out['error_iterations'][-3:]}")
 
 
+# Ptychographic tomography: three tilts about the x axis of a 48^3 potential
+# volume, each tilt its own seeded synthetic scan. Gradient descent with the
+# default collective update (one volume update per iteration), and with the
+# sequential update (the volume updated after every tilt) plus shrinkage, both
+# from a seeded smooth positive volume (`guess_peak`: its largest voxel). From
+# the default zero volume the first gradient steps are ill-conditioned (a change
+# of the float32 FFT alone moves the result by 1e-2); the zero-start case keeps
+# that default path covered.
+TOMO_CASES = {
+    "tomo_gd_collective": dict(
+        seeds=(40, 41, 42), tilts_deg=(-10.0, 0.0, 12.0), guess_peak=0.03,
+        gen=dict(scan_shape=(8, 8), step_ang=0.5, jitter_ang=0.05, detector=48,
+                 object_px=64, num_slices=2, slice_thickness=10.0),
+        ctor=dict(num_slices=4, object_padding_px=(8, 8)),
+        rec=dict(num_iter=3, max_batch_size=16, seed_random=1, step_size=0.5)),
+    "tomo_gd_sequential": dict(
+        seeds=(43, 44), tilts_deg=(-7.0, 9.0), guess_peak=0.03,
+        gen=dict(scan_shape=(8, 8), step_ang=0.5, jitter_ang=0.05, detector=48,
+                 object_px=64, num_slices=2, slice_thickness=10.0),
+        ctor=dict(num_slices=3, object_padding_px=(8, 8)),
+        rec=dict(num_iter=3, max_batch_size=20, seed_random=5, step_size=0.5,
+                 collective_measurement_updates=False, shrinkage_rad=1e-3)),
+    "tomo_gd_zero_start": dict(
+        seeds=(40, 41, 42), tilts_deg=(-10.0, 0.0, 12.0),
+        gen=dict(scan_shape=(8, 8), step_ang=0.5, jitter_ang=0.05, detector=48,
+                 object_px=64, num_slices=2, slice_thickness=10.0),
+        ctor=dict(num_slices=4, object_padding_px=(8, 8)),
+        rec=dict(num_iter=3, max_batch_size=16, seed_random=1, step_size=0.5)),
+}
+
+
+def smooth_volume(shape, seed, peak):
+    """Seeded smooth positive potential volume, values in [0.2, 1] x peak."""
+    rng = np.random.default_rng(seed)
+    f = rng.normal(size=shape)
+    k = [np.fft.fftfreq(n) for n in shape]
+    g = np.exp(-(k[0][:, None, None] ** 2 + k[1][None, :, None] ** 2
+                 + k[2][None, None, :] ** 2) * (shape[-1] / 6.0) ** 2)
+    v = np.fft.ifftn(np.fft.fftn(f) * g).real
+    v = (v - v.min()) / (v.max() - v.min())
+    return (peak * (0.2 + 0.8 * v)).astype(np.float32)
+
+
+def tilt_matrix(deg):
+    """Rotation by `deg` degrees about the x (first, vertical) axis in (x, y, z)."""
+    t = np.deg2rad(deg)
+    c, s = np.cos(t), np.sin(t)
+    return np.array([[1.0, 0.0, 0.0], [0.0, c, -s], [0.0, s, c]])
+
+
+def tomography_class(ref):
+    """The reference class with two defects of py4DSTEM 0.14.18 that stop its
+    preprocess() worked around: ptychographic_tomography.py:486-492 calls
+    _normalize_diffraction_intensities without its required
+    in_place_datacube_modification argument (passed here as False, the default
+    of the preprocess() argument of that name), and the constructor never sets
+    the _object_fov_ang that _initialize_object reads (set to None here, the
+    value that sizes the volume from the scan positions)."""
+
+    class Tomography(ref.PtychographicTomography):
+        def __init__(self, *args, **kwargs):
+            super().__init__(*args, **kwargs)
+            self._object_fov_ang = None
+
+        def _normalize_diffraction_intensities(self, *args, **kwargs):
+            if len(args) == 5:
+                kwargs.setdefault("in_place_datacube_modification", False)
+            return super()._normalize_diffraction_intensities(*args, **kwargs)
+
+    return Tomography
+
+
+def make_tomo_case(ref, name, spec):
+    cases = [synthetic.make_scan(name="tomo", seed=sd, **spec["gen"]) for sd in spec["seeds"]]
+    dcs = []
+    for c in cases:
+        q = c.datacube.calibration.get_Q_pixel_size()
+        r = c.datacube.calibration.get_R_pixel_size()
+        dcs.append(ref.DataCube(c.datacube.data, r_pixel_size=r, r_pixel_units="A",
+                                q_pixel_size=q, q_pixel_units="mrad"))
+    mats = np.stack([tilt_matrix(a) for a in spec["tilts_deg"]])
+    positions = np.stack([c.scan_positions_ang for c in cases])
+    ctor = dict(energy=300e3, semiangle_cutoff=20.0, defocus=100.0, **spec["ctor"])
+    cls = tomography_class(ref)
+    pre_args = dict(plot_probe_overlaps=False, diffraction_patterns_rotate_degrees=0.0,
+                    diffraction_patterns_transpose=False)
+    extra, guess = {}, None
+    if "guess_peak" in spec:
+        # the volume shape comes out of preprocess(): one pass to learn it
+        probe_pass = cls(tilt_orientation_matrices=list(mats), datacube=dcs,
+                         initial_scan_positions=list(positions), verbose=False, device="cpu",
+                         **ctor)
+        probe_pass.preprocess(**pre_args)
+        guess = smooth_volume(probe_pass._object.shape, spec["seeds"][0] + 100,
+                              spec["guess_peak"])
+        extra["initial_object_guess"] = guess.copy()
+    p = cls(tilt_orientation_matrices=list(mats), datacube=dcs,
+            initial_scan_positions=list(positions), verbose=False, device="cpu", **ctor,
+            **extra)
+    p.preprocess(**pre_args)
+    pre = dict(
+        mean_intensity=np.asarray(p._mean_diffraction_intensity, dtype=np.float32),
+        positions_px=np.asarray(p._positions_px_all).copy(),
+        probe_initial=np.stack(p._probes_all).copy(),
+        object_initial=p._object.copy(),
+        amplitude_sums=np.asarray(p._amplitudes).sum(axis=(-2, -1)),
+        propagators=np.asarray(p._propagator_arrays).copy(),
+    )
+    p.reconstruct(progress_bar=False, **spec["rec"])
+    out = dict(
+        error_iterations=np.asarray(p.error_iterations, dtype=np.float64),
+        object=np.asarray(p.object),
+        probes_corner=np.stack(p._probes_all),
+    )
+    data = np.stack([c.datacube.data for c in cases])
+    assert np.array_equal(data, np.round(data)) and data.max() < 65535
+    meta = dict(ctor=ctor, preprocess=pre_args, reconstruct=spec["rec"],
+                tilts_deg=spec["tilts_deg"], seeds=spec["seeds"], generator=spec["gen"],
+                r_pixel_size=[c.datacube.calibration.get_R_pixel_size() for c in cases],
+                q_pixel_size=[c.datacube.calibration.get_Q_pixel_size() for c in cases])
+    path = os.path.join(HERE, f"{name}.npz")
+    if guess is not None:
+        extra_arrays = {"initial_object_guess": guess}
+    else:
+        extra_arrays = {}
+    np.savez_compressed(
+        path, datacube=data.astype(np.uint16), scan_positions_ang=positions, tilt_matrices=mats,
+        meta=json.dumps(meta), **extra_arrays, **{f"pre_{k}": v for k, v in pre.items()},
+        **{f"out_{k}": v for k, v in out.items()})
+    print(f"{name}: {os.path.getsize(path) / 1e6:.2f} MB, errors {out['error_iterations']}")
+
+
+def make_volume_ops(ref):
+    """The reference's own volume operations on a seeded random volume:
+    _rotate_zxy_volume (float32 and float64 input), _project_sliced_object and
+    _expand_sliced_object (ptychographic_methods.py:783-868)."""
+    cls = tomography_class(ref)
+    p = cls.__new__(cls)
+    p._xp = np
+    import scipy
+
+    p._scipy = scipy
+    rng = np.random.default_rng(7)
+    vol = rng.random((20, 24, 28)).astype(np.float32)
+    vol64 = rng.normal(size=(20, 24, 28))
+    out = {"volume": vol, "volume64": vol64}
+    for k, deg in enumerate((-10.0, 12.0, 30.0, 90.0)):
+        r = tilt_matrix(deg) @ tilt_matrix(3.0 * k).T
+        out[f"matrix_{k}"] = r
+        out[f"rot32_{k}"] = p._rotate_zxy_volume(vol, r)
+        out[f"rot64_{k}"] = p._rotate_zxy_volume(vol64, r)
+    for T in (1, 3, 6, 7):
+        sl = p._project_sliced_object(vol, T)
+        out[f"project_{T}"] = sl
+        upd = (sl * np.float32(0.25)).astype(np.float32)
+        out[f"update_{T}"] = upd
+        out[f"expand_{T}"] = p._expand_sliced_object(upd, vol.shape[0])
+    path = os.path.join(HERE, "tomo_volume_ops.npz")
+    np.savez_compressed(path, **out)
+    print(f"tomo_volume_ops: {os.path.getsize(path) / 1e6:.2f} MB")
+
+
 def main():
     ref = load_reference()
     only = set(sys.argv[1:])
@@ -395,6 +557,11 @@ def main():
     for name, spec in PRE_CASES.items():
         if not only or name in only:
             make_pre_case(ref, name, spec)
+    for name, spec in TOMO_CASES.items():
+        if not only or name in only:
+            make_tomo_case(ref, name, spec)
+    if not only or "tomo_volume_ops" in only:
+        make_volume_ops(ref)
 
 
 if __name__ == "__main__":

@@ -19,8 +19,9 @@ def _all_names():
 
 
 def names():
-    """Reconstruction fixtures."""
-    return [n for n in _all_names() if not n.startswith("prep_")]
+    """Reconstruction fixtures of the 2D / multislice / mixed-state classes
+    (the tomography fixtures, tomo_*, have their own tests)."""
+    return [n for n in _all_names() if not n.startswith(("prep_", "tomo_"))]
 
 
 def prep_names():
