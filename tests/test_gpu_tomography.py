@@ -136,15 +136,15 @@ def test_reconstruction_matches_reference(cuda, name):
     """From a smooth initial volume (well conditioned: a change of the float32
     FFT alone moves the reference's result by about 3e-7) the float32 kernels
     agree with the reference, whose amplitudes and Fourier projection are
-    float64, to 1e-5 in the errors and 1e-4 in the volume and probes (relative
-    to their largest values)."""
+    float64, to 5e-6 in the errors and 1e-5 in the volume and probes (relative
+    to their largest values; measured on a GB300: 2e-7, 6e-7, 7e-7)."""
     p, f, meta = preprocessed(name)
     p.reconstruct(progress_bar=False, device="gpu", **meta["reconstruct"])
     assert p.object.shape == f["out_object"].shape and p.object.dtype == np.float32
     assert len(p.probe) == len(meta["seeds"])
     d = _distances(p.object, p._probes_all, p.error_iterations, f)
     print(f"{name}: error {d[0]:.2e} volume {d[1]:.2e} probes {d[2]:.2e}")
-    assert d[0] < 1e-5 and d[1] < 1e-4 and d[2] < 1e-4, d
+    assert d[0] < 5e-6 and d[1] < 1e-5 and d[2] < 1e-5, d
 
 
 def test_zero_start_within_float32_floor(cuda):
