@@ -22,7 +22,8 @@ each iteration).
 
 Other workloads (--workload): multiscan (16 mixed-state scans in one graph
 launch per iteration), multislice (8 slices), projection (DM_AP on whole-scan
-batches), poscorr (position correction), mixed-multislice (4 slices, 2 modes).
+batches), poscorr (position correction), mixed-multislice (4 slices, 2 modes),
+tomography (8 tilts through a rotated 3D volume, 8 slices).
 
 `--impl reference` times the reference algorithm (the float32 NumPy restatement
 in oracle/, which reproduces the reference CPU path bit for bit) on the host
