@@ -49,13 +49,9 @@ __global__ void volume_load_kernel(const void* in, int in_is_double, double* c, 
   }
 }
 
-// One thread per line along `axis` of the (n0, n1, n2) coefficient volume.
-__global__ void spline_prefilter_kernel(double* c, int n0, int n1, int n2, int axis) {
-  const int L = axis == 0 ? n0 : axis == 1 ? n1 : n2;
-  const size_t lines = (size_t)n0 * n1 * n2 / (size_t)L;
-  const size_t line = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (line >= lines || L < 2) return;
-  size_t base, stride;
+// First sample and sample stride of line `line` along `axis` of (n0, n1, n2).
+__device__ __forceinline__ void line_geometry(size_t line, int n1, int n2, int axis,
+                                              size_t& base, size_t& stride) {
   if (axis == 0) {
     base = line;
     stride = (size_t)n1 * n2;
@@ -67,13 +63,16 @@ __global__ void spline_prefilter_kernel(double* c, int n0, int n1, int n2, int a
     base = line * (size_t)n2;
     stride = 1;
   }
-  double* x = c + base;
+}
+
+// Cubic B-spline coefficients of one line of L >= 2 samples x[0], x[stride], ...
+// in place: gain, causal recursion from the exact initial value of the
+// mirror-symmetric extension (period 2L - 2: the sum over one period of z^k x_k
+// divided by 1 - z^(2L-2)), anti-causal recursion from its initial value.
+__device__ __forceinline__ void spline_line(double* x, size_t stride, int L) {
   const double z = __dadd_rn(sqrt(3.0), -2.0);
   const double gain = __dmul_rn(__dadd_rn(1.0, -z), __dadd_rn(1.0, -__ddiv_rn(1.0, z)));
   for (int i = 0; i < L; ++i) x[i * stride] = __dmul_rn(x[i * stride], gain);
-
-  // causal initial value of the mirror-symmetric extension (period 2L - 2):
-  // sum over one period of z^k x_k, divided by 1 - z^(2L-2)
   double zl = 1.0;
   for (int i = 0; i < L - 1; ++i) zl = __dmul_rn(zl, z);  // z^(L-1)
   double s = __dadd_rn(x[0], __dmul_rn(zl, x[(size_t)(L - 1) * stride]));
@@ -86,13 +85,64 @@ __global__ void spline_prefilter_kernel(double* c, int n0, int n1, int n2, int a
   x[0] = __ddiv_rn(s, __dadd_rn(1.0, -__dmul_rn(zl, zl)));
   for (int i = 1; i < L; ++i)
     x[i * stride] = __dadd_rn(x[i * stride], __dmul_rn(z, x[(size_t)(i - 1) * stride]));
-  // anti-causal initial value of the same extension
   const size_t last = (size_t)(L - 1) * stride;
   x[last] = __ddiv_rn(
       __dmul_rn(__dadd_rn(__dmul_rn(z, x[last - stride]), x[last]), z),
       __dadd_rn(__dmul_rn(z, z), -1.0));
   for (int i = L - 2; i >= 0; --i)
     x[i * stride] = __dmul_rn(z, __dadd_rn(x[(size_t)(i + 1) * stride], -x[i * stride]));
+}
+
+// One thread per line along `axis`, in global memory (lines too long to stage).
+__global__ void spline_prefilter_kernel(double* c, int n0, int n1, int n2, int axis) {
+  const int L = axis == 0 ? n0 : axis == 1 ? n1 : n2;
+  const size_t lines = (size_t)n0 * n1 * n2 / (size_t)L;
+  const size_t line = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (line >= lines || L < 2) return;
+  size_t base, stride;
+  line_geometry(line, n1, n2, axis, base, stride);
+  spline_line(c + base, stride, L);
+}
+
+// Lines staged in shared memory: each warp of the block owns 32 consecutive
+// lines, loaded and stored with coalesced accesses (row by row for the
+// contiguous axis), and runs the recursions there. Sample i of the warp's line l
+// sits at s[i * kLineLD + l]; the odd pitch spreads a row's samples over banks.
+constexpr int kLineLD = 33;
+
+__global__ void spline_prefilter_staged_kernel(double* c, int n0, int n1, int n2, int axis) {
+  extern __shared__ double staged[];
+  const int L = axis == 0 ? n0 : axis == 1 ? n1 : n2;
+  const size_t lines = (size_t)n0 * n1 * n2 / (size_t)L;
+  const int warps = blockDim.x / 32;
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const size_t first = ((size_t)blockIdx.x * warps + warp) * 32;
+  if (first >= lines || L < 2) return;  // the same for every lane of the warp
+  double* s = staged + (size_t)warp * kLineLD * L;
+  const size_t line = first + lane;
+  const bool active = line < lines;
+  const int nl = (int)(lines - first < 32 ? lines - first : 32);
+  size_t base = 0, stride = 1;
+  if (active) line_geometry(line, n1, n2, axis, base, stride);
+  if (axis == 2) {
+    for (int l = 0; l < nl; ++l) {
+      const double* row = c + (first + l) * (size_t)n2;
+      for (int i = lane; i < L; i += 32) s[i * kLineLD + l] = row[i];
+    }
+  } else if (active) {
+    for (int i = 0; i < L; ++i) s[i * kLineLD + lane] = c[base + (size_t)i * stride];
+  }
+  __syncwarp();
+  if (active) spline_line(s + lane, kLineLD, L);
+  __syncwarp();
+  if (axis == 2) {
+    for (int l = 0; l < nl; ++l) {
+      double* row = c + (first + l) * (size_t)n2;
+      for (int i = lane; i < L; i += 32) row[i] = s[i * kLineLD + l];
+    }
+  } else if (active) {
+    for (int i = 0; i < L; ++i) c[base + (size_t)i * stride] = s[i * kLineLD + lane];
+  }
 }
 
 __device__ __forceinline__ int mirror_index(int i, int n) {
@@ -242,12 +292,36 @@ cudaError_t launch_volume_rotate(const void* in, int in_is_double, void* out, in
   for (int k = 0; k < 9; ++k) tf.m[k] = matrix[k];
   for (int k = 0; k < 3; ++k) tf.off[k] = offset[k];
   volume_load_kernel<<<grid_for(total), kThreads, 0, s>>>(in, in_is_double, scratch, total);
+  static int smem_optin = -1;
+  if (smem_optin < 0) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess)
+      e = cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(spline_prefilter_staged_kernel,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin);
+    if (e != cudaSuccess) {
+      smem_optin = -1;
+      return e;
+    }
+  }
   const int n[3] = {n0, n1, n2};
   for (int axis = 0; axis < 3; ++axis) {
     if (n[axis] < 2) continue;
     const size_t lines = total / (size_t)n[axis];
-    spline_prefilter_kernel<<<(unsigned)((lines + 127) / 128), 128, 0, s>>>(scratch, n0, n1, n2,
-                                                                           axis);
+    const size_t per_warp = sizeof(double) * kLineLD * (size_t)n[axis];
+    if (per_warp <= (size_t)smem_optin) {
+      int warps = 4;
+      while (warps > 1 && (size_t)warps * per_warp > (size_t)smem_optin) warps /= 2;
+      const size_t per_block = (size_t)warps * 32;
+      spline_prefilter_staged_kernel<<<(unsigned)((lines + per_block - 1) / per_block),
+                                       warps * 32, warps * per_warp, s>>>(scratch, n0, n1, n2,
+                                                                          axis);
+    } else {
+      spline_prefilter_kernel<<<(unsigned)((lines + 127) / 128), 128, 0, s>>>(scratch, n0, n1,
+                                                                             n2, axis);
+    }
   }
   volume_affine_kernel<<<grid_for(total), kThreads, 0, s>>>(scratch, out, out_mode, n0, n1, n2,
                                                             tf);
