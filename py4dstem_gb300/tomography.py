@@ -399,8 +399,6 @@ class PtychographicTomography(_PtychographyBase):
     def _return_self_consistency_errors(self, **kwargs):
         raise NotImplementedError()
 
-    def save(self, path):
-        raise NotImplementedError("saving a tomography reconstruction is not implemented")
 
     def _reset_tomography(self, store_iterations, reset):
         """MultipleMeasurementsMethodsMixin._reset_reconstruction

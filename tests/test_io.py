@@ -64,3 +64,44 @@ def test_read_without_preprocess_asks_for_it(tmp_path):
     q = pg.read(tmp_path / "r.npz", device="cpu")
     with pytest.raises(ValueError, match="GPU only"):
         q.reconstruct(num_iter=1)
+
+
+def test_tomography_save_read_round_trip(tmp_path):
+    from test_tomography_oracle import preprocessed
+
+    p, _, meta = preprocessed("tomo_gd_sequential")
+    # a reconstruction state as reconstruct() leaves it
+    p._object = (p._object * np.float32(1.01) + np.float32(1e-3)).astype(np.float32)
+    p._probes_all = [(pr * np.complex64(0.99 + 0.01j)).astype(np.complex64)
+                     for pr in p._probes_all]
+    p.error_iterations = [0.5, 0.25, 0.125]
+    p.object_iterations = [p._object] * 3
+    p.probe_iterations = [p.probe_centered] * 3
+    p.set_save_defaults(save_datacube=True, save_iterations_frequency=2)
+    path = tmp_path / "tomo.npz"
+    p.save(path)
+
+    q = pg.read(path, device="cpu")
+    assert type(q) is type(p)
+    np.testing.assert_array_equal(q._object, p._object)
+    np.testing.assert_array_equal(q.object, p._object)
+    assert len(q._probes_all) == len(p._probes_all)
+    for a, b in zip(q._probes_all, p._probes_all):
+        np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(q._positions_px_all, p._positions_px_all)
+    np.testing.assert_array_equal(q._cum_probes_per_measurement, p._cum_probes_per_measurement)
+    np.testing.assert_array_equal(np.asarray(q._mean_diffraction_intensity),
+                                  np.asarray(p._mean_diffraction_intensity))
+    np.testing.assert_array_equal(q._propagator_arrays, p._propagator_arrays)
+    for a, b in zip(q._tilt_orientation_matrices, p._tilt_orientation_matrices):
+        np.testing.assert_array_equal(a, b)
+    assert q.error_iterations == p.error_iterations and q.error == 0.125
+    assert len(q.object_iterations) == 2 and len(q.probe_iterations[0]) == len(p._probes_all)
+    assert q.sampling == pytest.approx(p.sampling)
+    assert q._num_slices == p._num_slices and q._num_measurements == p._num_measurements
+    # the saved datacubes come back: preprocess() again from the saved state
+    q.preprocess(**meta["preprocess"])
+    np.testing.assert_array_equal(q._amplitudes, p._amplitudes)
+    np.testing.assert_array_equal(q._object, p._object)  # the saved volume as the guess
+    for a, b in zip(q._probes_all, p._probes_all):
+        np.testing.assert_array_equal(a, b)
