@@ -576,17 +576,19 @@ class PtychographicTomography(_PtychographyBase):
                     ops.expand(sliced, sliced_old, vol, 2)
                     ops.constraints(vol, shrinkage_rad, object_positivity)
                 old = rot
-                # float64 error as the reference forms it: float32 mean intensity
-                # times the tilt's pattern count (an int64) is a float64
-                measurement_error = float(engine.read_error(states[index]))
-                measurement_error /= np.float64(self._mean_diffraction_intensity[index]) * \
-                    np.float64(end - start)
-                error += measurement_error
             ops.rotate(vol, vol, np.asarray(old).T, 0)
-            error /= n_meas
             if collective is not None:
                 ops.add_scaled(vol, collective, n_meas)
                 ops.constraints(vol, shrinkage_rad, object_positivity)
+            # every tilt keeps its own error sum: one read-back per iteration.
+            # float64 error as the reference forms it: float32 mean intensity
+            # times the tilt's pattern count (an int64) is a float64
+            sums = torch.cat([states[i].error_accum for i in indices]).cpu().numpy()
+            for index, batch_sum in zip(indices, sums):
+                count = np.float64(cum[index + 1] - cum[index])
+                error += float(batch_sum) / (
+                    np.float64(self._mean_diffraction_intensity[index]) * count)
+            error /= n_meas
             self.error_iterations.append(float(error))
             if store_iterations:
                 self.object_iterations.append(vol.cpu().numpy())

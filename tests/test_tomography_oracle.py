@@ -140,3 +140,30 @@ def test_constructor_checks():
     with pytest.raises(ValueError):
         PtychographicTomography(energy=300e3, num_slices=2,
                                 tilt_orientation_matrices=[np.eye(3)], not_a_parameter=1.0)
+
+
+def test_reset_semantics():
+    """MultipleMeasurementsMethodsMixin._reset_reconstruction
+    (ptychographic_methods.py:3409-3462): reset=True restores the initial
+    volume, probes and positions; reset=None after a run warns and continues."""
+    p, _, _ = preprocessed("tomo_gd_sequential")
+    vol0 = p._object.copy()
+    probes0 = [pr.copy() for pr in p._probes_all]
+    pos0 = p._positions_px_all.copy()
+    p._object += 1.0
+    p._probes_all = [pr * 2 for pr in p._probes_all]
+    p._positions_px_all += 0.5
+    p.error = 0.1
+    p.error_iterations = [0.2, 0.1]
+    with pytest.warns(UserWarning, match="Continuing"):
+        p._reset_tomography(store_iterations=False, reset=None)
+    assert p.error_iterations == [0.2, 0.1]
+    p._reset_tomography(store_iterations=True, reset=True)
+    assert p.error_iterations == [] and p.object_iterations == [] and p.probe_iterations == []
+    np.testing.assert_array_equal(p._object, vol0)
+    np.testing.assert_array_equal(p._positions_px_all, pos0)
+    for a, b in zip(p._probes_all, probes0):
+        np.testing.assert_array_equal(a, b)
+    # the initial arrays are copies: changing the state leaves them alone
+    p._object += 1.0
+    np.testing.assert_array_equal(p._object_initial, vol0)
