@@ -514,6 +514,10 @@ class PtychographicTomography(_PtychographyBase):
             amps_dev = torch.from_numpy(np.ascontiguousarray(amplitudes, dtype=np.float32)).to(dev)
 
         T = self._num_slices
+        # a batch never spans tilts: the workspace holds the largest batch one tilt
+        # forms (max_batch_size=None means the whole scan, i.e. each tilt in one batch)
+        largest_tilt = int(np.max(np.diff(cum))) if n_meas else 1
+        ws_batch = max(1, min(int(max_batch_size), largest_tilt))
         vol = torch.from_numpy(np.ascontiguousarray(self._object, dtype=np.float32)).to(dev)
         ops = VolumeOps(vol.shape, T, dev)
         roi = tuple(int(v) for v in self._region_of_interest_shape)
@@ -525,7 +529,7 @@ class PtychographicTomography(_PtychographyBase):
                 st = engine.create_state(
                     roi_shape=roi, object_array=sliced_np, probe_array=self._probes_all[0],
                     amplitudes=amps_dev[start:end], positions_px=self._positions_px_all[start:end],
-                    num_slices=T, num_probes=1, potential=True, max_batch=int(max_batch_size),
+                    num_slices=T, num_probes=1, potential=True, max_batch=ws_batch,
                     storage="gpu", propagators=self._propagator_arrays,
                     detector_mask=detector_fourier_mask)
                 base = st
@@ -543,7 +547,7 @@ class PtychographicTomography(_PtychographyBase):
                     order_pinned=None, order_events=None, extra={})
             states.append(st)
             drivers.append(engine.IterationDriver(
-                st, max_batch=int(max_batch_size), step_size=step_size,
+                st, max_batch=ws_batch, step_size=step_size,
                 normalization_min=normalization_min, fix_probe=fix_probe, positivity=False,
                 fix_probe_com=False, object_constraints=False,
                 mean_intensity=self._mean_diffraction_intensity[index], graph=False))
