@@ -417,6 +417,19 @@ TOMO_CASES = {
 }
 
 
+# Tomography preprocess only: one 2D positions mask for every tilt (tiled by
+# the reference, with a warning) and forced centre-of-mass shifts for the first
+# tilt.
+TOMO_PRE_CASES = {
+    "tomo_pre_mask_shifts": dict(
+        seeds=(45, 46), tilts_deg=(-5.0, 6.0), mask_seed=9,
+        gen=dict(scan_shape=(8, 8), step_ang=0.5, jitter_ang=0.05, detector=48,
+                 object_px=64, num_slices=2, slice_thickness=10.0),
+        ctor=dict(num_slices=3, object_padding_px=(8, 8)),
+        pre_extra=dict(force_com_shifts=[[23.6, 24.3], None])),
+}
+
+
 def smooth_volume(shape, seed, peak):
     """Seeded smooth positive potential volume, values in [0.2, 1] x peak."""
     rng = np.random.default_rng(seed)
@@ -518,6 +531,45 @@ def make_tomo_case(ref, name, spec):
     print(f"{name}: {os.path.getsize(path) / 1e6:.2f} MB, errors {out['error_iterations']}")
 
 
+def make_tomo_pre_case(ref, name, spec):
+    cases = [synthetic.make_scan(name="tomo", seed=sd, **spec["gen"]) for sd in spec["seeds"]]
+    dcs = [ref.DataCube(c.datacube.data, r_pixel_size=c.datacube.calibration.get_R_pixel_size(),
+                        r_pixel_units="A", q_pixel_size=c.datacube.calibration.get_Q_pixel_size(),
+                        q_pixel_units="mrad") for c in cases]
+    mats = np.stack([tilt_matrix(a) for a in spec["tilts_deg"]])
+    positions = np.stack([c.scan_positions_ang for c in cases])
+    mask = np.random.default_rng(spec["mask_seed"]).random(spec["gen"]["scan_shape"]) > 0.15
+    ctor = dict(energy=300e3, semiangle_cutoff=20.0, defocus=100.0, **spec["ctor"])
+    pre_args = dict(plot_probe_overlaps=False, diffraction_patterns_rotate_degrees=0.0,
+                    diffraction_patterns_transpose=False, **spec["pre_extra"])
+    cls = tomography_class(ref)
+    # the reference indexes the scan positions with the mask: masked positions
+    p = cls(tilt_orientation_matrices=list(mats), datacube=dcs,
+            initial_scan_positions=[pos[mask.ravel()] for pos in positions],
+            positions_mask=mask.copy(), verbose=False, device="cpu", **ctor)
+    # the reference writes the per-tilt shifts it used back into the list it got
+    p.preprocess(**json.loads(json.dumps(pre_args)))
+    pre = dict(
+        mean_intensity=np.asarray(p._mean_diffraction_intensity, dtype=np.float32),
+        positions_px=np.asarray(p._positions_px_all).copy(),
+        cum_counts=np.asarray(p._cum_probes_per_measurement),
+        probe_initial=np.stack(p._probes_all).copy(),
+        object_initial=p._object.copy(),
+        amplitude_sums=np.asarray(p._amplitudes).sum(axis=(-2, -1)),
+        propagators=np.asarray(p._propagator_arrays).copy(),
+    )
+    data = np.stack([c.datacube.data for c in cases])
+    meta = dict(ctor=ctor, preprocess=pre_args, tilts_deg=spec["tilts_deg"], seeds=spec["seeds"],
+                generator=spec["gen"],
+                r_pixel_size=[c.datacube.calibration.get_R_pixel_size() for c in cases],
+                q_pixel_size=[c.datacube.calibration.get_Q_pixel_size() for c in cases])
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(
+        path, datacube=data.astype(np.uint16), scan_positions_ang=positions, tilt_matrices=mats,
+        positions_mask=mask, meta=json.dumps(meta), **{f"pre_{k}": v for k, v in pre.items()})
+    print(f"{name}: {os.path.getsize(path) / 1e6:.2f} MB, patterns {pre['cum_counts']}")
+
+
 def make_volume_ops(ref):
     """The reference's own volume operations on a seeded random volume:
     _rotate_zxy_volume (float32 and float64 input), _project_sliced_object and
@@ -560,6 +612,9 @@ def main():
     for name, spec in TOMO_CASES.items():
         if not only or name in only:
             make_tomo_case(ref, name, spec)
+    for name, spec in TOMO_PRE_CASES.items():
+        if not only or name in only:
+            make_tomo_pre_case(ref, name, spec)
     if not only or "tomo_volume_ops" in only:
         make_volume_ops(ref)
 

@@ -167,3 +167,30 @@ def test_reset_semantics():
     # the initial arrays are copies: changing the state leaves them alone
     p._object += 1.0
     np.testing.assert_array_equal(p._object_initial, vol0)
+
+
+def test_host_preprocess_mask_and_shifts_match_reference():
+    """One 2D positions mask for every tilt (tiled, with the reference's
+    warning) and forced centre-of-mass shifts for the first tilt only."""
+    from py4dstem_gb300 import DataCube, PtychographicTomography
+
+    f, meta = load_case("tomo_pre_mask_shifts")
+    mask = f["positions_mask"]
+    dcs = [DataCube(f["datacube"][i].astype(np.float32), r_pixel_size=meta["r_pixel_size"][i],
+                    r_pixel_units="A", q_pixel_size=meta["q_pixel_size"][i],
+                    q_pixel_units="mrad") for i in range(len(meta["seeds"]))]
+    p = PtychographicTomography(
+        tilt_orientation_matrices=list(f["tilt_matrices"]), datacube=dcs,
+        initial_scan_positions=[pos[mask.ravel()] for pos in f["scan_positions_ang"]],
+        positions_mask=mask, verbose=False, device="cpu", **meta["ctor"])
+    with pytest.warns(UserWarning, match="assumed the same for all measurements"):
+        p.preprocess(**meta["preprocess"])
+    np.testing.assert_array_equal(p._cum_probes_per_measurement, f["pre_cum_counts"])
+    assert np.array_equal(np.asarray(p._mean_diffraction_intensity, np.float32),
+                          f["pre_mean_intensity"])
+    assert np.array_equal(p._positions_px_all, f["pre_positions_px"])
+    assert np.array_equal(np.stack(p._probes_all), f["pre_probe_initial"])
+    assert np.array_equal(p._object, f["pre_object_initial"])
+    assert np.array_equal(p._amplitudes.astype(np.float64).sum(axis=(-2, -1)),
+                          f["pre_amplitude_sums"])
+    assert np.array_equal(p._propagator_arrays, f["pre_propagators"])
