@@ -419,6 +419,19 @@ int ptycho_volume_constraints(float* volume, int64_t count, float shrinkage,
                               int32_t apply_shrinkage, int32_t positivity, void* stream);
 
 /*
+ * The per-iteration error read-back: copies the device float *error_accum (the
+ * sum the batch calls add to) into *value, after the work queued on `stream`
+ * has finished, and returns PTYCHO_ERR_NONFINITE when it is NaN or infinite.
+ * A batch call makes its error sum NaN when a scan position is not finite (the
+ * position is then left out of every patch index and, under position
+ * correction, not moved) or when an update produced a NaN or infinite object or
+ * probe value; NaN or infinite amplitudes, probes or objects reach the sum
+ * through the forward model. Replaces the error read of reconstruct()
+ * (singleslice_ptychography.py:929-932), the one synchronisation per iteration.
+ */
+int ptycho_read_error(const float* error_accum, float* value, void* stream);
+
+/*
  * Instrumentation. When enabled, every launch of the fused per-position kernel
  * is bracketed by CUDA events recorded on its stream; ptycho_kernel_timing()
  * waits for the last one and returns the summed kernel time (ms) and the number
@@ -438,7 +451,10 @@ int ptycho_kernel_timing(float* total_ms, int32_t* launches);
  * PTYCHO_ERR_WORKSPACE. The first call on a device looks up the array's
  * address and should come before any stream capture. All calls share the
  * array: calls that can overlap on the GPU must be serialised on one stream.
- * No counterpart in the reference (its CuPy path always allocates).
+ * The batch-chaining flags PTYCHO_FLAG_SPECTRUM_READY, PTYCHO_FLAG_PREPARE_SPECTRUM
+ * and PTYCHO_FLAG_KEEP_FARFIELD are refused (PTYCHO_ERR_INVALID_ARGUMENT): each
+ * call computes its own probe spectrum. No counterpart in the reference (its
+ * CuPy path always allocates).
  */
 int ptycho_gd_batch_noalloc(const ptycho_geometry* geometry, void* object, void* probe,
                             const float* amplitudes, const int32_t* amplitude_rows,

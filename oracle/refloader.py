@@ -36,7 +36,9 @@ from unittest import mock
 
 import numpy as np
 
-DEFAULT_REFERENCE_ROOT = "/root/reference"
+# The checkout's location comes from the caller or from this variable; nothing
+# in this module assumes a path.
+REFERENCE_ENV = "PY4DSTEM_REFERENCE"
 
 _MOCKED_PREFIXES = (
     "matplotlib",
@@ -208,7 +210,10 @@ def load_reference(root: str | None = None):
     ``MixedstateMultislicePtychography``, ``PtychographicTomography``, ``DataCube`` (the
     duck type above), ``utils`` (``process/phase/utils.py``) and ``root``.
     """
-    root = root or os.environ.get("PY4DSTEM_REFERENCE", DEFAULT_REFERENCE_ROOT)
+    root = root or os.environ.get(REFERENCE_ENV)
+    if not root:
+        raise ReferenceUnavailable(
+            f"no py4DSTEM source checkout given: pass root= or set {REFERENCE_ENV}")
     if root in _LOADED:
         return _LOADED[root]
     pkg_root = os.path.join(root, "py4DSTEM")

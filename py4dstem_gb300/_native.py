@@ -13,6 +13,7 @@ import threading
 from . import build as _build
 
 PTYCHO_OK = 0
+PTYCHO_ERR_NONFINITE = 5
 FLAG_MIXED_STATE = 1
 FLAG_KEEP_FARFIELD = 2
 FLAG_SPECTRUM_READY = 4
@@ -118,6 +119,7 @@ _SIGNATURES = {
         [_vp, _vp, _i32, _i32, _i32, _i32, _vp, _i32, _vp], ctypes.c_int),
     "ptycho_volume_add_scaled": ([_vp, _vp, ctypes.c_int64, _i32, _vp], ctypes.c_int),
     "ptycho_volume_constraints": ([_vp, ctypes.c_int64, _f32, _i32, _i32, _vp], ctypes.c_int),
+    "ptycho_read_error": ([_vp, ctypes.POINTER(_f32), _vp], ctypes.c_int),
     "ptycho_gd_batch_noalloc": (
         [ctypes.POINTER(Geometry), _vp, _vp, _vp, _vp, _vp, _vp, _i32, _f32, _f32, _i32,
          _vp, _vp, _vp, _vp],

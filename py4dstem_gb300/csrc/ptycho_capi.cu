@@ -4,10 +4,13 @@
 // on the caller's stream.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <utility>
 #include <vector>
 
 #include "../../include/ptycho_gb300.h"
@@ -70,7 +73,23 @@ int check_geometry(const ptycho_geometry* g) {
   return PTYCHO_OK;
 }
 
+std::mutex g_smem_mu;
+std::map<std::pair<int, const void*>, int> g_smem_limits;  // (device, kernel) -> bytes set
+
 }  // namespace
+
+cudaError_t ensure_smem_limit(const void* fn, int bytes) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(g_smem_mu);
+  auto it = g_smem_limits.find({dev, fn});
+  if (it != g_smem_limits.end() && it->second >= bytes) return cudaSuccess;
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return e;
+  g_smem_limits[{dev, fn}] = bytes;
+  return cudaSuccess;
+}
 
 Workspace workspace_layout(int Sx, int Sy, int Px, int Py, int T, int M, int B,
                            bool keep_farfield) {
@@ -449,6 +468,23 @@ int ptycho_set_kernel_schedule(int32_t roi, int32_t schedule) {
   return set_schedule(roi, schedule);
 }
 
+int ptycho_read_error(const float* error_accum, float* value, void* stream) {
+  if (!error_accum || !value)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "error_accum and value must be non-null");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  float v = 0.0f;
+  cudaError_t e = cudaMemcpyAsync(&v, error_accum, sizeof(float), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "error read-back");
+  *value = v;
+  if (!std::isfinite(v))
+    return fail(PTYCHO_ERR_NONFINITE,
+                "the error sum is %s: a scan position, amplitude, probe or object value is "
+                "NaN or infinite, or an update overflowed",
+                std::isnan(v) ? "NaN" : "infinite");
+  return PTYCHO_OK;
+}
+
 int ptycho_enable_kernel_timing(int32_t enable) {
   std::lock_guard<std::mutex> lk(g_timing_mu);
   g_timing_on = enable != 0;
@@ -817,8 +853,15 @@ int ptycho_volume_constraints(float* volume, int64_t count, float shrinkage,
 //  - Every call on a device uses the same array. Two calls that may run at the
 //    same time on the GPU (different streams or host threads) overwrite each
 //    other's scratch: issue them in order on one stream.
-//  - The kernels write every scratch byte they read within the call, so no
-//    part of the array has to start at zero; nothing is cleared between calls.
+//  - Within one call the kernels write every scratch byte before they read it,
+//    so no part of the array has to start at zero and nothing is cleared
+//    between calls. That holds only while no call reads what an earlier call
+//    left behind, so the batch-chaining flags are refused here:
+//    PTYCHO_FLAG_SPECTRUM_READY (would read a probe spectrum left by the
+//    previous call, which may belong to another probe or geometry),
+//    PTYCHO_FLAG_PREPARE_SPECTRUM (prepares one for such a read) and
+//    PTYCHO_FLAG_KEEP_FARFIELD (keeps far fields for a position-correction call
+//    that cannot be given this array).
 namespace {
 constexpr size_t kNoallocScratchBytes = size_t(32) << 20;
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
@@ -835,6 +878,12 @@ extern "C" int ptycho_gd_batch_noalloc(const ptycho_geometry* g, void* object, v
                                        void* stream) {
   int st = check_geometry(g);
   if (st != PTYCHO_OK) return st;
+  if (g->flags & (PTYCHO_FLAG_SPECTRUM_READY | PTYCHO_FLAG_PREPARE_SPECTRUM |
+                  PTYCHO_FLAG_KEEP_FARFIELD))
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT,
+                "ptycho_gd_batch_noalloc does not take PTYCHO_FLAG_SPECTRUM_READY, "
+                "PTYCHO_FLAG_PREPARE_SPECTRUM or PTYCHO_FLAG_KEEP_FARFIELD (they pass data "
+                "between calls through the scratch, which every call shares)");
   if (batch < 1) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "batch must be >= 1 (got %d)", batch);
   const size_t need = ptycho_workspace_bytes(g, batch);
   if (need > kNoallocScratchBytes)

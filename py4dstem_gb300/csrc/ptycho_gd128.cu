@@ -265,8 +265,9 @@ __global__ void __launch_bounds__(NT, 1) gd128_kernel(BatchArgs a) {
   const int tid = threadIdx.x;
   const int prow = a.pos_rows ? a.pos_rows[b] : b;
   const int arow = a.amp_rows ? a.amp_rows[b] : b;
-  const float posx = a.positions[2 * prow];
-  const float posy = a.positions[2 * prow + 1];
+  const bool pos_ok = isfinite(a.positions[2 * prow]) && isfinite(a.positions[2 * prow + 1]);
+  const float posx = finite_or_zero(a.positions[2 * prow]);
+  const float posy = finite_or_zero(a.positions[2 * prow + 1]);
   const float rx = rintf(posx);
   const float ry = rintf(posy);
   const float dx = posx - rx;
@@ -421,7 +422,7 @@ __global__ void __launch_bounds__(NT, 1) gd128_kernel(BatchArgs a) {
     float t = 0.0f;
 #pragma unroll
     for (int w = 0; w < NT / 32; ++w) t += red[w];
-    a.err[b] = t;
+    a.err[b] = pos_ok ? t : __int_as_float(0x7fc00000);
   }
 }
 
@@ -448,12 +449,11 @@ bool position_v2_eligible(const BatchArgs& a) {
 
 cudaError_t launch_position_v2(const BatchArgs& a, cudaStream_t s) {
   const size_t smem = sizeof(float2) * N;
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(gd128_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = true;
+  {
+    const cudaError_t e0 =
+        ensure_smem_limit(reinterpret_cast<const void*>(gd128_kernel),
+                          (int)smem);
+    if (e0 != cudaSuccess) return e0;
   }
   timing_before(s);
   gd128_kernel<<<a.B, NT, smem, s>>>(a);

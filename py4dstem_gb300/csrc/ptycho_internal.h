@@ -87,6 +87,17 @@ void bind_workspace(BatchArgs& a, void* base, const Workspace& w);
 
 bool roi_supported(int Sx, int Sy);
 
+// A scan coordinate as the kernels use it. NaN and infinite coordinates have no
+// patch: they are replaced by 0, so every object index derived from them stays
+// inside the object, and the kernel reading them marks the position's error NaN
+// (reported by ptycho_read_error as PTYCHO_ERR_NONFINITE).
+__device__ __forceinline__ float finite_or_zero(float v) { return isfinite(v) ? v : 0.0f; }
+
+// Raises the dynamic shared-memory limit of kernel `fn` to at least `bytes` on
+// the current device. Function attributes are per device, so the setting is
+// made once per (device, kernel) pair and remembered under a mutex.
+cudaError_t ensure_smem_limit(const void* fn, int bytes);
+
 // Position-kernel timing (instrumentation); implemented in ptycho_capi.cu.
 void timing_before(cudaStream_t s);
 void timing_after(cudaStream_t s);

@@ -136,8 +136,9 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
   const int M = kM1 ? 1 : a.M;
   const int prow = a.pos_rows ? a.pos_rows[b] : b;
   const int arow = a.amp_rows ? a.amp_rows[b] : b;
-  const float posx = a.positions[2 * prow];
-  const float posy = a.positions[2 * prow + 1];
+  const bool pos_ok = isfinite(a.positions[2 * prow]) && isfinite(a.positions[2 * prow + 1]);
+  const float posx = finite_or_zero(a.positions[2 * prow]);
+  const float posy = finite_or_zero(a.positions[2 * prow + 1]);
   const float rx = rintf(posx);  // numpy.round: half to even
   const float ry = rintf(posy);
   const float dx = posx - rx;
@@ -669,7 +670,7 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
 
 done:
   const float tot = block_sum<NT>(err, red);
-  if (tid == 0) a.err[b] = tot;
+  if (tid == 0) a.err[b] = pos_ok ? tot : __int_as_float(0x7fc00000);
 }
 
 // One block per position. (A persistent form, one block per SM walking the
@@ -730,8 +731,9 @@ __global__ void __launch_bounds__(NT, 1) position_correction_kernel(BatchArgs a)
   const int M = a.M;
   const int prow = a.pos_rows ? a.pos_rows[b] : b;
   const int arow = a.amp_rows ? a.amp_rows[b] : b;
-  const float posx = a.positions_rw[2 * prow];
-  const float posy = a.positions_rw[2 * prow + 1];
+  const bool pos_ok = isfinite(a.positions_rw[2 * prow]) && isfinite(a.positions_rw[2 * prow + 1]);
+  const float posx = finite_or_zero(a.positions_rw[2 * prow]);
+  const float posy = finite_or_zero(a.positions_rw[2 * prow + 1]);
   const float rx = rintf(posx);
   const float ry = rintf(posy);
   const float dx = posx - rx;
@@ -880,20 +882,21 @@ __global__ void __launch_bounds__(NT, 1) position_correction_kernel(BatchArgs a)
       const float dist = sqrtf(__fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(ddy, ddy)));
       if ((double)dist > a.pc_max_total) ux = uy = 0.0f;
     }
-    a.positions_rw[2 * prow] = __fsub_rn(posx, ux);
-    a.positions_rw[2 * prow + 1] = __fsub_rn(posy, uy);
+    if (pos_ok) {  // a non-finite position stays as it is (its error is already NaN)
+      a.positions_rw[2 * prow] = __fsub_rn(posx, ux);
+      a.positions_rw[2 * prow + 1] = __fsub_rn(posy, uy);
+    }
   }
 }
 
 template <int SX, int SY, int NT>
 cudaError_t launch_correction_t(const BatchArgs& a, cudaStream_t s) {
   const size_t smem = Layout<SX, SY>::smem_bytes(false);
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(position_correction_kernel<SX, SY, NT>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = true;
+  {
+    const cudaError_t e0 =
+        ensure_smem_limit(reinterpret_cast<const void*>(position_correction_kernel<SX, SY, NT>),
+                          (int)smem);
+    if (e0 != cudaSuccess) return e0;
   }
   position_correction_kernel<SX, SY, NT><<<a.B, NT, smem, s>>>(a);
   return cudaGetLastError();
@@ -935,8 +938,8 @@ __global__ void __launch_bounds__(NT, 1) probe_intensity_kernel(BatchArgs a) {
   float2* rpy = rpx + SX;
   const int tid = threadIdx.x;
   const int b = blockIdx.x;
-  const float posx = a.positions[2 * b];
-  const float posy = a.positions[2 * b + 1];
+  const float posx = finite_or_zero(a.positions[2 * b]);
+  const float posy = finite_or_zero(a.positions[2 * b + 1]);
   const float rx = rintf(posx);
   const float ry = rintf(posy);
   const float dx = posx - rx;
@@ -971,12 +974,11 @@ __global__ void __launch_bounds__(NT, 1) probe_intensity_kernel(BatchArgs a) {
 template <int SX, int SY, int NT>
 cudaError_t launch_probe_intensity_t(const BatchArgs& a, cudaStream_t s) {
   const size_t smem = Layout<SX, SY>::smem_bytes(false);
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(probe_intensity_kernel<SX, SY, NT>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = true;
+  {
+    const cudaError_t e0 =
+        ensure_smem_limit(reinterpret_cast<const void*>(probe_intensity_kernel<SX, SY, NT>),
+                          (int)smem);
+    if (e0 != cudaSuccess) return e0;
   }
   probe_intensity_kernel<SX, SY, NT><<<a.B, NT, smem, s>>>(a);
   return cudaGetLastError();
@@ -1045,12 +1047,11 @@ __global__ void __launch_bounds__(NT, 1) probe_aperture_kernel(BatchArgs a) {
 template <int SX, int SY, int NT>
 cudaError_t launch_probe_aperture_t(const BatchArgs& a, cudaStream_t s) {
   const size_t smem = Layout<SX, SY>::smem_bytes(false);
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(probe_aperture_kernel<SX, SY, NT>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = true;
+  {
+    const cudaError_t e0 =
+        ensure_smem_limit(reinterpret_cast<const void*>(probe_aperture_kernel<SX, SY, NT>),
+                          (int)smem);
+    if (e0 != cudaSuccess) return e0;
   }
   probe_aperture_kernel<SX, SY, NT><<<1, NT, smem, s>>>(a);
   return cudaGetLastError();
@@ -1059,12 +1060,11 @@ cudaError_t launch_probe_aperture_t(const BatchArgs& a, cudaStream_t s) {
 template <int SX, int SY, int NT>
 cudaError_t launch_probe_inverse_t(const BatchArgs& a, cudaStream_t s) {
   const size_t smem = Layout<SX, SY>::smem_bytes(false);
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(probe_inverse_kernel<SX, SY, NT>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = true;
+  {
+    const cudaError_t e0 =
+        ensure_smem_limit(reinterpret_cast<const void*>(probe_inverse_kernel<SX, SY, NT>),
+                          (int)smem);
+    if (e0 != cudaSuccess) return e0;
   }
   probe_inverse_kernel<SX, SY, NT><<<a.M, NT, smem, s>>>(a);
   return cudaGetLastError();
@@ -1073,13 +1073,11 @@ cudaError_t launch_probe_inverse_t(const BatchArgs& a, cudaStream_t s) {
 template <int SX, int SY, int NT>
 cudaError_t launch_spectrum_t(const BatchArgs& a, cudaStream_t s) {
   const size_t smem = Layout<SX, SY>::smem_bytes(false);
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(probe_spectrum_kernel<SX, SY, NT>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)Layout<SX, SY>::smem_bytes(true));
-    if (e != cudaSuccess) return e;
-    configured = true;
+  {
+    const cudaError_t e0 =
+        ensure_smem_limit(reinterpret_cast<const void*>(probe_spectrum_kernel<SX, SY, NT>),
+                          (int)Layout<SX, SY>::smem_bytes(true));
+    if (e0 != cudaSuccess) return e0;
   }
   probe_spectrum_kernel<SX, SY, NT><<<a.M, NT, smem, s>>>(a);
   return cudaGetLastError();
@@ -1090,17 +1088,17 @@ cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
   const bool mixed_ms = a.T > 1 && a.M > 1;
   const bool mixed = (a.T == 1 && (a.M > 1 || a.mixed_formula)) || mixed_ms;
   const size_t smem = Layout<SX, SY>::smem_bytes(mixed);
-  static bool configured = false;
-  if (!configured) {
+  {
     const int bytes = (int)Layout<SX, SY>::smem_bytes(true);
-    const cudaFuncAttribute attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    cudaError_t e = cudaFuncSetAttribute(position_kernel<SX, SY, NT, 0>, attr, bytes);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(position_kernel<SX, SY, NT, 1>, attr, bytes);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(position_kernel<SX, SY, NT, 2>, attr, bytes);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(position_kernel<SX, SY, NT, 3>, attr, bytes);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(position_kernel<SX, SY, NT, 4>, attr, bytes);
-    if (e != cudaSuccess) return e;
-    configured = true;
+    const void* modes[5] = {reinterpret_cast<const void*>(position_kernel<SX, SY, NT, 0>),
+                            reinterpret_cast<const void*>(position_kernel<SX, SY, NT, 1>),
+                            reinterpret_cast<const void*>(position_kernel<SX, SY, NT, 2>),
+                            reinterpret_cast<const void*>(position_kernel<SX, SY, NT, 3>),
+                            reinterpret_cast<const void*>(position_kernel<SX, SY, NT, 4>)};
+    for (const void* fn : modes) {
+      const cudaError_t e0 = ensure_smem_limit(fn, bytes);
+      if (e0 != cudaSuccess) return e0;
+    }
   }
   // plain gradient-descent batches run an instantiation with the other modes
   // compiled out (see position_one); mixed-state multislice has its own

@@ -82,6 +82,13 @@ __device__ __forceinline__ float normaliser(float s, float smax, float m) {
   return 1.0f / sqrtf(__fadd_rn(__fadd_rn(1e-16f, __fmul_rn(a, a)), __fmul_rn(c, c)));
 }
 
+// A NaN or infinite object or probe value after an update makes the batch's
+// error sum NaN, so the per-iteration error read-back (ptycho_read_error)
+// reports PTYCHO_ERR_NONFINITE. Finite values leave the sum untouched.
+__device__ __forceinline__ void mark_nonfinite(const BatchArgs& a, float2 v) {
+  if (!(isfinite(v.x) && isfinite(v.y))) atomicAdd(a.error_accum, __int_as_float(0x7fc00000));
+}
+
 // ------------------------------------------------------------------ object side
 constexpr int kListChunk = 2048;
 
@@ -241,7 +248,9 @@ __global__ void __launch_bounds__(NT) object_update_kernel(BatchArgs a, int ntil
     const int hi = min(a.B, lo + per);
     for (int i = lo; i < hi; ++i) e += a.err[i];
     const float tot = block_sum_all(e, red);
-    if (threadIdx.x == 0) a.error_accum[0] = a.error_accum[0] + tot;
+    // atomic only so that a concurrent non-finite mark (below, or from the
+    // probe side) cannot be overwritten; one add per batch keeps the order
+    if (threadIdx.x == 0) atomicAdd(a.error_accum, tot);
   }
 
   const size_t P = (size_t)a.Px * a.Py;
@@ -251,21 +260,24 @@ __global__ void __launch_bounds__(NT) object_update_kernel(BatchArgs a, int ntil
   const float nrm = normaliser(a.obj_nrm[o], smax, a.norm_min);
   const float2 g = a.obj_grad[o];
   const bool mixed_order = a.M > 1 || a.mixed_formula;
+  float2 r;
   if (a.potential) {
     float* obj = reinterpret_cast<float*>(a.object);
     if (a.projection) {
-      obj[o] = __fmul_rn(g.x, nrm);
+      r.x = __fmul_rn(g.x, nrm);
     } else if (mixed_order) {
-      obj[o] = __fadd_rn(obj[o], __fmul_rn(__fmul_rn(a.step, g.x), nrm));
+      r.x = __fadd_rn(obj[o], __fmul_rn(__fmul_rn(a.step, g.x), nrm));
     } else {
-      obj[o] = __fadd_rn(obj[o], __fmul_rn(a.step, __fmul_rn(g.x, nrm)));
+      r.x = __fadd_rn(obj[o], __fmul_rn(a.step, __fmul_rn(g.x, nrm)));
     }
+    r.y = 0.0f;
+    obj[o] = r.x;
   } else {
     float2* obj = reinterpret_cast<float2*>(a.object);
     float2 u;
     if (a.projection) {
       u = make_float2(__fmul_rn(g.x, nrm), __fmul_rn(g.y, nrm));
-      obj[o] = u;
+      r = u;
     } else {
       if (mixed_order) {
         u = make_float2(__fmul_rn(__fmul_rn(a.step, g.x), nrm), __fmul_rn(__fmul_rn(a.step, g.y), nrm));
@@ -273,9 +285,11 @@ __global__ void __launch_bounds__(NT) object_update_kernel(BatchArgs a, int ntil
         u = make_float2(__fmul_rn(a.step, __fmul_rn(g.x, nrm)), __fmul_rn(a.step, __fmul_rn(g.y, nrm)));
       }
       const float2 v = obj[o];
-      obj[o] = make_float2(__fadd_rn(v.x, u.x), __fadd_rn(v.y, u.y));
+      r = make_float2(__fadd_rn(v.x, u.x), __fadd_rn(v.y, u.y));
     }
+    obj[o] = r;
   }
+  mark_nonfinite(a, r);
 }
 
 // overlap += the batch's |P|^2 sums (chunk partials added in chunk order): the
@@ -369,6 +383,7 @@ __global__ void __launch_bounds__(NT) probe_update_kernel(BatchArgs a, int nbloc
       const float2 v = a.probe[o];
       a.probe[o] = make_float2(__fadd_rn(v.x, u.x), __fadd_rn(v.y, u.y));
     }
+    mark_nonfinite(a, a.probe[o]);
   }
 }
 
@@ -555,12 +570,11 @@ __global__ void __launch_bounds__(NTF, 1) probe_shift_kernel(BatchArgs a) {
 template <int SX, int SY, int NTF>
 cudaError_t launch_shift_t(const BatchArgs& a, cudaStream_t s) {
   const size_t smem = sizeof(float2) * (size_t)(SX * (SY + 1) + 2 * SX + 2 * SY);
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(probe_shift_kernel<SX, SY, NTF>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = true;
+  {
+    const cudaError_t e0 =
+        ensure_smem_limit(reinterpret_cast<const void*>(probe_shift_kernel<SX, SY, NTF>),
+                          (int)smem);
+    if (e0 != cudaSuccess) return e0;
   }
   probe_shift_kernel<SX, SY, NTF><<<a.M, NTF, smem, s>>>(a);
   return cudaGetLastError();

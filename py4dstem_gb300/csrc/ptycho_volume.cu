@@ -292,19 +292,18 @@ cudaError_t launch_volume_rotate(const void* in, int in_is_double, void* out, in
   for (int k = 0; k < 9; ++k) tf.m[k] = matrix[k];
   for (int k = 0; k < 3; ++k) tf.off[k] = offset[k];
   volume_load_kernel<<<grid_for(total), kThreads, 0, s>>>(in, in_is_double, scratch, total);
-  static int smem_optin = -1;
-  if (smem_optin < 0) {
+  int smem_optin = 0;
+  {
+    // the staged prefilter may use up to the device's opt-in limit of dynamic
+    // shared memory; the attribute is set per device
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess)
       e = cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(spline_prefilter_staged_kernel,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin);
-    if (e != cudaSuccess) {
-      smem_optin = -1;
-      return e;
-    }
+      e = ensure_smem_limit(reinterpret_cast<const void*>(spline_prefilter_staged_kernel),
+                            smem_optin);
+    if (e != cudaSuccess) return e;
   }
   const int n[3] = {n0, n1, n2};
   for (int axis = 0; axis < 3; ++axis) {

@@ -91,6 +91,8 @@ def create_state(*, roi_shape, object_array, probe_array, amplitudes, positions_
                  num_slices, num_probes, potential, max_batch, storage="gpu",
                  propagators=None, detector_mask=None, fov_mask_inverse=None,
                  projection=False, mixed_state=False, positions_initial=None) -> DeviceState:
+    if not np.all(np.isfinite(np.asarray(positions_px))):
+        raise ValueError("scan positions contain NaN or infinite values")
     torch = _torch()
     lib = _native.lib()
     dev = torch.device("cuda", torch.cuda.current_device())
@@ -166,6 +168,8 @@ def refresh_state(st: DeviceState, *, object_array, probe_array, positions_px,
     (same shapes), so that kernels and captured graphs that hold its pointers run
     on them."""
     torch = _torch()
+    if not np.all(np.isfinite(np.asarray(positions_px))):
+        raise ValueError("scan positions contain NaN or infinite values")
 
     def put(dst, arr, dtype):
         src = torch.from_numpy(np.ascontiguousarray(arr, dtype=dtype).reshape(tuple(dst.shape)))
@@ -411,7 +415,14 @@ def probe_orthogonalization(st: DeviceState, on_device: bool = False) -> None:
 
 
 def read_error(st: DeviceState) -> np.float32:
-    return np.float32(st.error_accum.item())
+    """The iteration's error sum (one device-to-host synchronisation). Raises
+    _native.PtychoError (a RuntimeError) with status PTYCHO_ERR_NONFINITE when it
+    is NaN or infinite: a non-finite scan position, amplitude, probe or object
+    value, or an update that overflowed."""
+    value = ctypes.c_float(0.0)
+    _native.check(_native.lib().ptycho_read_error(_ptr(st.error_accum), ctypes.byref(value),
+                                                  _stream()))
+    return np.float32(value.value)
 
 
 class IterationDriver:

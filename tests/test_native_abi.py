@@ -145,3 +145,51 @@ def test_self_consistency_argument_checks(lib):
     st = lib.ptycho_self_consistency_errors(ctypes.byref(g), dummy, dummy, dummy, None, dummy,
                                             None, 4, None, dummy, dummy, 1 << 40, None)
     assert st == 1 and b"propagators" in lib.ptycho_last_error()
+
+
+def _noalloc(lib, g, batch):
+    dummy = ctypes.c_void_p(0x1000)
+    return lib.ptycho_gd_batch_noalloc(ctypes.byref(g), dummy, dummy, dummy, None, dummy, None,
+                                       batch, 0.5, 1.0, 0, None, None, dummy, None)
+
+
+def test_noalloc_refuses_batches_beyond_its_scratch(lib):
+    """The no-allocation entry point refuses a batch whose scratch exceeds its
+    fixed 32 MiB array, before any GPU work."""
+    g = _native.Geometry(128, 128, 512, 512, 1, 1, 0, 0)
+    assert lib.ptycho_workspace_bytes(ctypes.byref(g), 4096) > (32 << 20)
+    assert _noalloc(lib, g, 4096) == 3
+    assert b"no-allocation scratch" in lib.ptycho_last_error()
+
+
+@pytest.mark.parametrize("flag", ["FLAG_SPECTRUM_READY", "FLAG_PREPARE_SPECTRUM",
+                                  "FLAG_KEEP_FARFIELD"])
+def test_noalloc_refuses_batch_chaining_flags(lib, flag):
+    """Flags that pass data from one call to the next through the scratch are
+    refused: every no-allocation call shares that scratch."""
+    g = geometry()
+    g.flags = getattr(_native, flag)
+    assert _noalloc(lib, g, 4) == 1
+    assert b"ptycho_gd_batch_noalloc does not take" in lib.ptycho_last_error()
+
+
+def test_read_error_argument_checks(lib):
+    value = ctypes.c_float(0.0)
+    assert lib.ptycho_read_error(None, ctypes.byref(value), None) == 1
+    assert lib.ptycho_read_error(ctypes.c_void_p(0x1000), None, None) == 1
+    assert b"non-null" in lib.ptycho_last_error()
+
+
+def test_nonfinite_positions_rejected_on_the_host():
+    """NaN or infinite scan positions are refused before any device work."""
+    import numpy as np
+
+    from py4dstem_gb300 import engine
+
+    pos = np.zeros((4, 2), np.float32)
+    pos[1, 0] = np.nan
+    with pytest.raises(ValueError, match="NaN or infinite"):
+        engine.create_state(roi_shape=(64, 64), object_array=np.ones((96, 96), np.complex64),
+                            probe_array=np.ones((64, 64), np.complex64),
+                            amplitudes=np.ones((4, 64, 64), np.float32), positions_px=pos,
+                            num_slices=1, num_probes=1, potential=False, max_batch=4)
