@@ -202,14 +202,51 @@ def read_profile_traffic():
     return float(m.group(1)) if m else None
 
 
+# The reference's own reconstruct() on the benchmark scan (seed 1234), written by
+# tests/golden/make_golden.py --size: the bench checks its first iterations
+# against this error history.
+PARITY_FIXTURE = os.path.join(ROOT, "tests", "golden", "size_ss_scan128_det128.npz")
+PARITY_SEED = 1234
+
+
 def build_case(scan, seed, device):
+    """The benchmark scan. The 128 x 128 scan of seed 1234 is generated by the
+    NumPy backend, the same counts the reference reconstructed for the parity
+    fixture; other sizes and seeds use the faster torch backend."""
     from py4dstem_gb300 import synthetic
 
+    numpy_backend = scan == 128 and seed == PARITY_SEED
     case = synthetic.make_scan(
         "bench", seed, (scan, scan), 0.75, 0.05, 128, 512 if scan >= 128 else
-        int(2 ** math.ceil(math.log2(scan * 3 + 128))), dose=1e5, backend="torch",
-        device=device)
+        int(2 ** math.ceil(math.log2(scan * 3 + 128))), dose=1e5,
+        backend="numpy" if numpy_backend else "torch", device=device)
     return case
+
+
+def parity_check(case, batch):
+    """Three iterations of the public API on the benchmark scan against the
+    reference's error history for the same data, seed and batch size (the
+    fixture). Returns None when the fixture does not describe this workload."""
+    if not os.path.exists(PARITY_FIXTURE) or batch != 1024:
+        return None
+    z = np.load(PARITY_FIXTURE)
+    meta = json.loads(str(z["meta"]))
+    gen = meta["generator"]
+    if (gen["seed"] != PARITY_SEED or tuple(gen["scan_shape"]) != (128, 128)
+            or not np.array_equal(case.scan_positions_ang, z["scan_positions_ang"])):
+        return None
+    ref_err = np.asarray(z["out_error_iterations"], dtype=np.float64)
+    p = preprocess(case, storage="gpu")
+    p.reconstruct(progress_bar=False, **meta["reconstruct"])
+    err = np.asarray(p.error_iterations, dtype=np.float64)
+    d = float(np.max(np.abs(err - ref_err) / ref_err))
+    # the reference's own rounding floor on this workload (FFTs through complex128)
+    floor = float(meta["stats"]["floor_err"])
+    tol = max(1e-5, 3.0 * floor)
+    return {"iterations": len(err), "errors": err.tolist(), "reference_errors": ref_err.tolist(),
+            "max_rel_diff": d, "reference_floor": floor, "tolerance": tol, "ok": bool(d <= tol),
+            "reference": "reference reconstruct() on the same counts, seed and batch "
+                         "(tests/golden/size_ss_scan128_det128.npz)"}
 
 
 def preprocess(case, storage, device="gpu"):
@@ -331,15 +368,19 @@ def bench_config(scan, batch, object_shape, world):
 _REF = {}
 
 
-def _ref_init(scan, seed):
-    """Pool initializer: one small scan per worker process, preprocessed once."""
+REF_SCAN = 32  # positions per worker: one batch of 1024
+
+
+def _ref_init(seed):
+    """Pool initializer: each worker process preprocesses (host NumPy path) its
+    own 32 x 32 part of the benchmark workload: 0.75 A step, 128^2 detector, the
+    512^2 object at 0.25 A, 1e5 e-/pattern; 1024 positions = one batch of 1024."""
     from py4dstem_gb300 import synthetic
     from oracle.ptycho_np import Oracle, State
 
     seed = seed + os.getpid() % 1000
-    case = synthetic.make_scan("ref", seed, (scan, scan), 0.75, 0.05, 128,
-                               int(2 ** math.ceil(math.log2(scan * 3 + 128))), dose=1e5,
-                               backend="numpy")
+    case = synthetic.make_scan("ref", seed, (REF_SCAN, REF_SCAN), 0.75, 0.05, 128, 512,
+                               dose=1e5, backend="numpy")
     p = preprocess(case, storage="cpu", device="cpu")  # host NumPy preprocess
     st = State(amplitudes=p._amplitudes, positions_px=p._positions_px.copy(),
                probe=np.array(p._probe), object=np.array(p._object),
@@ -347,21 +388,19 @@ def _ref_init(scan, seed):
                fov_mask_inverse=p._object_fov_mask_inverse)
     _REF["oracle"] = Oracle(st)
     _REF["order"] = np.random.default_rng(seed).permutation(p._num_diffraction_patterns)
-    _REF["done"] = 0
 
 
 def _ref_step(seconds):
-    """Reference-algorithm GD batches of 64 positions for ~`seconds`."""
+    """Whole gradient-descent batches of 1024 positions on the 512^2 object (the
+    benchmark's batch size and object) for at least `seconds`."""
     o, order = _REF["oracle"], _REF["order"]
-    J = len(order)
     done = 0
     t0 = time.perf_counter()
-    while time.perf_counter() - t0 < seconds:
-        start = _REF["done"] % J
-        idx = order[start:start + 64]
-        _run_oracle_batch(o, idx)
-        done += len(idx)
-        _REF["done"] += len(idx)
+    while True:
+        _run_oracle_batch(o, order)
+        done += len(order)
+        if time.perf_counter() - t0 >= seconds:
+            break
     return done, time.perf_counter() - t0
 
 
@@ -374,12 +413,14 @@ def run_reference(args):
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
     if args.ref_cores:
         cores = min(cores, args.ref_cores)
-    # small scans per worker keep the per-process setup short; the per-position
-    # work (128^2 detector GD update) is the workload's
+    # NumPy's FFT, bincount and elementwise loops run on one thread; one worker
+    # process per host core, each on one thread
+    for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[var] = "1"
     per_step = max(1.0, min(20.0, 60.0 / max(1, args.steps + args.warmup)))
     ctx = mp.get_context("spawn")
     values = []
-    with ctx.Pool(cores, initializer=_ref_init, initargs=(16, 100)) as pool:
+    with ctx.Pool(cores, initializer=_ref_init, initargs=(100,)) as pool:
         for i in range(args.warmup + args.steps):
             res = pool.map(_ref_step, [per_step] * cores, chunksize=1)
             tot = sum(r[0] for r in res)
@@ -395,9 +436,10 @@ def run_reference(args):
         "config": bench_config(args.scan, args.batch, [512, 512] if args.scan >= 128 else None,
                                args.gpus),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{cores} processes x ~{per_step:.1f} s per step of "
-                                   "64-position batches of the 128^2-detector GD update "
-                                   "(16x16 scan per process)"},
+                         "sample": f"{cores} single-threaded processes (nproc {os.cpu_count()}), "
+                                   f"each >= {per_step:.1f} s per step of whole 1024-position "
+                                   "GD batches (128^2 detector, 512^2 object) of the float32 "
+                                   "NumPy restatement of the reference"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -567,6 +609,8 @@ def run_ours(args):
                "mode": "reconstruct(num_iter=1) per step, storage='cpu': amplitudes in "
                        "page-locked host memory, read in place by the kernels"}
 
+    parity = parity_check(case, B) if rank == 0 and args.scan == 128 else None
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -581,6 +625,7 @@ def run_ours(args):
             "gpu_launches": launches,
             "clocks": clocks.summary(),
             "final_error": errors[-1] if errors else None,
+            "parity": parity,
             "setup_s": setup_s,
             "preprocess": pre_timing,
             "wall_ms_timed": wall_ms,

@@ -23,6 +23,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+# this script reads the reference checkout of this container
+os.environ.setdefault("PY4DSTEM_REFERENCE", "/root/reference")
 
 from oracle.refloader import load_reference  # noqa: E402
 from py4dstem_gb300 import synthetic  # noqa: E402
@@ -600,9 +602,162 @@ def make_volume_ops(ref):
     print(f"tomo_volume_ops: {os.path.getsize(path) / 1e6:.2f} MB")
 
 
+# Workloads at the sizes that are timed ("size_" prefix). Their datacubes are too
+# large to commit (1 GiB of counts for the 128 x 128 scan), so a fixture keeps
+# the generator arguments and a SHA-256 digest of the uint16 counts instead; the
+# GPU test regenerates the counts (synthetic.make_scan, NumPy backend: integer
+# Poisson counts drawn from PCG64, which agree across CPU architectures) and
+# checks the digest before it compares anything. The reference's float32
+# amplitudes are pinned the same way (digest and per-pattern sums). The float32
+# oracle with every FFT rounded through complex128 (the reference's own
+# rounding floor) and the float64 oracle run here, on the reference's
+# preprocessed state; the fixture keeps their distances and the float64 object
+# and probe.
+SIZE_CASES = {
+    # single-slice throughput workload: 128 x 128 scan at 0.75 A (J = 16384),
+    # 128^2 detector, 512^2 object, 1e5 e-/pattern, batch 1024, uniform start
+    "size_ss_scan128_det128": dict(
+        gen=dict(name="size_ss", seed=1234, scan_shape=(128, 128), step_ang=0.75,
+                 jitter_ang=0.05, detector=128, object_px=512, dose=1e5),
+        cls="single", ctor=dict(object_fov_ang=(128.0, 128.0)),
+        rec=dict(num_iter=3, max_batch_size=1024, step_size=0.5, seed_random=1234)),
+    # multislice through the adjoint: 8 slices of 20 A, 64 x 64 scan at 0.4 A,
+    # 128^2 detector, 25 mrad, defocus 50 A
+    "size_ms_T8_scan64_det128": dict(
+        gen=dict(name="size_ms", seed=2, scan_shape=(64, 64), step_ang=0.4, jitter_ang=0.05,
+                 detector=128, object_px=256, semiangle=25.0, defocus=50.0, dose=1e4,
+                 num_slices=8, slice_thickness=20.0),
+        cls="multi", ctor=dict(object_fov_ang=(64.0, 64.0), num_slices=8,
+                               slice_thicknesses=20.0),
+        ctor_optics=dict(semiangle_cutoff=25.0, defocus=50.0),
+        rec=dict(num_iter=2, max_batch_size=256, step_size=0.5, seed_random=2)),
+    # one scan of the batched mixed-state workload at its largest size: 96 x 96
+    # scan, 128^2 detector, 4 modes (weights 0.7 / 0.15 / 0.1 / 0.05) given as the
+    # initial probe
+    "size_mixed_M4_scan96_det128": dict(
+        gen=dict(name="size_mx", seed=3, scan_shape=(96, 96), step_ang=0.5, jitter_ang=0.05,
+                 detector=128, object_px=512, dose=1e4, num_modes=4,
+                 mode_weights=(0.7, 0.15, 0.1, 0.05)),
+        cls="mixed", ctor=dict(object_fov_ang=(128.0, 128.0), num_probes=4),
+        probe_guess=True,
+        rec=dict(num_iter=2, max_batch_size=256, step_size=0.5, seed_random=3)),
+}
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, dtype=np.complex128)
+    b = np.asarray(b, dtype=np.complex128)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def counts_digest(data):
+    """SHA-256 of the datacube as uint16 counts (C order)."""
+    import hashlib
+
+    return hashlib.sha256(np.ascontiguousarray(data.astype(np.uint16)).tobytes()).hexdigest()
+
+
+def array_digest(a):
+    import hashlib
+
+    a = np.ascontiguousarray(a)
+    return hashlib.sha256(a.tobytes()).hexdigest() + f":{a.dtype.str}:{list(a.shape)}"
+
+
+def make_size_case(ref, name, spec):
+    import time
+
+    from oracle.ptycho_np import Oracle, State
+
+    t0 = time.time()
+    case = synthetic.make_scan(**spec["gen"])
+    data = case.datacube.data
+    assert np.array_equal(data, np.round(data)) and data.max() < 65535
+    q = case.datacube.calibration.get_Q_pixel_size()
+    r = case.datacube.calibration.get_R_pixel_size()
+    dc = ref.DataCube(data, r_pixel_size=r, r_pixel_units="A", q_pixel_size=q,
+                      q_pixel_units="mrad")
+    optics = dict(semiangle_cutoff=20.0, defocus=100.0)
+    optics.update(spec.get("ctor_optics", {}))
+    ctor = dict(energy=300e3, **optics, **spec["ctor"])
+    cls = {"single": ref.SingleslicePtychography, "multi": ref.MultislicePtychography,
+           "mixed": ref.MixedstatePtychography}[spec["cls"]]
+    extra = {}
+    probe_guess = None
+    if spec.get("probe_guess"):
+        probe_guess = np.asarray(case.probe_modes, dtype=np.complex64)
+        extra["initial_probe_guess"] = probe_guess.copy()
+    print(f"{name}: generated {data.shape} in {time.time() - t0:.0f} s", flush=True)
+    p = cls(datacube=dc, initial_scan_positions=case.scan_positions_ang, verbose=False,
+            device="cpu", **ctor, **extra)
+    p.preprocess(**PRE)
+    print(f"{name}: reference preprocess done at {time.time() - t0:.0f} s", flush=True)
+    pre = dict(
+        mean_intensity=np.float32(p._mean_diffraction_intensity),
+        positions_px=p._positions_px.copy(),
+        probe_initial=p._probe.copy(),
+        object_initial=p._object.copy(),
+        fov_mask=p._object_fov_mask.copy(),
+        amplitude_sums=p._amplitudes.astype(np.float64).sum(axis=(-2, -1)),
+    )
+    amp_digest = array_digest(p._amplitudes)
+    state = State(
+        amplitudes=p._amplitudes.copy(), positions_px=p._positions_px.copy(),
+        probe=np.array(p._probe, copy=True), object=np.array(p._object, copy=True),
+        mean_intensity=p._mean_diffraction_intensity,
+        fov_mask_inverse=p._object_fov_mask_inverse.copy(), object_type=p._object_type,
+        num_slices=spec["ctor"].get("num_slices", 1),
+        num_probes=spec["ctor"].get("num_probes", 1), mixed=spec["cls"] == "mixed",
+        propagators=(np.array(p._propagator_arrays) if spec["cls"] == "multi" else None),
+        sampling=tuple(p.sampling))
+    p.reconstruct(progress_bar=False, **spec["rec"])
+    print(f"{name}: reference reconstruct done at {time.time() - t0:.0f} s", flush=True)
+    out = dict(
+        error_iterations=np.asarray(p.error_iterations, dtype=np.float64),
+        object=p.object,
+        probe_corner=np.asarray(p._probe),
+    )
+    # the oracle on the same state: float32 (must equal the reference), FFTs
+    # rounded through complex128 (the floor), float64 (the FP64 model)
+    o32 = Oracle(state.copy()).reconstruct(**spec["rec"])
+    assert np.array_equal(np.asarray(o32.error_iterations), out["error_iterations"]), name
+    assert np.array_equal(o32.object, out["object"]), name
+    floor = Oracle(state.copy(), fft_round_trip=True).reconstruct(**spec["rec"])
+    o64 = Oracle(state.copy(), "float64").reconstruct(**spec["rec"])
+    ref_err = out["error_iterations"]
+    stats = dict(
+        floor_err=float(np.max(np.abs(np.asarray(floor.error_iterations) - ref_err) / ref_err)),
+        floor_obj=rel_l2(floor.object, out["object"]),
+        floor_probe=rel_l2(floor.probe, out["probe_corner"]),
+        ref_vs_fp64_obj=rel_l2(out["object"], o64.object),
+        ref_vs_fp64_probe=rel_l2(out["probe_corner"], o64.probe),
+    )
+    print(f"{name}: oracle checks done at {time.time() - t0:.0f} s: {stats}", flush=True)
+    meta = dict(cls=spec["cls"], ctor=ctor, preprocess=PRE, reconstruct=spec["rec"],
+                r_pixel_size=r, q_pixel_size=q, generator=spec["gen"],
+                counts_digest=counts_digest(data), amplitudes_digest=amp_digest,
+                probe_guess=bool(spec.get("probe_guess")), stats=stats)
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(
+        path, scan_positions_ang=case.scan_positions_ang, meta=json.dumps(meta),
+        **{f"pre_{k}": v for k, v in pre.items()},
+        **{f"out_{k}": v for k, v in out.items()},
+        fp64_object=np.asarray(o64.object).astype(
+            np.float32 if p._object_type == "potential" else np.complex64),
+        fp64_probe=np.asarray(o64.probe).astype(np.complex64))
+    print(f"{name}: {os.path.getsize(path) / 1e6:.2f} MB, errors {out['error_iterations']}",
+          flush=True)
+
+
 def main():
     ref = load_reference()
     only = set(sys.argv[1:])
+    if "--size" in only:
+        only.discard("--size")
+        for name, spec in SIZE_CASES.items():
+            if not only or name in only:
+                make_size_case(ref, name, spec)
+        return
     for name, spec in CASES.items():
         if not only or name in only:
             make_case(ref, name, spec)
