@@ -481,6 +481,80 @@ int ptycho_set_kernel_schedule(int32_t roi, int32_t schedule);
  */
 int ptycho_fp32_fma_probe(int32_t blocks, int32_t iters, float* sink, void* stream);
 
+/*
+ * Learned initializer (no counterpart in the reference). A 4-level U-Net with
+ * 32 base channels maps a scan's virtual bright-field and centre-of-mass
+ * magnitude images to an initial object phase. Weights and activations are
+ * bfloat16 (passed as raw 16-bit words), accumulation is float32, and the 3 x 3
+ * convolutions are implicit GEMMs on the tensor cores (tcgen05.mma with TMEM
+ * accumulators). Every buffer belongs to the caller; no call allocates. Waits
+ * inside the tensor-core kernels are bounded: on time-out they set the int
+ * error word the call names (err_flag, or the U-Net workspace's own word) and
+ * return.
+ *
+ * ptycho_nn_gemm_bf16: c (m, n) float32 = a (m, k) b (n, k)^T, bf16 row-major
+ * operands; n a multiple of 16, k a multiple of 8.
+ *
+ * ptycho_nn_conv3x3_*: 3 x 3 convolution, stride 1, zero padding 1, NHWC bf16
+ * activations (batch, height, width, channels); cin a multiple of 8, cout a
+ * multiple of 16, width a multiple of 8. weight (cout, 9, cin) bf16 with the
+ * tap index ky * 3 + kx; weight_t (cin, 9, cout) the same values with the
+ * channel axes exchanged. forward: y = act(conv(x) + bias) in bf16 (bias may be
+ * NULL; relu != 0 applies max(0, .)). backward_data: dx (batch, height, width,
+ * cin) float32 = the gradient wrt x for the gradient dy wrt the convolution's
+ * output. backward_weight: dweight (cout, 9, cin) and dbias (cout, or NULL)
+ * float32, summed over the batch in a fixed order (workspace:
+ * ptycho_nn_conv3x3_wgrad_workspace_bytes).
+ */
+int ptycho_nn_gemm_bf16(const void* a, const void* b, float* c, int32_t m, int32_t n, int32_t k,
+                        int32_t* err_flag, void* stream);
+int ptycho_nn_conv3x3_forward(const void* x, int32_t batch, int32_t height, int32_t width,
+                              int32_t cin, const void* weight, const float* bias, int32_t cout,
+                              int32_t relu, void* y, int32_t* err_flag, void* stream);
+int ptycho_nn_conv3x3_backward_data(const void* dy, int32_t batch, int32_t height,
+                                    int32_t width, int32_t cout, const void* weight_t,
+                                    int32_t cin, float* dx, int32_t* err_flag, void* stream);
+size_t ptycho_nn_conv3x3_wgrad_workspace_bytes(int32_t batch, int32_t height, int32_t width,
+                                               int32_t cin, int32_t cout);
+int ptycho_nn_conv3x3_backward_weight(const void* x, const void* dy, int32_t batch,
+                                      int32_t height, int32_t width, int32_t cin, int32_t cout,
+                                      float* dweight, float* dbias, void* workspace,
+                                      size_t workspace_bytes, int32_t* err_flag, void* stream);
+
+/*
+ * The U-Net. params: ptycho_nn_unet_param_bytes() bytes (256-byte aligned)
+ * holding, per layer, the bf16 weights and their transpose, float32 master
+ * weights and biases, their gradients of the last training step and the Adam
+ * moments; ptycho_nn_unet_param_offset(layer, field) gives the byte offset of
+ * one of them (layers 0..13 the 3 x 3 convolutions, 14 the 1 x 1 head; field 0
+ * bf16 weights, 1 bf16 transposed weights, 2 float32 weights, 3 float32 bias,
+ * 4 weight gradient, 5 bias gradient) or -1. ptycho_nn_unet_init fills them
+ * (He-normal weights from `seed`, zero biases and moments).
+ * workspace: ptycho_nn_unet_workspace_bytes(batch, height, width) bytes,
+ * 256-byte aligned and zeroed once by the caller (it holds the error word that
+ * ptycho_nn_check reads and clears); height and width multiples of 64.
+ * input (batch, height, width, 2) float32, output / target / mask (batch,
+ * height, width) float32. train_step: forward, loss = sum(mask (out - target)^2)
+ * / mask_count (mask NULL = all ones) into *loss (device float), backward, one
+ * Adam step (learning_rate, step >= 1 counts the steps for the bias
+ * correction; beta 0.9 / 0.999, eps 1e-8).
+ */
+size_t ptycho_nn_unet_param_bytes(void);
+int64_t ptycho_nn_unet_param_offset(int32_t layer, int32_t field);
+size_t ptycho_nn_unet_workspace_bytes(int32_t batch, int32_t height, int32_t width);
+int ptycho_nn_unet_init(void* params, uint64_t seed, void* stream);
+int ptycho_nn_unet_forward(const void* params, const float* input, int32_t batch, int32_t height,
+                           int32_t width, float* output, void* workspace, size_t workspace_bytes,
+                           void* stream);
+int ptycho_nn_unet_train_step(void* params, const float* input, const float* target,
+                              const float* mask, float mask_count, int32_t batch, int32_t height,
+                              int32_t width, float learning_rate, int32_t step, float* loss,
+                              void* workspace, size_t workspace_bytes, void* stream);
+/* Waits for `stream`, then returns PTYCHO_ERR_CUDA (and clears the word) if a
+ * tensor-core wait of the U-Net kernels timed out since the last check. */
+int ptycho_nn_check(void* workspace, int32_t batch, int32_t height, int32_t width, void* stream);
+const char* ptycho_nn_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -120,6 +120,24 @@ _SIGNATURES = {
     "ptycho_volume_add_scaled": ([_vp, _vp, ctypes.c_int64, _i32, _vp], ctypes.c_int),
     "ptycho_volume_constraints": ([_vp, ctypes.c_int64, _f32, _i32, _i32, _vp], ctypes.c_int),
     "ptycho_read_error": ([_vp, ctypes.POINTER(_f32), _vp], ctypes.c_int),
+    "ptycho_nn_gemm_bf16": ([_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp], ctypes.c_int),
+    "ptycho_nn_conv3x3_forward": (
+        [_vp, _i32, _i32, _i32, _i32, _vp, _vp, _i32, _i32, _vp, _vp, _vp], ctypes.c_int),
+    "ptycho_nn_conv3x3_backward_data": (
+        [_vp, _i32, _i32, _i32, _i32, _vp, _i32, _vp, _vp, _vp], ctypes.c_int),
+    "ptycho_nn_conv3x3_wgrad_workspace_bytes": ([_i32, _i32, _i32, _i32, _i32], _sz),
+    "ptycho_nn_conv3x3_backward_weight": (
+        [_vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp, _vp, _vp, _sz, _vp, _vp], ctypes.c_int),
+    "ptycho_nn_unet_param_bytes": ([], _sz),
+    "ptycho_nn_unet_param_offset": ([_i32, _i32], ctypes.c_int64),
+    "ptycho_nn_unet_workspace_bytes": ([_i32, _i32, _i32], _sz),
+    "ptycho_nn_unet_init": ([_vp, ctypes.c_uint64, _vp], ctypes.c_int),
+    "ptycho_nn_unet_forward": ([_vp, _vp, _i32, _i32, _i32, _vp, _vp, _sz, _vp], ctypes.c_int),
+    "ptycho_nn_unet_train_step": (
+        [_vp, _vp, _vp, _vp, _f32, _i32, _i32, _i32, _f32, _i32, _vp, _vp, _sz, _vp],
+        ctypes.c_int),
+    "ptycho_nn_check": ([_vp, _i32, _i32, _i32, _vp], ctypes.c_int),
+    "ptycho_nn_last_error": ([], ctypes.c_char_p),
     "ptycho_gd_batch_noalloc": (
         [ctypes.POINTER(Geometry), _vp, _vp, _vp, _vp, _vp, _vp, _i32, _f32, _f32, _i32,
          _vp, _vp, _vp, _vp],
