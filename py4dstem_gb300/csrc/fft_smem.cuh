@@ -193,11 +193,82 @@ __device__ __forceinline__ void fill_twiddles(float2* tw) {
   for (int m = threadIdx.x; m < L; m += NT) tw[m] = twiddle_detail::kTable<L>.v[m];
 }
 
-// exp(i phi) for a float32 phase, cos/sin evaluated in double and rounded once.
+// exp(i phi) for a float32 phase |phi| <= 1.6 (the sub-pixel shift ramps:
+// |2 pi k d| <= pi / 2), cos and sin each rounded once to float.
+//
+// GB300 runs float64 at a small fraction of its float32 rate, so the values
+// are summed in double-float arithmetic (an unevaluated float pair hi + lo,
+// about 44 significant bits) from their Taylor series: sin phi = phi S(phi^2),
+// cos phi = C(phi^2), with S and C evaluated by Horner's rule over 12 terms
+// (truncation below 2e-18 for |phi| <= 1.6). The pair's leading float is the
+// float nearest to the sum. The coefficients (-1)^n / (2n+1)! and
+// (-1)^n / (2n)! are split into float pairs at compile time. Larger arguments
+// fall back to float64.
+namespace cis_detail {
+struct DF {
+  float hi, lo;
+};
+__device__ __forceinline__ DF two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+__device__ __forceinline__ DF quick_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return quick_two_sum(p, e);
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  DF s = two_sum(a.hi, b.hi);
+  s.lo = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+  return quick_two_sum(s.hi, s.lo);
+}
+constexpr double factorial(int n) { return n <= 1 ? 1.0 : n * factorial(n - 1); }
+constexpr double coef(int n, bool sine) {
+  return (n % 2 ? -1.0 : 1.0) / factorial(sine ? 2 * n + 1 : 2 * n);
+}
+struct Coefs {
+  float shi[12], slo[12], chi[12], clo[12];
+};
+constexpr Coefs make_coefs() {
+  Coefs c{};
+  for (int n = 0; n < 12; ++n) {
+    const double s = coef(n, true), k = coef(n, false);
+    c.shi[n] = (float)s;
+    c.slo[n] = (float)(s - (double)(float)s);
+    c.chi[n] = (float)k;
+    c.clo[n] = (float)(k - (double)(float)k);
+  }
+  return c;
+}
+__device__ constexpr Coefs kCoefs = make_coefs();
+}  // namespace cis_detail
+
 __device__ __forceinline__ float2 cis_rounded(float phi) {
-  double s, c;
-  sincos((double)phi, &s, &c);
-  return make_float2((float)c, (float)s);
+  using namespace cis_detail;
+  if (!(fabsf(phi) <= 1.6f)) {
+    double s, c;
+    sincos((double)phi, &s, &c);
+    return make_float2((float)c, (float)s);
+  }
+  const DF x{phi, 0.0f};
+  const DF x2 = df_mul(x, x);
+  DF s{kCoefs.shi[11], kCoefs.slo[11]};
+  DF c{kCoefs.chi[11], kCoefs.clo[11]};
+#pragma unroll
+  for (int n = 10; n >= 0; --n) {
+    s = df_add(df_mul(s, x2), DF{kCoefs.shi[n], kCoefs.slo[n]});
+    c = df_add(df_mul(c, x2), DF{kCoefs.chi[n], kCoefs.clo[n]});
+  }
+  s = df_mul(s, x);
+  return make_float2(__fadd_rn(c.hi, c.lo), __fadd_rn(s.hi, s.lo));
 }
 
 // One Stockham pass over NLINES lines of length L with radix R; NS is the length

@@ -20,8 +20,9 @@ def _all_names():
 
 def names():
     """Reconstruction fixtures of the 2D / multislice / mixed-state classes
-    (the tomography fixtures, tomo_*, have their own tests)."""
-    return [n for n in _all_names() if not n.startswith(("prep_", "tomo_"))]
+    (the tomography fixtures, tomo_*, and the fixtures at the timed sizes,
+    size_*, which keep no datacube, have their own tests)."""
+    return [n for n in _all_names() if not n.startswith(("prep_", "tomo_", "size_"))]
 
 
 def prep_names():
