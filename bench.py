@@ -74,12 +74,20 @@ def parse_args(argv=None):
     ap.add_argument("--ref-cores", type=int, default=0,
                     help="reference arm: limit the worker processes (0 = all host cores)")
     ap.add_argument("--workload", choices=["gd128", "multiscan", "multislice", "projection",
-                                           "poscorr", "mixed-multislice", "tomography"],
+                                           "poscorr", "mixed-multislice", "tomography",
+                                           "learned-init"],
                     default="gd128",
                     help="gd128: the single-slice 128^2-detector workload (default); multiscan: "
                          "16 mixed-state scans of uneven sizes in one graph-captured launch")
     ap.add_argument("--scans", type=int, default=16, help="multiscan: number of scans")
     ap.add_argument("--ms-batch", type=int, default=256, help="multiscan: max_batch_size")
+    ap.add_argument("--li-scans", type=int, default=20000,
+                    help="learned-init: training scans (128x128 positions each)")
+    ap.add_argument("--li-epochs", type=int, default=8, help="learned-init: training epochs")
+    ap.add_argument("--li-seeds", type=int, default=8,
+                    help="learned-init: held-out seeds evaluated (the full evaluation: 64)")
+    ap.add_argument("--li-iterations", type=int, default=200,
+                    help="learned-init: iterations of the plain run")
     ap.add_argument("--schedule", type=int, default=0,
                     help="128^2 kernel schedule: 0 default, 1 shared-memory, 2 register")
     return ap.parse_args(argv)
@@ -211,15 +219,15 @@ PARITY_SEED = 1234
 
 def build_case(scan, seed, device):
     """The benchmark scan. The 128 x 128 scan of seed 1234 is generated by the
-    NumPy backend, the same counts the reference reconstructed for the parity
-    fixture; other sizes and seeds use the faster torch backend."""
+    portable NumPy backend, the same counts the reference reconstructed for the
+    parity fixture; other sizes and seeds use the faster torch backend."""
     from py4dstem_gb300 import synthetic
 
-    numpy_backend = scan == 128 and seed == PARITY_SEED
+    portable = scan == 128 and seed == PARITY_SEED
     case = synthetic.make_scan(
         "bench", seed, (scan, scan), 0.75, 0.05, 128, 512 if scan >= 128 else
         int(2 ** math.ceil(math.log2(scan * 3 + 128))), dose=1e5,
-        backend="numpy" if numpy_backend else "torch", device=device)
+        backend="portable" if portable else "torch", device=device)
     return case
 
 
@@ -235,6 +243,11 @@ def parity_check(case, batch):
     if (gen["seed"] != PARITY_SEED or tuple(gen["scan_shape"]) != (128, 128)
             or not np.array_equal(case.scan_positions_ang, z["scan_positions_ang"])):
         return None
+    import hashlib
+
+    counts = np.ascontiguousarray(case.datacube.data.astype(np.uint16))
+    if hashlib.sha256(counts.tobytes()).hexdigest() != meta["counts_digest"]:
+        return {"ok": False, "reason": "the generated counts differ from the reference's input"}
     ref_err = np.asarray(z["out_error_iterations"], dtype=np.float64)
     p = preprocess(case, storage="gpu")
     p.reconstruct(progress_bar=False, **meta["reconstruct"])
@@ -954,6 +967,89 @@ def run_tomography(args):
     return 0
 
 
+# ------------------------------------------------------------------ learned init
+def run_learned_init(args):
+    """The learned initializer on the throughput workload's generator: train the
+    U-Net on args.li_scans generated 128 x 128 scans (lattice 2.5-5 A, defocus
+    0-200 A, 1e5 e-/pattern), then for args.li_seeds held-out scans run the plain
+    reconstruction (args.li_iterations iterations of batch 1024) and the learned
+    start until it reaches the plain run's final error. value = median over the
+    seeds of (learned wall time, network included) / (plain wall time to first
+    reach that error); a seed whose learned run never reaches it falls back to
+    the plain start and counts as (learned attempt + plain run) / plain run."""
+    rank, world, local = dist_env()
+    if world > 1:
+        print(json.dumps({"workload": "learned-init", "unavailable": "single-GPU workload"}))
+        return 0
+    import torch
+
+    torch.cuda.set_device(local)
+    from py4dstem_gb300 import SingleslicePtychography, learned_init as li, synthetic
+
+    geom = li.ScanGeometry()
+    t0 = time.time()
+    X, Y = li.generate_training_set(args.li_scans, geom, seed=11)
+    torch.cuda.synchronize()
+    gen_s = time.time() - t0
+    net = li.UNet(seed=0)
+    t0 = time.time()
+    hist = li.train(net, X, Y, epochs=args.li_epochs, batch=16, lr=1e-3, seed=0)
+    torch.cuda.synchronize()
+    train_s = time.time() - t0
+    target_var = float(Y.var())
+    del X, Y
+    # convolution FLOPs of one forward pass of a 128 x 128 input (a training
+    # step is three such GEMM passes: forward, input and weight gradients)
+    conv_flops = 0
+    cin = (8, 32, 32, 64, 64, 128, 128, 256, 384, 128, 192, 64, 96, 32)
+    cout = (32, 32, 64, 64, 128, 128, 256, 256, 128, 128, 64, 64, 32, 32)
+    level = (0, 0, 1, 1, 2, 2, 3, 3, 2, 2, 1, 1, 0, 0)
+    for ci, co, lv in zip(cin, cout, level):
+        conv_flops += 2 * (128 >> lv) ** 2 * 9 * ci * co
+    steps = (args.li_scans // 16) * args.li_epochs
+    rng = np.random.default_rng(2026)
+    results = []
+    for k in range(args.li_seeds):
+        a = float(rng.uniform(2.5, 5.0))
+        df = float(rng.integers(0, 201))
+        case = synthetic.make_scan("held-out", 50000 + k, (128, 128), 0.75, 0.05, 128, 512,
+                                   dose=1e5, defocus=df, lattice_a=a, backend="torch",
+                                   device=f"cuda:{local}")
+        p = SingleslicePtychography(datacube=case.datacube, verbose=False, device="gpu",
+                                    **case.ctor_kwargs)
+        p.preprocess(**case.preprocess_kwargs)
+        r = li.compare_starts(net, p, geom, args.li_iterations, 1024, seed=k)
+        pe, le = r.pop("plain_errors"), r.pop("learned_errors")
+        if r["fallback"]:
+            r["time_ratio"] = (r["network_s"] + 2.0 * r["plain_s"]) / r["plain_s_to_target"]
+        r.update({"lattice_a": a, "defocus": df, "plain_error_curve": pe[::10],
+                  "learned_error_curve": le[::10]})
+        results.append(r)
+        del case, p
+    ratios = [r["time_ratio"] for r in results]
+    its = [r["learned_iterations"] for r in results if r["learned_iterations"]]
+    line = {
+        "metric": "time-to-target NMSE, learned vs plain init (learned wall time / plain)",
+        "value": float(statistics.median(ratios)), "unit": "ratio", "n_gpus": 1,
+        "higher_is_better": False, "steps": args.li_seeds, "warmup": 0, "dtype": "bf16",
+        "data": "synthetic",
+        "config": {"workload": "learned-init", "train_scans": args.li_scans,
+                   "epochs": args.li_epochs, "held_out_seeds": args.li_seeds,
+                   "plain_iterations": args.li_iterations, "scan": [128, 128],
+                   "detector": 128, "object": [512, 512], "batch": 1024},
+        "fallbacks": int(sum(r["fallback"] for r in results)),
+        "median_learned_iterations": float(statistics.median(its)) if its else None,
+        "median_plain_iterations_to_target": float(statistics.median(
+            [r["plain_first_at_target"] for r in results])),
+        "generation_s": gen_s, "train_s": train_s, "train_loss": hist,
+        "target_variance": target_var,
+        "conv_tflops_train": 3 * conv_flops * 16 * steps / train_s / 1e12,
+        "seeds": results,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main(argv=None):
     args = parse_args(argv)
     if args.impl == "reference":
@@ -964,6 +1060,8 @@ def main(argv=None):
         return run_multislice(args)
     if args.workload in ("projection", "poscorr", "mixed-multislice"):
         return run_variant(args)
+    if args.workload == "learned-init":
+        return run_learned_init(args)
     if args.workload == "tomography":
         return run_tomography(args)
     return run_ours(args)

@@ -556,22 +556,23 @@ int ptycho_nn_unet_train_step(void* params, const float* input, const float* tar
  * `sampling` Angstrom per pixel): phase = peak * sum of Gaussian atoms
  * (sigma Angstrom) on a square lattice, params (count, 5) float32 = lattice
  * constant (Angstrom), rotation (rad), lattice offset x, y (Angstrom), unused;
- * phase (count, P, P) float32 and object = exp(-0.1 phase) exp(i phase)
+ * phase and phase_blur (the phase blurred by a Gaussian of sigma_blur
+ * Angstrom) (count, P, P) float32, object = exp(-0.1 phase) exp(i phase)
  * complex64.
  * ptycho_nn_scan_images: for scan s and position j (128 x 128 detector): the
  * far field of the sub-pixel shifted probe (spectra (scans, 128, 128) complex64,
  * FFT2 of each scan's probe) times the object patch at positions_px (scans, J, 2),
- * its intensities scaled to `dose` counts and drawn with Poisson noise (keyed by
- * seed, s, j and the pixel; rounded-normal approximation above a mean of 12),
- * then bf = counts inside the bright-field disc (radius bf_radius_px), com_x /
- * com_y = centre of mass of the counts in detector pixels, and target = the
- * object phase at the position (bilinear); all (scans, J) float32.
+ * its intensities scaled to `dose` counts; bf = counts inside the bright-field
+ * disc (radius bf_radius_px), com_x / com_y = centre of mass of the counts in
+ * detector pixels, with the Poisson noise of those sums from their normal
+ * approximations (keyed by seed, s and j); target = `phase` (the caller passes
+ * the blurred phase) at the position, bilinear; all (scans, J) float32.
  * ptycho_nn_virtual_images: the same bright-field sum and centre of mass of
  * the intensities amplitudes^2 of `count` corner-centred (sx, sy) patterns.
  */
 int ptycho_nn_lattice_objects(int32_t count, int32_t object_px, float sampling,
-                              const float* params, float sigma, float peak, float* phase,
-                              void* object, void* stream);
+                              const float* params, float sigma, float peak, float sigma_blur,
+                              float* phase, float* phase_blur, void* object, void* stream);
 int ptycho_nn_scan_images(int32_t scans, int32_t positions, int32_t object_px,
                           const void* spectra, const void* objects, const float* phase,
                           const float* positions_px, float dose, float bf_radius_px,

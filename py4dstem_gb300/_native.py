@@ -138,8 +138,8 @@ _SIGNATURES = {
         ctypes.c_int),
     "ptycho_nn_check": ([_vp, _i32, _i32, _i32, _vp], ctypes.c_int),
     "ptycho_nn_last_error": ([], ctypes.c_char_p),
-    "ptycho_nn_lattice_objects": ([_i32, _i32, _f32, _vp, _f32, _f32, _vp, _vp, _vp],
-                                  ctypes.c_int),
+    "ptycho_nn_lattice_objects": ([_i32, _i32, _f32, _vp, _f32, _f32, _f32, _vp, _vp, _vp,
+                                   _vp], ctypes.c_int),
     "ptycho_nn_scan_images": (
         [_i32, _i32, _i32, _vp, _vp, _vp, _vp, _f32, _f32, ctypes.c_uint64, _vp, _vp, _vp, _vp,
          _vp], ctypes.c_int),

@@ -5,10 +5,11 @@
 //                    rotated square lattice, object = exp(-0.1 phase) exp(i phase)
 //   scan images      for every scan position: the ptychographic forward model
 //                    (sub-pixel shifted probe times the object patch, FFT2), the
-//                    far-field intensities scaled to a dose and drawn with Poisson
-//                    noise, then the virtual bright-field signal (counts inside
-//                    the bright-field disc) and the centre of mass of the counts;
-//                    plus the object phase at the position (the training target)
+//                    far-field intensities scaled to a dose, then the virtual
+//                    bright-field signal (counts inside the bright-field disc)
+//                    and the centre of mass of the counts, with the Poisson noise
+//                    of those sums (see scan_images_kernel); plus the blurred
+//                    object phase at the position (the training target)
 //   virtual images   the same bright-field sum and centre of mass from measured
 //                    (preprocessed) amplitudes, the network's input at inference
 // The forward model uses the shared-memory FFT of the reconstruction kernels
@@ -42,28 +43,15 @@ __device__ __forceinline__ float uniform01(uint64_t key) {
   return ((mix64(key) >> 40) + 0.5f) * (1.0f / 16777216.0f);
 }
 
-// Poisson(lambda): multiplication method below 12, rounded normal approximation
-// N(lambda, lambda) above (training data only; documented approximation).
-__device__ __forceinline__ float poisson(float lam, uint64_t key) {
-  if (!(lam > 0.0f)) return 0.0f;
-  if (lam < 12.0f) {
-    const float L = __expf(-lam);
-    float p = 1.0f;
-    int k = -1;
-    uint64_t j = 0;
-    do {
-      ++k;
-      p *= uniform01(key * 64 + j++);
-    } while (p > L && k < 64);
-    return (float)k;
-  }
-  const float u1 = uniform01(key * 64 + 62), u2 = uniform01(key * 64 + 63);
-  const float z = sqrtf(-2.0f * __logf(u1)) * __cosf(6.2831853f * u2);
-  return fmaxf(0.0f, rintf(lam + sqrtf(lam) * z));
+// Standard normal from two counter-based uniforms (Box-Muller).
+__device__ __forceinline__ float normal01(uint64_t key) {
+  const float u1 = uniform01(2 * key), u2 = uniform01(2 * key + 1);
+  return sqrtf(-2.0f * __logf(u1)) * __cosf(6.2831853f * u2);
 }
 
 __global__ void lattice_objects_kernel(int count, int P, float sampling, const float* params,
-                                       float sigma, float peak, float* phase, float2* object) {
+                                       float sigma, float peak, float sigma_blur, float* phase,
+                                       float* phase_blur, float2* object) {
   const size_t total = (size_t)count * P * P;
   const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= total) return;
@@ -80,15 +68,21 @@ __global__ void lattice_objects_kernel(int count, int P, float sampling, const f
   const float qu = c * px + sn * py - ox;
   const float qv = -sn * px + c * py - oy;
   const int mu = (int)floorf(qu / a), mv = (int)floorf(qv / a);
-  const float inv2s2 = 1.0f / (2.0f * sigma * sigma);
-  float ph = 0.0f;
-  for (int du = -1; du <= 2; ++du)
-    for (int dv = -1; dv <= 2; ++dv) {
+  // the atoms, and the same atoms blurred by a Gaussian of sigma_blur (a
+  // Gaussian of variance sigma^2 + sigma_blur^2 with the same integral)
+  const float s2 = sigma * sigma, t2 = s2 + sigma_blur * sigma_blur;
+  const float inv2s2 = 1.0f / (2.0f * s2), inv2t2 = 1.0f / (2.0f * t2);
+  const float peak_t = peak * s2 / t2;
+  float ph = 0.0f, pb = 0.0f;
+  for (int du = -2; du <= 3; ++du)
+    for (int dv = -2; dv <= 3; ++dv) {
       const float eu = qu - (mu + du) * a, ev = qv - (mv + dv) * a;
       const float d2 = eu * eu + ev * ev;
-      if (d2 < 25.0f * sigma * sigma) ph += peak * __expf(-d2 * inv2s2);
+      if (d2 < 25.0f * s2) ph += peak * __expf(-d2 * inv2s2);
+      if (d2 < 25.0f * t2) pb += peak_t * __expf(-d2 * inv2t2);
     }
   phase[idx] = ph;
+  phase_blur[idx] = pb;
   const float amp = __expf(-0.1f * ph);
   float sv, cv;
   sincosf(ph, &sv, &cv);
@@ -132,7 +126,6 @@ __global__ void __launch_bounds__(NT, 1)
   float2* rpx = twy + S;
   float2* rpy = rpx + S;
   __shared__ float red[5][NT / 32];
-  __shared__ float total_s;
   const int j = blockIdx.x;
   const int sc = blockIdx.y;
   const int tid = threadIdx.x;
@@ -168,29 +161,41 @@ __global__ void __launch_bounds__(NT, 1)
   }
   __syncthreads();
   fft2d<S, S, NT, -1>(buf, twx, twy);
-  float v[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-  for (int e = tid; e < N; e += NT) v[0] += c_abs2(buf[(e / S) * LD + e % S]);
-  block_sum5(v, red);
-  if (tid == 0) total_s = v[0];
-  __syncthreads();
-  const float scale = dose / total_s;
-  const uint64_t key0 = mix64(seed ^ mix64(((uint64_t)sc << 32) | (uint32_t)j));
-  float w[5] = {0.f, 0.f, 0.f, 0.f, 0.f};  // bf, sum, sum kx, sum ky
+  // moments of the intensities: the bright-field sum, the total, the first and
+  // second moments along kx and ky
+  float w[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  float w2[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
   for (int e = tid; e < N; e += NT) {
     const int x = e / S, y = e % S;
-    const float n = poisson(c_abs2(buf[x * LD + y]) * scale, key0 + (uint64_t)e);
+    const float I = c_abs2(buf[x * LD + y]);
     const float kx = (float)fint(x), ky = (float)fint(y);
-    if (kx * kx + ky * ky < bf_r2) w[0] += n;
-    w[1] += n;
-    w[2] += n * kx;
-    w[3] += n * ky;
+    if (kx * kx + ky * ky < bf_r2) w[0] += I;
+    w[1] += I;
+    w[2] += I * kx;
+    w[3] += I * ky;
+    w2[0] += I * kx * kx;
+    w2[1] += I * ky * ky;
   }
   block_sum5(w, red);
+  block_sum5(w2, red);
   if (tid == 0) {
+    // Counts: the intensities scaled to `dose`. Sums of independent Poisson
+    // counts are Poisson with the summed means; at these doses (1e4 - 1e5 per
+    // pattern) they are drawn from their normal approximations: bright field
+    // N(m, m), total N(dose, dose), first moments with variances
+    // sum(k^2 lambda). The centre of mass is their ratio.
+    const float scale = dose / w[1];
+    const uint64_t key = mix64(seed ^ mix64(((uint64_t)sc << 32) | (uint32_t)j)) * 8;
+    const float mbf = w[0] * scale, mx = w[2] * scale, my = w[3] * scale;
+    const float vx = w2[0] * scale, vy = w2[1] * scale;
+    const float nbf = fmaxf(0.f, mbf + sqrtf(mbf) * normal01(key));
+    const float ntot = fmaxf(1.f, dose + sqrtf(dose) * normal01(key + 1));
+    const float nx = mx + sqrtf(vx) * normal01(key + 2);
+    const float ny = my + sqrtf(vy) * normal01(key + 3);
     const size_t o = (size_t)sc * J + j;
-    bf[o] = w[0];
-    com_x[o] = w[1] > 0.f ? w[2] / w[1] : 0.f;
-    com_y[o] = w[1] > 0.f ? w[3] / w[1] : 0.f;
+    bf[o] = nbf;
+    com_x[o] = nx / ntot;
+    com_y[o] = ny / ntot;
     // bilinear phase at the (continuous) position, periodic
     const float* ph = phase + (size_t)sc * P * P;
     const float fx = floorf(posx), fy = floorf(posy);
@@ -247,15 +252,16 @@ using namespace pty::nn_data;
 extern "C" {
 
 int ptycho_nn_lattice_objects(int32_t count, int32_t object_px, float sampling,
-                              const float* params, float sigma, float peak, float* phase,
-                              void* object, void* stream) {
-  if (count < 1 || object_px < 8 || !params || !phase || !object || !(sampling > 0.f) ||
-      !(sigma > 0.f))
+                              const float* params, float sigma, float peak, float sigma_blur,
+                              float* phase, float* phase_blur, void* object, void* stream) {
+  if (count < 1 || object_px < 8 || !params || !phase || !phase_blur || !object ||
+      !(sampling > 0.f) || !(sigma > 0.f) || !(sigma_blur >= 0.f))
     return PTYCHO_ERR_INVALID_ARGUMENT;
   const size_t total = (size_t)count * object_px * object_px;
   lattice_objects_kernel<<<(unsigned)((total + 255) / 256), 256, 0,
                            static_cast<cudaStream_t>(stream)>>>(
-      count, object_px, sampling, params, sigma, peak, phase, static_cast<float2*>(object));
+      count, object_px, sampling, params, sigma, peak, sigma_blur, phase, phase_blur,
+      static_cast<float2*>(object));
   return cudaGetLastError() == cudaSuccess ? PTYCHO_OK : PTYCHO_ERR_CUDA;
 }
 

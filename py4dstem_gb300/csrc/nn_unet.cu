@@ -140,7 +140,9 @@ ActLayout act_layout(int nb, int H, int W) {
   A.g[0] = take(2 * max_out);
   A.g[1] = take(2 * max_out);
   A.wpart = take(max_part);
-  A.red = take(4 * 4096);
+  // per-block partials of the loss (one float per block) and of the head's
+  // gradient (kHeadC + 1 floats per block), blocks of kT pixels
+  A.red = take(4 * (size_t)((n0 + kT - 1) / kT) * (kHeadC + 1));
   A.err = take(sizeof(int));
   A.total = off;
   return A;

@@ -248,6 +248,13 @@ static int run_batch(const ptycho_geometry* g, void* object, void* probe,
   if (e != cudaSuccess) return cuda_fail(e, "probe spectrum kernel");
   a.prepare_spectrum = (g->flags & PTYCHO_FLAG_PREPARE_SPECTRUM) && !a.fix_probe ? 1 : 0;
   a.staging_t = position_v2_eligible(a) ? 1 : 0;
+  // the plain single-slice GD instantiation of the position kernel stages no
+  // |O|^2 terms; the probe-side reduction gathers them from the object
+  a.nprobe_from_object = !a.staging_t && !a.projection && !a.forward_only &&
+                                 !a.keep_farfield && !a.exact_probe_grad && a.T == 1 &&
+                                 a.M == 1 && !a.mixed_formula
+                             ? 1
+                             : 0;
   e = a.staging_t ? launch_position_v2(a, s) : launch_position_kernel(a, s);
   if (e != cudaSuccess) return cuda_fail(e, "position kernel");
   e = launch_reduce_and_update(a, s);

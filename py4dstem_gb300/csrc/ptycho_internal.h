@@ -29,6 +29,8 @@ struct BatchArgs {
   int exact_probe_grad;    // probe term through the adjoint of the sub-pixel shift
   int prepare_spectrum;    // after the probe update, the next batch's probe spectrum
   int nobj_only;           // object reduction of the |P|^2 terms alone (probe overlap)
+  int nprobe_from_object;  // plain single-slice GD: the probe side gathers |O|^2 from the
+                           // object instead of reading staged terms (none are written)
   const float* aperture;   // (N) Fourier amplitude of the initial probe (aperture constraint)
 
   void* object;                 // (T,Px,Py) float2 or float

@@ -524,7 +524,9 @@ __device__ __forceinline__ void position_one(const BatchArgs& a, const int b, fl
         }
         const float2 yv = c_conj_mul(o, chi);
         if (exact) buf[x * LD + y] = yv; else pst[e] = yv;
-        if (m == 0) a.st_nprobe[(size_t)b * N + e] = c_abs2(o);
+        // (the plain GD instantiation stages no |O|^2: the probe-side
+        // reduction gathers it from the object, nprobe_from_object)
+        if (kMode != 1 && m == 0) a.st_nprobe[(size_t)b * N + e] = c_abs2(o);
       }
       }
       __syncthreads();

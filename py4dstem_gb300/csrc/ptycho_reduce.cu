@@ -327,8 +327,32 @@ __global__ void __launch_bounds__(NT) probe_reduce_kernel(BatchArgs a) {
     a.probe_part[((size_t)c * a.M + m) * N + e] = acc;
   }
   float n = 0.f;
+  if (a.nprobe_from_object) {
+    // |O|^2 of each position's patch at this probe pixel, gathered from the
+    // object (the plain GD position kernel stages none)
+    const int x = e / a.Sy, y = e % a.Sy;
+#pragma unroll 4
+    for (int b = lo; b < hi; ++b) {
+      const int2 r = a.pos_round[b];
+      int ox = pmod(r.x - a.Sx / 2, a.Px) + (x + a.Sx / 2) % a.Sx;
+      int oy = pmod(r.y - a.Sy / 2, a.Py) + (y + a.Sy / 2) % a.Sy;
+      if (ox >= a.Px) ox -= a.Px;
+      if (oy >= a.Py) oy -= a.Py;
+      const size_t idx = (size_t)ox * a.Py + oy;
+      float2 o;
+      if (a.potential) {
+        float sv, cv;
+        sincosf(reinterpret_cast<const float*>(a.object)[idx], &sv, &cv);
+        o = make_float2(cv, sv);
+      } else {
+        o = reinterpret_cast<const float2*>(a.object)[idx];
+      }
+      n += o.x * o.x + o.y * o.y;
+    }
+  } else {
 #pragma unroll 8
-  for (int b = lo; b < hi; ++b) n += snp[(size_t)b * N + e];
+    for (int b = lo; b < hi; ++b) n += snp[(size_t)b * N + e];
+  }
   a.probe_npart[(size_t)c * N + e] = n;
 }
 

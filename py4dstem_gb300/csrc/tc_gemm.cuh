@@ -19,8 +19,9 @@
 // Pipeline: two shared-memory stages. The threads fill stage s while the tensor
 // core works on stage s^1; tcgen05.commit signals an mbarrier per stage when
 // the MMAs reading it are done. Every wait is bounded (about one second of
-// %globaltimer): on time-out the kernel records an error in *err, stops issuing
-// and frees its TMEM before it returns.
+// %globaltimer): on time-out the kernel records where in *err (non-zero), stops
+// issuing, waits (bounded) for the MMAs in flight and frees its TMEM before it
+// returns.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -205,7 +206,7 @@ __global__ void __launch_bounds__(kGemmThreads) tc_gemm_kernel(int M, int N, int
     const int s = it & 1;
     if (it >= 2) {
       // the MMAs of iteration it - 2 read this stage
-      if (!mbar_wait_bounded(&bar[s], ((it >> 1) - 1) & 1)) atomicExch(&abort_flag, 1);
+      if (!mbar_wait_bounded(&bar[s], ((it >> 1) - 1) & 1)) atomicExch(&abort_flag, 2 + it);
     }
     __syncthreads();
     if (abort_flag) break;
@@ -249,7 +250,9 @@ __global__ void __launch_bounds__(kGemmThreads) tc_gemm_kernel(int M, int N, int
   __syncthreads();
   tc_fence_after();
   const bool ok = !abort_flag;
-  if (!ok && tid == 0) atomicExch(err, 1);
+  // *err: 1 = the final wait timed out, 2 + it = the wait before refilling a
+  // stage at iteration it (the largest code of any CTA is kept)
+  if (!ok && tid == 0) atomicMax(err, abort_flag);
   // epilogue: warp w reads TMEM lanes 32w..32w+31 (rows), 16 columns at a time
   const int row = row0 + warp * 32 + (tid & 31);
   if (ok) {

@@ -12,8 +12,9 @@ instead (:func:`reconstruct_with_fallback`).
 
 Everything runs on the GPU in this library's own kernels: the network
 (tensor-core implicit-GEMM convolutions, libptycho_gb300 ``ptycho_nn_*``), its
-training data (the ptychographic forward model of the benchmark generator with
-Poisson noise, ``ptycho_nn_lattice_objects`` / ``ptycho_nn_scan_images``), and
+training data (the ptychographic forward model of the benchmark generator, the
+Poisson noise of the virtual-detector sums, ``ptycho_nn_lattice_objects`` /
+``ptycho_nn_scan_images``), and
 its input at inference (``ptycho_nn_virtual_images`` on the preprocessed
 amplitudes). PyTorch only holds device memory.
 
@@ -77,6 +78,10 @@ class ScanGeometry:
     dose: float = 1e5
     lattice_range: tuple = (2.5, 5.0)
     defocus_range: tuple = (0.0, 200.0)
+    # the target is the object phase blurred to about the probe's resolution
+    # (a point sample between scan positions 3 pixels apart would alias the
+    # 0.4 A atoms)
+    target_blur_ang: float = 0.5
 
     @property
     def bf_radius_px(self) -> float:
@@ -146,12 +151,14 @@ def generate_training_set(num_scans: int, geom: ScanGeometry = ScanGeometry(), s
         tpos = torch.from_numpy(pos).to(dev)
         spectra = spectra_all[torch.from_numpy(dfi).to(dev)].contiguous()
         phase = torch.empty((n, P, P), dtype=torch.float32, device=dev)
+        blur = torch.empty_like(phase)
         obj = torch.empty((n, P, P), dtype=torch.complex64, device=dev)
         _check(lib.ptycho_nn_lattice_objects(n, P, geom.sampling_ang, _p(tparams), 0.4, 0.3,
-                                             _p(phase), _p(obj), stream))
+                                             geom.target_blur_ang, _p(phase), _p(blur), _p(obj),
+                                             stream))
         bf = torch.empty((n, J), dtype=torch.float32, device=dev)
         cx, cy, tg = torch.empty_like(bf), torch.empty_like(bf), torch.empty_like(bf)
-        _check(lib.ptycho_nn_scan_images(n, J, P, _p(spectra), _p(obj), _p(phase), _p(tpos),
+        _check(lib.ptycho_nn_scan_images(n, J, P, _p(spectra), _p(obj), _p(blur), _p(tpos),
                                          geom.dose, geom.bf_radius_px,
                                          seed * 1000003 + s0, _p(bf), _p(cx), _p(cy), _p(tg),
                                          stream))
@@ -374,7 +381,8 @@ def run_to_target(ptycho, object_init, max_iter: int, target: Optional[float], b
     `object_init` (None: its own initial object) through the device state and
     the graph-replayed iteration driver of reconstruct(), reading the error
     after every iteration like the reference; stops after max_iter iterations or
-    at the first error <= target. Returns (errors, seconds)."""
+    at the first error <= target. Returns the errors and, for each iteration,
+    the seconds since the start (state set-up included)."""
     torch = _torch()
     from . import engine
 
@@ -395,27 +403,31 @@ def run_to_target(ptycho, object_init, max_iter: int, target: Optional[float], b
                                  mean_intensity=p._mean_diffraction_intensity)
     rs = np.random.RandomState(seed)
     order = np.arange(J)
-    errors = []
+    errors, times = [], []
     for _ in range(max_iter):
         rs.shuffle(order)
         drv.iterate(order)
-        errors.append(float(drv.error()))
+        errors.append(float(drv.error()))  # synchronises
+        times.append(time.perf_counter() - t0)
         if target is not None and errors[-1] <= target:
             break
-    torch.cuda.synchronize()
-    return errors, time.perf_counter() - t0
+    return errors, times
 
 
 def compare_starts(net: UNet, ptycho, geom: ScanGeometry, plain_iter: int, batch: int,
                    seed: int):
     """The plain start run for plain_iter iterations, then the learned start run
     until it reaches the plain run's final error (at most plain_iter
-    iterations). The learned run's time includes the network input, the network
+    iterations). Times compare the first iteration at which each run reaches
+    that error; the learned run's time includes the network input, the network
     and the start object. Returns a dict; `fallback` is True when the learned
     run did not reach the target (the plain result then stands)."""
     torch = _torch()
     plain, t_plain = run_to_target(ptycho, None, plain_iter, None, batch, seed)
     target = plain[-1]
+    # the plain run reaches its final error first at iteration kp (its error
+    # need not fall monotonically)
+    kp = iterations_to_target(plain, target)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     guess = initial_object(net, ptycho, geom)
@@ -423,8 +435,11 @@ def compare_starts(net: UNet, ptycho, geom: ScanGeometry, plain_iter: int, batch
     t_net = time.perf_counter() - t0
     learned, t_learned = run_to_target(ptycho, guess, plain_iter, target, batch, seed)
     k = iterations_to_target(learned, target)
-    return {"plain_iterations": plain_iter, "plain_error": target, "plain_s": t_plain,
-            "learned_iterations": k, "learned_s": t_net + t_learned, "network_s": t_net,
-            "learned_first_error": learned[0], "plain_first_error": plain[0],
-            "fallback": k is None,
-            "time_ratio": (t_net + t_learned) / t_plain if k is not None else None}
+    t_l = t_net + t_learned[k - 1] if k is not None else None
+    return {"plain_iterations": plain_iter, "plain_error": target,
+            "plain_first_at_target": kp, "plain_s_to_target": t_plain[kp - 1],
+            "plain_s": t_plain[-1], "learned_iterations": k, "learned_s": t_l,
+            "network_s": t_net, "learned_first_error": learned[0],
+            "plain_first_error": plain[0], "fallback": k is None,
+            "time_ratio": t_l / t_plain[kp - 1] if k is not None else None,
+            "plain_errors": plain, "learned_errors": learned}

@@ -88,11 +88,54 @@ def atom_lattice_phase(shape, sampling, lattice_a, rng, sigma_ang=0.4, peak_rad=
     return phase
 
 
+def portable_normal(rng, size):
+    """Standard normal variates by Box-Muller from the generator's uniform
+    doubles, which every NumPy version and CPU draws identically from the same
+    PCG64 state (unlike Generator.normal / Generator.poisson, whose algorithms
+    and rounding may differ between NumPy versions and CPUs)."""
+    n = int(np.prod(size))
+    u = rng.random(2 * ((n + 1) // 2)).reshape(2, -1)
+    r = np.sqrt(-2.0 * np.log1p(-u[0]))
+    z = np.concatenate([r * np.cos(2 * np.pi * u[1]), r * np.sin(2 * np.pi * u[1])])
+    return z[:n].reshape(size)
+
+
+def portable_poisson(lam, rng):
+    """Poisson counts by inversion of the cumulative distribution (SciPy's
+    pdtr) against the generator's uniform doubles: the smallest k with
+    u <= P(X <= k). A count changes between machines only when a uniform falls
+    within rounding (~1e-15) of a cumulative probability, so the counts agree
+    across CPUs and library versions with near certainty."""
+    from scipy.special import ndtri, pdtr
+
+    lam = np.asarray(lam, dtype=np.float64)
+    flat = lam.ravel()
+    u = rng.random(flat.size)
+    k = np.zeros(flat.size)
+    # k = 0 where u <= P(X = 0) = exp(-lambda) (most dark-field pixels)
+    rest = np.nonzero(u > np.exp(-flat))[0]
+    lr, ur = flat[rest], u[rest]
+    # a starting guess from the normal approximation, then exact corrections
+    kr = np.maximum(1.0, np.floor(lr + np.sqrt(lr) * ndtri(ur) + 0.5))
+    act = np.nonzero(ur > pdtr(kr, lr))[0]
+    while act.size:  # too small: step up
+        kr[act] += 1
+        act = act[ur[act] > pdtr(kr[act], lr[act])]
+    act = np.nonzero((kr >= 2) & (ur <= pdtr(kr - 1, lr)))[0]
+    while act.size:  # too large: step down (k >= 1 holds: u > P(X = 0))
+        kr[act] -= 1
+        act = act[(kr[act] >= 2) & (ur[act] <= pdtr(kr[act] - 1, lr[act]))]
+    k[rest] = kr
+    return k.astype(np.int64).reshape(lam.shape)
+
+
 def random_object(shape, sampling, rng, lattice_a=3.9, noise_std=0.05, smooth_px=4.0,
-                  sigma_ang=0.4, peak_rad=0.3):
+                  sigma_ang=0.4, peak_rad=0.3, portable=False):
     """Complex transmission function exp(-0.1 phi) exp(i phi) (complex128)."""
     phase = atom_lattice_phase(shape, sampling, lattice_a, rng, sigma_ang, peak_rad)
-    phase += gaussian_filter(rng.normal(0.0, noise_std, size=shape), smooth_px)
+    noise = (noise_std * portable_normal(rng, shape) if portable
+             else rng.normal(0.0, noise_std, size=shape))
+    phase += gaussian_filter(noise, smooth_px)
     return np.exp(-0.1 * phase) * np.exp(1j * phase)
 
 
@@ -125,7 +168,7 @@ def _fresnel(gpts, sampling, wavelength, dz):
 
 
 def _simulate_numpy(objects, probes, weights, positions_px, propagators, dose, rng,
-                    batch=256):
+                    batch=256, portable=False):
     """Far-field intensities, (J, Sx, Sy) float32, detector-centred, Poisson noise."""
     T = objects.shape[0]
     M, sx, sy = probes.shape
@@ -155,7 +198,8 @@ def _simulate_numpy(objects, probes, weights, positions_px, propagators, dose, r
                     wave = np.fft.ifft2(np.fft.fft2(wave) * propagators[s])
             intensity += weights[m] * np.abs(np.fft.fft2(wave)) ** 2
         intensity *= dose / intensity.sum(axis=(-2, -1), keepdims=True)
-        counts = rng.poisson(intensity).astype(np.float32)
+        counts = (portable_poisson(intensity, rng) if portable
+                  else rng.poisson(intensity)).astype(np.float32)
         out[start:start + batch] = np.fft.fftshift(counts, axes=(-2, -1))
     return out
 
@@ -226,11 +270,19 @@ def make_scan(
     backend: str = "numpy",
     device: str = "cuda",
 ) -> ScanCase:
-    """Generate one seeded scan (see module docstring for the model)."""
+    """Generate one seeded scan (see module docstring for the model).
+
+    backend: "numpy" (complex128 model, NumPy's Poisson and normal samplers),
+    "portable" (the same model with every random variate drawn from the
+    generator's uniform doubles, so that the counts agree across CPUs and NumPy
+    versions: the reference fixtures at the timed sizes are regenerated from
+    their seed instead of stored), or "torch" (complex64 on a CUDA device)."""
     rng = np.random.default_rng(seed)
     roi = (detector, detector)
     obj_shape = (object_px, object_px)
-    objects = np.stack([random_object(obj_shape, sampling, rng, lattice_a=lattice_a)
+    portable = backend == "portable"
+    objects = np.stack([random_object(obj_shape, sampling, rng, lattice_a=lattice_a,
+                                      portable=portable)
                         for _ in range(num_slices)])
     pos_ang = raster_positions(scan_shape[0], scan_shape[1], step_ang, jitter_ang, rng)
     pos_px = positions_in_pixels(pos_ang, sampling, roi, obj_shape)
@@ -241,11 +293,16 @@ def make_scan(
                         parameters={"defocus": defocus}).build()._array
     probes = [base.astype(np.complex128)]
     for m in range(1, num_modes):
-        perturb = {
-            "defocus": defocus + rng.normal(0.0, 20.0),
-            "astigmatism": abs(rng.normal(0.0, 10.0)),
-            "astigmatism_angle": rng.uniform(0, np.pi),
-        }
+        if portable:
+            z = portable_normal(rng, 2)
+            perturb = {"defocus": defocus + 20.0 * z[0], "astigmatism": abs(10.0 * z[1]),
+                       "astigmatism_angle": rng.uniform(0, np.pi)}
+        else:
+            perturb = {
+                "defocus": defocus + rng.normal(0.0, 20.0),
+                "astigmatism": abs(rng.normal(0.0, 10.0)),
+                "astigmatism_angle": rng.uniform(0, np.pi),
+            }
         pm = ComplexProbe(energy=energy, gpts=roi, sampling=(sampling, sampling),
                           semiangle_cutoff=semiangle, rolloff=2.0,
                           parameters=perturb).build()._array
@@ -256,8 +313,9 @@ def make_scan(
     propagators = [_fresnel(roi, sampling, wavelength, slice_thickness)
                    for _ in range(num_slices - 1)]
 
-    if backend == "numpy":
-        patterns = _simulate_numpy(objects, probes, weights, pos_px, propagators, dose, rng)
+    if backend in ("numpy", "portable"):
+        patterns = _simulate_numpy(objects, probes, weights, pos_px, propagators, dose, rng,
+                                   portable=portable)
     elif backend == "torch":
         patterns = _simulate_torch(objects, probes, weights, pos_px, propagators, dose,
                                    seed, device)

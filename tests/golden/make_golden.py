@@ -605,9 +605,10 @@ def make_volume_ops(ref):
 # Workloads at the sizes that are timed ("size_" prefix). Their datacubes are too
 # large to commit (1 GiB of counts for the 128 x 128 scan), so a fixture keeps
 # the generator arguments and a SHA-256 digest of the uint16 counts instead; the
-# GPU test regenerates the counts (synthetic.make_scan, NumPy backend: integer
-# Poisson counts drawn from PCG64, which agree across CPU architectures) and
-# checks the digest before it compares anything. The reference's float32
+# GPU test regenerates the counts (synthetic.make_scan with the "portable"
+# backend: every random variate from the generator's uniform doubles, Poisson
+# counts by inversion, so that the counts agree across CPUs and NumPy versions)
+# and checks the digest before it compares anything. The reference's float32
 # amplitudes are pinned the same way (digest and per-pattern sums). The float32
 # oracle with every FFT rounded through complex128 (the reference's own
 # rounding floor) and the float64 oracle run here, on the reference's
@@ -618,7 +619,7 @@ SIZE_CASES = {
     # 128^2 detector, 512^2 object, 1e5 e-/pattern, batch 1024, uniform start
     "size_ss_scan128_det128": dict(
         gen=dict(name="size_ss", seed=1234, scan_shape=(128, 128), step_ang=0.75,
-                 jitter_ang=0.05, detector=128, object_px=512, dose=1e5),
+                 jitter_ang=0.05, detector=128, object_px=512, dose=1e5, backend="portable"),
         cls="single", ctor=dict(object_fov_ang=(128.0, 128.0)),
         rec=dict(num_iter=3, max_batch_size=1024, step_size=0.5, seed_random=1234)),
     # multislice through the adjoint: 8 slices of 20 A, 64 x 64 scan at 0.4 A,
@@ -626,7 +627,7 @@ SIZE_CASES = {
     "size_ms_T8_scan64_det128": dict(
         gen=dict(name="size_ms", seed=2, scan_shape=(64, 64), step_ang=0.4, jitter_ang=0.05,
                  detector=128, object_px=256, semiangle=25.0, defocus=50.0, dose=1e4,
-                 num_slices=8, slice_thickness=20.0),
+                 num_slices=8, slice_thickness=20.0, backend="portable"),
         cls="multi", ctor=dict(object_fov_ang=(64.0, 64.0), num_slices=8,
                                slice_thicknesses=20.0),
         ctor_optics=dict(semiangle_cutoff=25.0, defocus=50.0),
@@ -637,7 +638,7 @@ SIZE_CASES = {
     "size_mixed_M4_scan96_det128": dict(
         gen=dict(name="size_mx", seed=3, scan_shape=(96, 96), step_ang=0.5, jitter_ang=0.05,
                  detector=128, object_px=512, dose=1e4, num_modes=4,
-                 mode_weights=(0.7, 0.15, 0.1, 0.05)),
+                 mode_weights=(0.7, 0.15, 0.1, 0.05), backend="portable"),
         cls="mixed", ctor=dict(object_fov_ang=(128.0, 128.0), num_probes=4),
         probe_guess=True,
         rec=dict(num_iter=2, max_batch_size=256, step_size=0.5, seed_random=3)),
@@ -736,6 +737,7 @@ def make_size_case(ref, name, spec):
     meta = dict(cls=spec["cls"], ctor=ctor, preprocess=PRE, reconstruct=spec["rec"],
                 r_pixel_size=r, q_pixel_size=q, generator=spec["gen"],
                 counts_digest=counts_digest(data), amplitudes_digest=amp_digest,
+                counts_total=int(data.astype(np.int64).sum()),
                 probe_guess=bool(spec.get("probe_guess")), stats=stats)
     path = os.path.join(HERE, f"{name}.npz")
     np.savez_compressed(

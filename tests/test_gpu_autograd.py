@@ -25,6 +25,9 @@ CASES = {
     "multislice": dict(S=64, J=16, slices=3),
     "mixed": dict(S=64, J=16, modes=2),
     "mixed_multislice": dict(S=64, J=16, slices=2, modes=2),
+    # the multislice workload's depth and detector: 8 slices at 128^2 (a 3 x 3
+    # scan keeps the float64 finite differences short)
+    "multislice_T8_det128": dict(S=128, J=9, slices=8),
 }
 
 
@@ -145,3 +148,36 @@ def test_gradient_descent_with_torch_optimizer(cuda):
         losses.append(float(loss))
     assert losses[-1] < losses[0]
     assert probe.grad is None
+
+
+def test_sixteen_slices_at_128_det_fit_and_report_memory(cuda):
+    """16 slices of a 256^2 object at a 128^2 detector, one batch of 1024
+    positions: the backward recomputes the batch (forward through every
+    slice, then the adjoint) with that batch's per-slice probes in the
+    workspace, T B N 12 bytes (3.2 GB here), whatever the scan size. The peak
+    device memory of loss and gradient stays within a few times that."""
+    torch = cuda
+    from py4dstem_gb300.autograd import PtychoForwardModel
+
+    rng = np.random.default_rng(8)
+    T, S, P, J = 16, 128, 256, 1024
+    amps = rng.random((J, S, S), dtype=np.float32)
+    pos = (rng.random((J, 2)) * (P - S) + S / 2).astype(np.float32)
+    k = np.fft.fftfreq(S, 0.25)
+    h = np.exp(-1j * np.pi * 0.0197 * 20.0 * (k[:, None] ** 2 + k[None] ** 2))
+    props = np.stack([h] * (T - 1)).astype(np.complex64)
+    torch.cuda.synchronize()
+    torch.cuda.reset_peak_memory_stats()
+    base = torch.cuda.memory_allocated()
+    model = PtychoForwardModel(amps, pos, (P, P), num_slices=T, num_probes=1, potential=False,
+                               propagators=props, mixed_state=False, max_batch=J)
+    obj = torch.ones((T, P, P), dtype=torch.complex64, device="cuda")
+    probe = torch.from_numpy((rng.standard_normal((1, S, S)) + 0j).astype(np.complex64)).cuda()
+    loss, g_obj, g_probe = model.loss_and_gradient(obj, probe)
+    torch.cuda.synchronize()
+    peak = torch.cuda.max_memory_allocated() - base
+    stash = T * J * S * S * 12
+    print(f"\n16 slices, B=1024, 128^2: peak {peak / 1e9:.2f} GB, slice stash {stash / 1e9:.2f} GB")
+    assert np.isfinite(float(loss))
+    assert bool(torch.isfinite(g_obj).all()) and bool(torch.isfinite(g_probe).all())
+    assert peak < 3 * stash

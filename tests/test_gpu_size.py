@@ -61,11 +61,12 @@ class SizeGolden:
     def regenerate(self):
         """The seeded counts, checked against the digest of the reference's input."""
         case = synthetic.make_scan(**self.meta["generator"])
+        np.testing.assert_array_equal(case.scan_positions_ang, self.scan_positions_ang)
         counts = np.ascontiguousarray(case.datacube.data.astype(np.uint16))
         digest = hashlib.sha256(counts.tobytes()).hexdigest()
         assert digest == self.meta["counts_digest"], (
-            f"{self.name}: regenerated counts differ from the reference's input")
-        np.testing.assert_array_equal(case.scan_positions_ang, self.scan_positions_ang)
+            f"{self.name}: regenerated counts differ from the reference's input (total "
+            f"{int(counts.sum(dtype=np.int64))}, reference {self.meta.get('counts_total')})")
         return case
 
     def build(self, case):
