@@ -143,13 +143,17 @@ class MultiScanReconstruction:
             root.wait_stream(s)
 
     def _graph(self, concurrent: bool):
-        if concurrent not in self._graphs:
+        # a captured graph holds the kernels chosen at capture time, so it is
+        # kept per 128^2 kernel schedule as well
+        key = (concurrent, _native.lib().ptycho_set_kernel_schedule(128, 0))
+        _native.lib().ptycho_set_kernel_schedule(128, key[1])
+        if key not in self._graphs:
             torch = self.torch
             g = torch.cuda.CUDAGraph()
             with torch.cuda.graph(g, stream=self.root):
                 self._issue(concurrent)
-            self._graphs[concurrent] = g
-        return self._graphs[concurrent]
+            self._graphs[key] = g
+        return self._graphs[key]
 
     def _next_orders(self):
         rows = np.zeros(tuple(self.order_all.shape), dtype=np.int32)
@@ -181,17 +185,30 @@ class MultiScanReconstruction:
         key = ("multiscan", self.use_graph, tuple(self.J), tuple(self.batch),
                tuple(tuple(p._region_of_interest_shape) for p in self.scans),
                tuple((p._num_slices, p._num_probes) for p in self.scans))
-        cands = [{"concurrent": True}, {"concurrent": False}]
-        if self.concurrent != "auto":
-            cands = [{"concurrent": bool(self.concurrent)}]
-        key = key + (tuple(c["concurrent"] for c in cands),)
+        concs = [True, False] if self.concurrent == "auto" else [bool(self.concurrent)]
+        # the 128 x 128 kernel schedule (1: shared-memory transforms, 2:
+        # register-resident four-step transforms) matters for single-slice,
+        # single-probe gradient-descent scans at a 128^2 detector only
+        eligible = any(tuple(p._region_of_interest_shape) == (128, 128) and p._num_slices == 1
+                       and p._num_probes == 1 and not p._mixed for p in self.scans)
+        scheds = [1, 2] if eligible else [0]
+        cands = [{"concurrent": c, "schedule": sc} for c in concs for sc in scheds]
+        key = key + (tuple((c["concurrent"], c["schedule"]) for c in cands),)
+        lib = _native.lib()
+
+        def run(c):
+            prev = lib.ptycho_set_kernel_schedule(128, c["schedule"])
+            try:
+                self._run_iteration(c["concurrent"], orders_dev, 0)
+            finally:
+                lib.ptycho_set_kernel_schedule(128, prev)
+
         torch.cuda.synchronize()  # the snapshot must see the finished iteration
         snap = self._snapshot()
         torch.cuda.synchronize()
         with torch.cuda.stream(self.root):
-            best, timings = autotune.tune(
-                key, cands, lambda c: self._run_iteration(c["concurrent"], orders_dev, 0),
-                warmup=1, reps=3)
+            best, timings = autotune.tune(key, cands, run, warmup=1, reps=3,
+                                          device=autotune.device_key())
         torch.cuda.synchronize()
         self._restore(snap)
         torch.cuda.synchronize()  # later iterations run on other streams
@@ -203,6 +220,17 @@ class MultiScanReconstruction:
         the time of one concurrent, eager iteration from the initial state; the
         state is rebuilt from the scans' host arrays for every candidate."""
         torch = self.torch
+        key = ("multiscan-batch", tuple(self.J),
+               tuple(tuple(p._region_of_interest_shape) for p in self.scans),
+               tuple((p._num_slices, p._num_probes) for p in self.scans))
+        dev = autotune.device_key()
+        hit = autotune.lookup(key, dev)
+        if hit is not None:
+            b_best = hit[0]["batch"]
+            self._rebuild([min(b_best, j) for j in self.J])
+            torch.cuda.synchronize()
+            self.tuning = dict(self.tuning or {}, batch=b_best, batch_timings_ms=hit[1])
+            return
         timings = []
         for b in (128, 256, 512, 1024):
             self._rebuild([min(b, j) for j in self.J])
@@ -214,6 +242,7 @@ class MultiScanReconstruction:
             timings.append(({"batch": b}, t))
         torch.cuda.synchronize()
         b_best = min(timings, key=lambda x: x[1])[0]["batch"]
+        autotune.remember(key, {"batch": b_best}, timings, dev)
         self._rebuild([min(b_best, j) for j in self.J])
         torch.cuda.synchronize()
         self.tuning = dict(self.tuning or {}, batch=b_best, batch_timings_ms=timings)
@@ -253,10 +282,15 @@ class MultiScanReconstruction:
             best = (self.tuning or {}).get("choice",
                                            {"concurrent": self.concurrent is not False})
         concurrent = bool(best["concurrent"])
-        with torch.cuda.stream(self.root):
-            for it in range(1, num_iter):
-                self._run_iteration(concurrent, orders_dev, it)
-                errs[it].copy_(self.acc_all)
+        lib = _native.lib()
+        prev = lib.ptycho_set_kernel_schedule(128, int(best.get("schedule", 0)))
+        try:
+            with torch.cuda.stream(self.root):
+                for it in range(1, num_iter):
+                    self._run_iteration(concurrent, orders_dev, it)
+                    errs[it].copy_(self.acc_all)
+        finally:
+            lib.ptycho_set_kernel_schedule(128, prev)
         torch.cuda.synchronize()
         self._finish(errs.cpu().numpy())
         return self
