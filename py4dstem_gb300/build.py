@@ -21,6 +21,7 @@ LIB_NAME = "libptycho_gb300.so"
 LIB_PATH = os.path.join(LIB_DIR, LIB_NAME)
 
 SOURCES = ["ptycho_position_128.cu", "ptycho_position_96.cu", "ptycho_position_64.cu",
+           "ptycho_position_96x128.cu", "ptycho_position_128x96.cu",
            "ptycho_position_48.cu", "ptycho_position_32.cu", "ptycho_gd128.cu",
            "ptycho_reduce.cu", "ptycho_preprocess.cu", "ptycho_volume.cu", "ptycho_position.cu",
            "ptycho_capi.cu", "nn_conv.cu", "nn_unet.cu", "nn_data.cu"]

@@ -63,7 +63,8 @@ int check_geometry(const ptycho_geometry* g) {
   if (g->num_probes > 16) return fail(PTYCHO_ERR_UNSUPPORTED, "at most 16 probe modes");
   if (!roi_supported(g->roi_x, g->roi_y))
     return fail(PTYCHO_ERR_UNSUPPORTED,
-                "ROI %dx%d has no fused kernel (supported: square 32, 48, 64, 96, 128)",
+                "ROI %dx%d has no fused kernel (supported: square 32, 48, 64, 96, 128 "
+                "and 96 x 128, 128 x 96)",
                 g->roi_x, g->roi_y);
   if (g->object_x < g->roi_x || g->object_y < g->roi_y)
     return fail(PTYCHO_ERR_UNSUPPORTED, "object %dx%d smaller than ROI %dx%d", g->object_x,

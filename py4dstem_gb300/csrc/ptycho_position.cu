@@ -1,6 +1,6 @@
-// Dispatch of the fused per-position kernels on the region-of-interest edge.
-// The kernels are templates in ptycho_position.cuh, instantiated once per edge
-// in ptycho_position_<S>.cu.
+// Dispatch of the fused per-position kernels on the region-of-interest shape.
+// The kernels are templates in ptycho_position.cuh, instantiated once per
+// shape in ptycho_position_<S>.cu (square) and ptycho_position_<SX>x<SY>.cu.
 #include <cuda_runtime.h>
 
 #include "ptycho_internal.h"
@@ -20,29 +20,38 @@ PTY_DECLARE_SIZE(48)
 PTY_DECLARE_SIZE(64)
 PTY_DECLARE_SIZE(96)
 PTY_DECLARE_SIZE(128)
+PTY_DECLARE_SIZE(96x128)
+PTY_DECLARE_SIZE(128x96)
+
+namespace {
+constexpr int roi_key(int sx, int sy) { return sx * 4096 + sy; }
+}  // namespace
 
 bool roi_supported(int Sx, int Sy) {
-  if (Sx != Sy) return false;
-  switch (Sx) {
-    case 32:
-    case 48:
-    case 64:
-    case 96:
-    case 128:
+  switch (roi_key(Sx, Sy)) {
+    case roi_key(32, 32):
+    case roi_key(48, 48):
+    case roi_key(64, 64):
+    case roi_key(96, 96):
+    case roi_key(128, 128):
+    case roi_key(96, 128):
+    case roi_key(128, 96):
       return true;
     default:
       return false;
   }
 }
 
-#define PTY_DISPATCH(FN, A, S)                 \
-  switch ((A).Sx) {                            \
-    case 32: return FN##_32(A, S);             \
-    case 48: return FN##_48(A, S);             \
-    case 64: return FN##_64(A, S);             \
-    case 96: return FN##_96(A, S);             \
-    case 128: return FN##_128(A, S);           \
-    default: return cudaErrorInvalidValue;     \
+#define PTY_DISPATCH(FN, A, S)                                  \
+  switch (roi_key((A).Sx, (A).Sy)) {                            \
+    case roi_key(32, 32): return FN##_32(A, S);                 \
+    case roi_key(48, 48): return FN##_48(A, S);                 \
+    case roi_key(64, 64): return FN##_64(A, S);                 \
+    case roi_key(96, 96): return FN##_96(A, S);                 \
+    case roi_key(128, 128): return FN##_128(A, S);              \
+    case roi_key(96, 128): return FN##_96x128(A, S);            \
+    case roi_key(128, 96): return FN##_128x96(A, S);            \
+    default: return cudaErrorInvalidValue;                      \
   }
 
 cudaError_t launch_probe_spectrum(const BatchArgs& a, cudaStream_t s) {

@@ -1125,26 +1125,30 @@ cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
 }  // namespace
 }  // namespace pty
 
-// Externally visible launchers of the kernels for one square region of
-// interest S x S with NT threads per block (one translation unit per S).
-#define PTY_POSITION_INSTANCES(S, NT)                                                    \
+// Externally visible launchers of the kernels for one region of interest
+// SX x SY with NT threads per block, named launch_<kernel>_<NAME> (one
+// translation unit per size).
+#define PTY_POSITION_INSTANCES_XY(SX, SY, NAME, NT)                                      \
   namespace pty {                                                                        \
-  cudaError_t launch_probe_spectrum_##S(const BatchArgs& a, cudaStream_t s) {            \
-    return launch_spectrum_t<S, S, NT>(a, s);                                            \
+  cudaError_t launch_probe_spectrum_##NAME(const BatchArgs& a, cudaStream_t s) {         \
+    return launch_spectrum_t<SX, SY, NT>(a, s);                                          \
   }                                                                                      \
-  cudaError_t launch_position_kernel_##S(const BatchArgs& a, cudaStream_t s) {           \
-    return launch_position_t<S, S, NT>(a, s);                                            \
+  cudaError_t launch_position_kernel_##NAME(const BatchArgs& a, cudaStream_t s) {        \
+    return launch_position_t<SX, SY, NT>(a, s);                                          \
   }                                                                                      \
-  cudaError_t launch_position_correction_##S(const BatchArgs& a, cudaStream_t s) {       \
-    return launch_correction_t<S, S, NT>(a, s);                                          \
+  cudaError_t launch_position_correction_##NAME(const BatchArgs& a, cudaStream_t s) {    \
+    return launch_correction_t<SX, SY, NT>(a, s);                                        \
   }                                                                                      \
-  cudaError_t launch_probe_inverse_##S(const BatchArgs& a, cudaStream_t s) {             \
-    return launch_probe_inverse_t<S, S, NT>(a, s);                                       \
+  cudaError_t launch_probe_inverse_##NAME(const BatchArgs& a, cudaStream_t s) {          \
+    return launch_probe_inverse_t<SX, SY, NT>(a, s);                                     \
   }                                                                                      \
-  cudaError_t launch_probe_intensity_##S(const BatchArgs& a, cudaStream_t s) {           \
-    return launch_probe_intensity_t<S, S, NT>(a, s);                                     \
+  cudaError_t launch_probe_intensity_##NAME(const BatchArgs& a, cudaStream_t s) {        \
+    return launch_probe_intensity_t<SX, SY, NT>(a, s);                                   \
   }                                                                                      \
-  cudaError_t launch_probe_aperture_##S(const BatchArgs& a, cudaStream_t s) {            \
-    return launch_probe_aperture_t<S, S, NT>(a, s);                                      \
+  cudaError_t launch_probe_aperture_##NAME(const BatchArgs& a, cudaStream_t s) {         \
+    return launch_probe_aperture_t<SX, SY, NT>(a, s);                                    \
   }                                                                                      \
   }
+
+// Square regions of interest S x S.
+#define PTY_POSITION_INSTANCES(S, NT) PTY_POSITION_INSTANCES_XY(S, S, S, NT)

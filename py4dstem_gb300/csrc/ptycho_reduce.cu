@@ -1026,12 +1026,14 @@ cudaError_t launch_probe_com(const BatchArgs& a, cudaStream_t s) {
   probe_com_kernel<<<1, NT, 0, s>>>(a);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  switch (a.Sx) {
-    case 32: return launch_shift_t<32, 32, 128>(a, s);
-    case 48: return launch_shift_t<48, 48, 192>(a, s);
-    case 64: return launch_shift_t<64, 64, 256>(a, s);
-    case 96: return launch_shift_t<96, 96, 384>(a, s);
-    case 128: return launch_shift_t<128, 128, 512>(a, s);
+  switch (a.Sx * 4096 + a.Sy) {
+    case 32 * 4096 + 32: return launch_shift_t<32, 32, 128>(a, s);
+    case 48 * 4096 + 48: return launch_shift_t<48, 48, 192>(a, s);
+    case 64 * 4096 + 64: return launch_shift_t<64, 64, 256>(a, s);
+    case 96 * 4096 + 96: return launch_shift_t<96, 96, 384>(a, s);
+    case 128 * 4096 + 128: return launch_shift_t<128, 128, 512>(a, s);
+    case 96 * 4096 + 128: return launch_shift_t<96, 128, 512>(a, s);
+    case 128 * 4096 + 96: return launch_shift_t<128, 96, 512>(a, s);
     default: return cudaErrorInvalidValue;
   }
 }

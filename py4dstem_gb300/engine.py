@@ -103,7 +103,7 @@ def create_state(*, roi_shape, object_array, probe_array, amplitudes, positions_
     if not lib.ptycho_roi_supported(geom.roi_x, geom.roi_y):
         raise NotImplementedError(
             f"no fused GPU kernel for a {geom.roi_x}x{geom.roi_y} region of interest "
-            "(supported: square 32, 48, 64, 96, 128)")
+            "(supported: square 32, 48, 64, 96, 128 and 96 x 128, 128 x 96)")
     ws_bytes = int(lib.ptycho_workspace_bytes(ctypes.byref(geom), int(max_batch)))
     if ws_bytes == 0:
         raise ValueError("invalid geometry for the workspace query")

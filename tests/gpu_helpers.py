@@ -13,19 +13,20 @@ def make_state(S=64, J=36, modes=1, slices=1, potential=False, seed=0, obj_px=No
     """Random but well-conditioned state: non-uniform initial object (no exact
     zeros in the far field), amplitudes from a different true object plus noise."""
     rng = np.random.default_rng(seed)
+    Sx, Sy = (S, S) if np.isscalar(S) else (int(S[0]), int(S[1]))
     sampling = 0.25
     n = int(np.ceil(np.sqrt(J)))
     step = 2.3
     span = (n - 1) * step
-    P = obj_px or int(S + span + 8)
-    probe = ComplexProbe(energy=300e3, gpts=(S, S), sampling=(sampling, sampling),
+    P = obj_px or int(max(Sx, Sy) + span + 8)
+    probe = ComplexProbe(energy=300e3, gpts=(Sx, Sy), sampling=(sampling, sampling),
                          semiangle_cutoff=20.0, rolloff=2.0,
                          parameters={"defocus": 100.0}).build()._array.astype(np.complex64)
     probe *= np.float32(30.0)
     probes = [probe]
     for m in range(1, modes):
-        ramp_x = np.exp(-2j * np.pi * rng.uniform(-0.5, 0.5) * np.fft.fftfreq(S))
-        ramp_y = np.exp(-2j * np.pi * rng.uniform(-0.5, 0.5) * np.fft.fftfreq(S))
+        ramp_x = np.exp(-2j * np.pi * rng.uniform(-0.5, 0.5) * np.fft.fftfreq(Sx))
+        ramp_y = np.exp(-2j * np.pi * rng.uniform(-0.5, 0.5) * np.fft.fftfreq(Sy))
         probes.append((probes[-1] * ramp_x[:, None] * ramp_y[None] * 0.5).astype(np.complex64))
     probe_arr = np.stack(probes) if modes > 1 else probe
 
@@ -64,21 +65,24 @@ def make_state(S=64, J=36, modes=1, slices=1, potential=False, seed=0, obj_px=No
     lam = electron_wavelength_angstrom(300e3)
     props = None
     if slices > 1:
-        kx = np.fft.fftfreq(S, sampling).astype(np.float32)
-        h = np.exp(-1j * np.pi * lam * 20.0 * (kx[:, None] ** 2 + kx[None] ** 2))
+        kx = np.fft.fftfreq(Sx, sampling).astype(np.float32)
+        ky = np.fft.fftfreq(Sy, sampling).astype(np.float32)
+        h = np.exp(-1j * np.pi * lam * 20.0 * (kx[:, None] ** 2 + ky[None] ** 2))
         props = np.stack([h] * (slices - 1)).astype(np.complex64)
 
     # amplitudes from the true object (float64 model)
-    fx = np.fft.fftfreq(S, 1 / S).astype(int)
-    kk = np.fft.fftfreq(S)
-    amps = np.empty((J, S, S), np.float32)
+    fx = np.fft.fftfreq(Sx, 1 / Sx).astype(int)
+    fy = np.fft.fftfreq(Sy, 1 / Sy).astype(int)
+    kk = np.fft.fftfreq(Sx)
+    kl = np.fft.fftfreq(Sy)
+    amps = np.empty((J, Sx, Sy), np.float32)
     for j in range(J):
         r = np.round(pos[j].astype(np.float64))
         d = pos[j] - r
         rows = (int(r[0]) + fx) % P
-        cols = (int(r[1]) + fx) % P
-        ramp = np.exp(-2j * np.pi * kk[:, None] * d[0]) * np.exp(-2j * np.pi * kk[None] * d[1])
-        inten = np.zeros((S, S))
+        cols = (int(r[1]) + fy) % P
+        ramp = np.exp(-2j * np.pi * kk[:, None] * d[0]) * np.exp(-2j * np.pi * kl[None] * d[1])
+        inten = np.zeros((Sx, Sy))
         for m in range(modes):
             w = np.fft.ifft2(np.fft.fft2(np.asarray(probes[m], np.complex128)) * ramp)
             for s in range(slices):
@@ -89,7 +93,7 @@ def make_state(S=64, J=36, modes=1, slices=1, potential=False, seed=0, obj_px=No
         amps[j] = np.sqrt(rng.poisson(inten * 0.05) / 0.05).astype(np.float32)
     mean_int = np.float32(np.mean(np.sum(amps.astype(np.float64) ** 2, axis=(-2, -1))))
     fov_inv = np.ones((P, P), bool)
-    fov_inv[S // 2: P - S // 2, S // 2: P - S // 2] = False
+    fov_inv[Sx // 2: P - Sx // 2, Sy // 2: P - Sy // 2] = False
     return State(amplitudes=amps, positions_px=pos, probe=probe_arr, object=init_o,
                  mean_intensity=mean_int, fov_mask_inverse=fov_inv,
                  object_type="potential" if potential else "complex", num_slices=slices,

@@ -68,6 +68,23 @@ def test_both_128_schedules_agree_with_oracle(cuda):
         lib.ptycho_set_kernel_schedule(128, 0)
 
 
+@pytest.mark.parametrize("S", [(96, 128), (128, 96)])
+def test_non_square_roi(cuda, S):
+    """Non-square regions of interest (a 96 x 128 detector either way round):
+    gradient descent, then a mixed state and a multislice model, one iteration
+    each against the oracle."""
+    st = make_state(S=S, J=16, seed=sum(S))
+    compare(st, 2e-5, 2e-5, 2e-5, num_iter=1, max_batch_size=8, seed_random=1, **OFF)
+    st = make_state(S=S, J=16, modes=2, seed=sum(S) + 1)
+    compare(st, 2e-5, 2e-5, 2e-5, num_iter=1, max_batch_size=8, seed_random=2, **OFF)
+    st = make_state(S=S, J=16, slices=2, seed=sum(S) + 2)
+    compare(st, 2e-5, 2e-5, 2e-5, num_iter=1, max_batch_size=8, seed_random=3, **OFF)
+    # the probe centre-of-mass constraint shifts non-square probes too
+    st = make_state(S=S, J=16, seed=sum(S) + 3)
+    compare(st, 2e-5, 2e-5, 2e-5, num_iter=2, max_batch_size=8, seed_random=4,
+            fix_potential_baseline=False, orthogonalize_probe=False)
+
+
 def test_potential_object(cuda):
     st = make_state(S=64, J=25, potential=True, seed=3)
     compare(st, 2e-5, 2e-5, 2e-5, num_iter=1, max_batch_size=9, seed_random=2, **OFF)

@@ -43,6 +43,12 @@ def test_roi_supported(lib, n, ok):
     assert lib.ptycho_roi_supported(n, n * 2) == 0
 
 
+def test_non_square_roi_supported(lib):
+    assert lib.ptycho_roi_supported(96, 128) == 1
+    assert lib.ptycho_roi_supported(128, 96) == 1
+    assert lib.ptycho_roi_supported(64, 128) == 0
+
+
 def geometry(roi=64, obj=128, T=1, M=1, potential=0):
     return _native.Geometry(roi, roi, obj, obj, T, M, potential, 0)
 
