@@ -1018,12 +1018,15 @@ def run_learned_init(args):
         p = SingleslicePtychography(datacube=case.datacube, verbose=False, device="gpu",
                                     **case.ctor_kwargs)
         p.preprocess(**case.preprocess_kwargs)
-        r = li.compare_starts(net, p, geom, args.li_iterations, 1024, seed=k)
+        r = li.compare_starts(net, p, geom, args.li_iterations, 1024, seed=k,
+                              true_object=case.true_object)
         pe, le = r.pop("plain_errors"), r.pop("learned_errors")
+        po, lo = r.pop("plain_object_errors"), r.pop("learned_object_errors")
         if r["fallback"]:
             r["time_ratio"] = (r["network_s"] + 2.0 * r["plain_s"]) / r["plain_s_to_target"]
         r.update({"lattice_a": a, "defocus": df, "plain_error_curve": pe[::10],
-                  "learned_error_curve": le[::10]})
+                  "learned_error_curve": le[::10], "plain_object_error_curve": po[::10],
+                  "learned_object_error_curve": lo[::10]})
         results.append(r)
         del case, p
     ratios = [r["time_ratio"] for r in results]
@@ -1038,6 +1041,11 @@ def run_learned_init(args):
                    "plain_iterations": args.li_iterations, "scan": [128, 128],
                    "detector": 128, "object": [512, 512], "batch": 1024},
         "fallbacks": int(sum(r["fallback"] for r in results)),
+        "object_error_time_ratio_median": (float(statistics.median(
+            [r["object_time_ratio"] for r in results if r["object_time_ratio"] is not None]))
+            if any(r["object_time_ratio"] is not None for r in results) else None),
+        "object_error_reached": int(sum(r["learned_object_iterations"] is not None
+                                        for r in results)),
         "median_learned_iterations": float(statistics.median(its)) if its else None,
         "median_plain_iterations_to_target": float(statistics.median(
             [r["plain_first_at_target"] for r in results])),

@@ -375,14 +375,29 @@ def reconstruct_with_fallback(make_ptycho, net: UNet, num_iter: int, geom: ScanG
     return q, None, dt, False
 
 
+def object_nmse(obj, true_obj, mask):
+    """min over a complex scalar c of sum_mask |O - c T|^2 / sum_mask |T|^2 (the
+    object error up to the global phase and scale the data do not fix); torch
+    tensors on the device, mask boolean."""
+    o = obj[mask].to(_torch().complex128)
+    t = true_obj[mask].to(_torch().complex128)
+    tt = (t.conj() * t).real.sum()
+    c = (t.conj() * o).sum() / tt
+    r = o - c * t
+    return float(((r.conj() * r).real.sum() / tt).item())
+
+
 def run_to_target(ptycho, object_init, max_iter: int, target: Optional[float], batch: int,
-                  seed: int, step_size: float = 0.5):
+                  seed: int, step_size: float = 0.5, true_object=None):
     """Gradient-descent iterations of a preprocessed single-slice object from
     `object_init` (None: its own initial object) through the device state and
     the graph-replayed iteration driver of reconstruct(), reading the error
     after every iteration like the reference; stops after max_iter iterations or
     at the first error <= target. Returns the errors and, for each iteration,
-    the seconds since the start (state set-up included)."""
+    the seconds since the start (state set-up included). With `true_object`
+    (the object on the reconstruction grid) the object error (object_nmse over
+    the field-of-view mask) after each iteration is returned too; its
+    evaluation is not counted in the times."""
     torch = _torch()
     from . import engine
 
@@ -403,27 +418,42 @@ def run_to_target(ptycho, object_init, max_iter: int, target: Optional[float], b
                                  mean_intensity=p._mean_diffraction_intensity)
     rs = np.random.RandomState(seed)
     order = np.arange(J)
-    errors, times = [], []
+    errors, times, obj_err = [], [], []
+    if true_object is not None:
+        tobj = torch.from_numpy(np.asarray(true_object, dtype=np.complex64)).to(st.object.device)
+        mask = torch.from_numpy(np.asarray(p._object_fov_mask, dtype=bool)).to(st.object.device)
+    excluded = 0.0
     for _ in range(max_iter):
         rs.shuffle(order)
         drv.iterate(order)
         errors.append(float(drv.error()))  # synchronises
-        times.append(time.perf_counter() - t0)
+        times.append(time.perf_counter() - t0 - excluded)
+        if true_object is not None:
+            t1 = time.perf_counter()
+            obj_err.append(object_nmse(st.object.view(tobj.shape), tobj, mask))
+            excluded += time.perf_counter() - t1
         if target is not None and errors[-1] <= target:
             break
+    if true_object is not None:
+        return errors, times, obj_err
     return errors, times
 
 
 def compare_starts(net: UNet, ptycho, geom: ScanGeometry, plain_iter: int, batch: int,
-                   seed: int):
+                   seed: int, true_object=None):
     """The plain start run for plain_iter iterations, then the learned start run
-    until it reaches the plain run's final error (at most plain_iter
+    until it reaches the plain run's final data error (at most plain_iter
     iterations). Times compare the first iteration at which each run reaches
     that error; the learned run's time includes the network input, the network
     and the start object. Returns a dict; `fallback` is True when the learned
-    run did not reach the target (the plain result then stands)."""
+    run did not reach the target (the plain result then stands). With
+    `true_object`, both runs also record the object error after each iteration
+    and the dict gives the iterations each needs to reach the plain run's final
+    object error (both runs then go the full plain_iter iterations)."""
     torch = _torch()
-    plain, t_plain = run_to_target(ptycho, None, plain_iter, None, batch, seed)
+    track = true_object is not None
+    out = run_to_target(ptycho, None, plain_iter, None, batch, seed, true_object=true_object)
+    plain, t_plain = out[0], out[1]
     target = plain[-1]
     # the plain run reaches its final error first at iteration kp (its error
     # need not fall monotonically)
@@ -433,13 +463,27 @@ def compare_starts(net: UNet, ptycho, geom: ScanGeometry, plain_iter: int, batch
     guess = initial_object(net, ptycho, geom)
     torch.cuda.synchronize()
     t_net = time.perf_counter() - t0
-    learned, t_learned = run_to_target(ptycho, guess, plain_iter, target, batch, seed)
+    out_l = run_to_target(ptycho, guess, plain_iter, None if track else target, batch, seed,
+                          true_object=true_object)
+    learned, t_learned = out_l[0], out_l[1]
     k = iterations_to_target(learned, target)
     t_l = t_net + t_learned[k - 1] if k is not None else None
-    return {"plain_iterations": plain_iter, "plain_error": target,
-            "plain_first_at_target": kp, "plain_s_to_target": t_plain[kp - 1],
-            "plain_s": t_plain[-1], "learned_iterations": k, "learned_s": t_l,
-            "network_s": t_net, "learned_first_error": learned[0],
-            "plain_first_error": plain[0], "fallback": k is None,
-            "time_ratio": t_l / t_plain[kp - 1] if k is not None else None,
-            "plain_errors": plain, "learned_errors": learned}
+    res = {"plain_iterations": plain_iter, "plain_error": target,
+           "plain_first_at_target": kp, "plain_s_to_target": t_plain[kp - 1],
+           "plain_s": t_plain[-1], "learned_iterations": k, "learned_s": t_l,
+           "network_s": t_net, "learned_first_error": learned[0],
+           "plain_first_error": plain[0], "fallback": k is None,
+           "time_ratio": t_l / t_plain[kp - 1] if k is not None else None,
+           "plain_errors": plain, "learned_errors": learned[:k] if k else learned}
+    if track:
+        po, lo = out[2], out_l[2]
+        ot = po[-1]
+        kpo = iterations_to_target(po, ot)
+        klo = iterations_to_target(lo, ot)
+        res.update({"plain_object_error": ot, "learned_start_object_error": lo[0],
+                    "plain_start_object_error": po[0],
+                    "plain_object_first_at_target": kpo, "learned_object_iterations": klo,
+                    "object_time_ratio": ((t_net + t_learned[klo - 1]) / t_plain[kpo - 1]
+                                          if klo is not None else None),
+                    "plain_object_errors": po, "learned_object_errors": lo})
+    return res
