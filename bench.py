@@ -74,7 +74,7 @@ def parse_args(argv=None):
     ap.add_argument("--ref-cores", type=int, default=0,
                     help="reference arm: limit the worker processes (0 = all host cores)")
     ap.add_argument("--workload", choices=["gd128", "multiscan", "multislice", "projection",
-                                           "poscorr", "mixed-multislice", "tomography",
+                                           "poscorr", "mixed-multislice", "gd256", "tomography",
                                            "learned-init"],
                     default="gd128",
                     help="gd128: the single-slice 128^2-detector workload (default); multiscan: "
@@ -793,7 +793,9 @@ def run_variant(args):
                         2 GiB of persistent exit waves;
       poscorr           gradient descent, batch 1024, position correction with
                         both distance limits and the positions CoM constraint;
-      mixed-multislice  a 64x64 scan through 4 slices with 2 probe modes, batch 256.
+      mixed-multislice  a 64x64 scan through 4 slices with 2 probe modes, batch 256;
+      gd256             gradient descent on a 256^2 detector (the staged batch-wide
+                        kernels): a 64x64 scan at 0.75 A, 512^2 object, batch 256.
     value = position updates/s over K full iterations (device-resident amplitudes)."""
     rank, world, local = dist_env()
     if world > 1:
@@ -806,8 +808,14 @@ def run_variant(args):
     from py4dstem_gb300.ptychography import method_parameters
 
     w = args.workload
-    n = 128 * 128
-    if w == "mixed-multislice":
+    det = 256 if w == "gd256" else 128
+    n = det * det
+    if w == "gd256":
+        case = synthetic.make_scan("ss256", 7, (64, 64), 0.75, 0.05, 256, 512, dose=1e5,
+                                   backend="torch", device=f"cuda:{local}")
+        p = preprocess(case, storage="gpu")
+        B, T, M = 256, 1, 1
+    elif w == "mixed-multislice":
         from py4dstem_gb300 import MixedstateMultislicePtychography
 
         case = synthetic.make_scan("mms", 5, (64, 64), 0.4, 0.05, 128, 256, dose=1e5,
@@ -866,13 +874,13 @@ def run_variant(args):
     ms = ev0.elapsed_time(ev1)
     fl = roofline.flops_per_position(n, num_slices=T, num_probes=M)
     line = {
-        "metric": f"position updates/s ({w}, 128^2 det)",
+        "metric": f"position updates/s ({w}, {det}^2 det)",
         "value": J * args.steps / (ms * 1e-3), "unit": UNIT, "n_gpus": 1,
         "steps": args.steps, "warmup": max(args.warmup, 2), "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": w, "positions": J, "batch": B, "slices": T, "modes": M,
-                   "detector": 128, "object": list(np.shape(p._object)),
+                   "detector": det, "object": list(np.shape(p._object)),
                    "method": "DM_AP" if projection else "GD",
                    "position_correction": poscorr},
         "flops_per_position": fl,
@@ -1066,7 +1074,7 @@ def main(argv=None):
         return run_multiscan(args)
     if args.workload == "multislice":
         return run_multislice(args)
-    if args.workload in ("projection", "poscorr", "mixed-multislice"):
+    if args.workload in ("projection", "poscorr", "mixed-multislice", "gd256"):
         return run_variant(args)
     if args.workload == "learned-init":
         return run_learned_init(args)

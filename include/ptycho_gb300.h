@@ -80,8 +80,17 @@ typedef struct ptycho_geometry {
 /* Library identity and capability queries. */
 int ptycho_abi_version(void);
 const char* ptycho_last_error(void);
-/* 1 if a fused kernel exists for this ROI (Sx, Sy), else 0. */
+/* 1 if kernels exist for this ROI (Sx, Sy), else 0: the fused per-position
+ * kernel for square 32, 48, 64, 96, 128 and 96 x 128, 128 x 96 (every model);
+ * batch-wide staged kernels for 256 x 256, whose geometry must be single slice,
+ * single probe, without PTYCHO_FLAG_MIXED_STATE and PTYCHO_FLAG_KEEP_FARFIELD
+ * (else PTYCHO_ERR_UNSUPPORTED), and which have no projection sets and no
+ * probe gradient in ptycho_gd_gradient. */
 int ptycho_roi_supported(int32_t roi_x, int32_t roi_y);
+/* PTYCHO_OK if the batch entry points take this geometry, else the error code
+ * (PTYCHO_ERR_UNSUPPORTED or PTYCHO_ERR_INVALID_ARGUMENT) they would return,
+ * with the reason in ptycho_last_error(). Host only; touches no device. */
+int ptycho_geometry_supported(const ptycho_geometry* geometry);
 
 /* Scratch bytes one batch call needs for up to max_batch positions. */
 size_t ptycho_workspace_bytes(const ptycho_geometry* geometry, int32_t max_batch);
@@ -329,7 +338,8 @@ int ptycho_rotation_search(const void* com_x, const void* com_y, int32_t com_is_
  * (2 crop_w, 2 crop_w) pattern. The mean diffraction intensity is the float32
  * running sum of pattern_sums in order, divided by num_out. Replaces
  * _normalize_diffraction_intensities (phase_base_class.py:1347-1460).
- * qx * qy <= 20000.
+ * Patterns that fit one block's shared memory are staged there; larger ones
+ * (256 x 256) are read from global memory where each value is formed.
  */
 int ptycho_normalize_patterns(const float* intensities, int32_t qx, int32_t qy,
                               const int32_t* rows, int32_t num_out, const float* com_fitted_x,

@@ -58,6 +58,7 @@ _SIGNATURES = {
     "ptycho_abi_version": ([], ctypes.c_int),
     "ptycho_last_error": ([], ctypes.c_char_p),
     "ptycho_roi_supported": ([_i32, _i32], ctypes.c_int),
+    "ptycho_geometry_supported": ([ctypes.POINTER(Geometry)], ctypes.c_int),
     "ptycho_workspace_bytes": ([ctypes.POINTER(Geometry), _i32], _sz),
     "ptycho_gd_batch": (
         [ctypes.POINTER(Geometry), _vp, _vp, _vp, _vp, _vp, _vp, _i32, _f32, _f32, _i32,

@@ -83,7 +83,9 @@ class PtychoForwardModel:
                                          self.num_probes, 1 if potential else 0, flags)
         lib = _native.lib()
         if not lib.ptycho_roi_supported(int(sx), int(sy)):
-            raise NotImplementedError(f"no fused GPU kernel for a {sx}x{sy} region of interest")
+            raise NotImplementedError(f"no GPU kernel for a {sx}x{sy} region of interest")
+        if lib.ptycho_geometry_supported(ctypes.byref(self.geometry)) != _native.PTYCHO_OK:
+            raise NotImplementedError(lib.ptycho_last_error().decode())
         self.max_batch = int(min(max_batch, J))
         self.ws_bytes = int(lib.ptycho_workspace_bytes(ctypes.byref(self.geometry),
                                                        self.max_batch))

@@ -374,6 +374,14 @@ struct Schedule<128> {
     line_pass<128, 8, 16, NLINES, NT, DIR>(b, ls, es, tw);
   }
 };
+template <>
+struct Schedule<256> {
+  template <int NLINES, int NT, int DIR>
+  __device__ static void run(float2* b, int ls, int es, const float2* tw) {
+    line_pass<256, 16, 1, NLINES, NT, DIR>(b, ls, es, tw);
+    line_pass<256, 16, 16, NLINES, NT, DIR>(b, ls, es, tw);
+  }
+};
 
 // Full 2D transform of the SX x SY block in shared memory (pitch SY + 1).
 // twx: table for length SX, twy: table for length SY.

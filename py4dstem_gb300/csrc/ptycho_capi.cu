@@ -63,8 +63,15 @@ int check_geometry(const ptycho_geometry* g) {
   if (g->num_probes > 16) return fail(PTYCHO_ERR_UNSUPPORTED, "at most 16 probe modes");
   if (!roi_supported(g->roi_x, g->roi_y))
     return fail(PTYCHO_ERR_UNSUPPORTED,
-                "ROI %dx%d has no fused kernel (supported: square 32, 48, 64, 96, 128 "
+                "ROI %dx%d has no kernel (supported: square 32, 48, 64, 96, 128, 256 "
                 "and 96 x 128, 128 x 96)",
+                g->roi_x, g->roi_y);
+  if (staged_roi(g->roi_x, g->roi_y) &&
+      (g->num_slices != 1 || g->num_probes != 1 ||
+       (g->flags & (PTYCHO_FLAG_MIXED_STATE | PTYCHO_FLAG_KEEP_FARFIELD)) != 0))
+    return fail(PTYCHO_ERR_UNSUPPORTED,
+                "a %d x %d ROI runs the single-slice, single-probe model only, without "
+                "PTYCHO_FLAG_MIXED_STATE or PTYCHO_FLAG_KEEP_FARFIELD (position correction)",
                 g->roi_x, g->roi_y);
   if (g->object_x < g->roi_x || g->object_y < g->roi_y)
     return fail(PTYCHO_ERR_UNSUPPORTED, "object %dx%d smaller than ROI %dx%d", g->object_x,
@@ -217,6 +224,8 @@ const char* ptycho_last_error(void) { return g_last_error; }
 
 int ptycho_roi_supported(int32_t roi_x, int32_t roi_y) { return roi_supported(roi_x, roi_y) ? 1 : 0; }
 
+int ptycho_geometry_supported(const ptycho_geometry* g) { return check_geometry(g); }
+
 size_t ptycho_workspace_bytes(const ptycho_geometry* g, int32_t max_batch) {
   if (!g || max_batch < 1) return 0;
   return workspace_layout(g->roi_x, g->roi_y, g->object_x, g->object_y, g->num_slices,
@@ -294,6 +303,9 @@ int ptycho_projection_batch(const ptycho_geometry* g, void* object, void* probe,
   int st = prepare(g, batch, workspace, workspace_bytes, a);
   if (st != PTYCHO_OK) return st;
   if (!exit_waves) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "exit_waves must be non-null");
+  if (staged_roi(g->roi_x, g->roi_y))
+    return fail(PTYCHO_ERR_UNSUPPORTED, "projection sets are not available for a %d x %d ROI",
+                g->roi_x, g->roi_y);
   a.projection = 1;
   a.keep_farfield = (g->flags & PTYCHO_FLAG_KEEP_FARFIELD) ? 1 : 0;
   a.pa = projection_a;
@@ -393,6 +405,10 @@ int ptycho_gd_gradient(const ptycho_geometry* g, const void* object, const void*
                                              "and loss must be non-null");
   if (g->num_slices > 1 && !propagators)
     return fail(PTYCHO_ERR_INVALID_ARGUMENT, "multislice needs propagators");
+  if (probe_grad && staged_roi(g->roi_x, g->roi_y))
+    return fail(PTYCHO_ERR_UNSUPPORTED, "the probe gradient is not available for a %d x %d ROI "
+                                        "(pass probe_grad = null for the object gradient)",
+                g->roi_x, g->roi_y);
   a.mixed_formula = (g->num_probes > 1 || (g->flags & PTYCHO_FLAG_MIXED_STATE)) ? 1 : 0;
   a.object = const_cast<void*>(object);
   a.probe = static_cast<float2*>(const_cast<void*>(probe));

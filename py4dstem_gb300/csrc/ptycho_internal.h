@@ -149,6 +149,17 @@ cudaError_t launch_probe_orthogonalize(const BatchArgs& a, float2* scratch_probe
 cudaError_t launch_probe_mix(const BatchArgs& a, const float2* in, const float2* coeffs,
                              float2* out, cudaStream_t s);
 
+// ---- ptycho_staged.cu: the 256 x 256 region of interest as batch-wide kernels
+bool staged_roi(int Sx, int Sy);
+// single slice, single probe, gradient descent or forward only
+bool staged_batch_supported(const BatchArgs& a);
+cudaError_t launch_staged_spectrum(const BatchArgs& a, cudaStream_t s);
+cudaError_t launch_staged_positions(const BatchArgs& a, cudaStream_t s);
+cudaError_t launch_staged_intensity(const BatchArgs& a, cudaStream_t s);
+// every probe mode shifted by -a.com (after probe_com_kernel)
+cudaError_t launch_staged_probe_shift(const BatchArgs& a, cudaStream_t s);
+cudaError_t launch_staged_aperture(const BatchArgs& a, cudaStream_t s);
+
 // Preprocessing kernels (ptycho_preprocess.cu).
 cudaError_t launch_pattern_com(const float* in, int num, int Qx, int Qy, const void* mask,
                                int mask_mode, void* cx, void* cy, cudaStream_t s);

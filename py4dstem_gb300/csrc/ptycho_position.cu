@@ -1,6 +1,7 @@
-// Dispatch of the fused per-position kernels on the region-of-interest shape.
-// The kernels are templates in ptycho_position.cuh, instantiated once per
-// shape in ptycho_position_<S>.cu (square) and ptycho_position_<SX>x<SY>.cu.
+// Dispatch of the per-position kernels on the region-of-interest shape. The
+// fused kernels are templates in ptycho_position.cuh, instantiated once per
+// shape in ptycho_position_<S>.cu (square) and ptycho_position_<SX>x<SY>.cu;
+// 256 x 256 runs the batch-wide kernels of ptycho_staged.cu.
 #include <cuda_runtime.h>
 
 #include "ptycho_internal.h"
@@ -36,6 +37,7 @@ bool roi_supported(int Sx, int Sy) {
     case roi_key(128, 128):
     case roi_key(96, 128):
     case roi_key(128, 96):
+    case roi_key(256, 256):
       return true;
     default:
       return false;
@@ -54,27 +56,35 @@ bool roi_supported(int Sx, int Sy) {
     default: return cudaErrorInvalidValue;                      \
   }
 
+// (the staged path has no position correction and no exact probe gradient:
+// the C ABI refuses both at 256 x 256)
 cudaError_t launch_probe_spectrum(const BatchArgs& a, cudaStream_t s) {
+  if (staged_roi(a.Sx, a.Sy)) return launch_staged_spectrum(a, s);
   PTY_DISPATCH(launch_probe_spectrum, a, s)
 }
 
 cudaError_t launch_position_kernel(const BatchArgs& a, cudaStream_t s) {
+  if (staged_roi(a.Sx, a.Sy)) return launch_staged_positions(a, s);
   PTY_DISPATCH(launch_position_kernel, a, s)
 }
 
 cudaError_t launch_position_correction(const BatchArgs& a, cudaStream_t s) {
+  if (staged_roi(a.Sx, a.Sy)) return cudaErrorNotSupported;
   PTY_DISPATCH(launch_position_correction, a, s)
 }
 
 cudaError_t launch_probe_inverse(const BatchArgs& a, cudaStream_t s) {
+  if (staged_roi(a.Sx, a.Sy)) return cudaErrorNotSupported;
   PTY_DISPATCH(launch_probe_inverse, a, s)
 }
 
 cudaError_t launch_probe_intensity(const BatchArgs& a, cudaStream_t s) {
+  if (staged_roi(a.Sx, a.Sy)) return launch_staged_intensity(a, s);
   PTY_DISPATCH(launch_probe_intensity, a, s)
 }
 
 cudaError_t launch_probe_aperture(const BatchArgs& a, cudaStream_t s) {
+  if (staged_roi(a.Sx, a.Sy)) return launch_staged_aperture(a, s);
   PTY_DISPATCH(launch_probe_aperture, a, s)
 }
 

@@ -317,6 +317,59 @@ __global__ void __launch_bounds__(kPreThreads) pattern_normalize_general_kernel(
 }
 
 
+// Normalisation of patterns too large to stage in shared memory (256 x 256):
+// the same values as pattern_normalize_general_kernel, each shifted value
+// formed from the pattern in global memory where it is used (leaf sums, one
+// thread per leaf; then the amplitudes of the kept pixels).
+__global__ void __launch_bounds__(kPreThreads) pattern_normalize_global_kernel(
+    const float* __restrict__ in, int Qx, int Qy, const int32_t* __restrict__ rows,
+    const float* __restrict__ cfx, const float* __restrict__ cfy, int crop_w, int max_leaves,
+    float* __restrict__ amps, float* __restrict__ sums) {
+  extern __shared__ float4 smem4[];
+  const int N = Qx * Qy;
+  float* leaf = reinterpret_cast<float*>(smem4);
+  int* llo = reinterpret_cast<int*>(leaf + max_leaves);
+  int* llen = llo + max_leaves;
+  __shared__ int nleaves;
+  const int o = blockIdx.x;
+  const int r = rows ? rows[o] : o;
+  const float* src = in + (size_t)r * N;
+  if (threadIdx.x == 0) nleaves = pairwise_leaves(N, llo, llen);
+  const float xs = -cfx[r], ys = -cfy[r];
+  const float xf = floorf(xs), yf = floorf(ys);
+  const float wx = __fsub_rn(xs, xf), wy = __fsub_rn(ys, yf);
+  const float ux = __fsub_rn(1.0f, wx), uy = __fsub_rn(1.0f, wy);
+  const float w00 = __fmul_rn(ux, uy), w10 = __fmul_rn(wx, uy);
+  const float w01 = __fmul_rn(ux, wy), w11 = __fmul_rn(wx, wy);
+  const int ix = (int)xf, iy = (int)yf;
+  auto shifted = [&](int e) {
+    const int i = e / Qy, j = e - (e / Qy) * Qy;
+    const int i0 = pmod(i - ix, Qx), i1 = pmod(i - ix - 1, Qx);
+    const int j0 = pmod(j - iy, Qy), j1 = pmod(j - iy - 1, Qy);
+    float v = __fmul_rn(__ldg(src + i0 * Qy + j0), w00);
+    v = __fadd_rn(v, __fmul_rn(__ldg(src + i1 * Qy + j0), w10));
+    v = __fadd_rn(v, __fmul_rn(__ldg(src + i0 * Qy + j1), w01));
+    v = __fadd_rn(v, __fmul_rn(__ldg(src + i1 * Qy + j1), w11));
+    return v;
+  };
+  __syncthreads();
+  for (int j = threadIdx.x; j < nleaves; j += kPreThreads)
+    leaf[j] = leaf_sum<float>(shifted, llo[j], llen[j]);
+  const int Cx = crop_w > 0 ? 2 * crop_w : Qx;
+  const int Cy = crop_w > 0 ? 2 * crop_w : Qy;
+  float* dst = amps + (size_t)o * Cx * Cy;
+  for (int e = threadIdx.x; e < Cx * Cy; e += kPreThreads) {
+    const int u = e / Cy, w = e - (e / Cy) * Cy;
+    const int x = crop_w > 0 && u >= crop_w ? Qx - Cx + u : u;
+    const int y = crop_w > 0 && w >= crop_w ? Qy - Cy + w : w;
+    float v = shifted(x * Qy + y);
+    if (!(v >= 0.0f) && !isnan(v)) v = 0.0f;
+    dst[e] = __fsqrt_rn(v);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) sums[o] = __fadd_rn(0.0f, pairwise_combine<float>(N, leaf));
+}
+
 // ------------------------------------------------------- perfect-tree kernels
 // Chain j (0..7) of a leaf of length l starting at element `lo`: r = a[lo + j],
 // then r += a[lo + j + 8 k] for k = 1 .. l/8 - 1 (values from `val`). Lane j of
@@ -590,7 +643,16 @@ cudaError_t launch_pattern_normalize(const float* in, int Qx, int Qy, const int3
   }
   const int L = pairwise_leaf_count(N);
   const size_t smem = sizeof(float) * (2 * (size_t)N + L) + sizeof(int) * 2 * L;
-  if (smem > preprocess_smem_limit()) return cudaErrorInvalidValue;
+  if (smem > preprocess_smem_limit()) {
+    // too large to stage: values formed from global memory
+    const size_t gsmem = (sizeof(float) + 2 * sizeof(int)) * (size_t)L;
+    if (gsmem > preprocess_smem_limit()) return cudaErrorInvalidValue;
+    cudaError_t e = set_smem((const void*)pattern_normalize_global_kernel, gsmem);
+    if (e != cudaSuccess) return e;
+    pattern_normalize_global_kernel<<<num_out, kPreThreads, gsmem, s>>>(
+        in, Qx, Qy, rows, cfx, cfy, crop_w, L, amps, sums);
+    return cudaGetLastError();
+  }
   cudaError_t e = set_smem((const void*)pattern_normalize_general_kernel, smem);
   if (e != cudaSuccess) return e;
   pattern_normalize_general_kernel<<<num_out, kPreThreads, smem, s>>>(in, Qx, Qy, rows, cfx, cfy,

@@ -1034,6 +1034,7 @@ cudaError_t launch_probe_com(const BatchArgs& a, cudaStream_t s) {
     case 128 * 4096 + 128: return launch_shift_t<128, 128, 512>(a, s);
     case 96 * 4096 + 128: return launch_shift_t<96, 128, 512>(a, s);
     case 128 * 4096 + 96: return launch_shift_t<128, 96, 512>(a, s);
+    case 256 * 4096 + 256: return launch_staged_probe_shift(a, s);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -144,8 +144,8 @@ def probe_overlap(probe_single: np.ndarray, positions_px: np.ndarray, object_sha
     roi = probe_single.shape[-2:]
     if not lib.ptycho_roi_supported(int(roi[0]), int(roi[1])):
         raise NotImplementedError(
-            f"no fused GPU kernel for a {roi[0]}x{roi[1]} region of interest "
-            "(supported: square 32, 48, 64, 96, 128 and 96 x 128, 128 x 96)")
+            f"no GPU kernel for a {roi[0]}x{roi[1]} region of interest "
+            "(supported: square 32, 48, 64, 96, 128, 256 and 96 x 128, 128 x 96)")
     J = int(positions_px.shape[0])
     batch = max(1, min(int(max_batch_size or J), _OVERLAP_BATCH, J))
     geom = make_geometry(roi, object_shape, 1, 1, False)

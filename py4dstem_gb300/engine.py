@@ -75,6 +75,12 @@ class DeviceState:
     extra: dict = field(default_factory=dict)
 
 
+# The region of interest whose model runs as batch-wide staged kernels (a wave
+# does not fit one block's shared memory): single slice, single probe, gradient
+# descent only.
+STAGED_ROI = (256, 256)
+
+
 def supported_roi(shape) -> bool:
     return bool(_native.lib().ptycho_roi_supported(int(shape[0]), int(shape[1])))
 
@@ -93,17 +99,22 @@ def create_state(*, roi_shape, object_array, probe_array, amplitudes, positions_
                  projection=False, mixed_state=False, positions_initial=None) -> DeviceState:
     if not np.all(np.isfinite(np.asarray(positions_px))):
         raise ValueError("scan positions contain NaN or infinite values")
-    torch = _torch()
     lib = _native.lib()
-    dev = torch.device("cuda", torch.cuda.current_device())
     geom = make_geometry(roi_shape, object_array.shape, num_slices, num_probes, potential,
                          mixed_state or num_probes > 1)
     if positions_initial is not None:
         geom.flags |= _native.FLAG_KEEP_FARFIELD
     if not lib.ptycho_roi_supported(geom.roi_x, geom.roi_y):
         raise NotImplementedError(
-            f"no fused GPU kernel for a {geom.roi_x}x{geom.roi_y} region of interest "
-            "(supported: square 32, 48, 64, 96, 128 and 96 x 128, 128 x 96)")
+            f"no GPU kernel for a {geom.roi_x}x{geom.roi_y} region of interest "
+            "(supported: square 32, 48, 64, 96, 128, 256 and 96 x 128, 128 x 96)")
+    if lib.ptycho_geometry_supported(ctypes.byref(geom)) != _native.PTYCHO_OK:
+        raise NotImplementedError(lib.ptycho_last_error().decode())
+    if projection and (geom.roi_x, geom.roi_y) == STAGED_ROI:
+        raise NotImplementedError(
+            f"projection sets are not available for a {geom.roi_x}x{geom.roi_y} region of interest")
+    torch = _torch()
+    dev = torch.device("cuda", torch.cuda.current_device())
     ws_bytes = int(lib.ptycho_workspace_bytes(ctypes.byref(geom), int(max_batch)))
     if ws_bytes == 0:
         raise ValueError("invalid geometry for the workspace query")

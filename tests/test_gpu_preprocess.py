@@ -50,7 +50,7 @@ def _host():
 
 @pytest.mark.parametrize("shape,masked", [((5, 7, 48, 48), False), ((3, 4, 96, 96), True),
                                           ((2, 3, 128, 128), False), ((4, 4, 37, 41), True),
-                                          ((1, 2, 5, 3), False)])
+                                          ((1, 2, 5, 3), False), ((2, 2, 256, 256), True)])
 def test_pattern_com_bits(cuda, shape, masked):
     from py4dstem_gb300 import device_preprocess
 
@@ -125,7 +125,8 @@ def test_rotation_search_bits(cuda, scan, divergence, dtype):
 
 
 @pytest.mark.parametrize("qshape,crop,pmask", [((64, 64), False, False), ((96, 96), True, True),
-                                               ((128, 128), False, True), ((40, 52), True, False)])
+                                               ((128, 128), False, True), ((40, 52), True, False),
+                                               ((256, 256), False, True), ((256, 256), True, False)])
 def test_normalize_bits(cuda, qshape, crop, pmask):
     from py4dstem_gb300 import device_preprocess
 
@@ -150,7 +151,8 @@ def test_normalize_bits(cuda, qshape, crop, pmask):
         np.testing.assert_array_equal(crop_mask, ref_crop)
 
 
-@pytest.mark.parametrize("roi,J,batch", [(64, 300, 64), (128, 100, None), (48, 77, 1000)])
+@pytest.mark.parametrize("roi,J,batch", [(64, 300, 64), (128, 100, None), (48, 77, 1000),
+                                         (256, 40, 16)])
 def test_probe_overlap_close(cuda, roi, J, batch):
     from py4dstem_gb300 import device_preprocess
     from py4dstem_gb300.optics import ComplexProbe

@@ -37,7 +37,7 @@ def test_abi_version(lib):
 
 
 @pytest.mark.parametrize("n,ok", [(32, 1), (48, 1), (64, 1), (96, 1), (128, 1), (80, 0),
-                                  (256, 0), (100, 0)])
+                                  (256, 1), (100, 0), (512, 0)])
 def test_roi_supported(lib, n, ok):
     assert lib.ptycho_roi_supported(n, n) == ok
     assert lib.ptycho_roi_supported(n, n * 2) == 0
@@ -79,6 +79,46 @@ def test_rejects_null_geometry(lib):
 def test_rejects_unsupported_roi(lib):
     assert _gd(lib, geometry(roi=80)) == 2
     assert b"80x80" in lib.ptycho_last_error()
+
+
+@pytest.mark.parametrize("T,M,flags,ok", [
+    (1, 1, 0, True), (2, 1, 0, False), (1, 2, 0, False), (1, 1, "FLAG_MIXED_STATE", False),
+    (1, 1, "FLAG_KEEP_FARFIELD", False)])
+def test_staged_roi_models(lib, T, M, flags, ok):
+    """256 x 256 runs the single-slice, single-probe model only: other
+    geometries are refused on the host with the reason."""
+    g = geometry(roi=256, obj=320, T=T, M=M)
+    g.flags = getattr(_native, flags) if flags else 0
+    status = lib.ptycho_geometry_supported(ctypes.byref(g))
+    if ok:
+        assert status == 0
+        assert _gd(lib, g) == 3  # the geometry passed; the null workspace did not
+    else:
+        assert status == 2
+        assert b"single-slice, single-probe" in lib.ptycho_last_error()
+        assert _gd(lib, g) == 2
+
+
+def test_geometry_supported_matches_the_batch_checks(lib):
+    assert lib.ptycho_geometry_supported(None) == 1
+    assert lib.ptycho_geometry_supported(ctypes.byref(geometry(roi=80))) == 2
+    assert lib.ptycho_geometry_supported(ctypes.byref(geometry(roi=64, obj=48))) == 2
+    assert lib.ptycho_geometry_supported(ctypes.byref(geometry(T=2, M=2))) == 0
+
+
+def test_staged_roi_refused_by_the_engine():
+    """The engine raises NotImplementedError for models the 256 x 256 kernels
+    do not run, before any device work."""
+    import numpy as np
+
+    from py4dstem_gb300 import engine
+
+    with pytest.raises(NotImplementedError, match="single-slice, single-probe"):
+        engine.create_state(roi_shape=(256, 256), object_array=np.ones((2, 320, 320), np.complex64),
+                            probe_array=np.ones((256, 256), np.complex64),
+                            amplitudes=np.ones((4, 256, 256), np.float32),
+                            positions_px=np.zeros((4, 2), np.float32), num_slices=2,
+                            num_probes=1, potential=False, max_batch=4)
 
 
 def test_rejects_object_smaller_than_roi(lib):
