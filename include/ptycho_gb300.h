@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define PTYCHO_ABI_VERSION 2
+#define PTYCHO_ABI_VERSION 3
 
 enum ptycho_status {
   PTYCHO_OK = 0,
@@ -55,7 +55,22 @@ typedef struct ptycho_geometry {
   int32_t num_probes;          /* M: 1 = single probe                         */
   int32_t object_is_potential; /* 0: complex64 object, 1: float32 potential   */
   int32_t flags;               /* PTYCHO_FLAG_* bits; unknown bits must be 0  */
+  int32_t detector_x;          /* Ax: detector pixels along x; 0 = roi_x       */
+  int32_t detector_y;          /* Ay; 0 = roi_y                                */
 } ptycho_geometry;
+
+/* A detector shape (Ax, Ay) different from the ROI (Sx, Sy) is the reference's
+ * region_of_interest_shape (singleslice_ptychography.py:431-436): the
+ * amplitudes and the detector mask are Ax x Ay, and every Fourier projection
+ * resamples the far field onto the detector grid and the modified far field
+ * back onto the ROI grid as the reference's bilinear_resample does
+ * (ptychographic_methods.py:1601-1631, utils.py:2347-2428; SciPy's zoom of a
+ * complex array maps output index k to input coordinate
+ * k (n_in - 1) / (n_out - 1), linear between neighbours, and the sums are
+ * kept by dividing by the ratio of pixel counts). Gradient descent of every
+ * model, the self-consistency errors and the object gradient; projection sets,
+ * PTYCHO_FLAG_KEEP_FARFIELD (position correction) and the probe gradient are
+ * refused with PTYCHO_ERR_UNSUPPORTED. */
 
 /* Use the mixed-state Fourier projection (shared ratio A/sqrt(sum_m |F_m|^2),
  * mixedstate class) even when num_probes == 1. Implied when num_probes > 1. */
@@ -82,10 +97,9 @@ int ptycho_abi_version(void);
 const char* ptycho_last_error(void);
 /* 1 if kernels exist for this ROI (Sx, Sy), else 0: the fused per-position
  * kernel for square 32, 48, 64, 96, 128 and 96 x 128, 128 x 96 (every model);
- * batch-wide staged kernels for 256 x 256, whose geometry must be single slice,
- * single probe, without PTYCHO_FLAG_MIXED_STATE and PTYCHO_FLAG_KEEP_FARFIELD
- * (else PTYCHO_ERR_UNSUPPORTED), and which have no projection sets and no
- * probe gradient in ptycho_gd_gradient. */
+ * batch-wide staged kernels for 256 x 256 (gradient descent of every model,
+ * the self-consistency errors and the object gradient; projection sets,
+ * PTYCHO_FLAG_KEEP_FARFIELD and the probe gradient are refused). */
 int ptycho_roi_supported(int32_t roi_x, int32_t roi_y);
 /* PTYCHO_OK if the batch entry points take this geometry, else the error code
  * (PTYCHO_ERR_UNSUPPORTED or PTYCHO_ERR_INVALID_ARGUMENT) they would return,

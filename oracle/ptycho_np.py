@@ -43,6 +43,8 @@ class State:
     mixed: bool = False
     propagators: Optional[np.ndarray] = None  # (T-1,Sx,Sy) complex64
     sampling: tuple = (1.0, 1.0)    # real-space pixel size (A), for position limits
+    roi_shape: Optional[tuple] = None  # region_of_interest_shape; None: the detector's
+    resample_exit_waves: bool = False  # set whenever region_of_interest_shape was given
 
     def copy(self):
         return dataclasses.replace(
@@ -79,7 +81,9 @@ class Oracle:
         self.num_probes = s.num_probes
         self.propagators = (None if s.propagators is None
                             else np.asarray(s.propagators, dtype=self.c))
-        self.roi = np.array(self.amplitudes.shape[-2:])
+        self.amp_shape = np.array(self.amplitudes.shape[-2:])
+        self.roi = np.array(s.roi_shape) if s.roi_shape is not None else self.amp_shape
+        self.resample = bool(s.resample_exit_waves)
         self.object_shape = self.object.shape[-2:]
         self.J = self.amplitudes.shape[0]
         self.exit_waves = None
@@ -200,6 +204,28 @@ class Oracle:
             return shifted, patches, shifted * np.expand_dims(patches, axis=1)
         return shifted, patches, shifted * patches
 
+    @staticmethod
+    def bilinear_resample(array, output_size):
+        """utils.py:2347-2428 (vectorized, conserve_array_sums=True): scipy.ndimage.zoom
+        with order 1, mode "grid-wrap", grid_mode=True over the last two axes,
+        divided by the ratio of pixel counts (a float64 scalar: complex64 input
+        comes back complex128, as in the reference)."""
+        from scipy.ndimage import zoom
+
+        input_size = np.array(array.shape[-2:])
+        scale = tuple(np.array(output_size) / input_size)
+        scale = (1,) * (array.ndim - 2) + scale
+        out = zoom(array, scale, order=1, mode="grid-wrap", grid_mode=True)
+        return out / np.array(scale).prod()
+
+    def to_detector(self, fo):
+        """ptychographic_methods.py:1601-1609: resample to match the data."""
+        return self.bilinear_resample(fo, self.amp_shape) if self.resample else fo
+
+    def to_roi(self, fo):
+        """ptychographic_methods.py:1623-1631: back to region_of_interest_shape."""
+        return self.bilinear_resample(fo, self.roi) if self.resample else fo
+
     def farfield(self, fo):
         if self.mixed:
             return np.sqrt(np.sum(np.abs(fo) ** 2, axis=1))
@@ -207,7 +233,7 @@ class Oracle:
 
     def gd_projection(self, amplitudes, overlap, mask):
         """ptychographic_methods.py:1576-1635 and 2742-2804."""
-        fo = self.fft2(overlap)
+        fo = self.to_detector(self.fft2(overlap))
         if mask is not None:
             fo *= mask
         ff = self.farfield(fo)
@@ -219,7 +245,7 @@ class Oracle:
             mod = amplitudes * np.exp(1j * np.angle(fo)) - fo
         if mask is not None:
             mod *= mask
-        return self.ifft2(mod), error
+        return self.ifft2(self.to_roi(mod)), error
 
     def ps_projection(self, amplitudes, overlap, exit_waves, a, b, c):
         """ptychographic_methods.py:1637-1734 and 2806-2904."""
@@ -228,7 +254,7 @@ class Oracle:
         if exit_waves is None:
             exit_waves = overlap.copy()
         factor = c * overlap + y * exit_waves
-        fp = self.fft2(factor)
+        fp = self.to_detector(self.fft2(factor))
         ff = self.farfield(fp)
         error = np.sum(np.abs(amplitudes - ff) ** 2)
         if self.mixed:
@@ -236,7 +262,7 @@ class Oracle:
             fp *= (amplitudes / ff)[:, None]
         else:
             fp = amplitudes * np.exp(1j * np.angle(fp))
-        projected = self.ifft2(fp)
+        projected = self.ifft2(self.to_roi(fp))
         return x * exit_waves + a * overlap + b * projected, error
 
     # --------------------------------------------------------------- adjoint A13-A14
@@ -316,7 +342,10 @@ class Oracle:
             if not fix_probe:
                 on = self._normaliser(np.sum(np.abs(patches) ** 2, axis=0), m)
                 g = np.sum(np.expand_dims(np.conj(patches), axis=1) * ew, axis=0) * on[None]
-                probe = g if projection else probe + step * g
+                if projection:
+                    probe = g
+                else:
+                    probe += step * g  # in place, :2992 (a complex128 term is cast back)
             self.object, self.probe = obj, probe
             return
         pn = self._normaliser(self.scatter(np.abs(shifted) ** 2, positions_px), m)
@@ -328,18 +357,22 @@ class Oracle:
         if not fix_probe:
             on = self._normaliser(np.sum(np.abs(patches) ** 2, axis=0), m)
             g = np.sum(np.conj(patches) * ew, axis=0) * on
-            probe = g if projection else probe + step * g
+            if projection:
+                probe = g
+            else:
+                probe += step * g  # in place, :1900
         self.object, self.probe = obj, probe
 
     # ------------------------------------------------------- position correction A16
     def position_correction(self, rows, cols, shifted, ov, amps, pos, pos_init, step,
                             max_update, max_total):
-        """ptychographic_methods.py:2071-2225 (without diffraction resampling): a
+        """ptychographic_methods.py:2071-2225 (far fields resampled to the detector
+        as at :2119-2173 when region_of_interest_shape was given): a
         per-position 2x2 least-squares shift from the intensity change of one-pixel
         object shifts, computed with the object after this batch's update, the
         overlap of the forward pass and `shifted` (the forward pass's shifted probes,
         or for multislice the updated probe)."""
-        fo = self.fft2(ov)
+        fo = self.to_detector(self.fft2(ov))
         fo_conj = np.conj(fo)
         estimated = self.farfield(fo) ** 2
         measured = amps ** 2
@@ -347,8 +380,8 @@ class Oracle:
         difference = (measured - estimated).reshape(flat)
         _, _, ov_dx = self.overlap((rows + 1) % self.object_shape[0], cols, shifted)
         _, _, ov_dy = self.overlap(rows, (cols + 1) % self.object_shape[1], shifted)
-        fdx = fo - self.fft2(ov_dx)
-        fdy = fo - self.fft2(ov_dy)
+        fdx = fo - self.to_detector(self.fft2(ov_dx))
+        fdy = fo - self.to_detector(self.fft2(ov_dy))
         pdx = 2 * np.real(fdx * fo_conj)
         pdy = 2 * np.real(fdy * fo_conj)
         if pdx.ndim == 4:
@@ -391,7 +424,7 @@ class Oracle:
             rows, cols = self.patch_indices(pos)
             shifted = self.fft_shift(self.probe, frac)
             _, _, ov = self.overlap(rows, cols, shifted)
-            ff = self.farfield(self.fft2(ov))
+            ff = self.farfield(self.to_detector(self.fft2(ov)))
             errors = np.hstack((errors, np.sum(np.abs(self.amplitudes[start:end] - ff) ** 2,
                                                axis=(-2, -1))))
         errors /= self.mean_intensity

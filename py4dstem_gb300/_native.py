@@ -45,6 +45,8 @@ class Geometry(ctypes.Structure):
         ("num_probes", ctypes.c_int32),
         ("object_is_potential", ctypes.c_int32),
         ("flags", ctypes.c_int32),
+        ("detector_x", ctypes.c_int32),   # 0: the ROI shape (no resampling)
+        ("detector_y", ctypes.c_int32),
     ]
 
 

@@ -53,6 +53,9 @@ cudaEvent_t take_event() {
   return e;
 }
 
+int detector_x(const ptycho_geometry* g) { return g->detector_x ? g->detector_x : g->roi_x; }
+int detector_y(const ptycho_geometry* g) { return g->detector_y ? g->detector_y : g->roi_y; }
+
 int check_geometry(const ptycho_geometry* g) {
   if (!g) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "geometry is null");
   if ((g->flags & ~(PTYCHO_FLAG_MIXED_STATE | PTYCHO_FLAG_KEEP_FARFIELD |
@@ -66,13 +69,20 @@ int check_geometry(const ptycho_geometry* g) {
                 "ROI %dx%d has no kernel (supported: square 32, 48, 64, 96, 128, 256 "
                 "and 96 x 128, 128 x 96)",
                 g->roi_x, g->roi_y);
-  if (staged_roi(g->roi_x, g->roi_y) &&
-      (g->num_slices != 1 || g->num_probes != 1 ||
-       (g->flags & (PTYCHO_FLAG_MIXED_STATE | PTYCHO_FLAG_KEEP_FARFIELD)) != 0))
+  if ((g->detector_x == 0) != (g->detector_y == 0) || g->detector_x < 0 ||
+      g->detector_y < 0 || (g->detector_x != 0 && (g->detector_x < 2 || g->detector_y < 2)))
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT,
+                "detector_x and detector_y must both be 0 (the ROI shape) or both >= 2 "
+                "(got %d x %d)", g->detector_x, g->detector_y);
+  if (detector_x(g) > 4096 || detector_y(g) > 4096)
+    return fail(PTYCHO_ERR_UNSUPPORTED, "detector %d x %d larger than 4096 x 4096",
+                detector_x(g), detector_y(g));
+  if ((staged_roi(g->roi_x, g->roi_y) || detector_x(g) != g->roi_x ||
+       detector_y(g) != g->roi_y) &&
+      (g->flags & PTYCHO_FLAG_KEEP_FARFIELD) != 0)
     return fail(PTYCHO_ERR_UNSUPPORTED,
-                "a %d x %d ROI runs the single-slice, single-probe model only, without "
-                "PTYCHO_FLAG_MIXED_STATE or PTYCHO_FLAG_KEEP_FARFIELD (position correction)",
-                g->roi_x, g->roi_y);
+                "PTYCHO_FLAG_KEEP_FARFIELD (position correction) is not available for a %d x %d "
+                "ROI or a resampled far field", g->roi_x, g->roi_y);
   if (g->object_x < g->roi_x || g->object_y < g->roi_y)
     return fail(PTYCHO_ERR_UNSUPPORTED, "object %dx%d smaller than ROI %dx%d", g->object_x,
                 g->object_y, g->roi_x, g->roi_y);
@@ -100,9 +110,13 @@ cudaError_t ensure_smem_limit(const void* fn, int bytes) {
 }
 
 Workspace workspace_layout(int Sx, int Sy, int Px, int Py, int T, int M, int B,
-                           bool keep_farfield) {
+                           bool keep_farfield, int Ax, int Ay) {
   Workspace w{};
   const size_t N = (size_t)Sx * Sy;
+  const bool resample = Ax != Sx || Ay != Sy;
+  const bool staged = staged_roi(Sx, Sy) || resample;
+  const size_t Nd = (size_t)Ax * Ay;
+  const size_t chunks = ((resample ? Nd : N) + 2047) / 2048;
   const size_t P = (size_t)Px * Py;
   const size_t ntiles = (size_t)((Px + kTile - 1) / kTile) * ((Py + kTile - 1) / kTile);
   const size_t nb = (N + kReduceThreads - 1) / kReduceThreads;
@@ -119,10 +133,13 @@ Workspace workspace_layout(int Sx, int Sy, int Px, int Py, int T, int M, int B,
   w.st_probe = take(sizeof(float2) * B * M * N);
   w.st_nprobe = take(sizeof(float) * B * N);
   const bool mixed_ms = T > 1 && M > 1;
-  w.scratch_f = take(T == 1 || keep_farfield || mixed_ms ? sizeof(float2) * B * M * N : 0);
+  w.scratch_f =
+      take(T == 1 || keep_farfield || mixed_ms || staged ? sizeof(float2) * B * M * N : 0);
   w.st_pm = take(mixed_ms ? sizeof(float2) * T * B * M * N : 0);
   w.pos_round = take(sizeof(int2) * B);
   w.err = take(sizeof(float) * B);
+  w.err_part = take(staged ? sizeof(float) * B * chunks : 0);
+  w.det_f = take(resample ? sizeof(float2) * B * M * Nd : 0);
   w.obj_grad = take(sizeof(float2) * T * P);
   w.obj_nrm = take(sizeof(float) * T * P);
   w.tile_max = take(sizeof(float) * T * ntiles);
@@ -151,6 +168,8 @@ void bind_workspace(BatchArgs& a, void* base, const Workspace& w) {
   a.st_pm = reinterpret_cast<float2*>(p + w.st_pm);
   a.pos_round = reinterpret_cast<int2*>(p + w.pos_round);
   a.err = reinterpret_cast<float*>(p + w.err);
+  a.err_part = reinterpret_cast<float*>(p + w.err_part);
+  a.det_f = reinterpret_cast<float2*>(p + w.det_f);
   a.obj_grad = reinterpret_cast<float2*>(p + w.obj_grad);
   a.obj_nrm = reinterpret_cast<float*>(p + w.obj_nrm);
   a.tile_max = reinterpret_cast<float*>(p + w.tile_max);
@@ -177,13 +196,17 @@ int prepare(const ptycho_geometry* g, int32_t batch, void* workspace, size_t wor
     return fail(PTYCHO_ERR_WORKSPACE, "workspace must be 256-byte aligned");
   const Workspace w = workspace_layout(g->roi_x, g->roi_y, g->object_x, g->object_y,
                                        g->num_slices, g->num_probes, batch,
-                                       (g->flags & PTYCHO_FLAG_KEEP_FARFIELD) != 0);
+                                       (g->flags & PTYCHO_FLAG_KEEP_FARFIELD) != 0,
+                                       detector_x(g), detector_y(g));
   if (workspace_bytes < w.total)
     return fail(PTYCHO_ERR_WORKSPACE, "workspace of %zu bytes is smaller than the %zu needed",
                 workspace_bytes, w.total);
   std::memset(&a, 0, sizeof(a));
   a.Sx = g->roi_x;
   a.Sy = g->roi_y;
+  a.Ax = detector_x(g);
+  a.Ay = detector_y(g);
+  a.resample = a.Ax != a.Sx || a.Ay != a.Sy ? 1 : 0;
   a.Px = g->object_x;
   a.Py = g->object_y;
   a.T = g->num_slices;
@@ -228,8 +251,10 @@ int ptycho_geometry_supported(const ptycho_geometry* g) { return check_geometry(
 
 size_t ptycho_workspace_bytes(const ptycho_geometry* g, int32_t max_batch) {
   if (!g || max_batch < 1) return 0;
+  if (check_geometry(g) != PTYCHO_OK) return 0;
   return workspace_layout(g->roi_x, g->roi_y, g->object_x, g->object_y, g->num_slices,
-                          g->num_probes, max_batch, (g->flags & PTYCHO_FLAG_KEEP_FARFIELD) != 0)
+                          g->num_probes, max_batch, (g->flags & PTYCHO_FLAG_KEEP_FARFIELD) != 0,
+                          detector_x(g), detector_y(g))
       .total;
 }
 
@@ -257,7 +282,7 @@ static int run_batch(const ptycho_geometry* g, void* object, void* probe,
   if (!(g->flags & PTYCHO_FLAG_SPECTRUM_READY)) e = launch_probe_spectrum(a, s);
   if (e != cudaSuccess) return cuda_fail(e, "probe spectrum kernel");
   a.prepare_spectrum = (g->flags & PTYCHO_FLAG_PREPARE_SPECTRUM) && !a.fix_probe ? 1 : 0;
-  a.staging_t = position_v2_eligible(a) ? 1 : 0;
+  a.staging_t = !staged_batch(a) && position_v2_eligible(a) ? 1 : 0;
   // the plain single-slice GD instantiation of the position kernel stages no
   // |O|^2 terms; the probe-side reduction gathers them from the object
   a.nprobe_from_object = !a.staging_t && !a.projection && !a.forward_only &&
@@ -303,9 +328,9 @@ int ptycho_projection_batch(const ptycho_geometry* g, void* object, void* probe,
   int st = prepare(g, batch, workspace, workspace_bytes, a);
   if (st != PTYCHO_OK) return st;
   if (!exit_waves) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "exit_waves must be non-null");
-  if (staged_roi(g->roi_x, g->roi_y))
-    return fail(PTYCHO_ERR_UNSUPPORTED, "projection sets are not available for a %d x %d ROI",
-                g->roi_x, g->roi_y);
+  if (staged_batch(a))
+    return fail(PTYCHO_ERR_UNSUPPORTED, "projection sets are not available for a %d x %d ROI "
+                "or a resampled far field", g->roi_x, g->roi_y);
   a.projection = 1;
   a.keep_farfield = (g->flags & PTYCHO_FLAG_KEEP_FARFIELD) ? 1 : 0;
   a.pa = projection_a;
@@ -405,9 +430,9 @@ int ptycho_gd_gradient(const ptycho_geometry* g, const void* object, const void*
                                              "and loss must be non-null");
   if (g->num_slices > 1 && !propagators)
     return fail(PTYCHO_ERR_INVALID_ARGUMENT, "multislice needs propagators");
-  if (probe_grad && staged_roi(g->roi_x, g->roi_y))
+  if (probe_grad && staged_batch(a))
     return fail(PTYCHO_ERR_UNSUPPORTED, "the probe gradient is not available for a %d x %d ROI "
-                                        "(pass probe_grad = null for the object gradient)",
+                "or a resampled far field (pass probe_grad = null for the object gradient)",
                 g->roi_x, g->roi_y);
   a.mixed_formula = (g->num_probes > 1 || (g->flags & PTYCHO_FLAG_MIXED_STATE)) ? 1 : 0;
   a.object = const_cast<void*>(object);

@@ -15,6 +15,8 @@ constexpr int kReduceThreads = 256;
 // Per-batch kernel arguments (device pointers into caller buffers/workspace).
 struct BatchArgs {
   int Sx, Sy, Px, Py, T, M;
+  int Ax, Ay;              // detector (amplitude) shape; = Sx, Sy without resampling
+  int resample;            // far field resampled between the ROI and the detector grid
   int potential;           // object is float32 potential
   int projection;          // projection-set update instead of gradient descent
   int mixed_formula;       // |F|_tot ratio form (mixed-state class)
@@ -63,6 +65,8 @@ struct BatchArgs {
   float2* st_pm;        // (T,B,M,N) probe of each slice and mode (mixed-state multislice)
   int2* pos_round;      // (B)
   float* err;           // (B)
+  float* err_part;      // (B, chunks) per-chunk error partials of the staged path
+  float2* det_f;        // (B,M,Ax Ay) detector-grid far fields (resampling only)
   float2* obj_grad;     // (T,P)
   float* obj_nrm;       // (T,P)
   float* tile_max;      // (T,ntiles)
@@ -79,12 +83,13 @@ struct BatchArgs {
 
 struct Workspace {
   size_t probe_spec, tw, st_obj, st_nobj, st_probe, st_nprobe, scratch_f, st_pm, pos_round, err,
-      obj_grad, obj_nrm, tile_max, obj_part, obj_npart, probe_part, probe_npart, probe_bmax, probe_grad,
-      probe_nrm, com, red, total;
+      err_part, det_f, obj_grad, obj_nrm, tile_max, obj_part, obj_npart, probe_part,
+      probe_npart, probe_bmax, probe_grad, probe_nrm, com, red, total;
 };
 
+// Ax, Ay: detector shape (resampling when it differs from Sx, Sy)
 Workspace workspace_layout(int Sx, int Sy, int Px, int Py, int T, int M, int B,
-                           bool keep_farfield);
+                           bool keep_farfield, int Ax, int Ay);
 void bind_workspace(BatchArgs& a, void* base, const Workspace& w);
 
 bool roi_supported(int Sx, int Sy);
@@ -149,9 +154,11 @@ cudaError_t launch_probe_orthogonalize(const BatchArgs& a, float2* scratch_probe
 cudaError_t launch_probe_mix(const BatchArgs& a, const float2* in, const float2* coeffs,
                              float2* out, cudaStream_t s);
 
-// ---- ptycho_staged.cu: the 256 x 256 region of interest as batch-wide kernels
+// ---- ptycho_staged.cu: the model as batch-wide kernels (256 x 256 ROI, resampling)
 bool staged_roi(int Sx, int Sy);
-// single slice, single probe, gradient descent or forward only
+// the batch runs on the staged path (256 x 256 ROI or a resampled far field)
+bool staged_batch(const BatchArgs& a);
+// gradient descent or forward only, no kept far fields, no exact probe gradient
 bool staged_batch_supported(const BatchArgs& a);
 cudaError_t launch_staged_spectrum(const BatchArgs& a, cudaStream_t s);
 cudaError_t launch_staged_positions(const BatchArgs& a, cudaStream_t s);

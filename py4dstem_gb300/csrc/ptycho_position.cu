@@ -57,14 +57,14 @@ bool roi_supported(int Sx, int Sy) {
   }
 
 // (the staged path has no position correction and no exact probe gradient:
-// the C ABI refuses both at 256 x 256)
+// the C ABI refuses both for 256 x 256 and resampled batches)
 cudaError_t launch_probe_spectrum(const BatchArgs& a, cudaStream_t s) {
   if (staged_roi(a.Sx, a.Sy)) return launch_staged_spectrum(a, s);
   PTY_DISPATCH(launch_probe_spectrum, a, s)
 }
 
 cudaError_t launch_position_kernel(const BatchArgs& a, cudaStream_t s) {
-  if (staged_roi(a.Sx, a.Sy)) return launch_staged_positions(a, s);
+  if (staged_batch(a)) return launch_staged_positions(a, s);
   PTY_DISPATCH(launch_position_kernel, a, s)
 }
 

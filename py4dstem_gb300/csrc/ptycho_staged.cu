@@ -1,42 +1,62 @@
-// The 256 x 256 region of interest: the per-position model as a sequence of
-// batch-wide kernels over waves in global memory.
+// The per-position model as a sequence of batch-wide kernels over waves in
+// global memory (the "staged" path), for what the fused one-block-per-position
+// kernel of ptycho_position.cuh cannot hold or does not do:
 //
-// A 256^2 complex64 wave is 512 KiB, more than the 227 KiB of shared memory one
-// block can hold, so the fused one-block-per-position kernel of
-// ptycho_position.cuh does not apply. Here the B waves of a batch live in the
-// workspace's far-field buffer (scratch_f, B x 256^2 complex64: 128 MiB for 256
-// positions) and each step of the model is one kernel over the whole batch:
+//  * the 256 x 256 region of interest: a 256^2 complex64 wave is 512 KiB, more
+//    than the 227 KiB of shared memory one block can hold;
+//  * a far field resampled to a detector of another shape (the reference's
+//    region_of_interest_shape, ptychographic_methods.py:1601-1631): the Fourier
+//    projection then runs on the detector grid, between two resampling steps.
+//
+// The waves of a batch (B x M, one per position and probe mode) live in the
+// workspace's far-field buffer and every step of the model is one kernel over
+// the whole batch:
 //
 //   ramps        per position: the sub-pixel shift ramps exp(-2 pi i k d) along x
 //                and y (phase formed in float32, cos/sin rounded once, as in the
 //                fused kernel) and the rounded origin
-//   shift        W = FFT2(P) . ramp_x ramp_y
-//   lines        a 2D transform is two passes of 1D transforms of length 256:
-//                16 lines of one position per block staged in shared memory and
-//                transformed by the radix-16 x 16 Stockham passes of
-//                fft_smem.cuh. Rows first (along y, as the fused kernel), then
-//                columns; a column block moves 16 adjacent columns, so every
-//                row segment it reads or writes is 128 bytes.
-//   overlap      P_s = W / N (stashed in st_probe), W = P_s O_patch
-//   projection   F = W: chunk partials of sum (A - |F|)^2, W = A F/|F| - F
-//                (detector mask applied to F and to the result)
-//   adjoint      chi = W / N: conj(P_s) chi (Re(-i conj(O) conj(P) chi) for a
-//                potential) and |P_s|^2 for the object, conj(O) chi for the
-//                probe; |O|^2 is gathered by the probe reduction from the object
+//   shift        W_m = FFT2(P_m) . ramp_x ramp_y
+//   lines        a 2D transform is two passes of 1D transforms: 16 lines of one
+//                wave per block staged in shared memory and transformed by the
+//                Stockham passes of fft_smem.cuh, rows (along y) first, then
+//                columns (a column block moves 16 adjacent columns, so each row
+//                segment it reads or writes is contiguous)
+//   overlap      P_{s,m} = W_m / N (stashed), W_m = P_{s,m} O_s patch; between
+//                slices W_m <- IFFT2(FFT2(W_m) H_s)
+//   projection   single probe: err = sum (A - |F|)^2, G = A F/|F| - F; mixed
+//                state: |F|_tot = sqrt(sum_m |F_m|^2), G_m = (A/|F|_tot) F_m - F_m;
+//                the detector mask multiplies F and G. With resampling, F_m is
+//                first interpolated onto the detector grid and G_m back onto the
+//                region of interest (bilinear_resample below)
+//   adjoint      chi_m = IFFT2(G_m), walking back through the slices: object term
+//                sum_m conj(P_{s,m}) chi_{s,m} (Re(-i conj(O) conj(P) chi) for a
+//                potential) and sum_m |P_{s,m}|^2, then chi_m conj(O_s) propagated
+//                back by conj(H); at slice 0 the probe term conj(O_0) chi_m
 //
 // then the deterministic reductions and updates of ptycho_reduce.cu, as for the
 // fused path. The operators are those of ptycho_position.cuh (reference:
-// py4DSTEM 0.14.18 ptychographic_methods.py:1482-1527 overlap, :1576-1640
-// Fourier projection, :1818-1908 adjoint). Gradient descent of the
-// single-slice, single-probe model, the forward-only pass (self-consistency
-// errors), the object gradient, the probe-overlap map and the probe
-// centre-of-mass and aperture constraints run at 256^2; the C ABI refuses the
-// other models at this size.
+// py4DSTEM 0.14.18 ptychographic_methods.py:1482-1527 and 2300-2351 overlap,
+// :1576-1635 and 2742-2804 Fourier projection, :1818-1908, 2353-2458 and
+// 2906-3000 adjoint). Gradient descent of every model (single slice,
+// multislice, mixed state, both), the forward-only pass (self-consistency
+// errors) and the object gradient run here; projection sets, position
+// correction and the exact probe gradient are refused by the C ABI for the
+// batches this path runs.
 //
-// Scratch inside the workspace: the ramps (B x 512 float2) sit in st_nobj and
-// the error partials (B x 32 floats) in st_nprobe, both free until the adjoint
-// writes st_nobj (the ramps are dead by then) and never read as |O|^2 (the
-// probe reduction of this model gathers |O|^2 from the object).
+// bilinear_resample (utils.py:2347-2428) calls scipy.ndimage.zoom(order=1,
+// mode="grid-wrap", grid_mode=True) on the complex far field. SciPy zooms a
+// complex array as its real and imaginary parts without passing grid_mode on,
+// so the interpolation it performs maps output index k to input coordinate
+// k (n_in - 1) / (n_out - 1) (end points aligned), linear between the two
+// neighbouring samples; the result is divided by the ratio of the two grids'
+// pixel counts (conserve_array_sums). The same mapping is used here, with the
+// weights formed in float64 and the sums in float32.
+//
+// Workspace use: the ramps sit in st_nobj (dead before the adjoint writes it),
+// the error partials in err_part, the detector-grid far fields (resampling
+// only) in det_f. The stash P_{s,m} is st_probe (single slice), st_obj
+// (multislice, one probe; overwritten by the object term of the same element)
+// or st_pm (mixed-state multislice), as in the fused kernel.
 #include <cuda_runtime.h>
 
 #include "ptycho_position.cuh"
@@ -44,29 +64,24 @@
 namespace pty {
 namespace {
 
-constexpr int S = 256;
-constexpr int N = S * S;
 constexpr int kLines = 16;        // lines per block of a transform pass
 constexpr int kLineThreads = 256;
-constexpr int kLD = S + 1;        // shared-memory pitch of a staged line
-constexpr int kEwThreads = 256;   // elementwise kernels: 8 samples per thread
+constexpr int kEwThreads = 256;   // elementwise kernels: up to 8 samples per thread
 constexpr int kPer = 8;
 constexpr int kChunk = kEwThreads * kPer;
-constexpr int kChunks = N / kChunk;  // elementwise blocks per position (32)
-static_assert(N % kChunk == 0, "chunking");
 
-// Object index of patch pixel (x, y) for a position with rounded origin r:
-// ((r - S/2) mod P + (x + S/2) mod S) mod P, as obj_x / obj_y of the fused kernel.
-__device__ __forceinline__ size_t patch_index(const BatchArgs& a, int2 r, int x, int y) {
-  int ox = pmod(r.x - S / 2, a.Px) + (x + S / 2) % S;
-  int oy = pmod(r.y - S / 2, a.Py) + (y + S / 2) % S;
+int chunks_of(int n) { return (n + kChunk - 1) / kChunk; }
+
+__device__ __forceinline__ size_t patch_index(const BatchArgs& a, int s, int2 r, int x, int y) {
+  int ox = pmod(r.x - a.Sx / 2, a.Px) + (x + a.Sx / 2) % a.Sx;
+  int oy = pmod(r.y - a.Sy / 2, a.Py) + (y + a.Sy / 2) % a.Sy;
   if (ox >= a.Px) ox -= a.Px;
   if (oy >= a.Py) oy -= a.Py;
-  return (size_t)ox * a.Py + oy;
+  return ((size_t)s * a.Px + ox) * a.Py + oy;
 }
 
-__device__ __forceinline__ float2 patch_value(const BatchArgs& a, int2 r, int x, int y) {
-  const size_t idx = patch_index(a, r, x, y);
+__device__ __forceinline__ float2 patch_value(const BatchArgs& a, int s, int2 r, int x, int y) {
+  const size_t idx = patch_index(a, s, r, x, y);
   if (a.potential) {
     float sv, cv;
     sincosf(reinterpret_cast<const float*>(a.object)[idx], &sv, &cv);
@@ -75,9 +90,17 @@ __device__ __forceinline__ float2 patch_value(const BatchArgs& a, int2 r, int x,
   return reinterpret_cast<const float2*>(a.object)[idx];
 }
 
-// One block per position: ramps[b] = (ramp_x[256], ramp_y[256]) and the rounded
+// P_{s,m} of position b, element e
+__device__ __forceinline__ float2* stash(const BatchArgs& a, int s, int b, int m) {
+  const size_t N = (size_t)a.Sx * a.Sy;
+  if (a.T == 1) return a.st_probe + ((size_t)b * a.M + m) * N;
+  if (a.M == 1) return a.st_obj + ((size_t)s * a.B + b) * N;
+  return a.st_pm + (((size_t)s * a.B + b) * a.M + m) * N;
+}
+
+// One block per position: ramps[b] = (ramp_x[Sx], ramp_y[Sy]) and the rounded
 // origin. `direct` positions are indexed by b (probe overlap), else by pos_rows.
-__global__ void __launch_bounds__(S) staged_ramps_kernel(BatchArgs a, float2* ramps, int direct) {
+__global__ void __launch_bounds__(256) staged_ramps_kernel(BatchArgs a, float2* ramps, int direct) {
   const int b = blockIdx.x;
   const int prow = (!direct && a.pos_rows) ? a.pos_rows[b] : b;
   const float posx = finite_or_zero(a.positions[2 * prow]);
@@ -85,174 +108,346 @@ __global__ void __launch_bounds__(S) staged_ramps_kernel(BatchArgs a, float2* ra
   const float rx = rintf(posx);  // numpy.round: half to even
   const float ry = rintf(posy);
   const float dx = posx - rx, dy = posy - ry;
-  const int i = threadIdx.x;
-  const float k = (float)fint(i, S) / (float)S;
-  ramps[(size_t)b * 2 * S + i] = cis_rounded(__fmul_rn(__fmul_rn(-6.2831855f, k), dx));
-  ramps[(size_t)b * 2 * S + S + i] = cis_rounded(__fmul_rn(__fmul_rn(-6.2831855f, k), dy));
-  if (i == 0) a.pos_round[b] = make_int2((int)rx, (int)ry);
+  float2* r = ramps + (size_t)b * (a.Sx + a.Sy);
+  for (int i = threadIdx.x; i < a.Sx + a.Sy; i += 256) {
+    const bool along_x = i < a.Sx;
+    const int j = along_x ? i : i - a.Sx;
+    const int n = along_x ? a.Sx : a.Sy;
+    const float k = (float)fint(j, n) / (float)n;
+    r[i] = cis_rounded(__fmul_rn(__fmul_rn(-6.2831855f, k), along_x ? dx : dy));
+  }
+  if (threadIdx.x == 0) a.pos_round[b] = make_int2((int)rx, (int)ry);
 }
 
-// W[b] = spec . ramp_x ramp_y (grid: B x kChunks)
-__global__ void __launch_bounds__(kEwThreads) staged_shift_kernel(const float2* __restrict__ spec,
+// W[b, m] = spec[m] . ramp_x ramp_y (grid: B M x chunks)
+__global__ void __launch_bounds__(kEwThreads) staged_shift_kernel(BatchArgs a,
                                                                   const float2* __restrict__ ramps,
                                                                   float2* W) {
-  const int b = blockIdx.x;
-  const float2* r = ramps + (size_t)b * 2 * S;
+  const int N = a.Sx * a.Sy;
+  const int b = blockIdx.x / a.M, m = blockIdx.x % a.M;
+  const float2* rx = ramps + (size_t)b * (a.Sx + a.Sy);
+  const float2* ry = rx + a.Sx;
+  const float2* spec = a.probe_spec + (size_t)m * N;
   const int e0 = blockIdx.y * kChunk + threadIdx.x;
 #pragma unroll
   for (int i = 0; i < kPer; ++i) {
     const int e = e0 + i * kEwThreads;
-    W[(size_t)b * N + e] = c_mul(__ldg(spec + e), c_mul(r[e / S], r[S + e % S]));
+    if (e < N)
+      W[(size_t)blockIdx.x * N + e] = c_mul(__ldg(spec + e), c_mul(rx[e / a.Sy], ry[e % a.Sy]));
   }
 }
 
-// One pass of 1D transforms of length 256 over 16 lines of wave blockIdx.x, rows
-// (along y) or columns (along x); the results are multiplied by `scale`.
-template <int DIR, bool ROWS>
-__global__ void __launch_bounds__(kLineThreads) staged_lines_kernel(float2* W, float scale) {
-  __shared__ float2 buf[kLines * kLD];
-  __shared__ float2 tw[S];
+// One pass of 1D transforms of length L over 16 lines of wave blockIdx.x: rows
+// (ROWS, line l is elements l Sy .. l Sy + Sy - 1, L = Sy) or columns (line l is
+// elements l, l + Sy, ..., L = Sx); the results times `scale`.
+template <int DIR, int L, bool ROWS>
+__global__ void __launch_bounds__(kLineThreads) staged_lines_kernel(float2* W, int N, int Sy,
+                                                                    float scale) {
+  constexpr int LD = L + 1;
+  __shared__ float2 buf[kLines * LD];
+  __shared__ float2 tw[L];
   float2* w = W + (size_t)blockIdx.x * N;
   const int l0 = blockIdx.y * kLines;
-  fill_twiddles<S, kLineThreads>(tw);
+  fill_twiddles<L, kLineThreads>(tw);
   if (ROWS) {
-    for (int e = threadIdx.x; e < kLines * S; e += kLineThreads) {
-      const int l = e / S, j = e % S;
-      buf[l * kLD + j] = w[(size_t)(l0 + l) * S + j];
+    for (int e = threadIdx.x; e < kLines * L; e += kLineThreads) {
+      const int l = e / L, j = e % L;
+      buf[l * LD + j] = w[(size_t)(l0 + l) * Sy + j];
     }
   } else {
-    // column l0 + l, element j is w[j * S + l0 + l]: 16 adjacent columns per row
-    for (int e = threadIdx.x; e < kLines * S; e += kLineThreads) {
+    for (int e = threadIdx.x; e < kLines * L; e += kLineThreads) {
       const int j = e / kLines, l = e % kLines;
-      buf[l * kLD + j] = w[(size_t)j * S + l0 + l];
+      buf[l * LD + j] = w[(size_t)j * Sy + l0 + l];
     }
   }
   __syncthreads();
-  Schedule<S>::template run<kLines, kLineThreads, DIR>(buf, kLD, 1, tw);
+  Schedule<L>::template run<kLines, kLineThreads, DIR>(buf, LD, 1, tw);
   if (ROWS) {
-    for (int e = threadIdx.x; e < kLines * S; e += kLineThreads) {
-      const int l = e / S, j = e % S;
-      w[(size_t)(l0 + l) * S + j] = c_scale(buf[l * kLD + j], scale);
+    for (int e = threadIdx.x; e < kLines * L; e += kLineThreads) {
+      const int l = e / L, j = e % L;
+      w[(size_t)(l0 + l) * Sy + j] = c_scale(buf[l * LD + j], scale);
     }
   } else {
-    for (int e = threadIdx.x; e < kLines * S; e += kLineThreads) {
+    for (int e = threadIdx.x; e < kLines * L; e += kLineThreads) {
       const int j = e / kLines, l = e % kLines;
-      w[(size_t)j * S + l0 + l] = c_scale(buf[l * kLD + j], scale);
+      w[(size_t)j * Sy + l0 + l] = c_scale(buf[l * LD + j], scale);
     }
   }
 }
 
-// FFT2 (DIR -1) or unnormalised inverse (DIR +1) of `count` waves in place,
-// times `scale`.
-template <int DIR>
-cudaError_t fft2_waves(float2* W, int count, float scale, cudaStream_t s) {
-  const dim3 grid(count, S / kLines);
-  staged_lines_kernel<DIR, true><<<grid, kLineThreads, 0, s>>>(W, 1.0f);
-  staged_lines_kernel<DIR, false><<<grid, kLineThreads, 0, s>>>(W, scale);
+template <int DIR, int L, bool ROWS>
+void lines_t(float2* W, int count, int Sx, int Sy, float scale, cudaStream_t s) {
+  const int nlines = ROWS ? Sx : Sy;
+  staged_lines_kernel<DIR, L, ROWS><<<dim3(count, nlines / kLines), kLineThreads, 0, s>>>(
+      W, Sx * Sy, Sy, scale);
+}
+
+template <int DIR, bool ROWS>
+cudaError_t lines(float2* W, int count, int L, int Sx, int Sy, float scale, cudaStream_t s) {
+  switch (L) {
+    case 32: lines_t<DIR, 32, ROWS>(W, count, Sx, Sy, scale, s); break;
+    case 48: lines_t<DIR, 48, ROWS>(W, count, Sx, Sy, scale, s); break;
+    case 64: lines_t<DIR, 64, ROWS>(W, count, Sx, Sy, scale, s); break;
+    case 96: lines_t<DIR, 96, ROWS>(W, count, Sx, Sy, scale, s); break;
+    case 128: lines_t<DIR, 128, ROWS>(W, count, Sx, Sy, scale, s); break;
+    case 256: lines_t<DIR, 256, ROWS>(W, count, Sx, Sy, scale, s); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 
-// P_s = W / N (stashed), W = P_s O_patch
-__global__ void __launch_bounds__(kEwThreads) staged_overlap_kernel(BatchArgs a, float2* W) {
+// FFT2 (DIR -1) or unnormalised inverse (DIR +1) of `count` Sx x Sy waves in
+// place, times `scale`.
+template <int DIR>
+cudaError_t fft2_waves(float2* W, int count, int Sx, int Sy, float scale, cudaStream_t s) {
+  cudaError_t e = lines<DIR, true>(W, count, Sy, Sx, Sy, 1.0f, s);
+  if (e != cudaSuccess) return e;
+  return lines<DIR, false>(W, count, Sx, Sx, Sy, scale, s);
+}
+
+// Slice s of the forward model: P_{s,m} = W_m / N (stashed), W_m = P_{s,m} O_s
+__global__ void __launch_bounds__(kEwThreads) staged_overlap_kernel(BatchArgs a, float2* W,
+                                                                    int s) {
+  const int N = a.Sx * a.Sy;
   const int b = blockIdx.x;
   const int2 r = a.pos_round[b];
   const float invN = 1.0f / (float)N;
   const int e0 = blockIdx.y * kChunk + threadIdx.x;
-  float2 ov[kPer];
 #pragma unroll
   for (int i = 0; i < kPer; ++i) {
     const int e = e0 + i * kEwThreads;
-    ov[i] = patch_value(a, r, e / S, e % S);
-  }
-#pragma unroll
-  for (int i = 0; i < kPer; ++i) {
-    const size_t k = (size_t)b * N + e0 + i * kEwThreads;
-    const float2 p = c_scale(W[k], invN);
-    a.st_probe[k] = p;
-    W[k] = c_mul(p, ov[i]);
+    if (e >= N) break;
+    const float2 o = patch_value(a, s, r, e / a.Sy, e % a.Sy);
+    for (int m = 0; m < a.M; ++m) {
+      const size_t k = ((size_t)b * a.M + m) * N + e;
+      const float2 p = c_scale(W[k], invN);
+      stash(a, s, b, m)[e] = p;
+      W[k] = c_mul(p, o);
+    }
   }
 }
 
-// Chunk partials of sum (A - |F|)^2; W = A F/|F| - F (masked) unless forward only.
-__global__ void __launch_bounds__(kEwThreads) staged_projection_kernel(BatchArgs a, float2* W,
-                                                                       float* err_part) {
+// W *= H_s (or conj(H_s)) for every wave of the batch (grid: B M x chunks)
+__global__ void __launch_bounds__(kEwThreads) staged_propagate_kernel(BatchArgs a, float2* W,
+                                                                      int s, int conjugate) {
+  const int N = a.Sx * a.Sy;
+  const float2* h = a.props + (size_t)s * N;
+  const int e0 = blockIdx.y * kChunk + threadIdx.x;
+#pragma unroll
+  for (int i = 0; i < kPer; ++i) {
+    const int e = e0 + i * kEwThreads;
+    if (e >= N) break;
+    float2 hv = h[e];
+    if (conjugate) hv.y = -hv.y;
+    const size_t k = (size_t)blockIdx.x * N + e;
+    W[k] = c_mul(W[k], hv);
+  }
+}
+
+// Fourier projection at one detector pixel of position b: `f[m]` are the far
+// fields of the modes there (modified in place into G_m), A the amplitude,
+// mk the mask value; returns (A - |F|)^2.
+template <bool kSingle>
+__device__ __forceinline__ float project_pixel(const BatchArgs& a, float2* f, float A, float mk,
+                                               bool masked) {
+  const bool mixed = !kSingle && (a.M > 1 || a.mixed_formula);
+  if (kSingle || !mixed) {
+    float2 v = f[0];
+    if (masked) v = c_scale(v, mk);
+    const float af = c_abs(v);
+    const float d = A - af;
+    const float q = af > 0.0f ? A / af : 0.0f;
+    float2 r = af > 0.0f ? make_float2(fmaf(v.x, q, -v.x), fmaf(v.y, q, -v.y))
+                         : c_sub(make_float2(A, 0.0f), v);
+    if (masked) r = c_scale(r, mk);
+    f[0] = r;
+    return d * d;
+  }
+  if constexpr (kSingle) return 0.0f;
+  float itot = 0.0f;
+  for (int m = 0; m < a.M; ++m) {
+    if (masked) f[m] = c_scale(f[m], mk);
+    const float av = hypotf(f[m].x, f[m].y);  // |F_m|^2 as numpy forms it
+    itot += av * av;
+  }
+  const float tot = sqrtf(itot);
+  const float d = A - tot;
+  const float ratio = tot == 0.0f ? 0.0f : A / tot;
+  for (int m = 0; m < a.M; ++m) {
+    float2 r = c_sub(c_scale(f[m], ratio), f[m]);
+    if (masked) r = c_scale(r, mk);
+    f[m] = r;
+  }
+  return d * d;
+}
+
+// Block partial of the error into err_part[b * chunks + blockIdx.y]
+__device__ __forceinline__ void store_partial(const BatchArgs& a, float err, int chunks) {
   __shared__ float red[kEwThreads / 32];
+  const float t = block_sum<kEwThreads>(err, red);
+  if (threadIdx.x == 0) a.err_part[(size_t)blockIdx.x * chunks + blockIdx.y] = t;
+}
+
+// Projection on the region-of-interest grid (no resampling), W in place;
+// kSingle: one probe without the mixed-state formula (M = 1)
+template <bool kSingle>
+__global__ void __launch_bounds__(kEwThreads) staged_projection_kernel(BatchArgs a, float2* W) {
+  const int N = a.Sx * a.Sy;
+  const int M = kSingle ? 1 : a.M;
   const int b = blockIdx.x;
   const int arow = a.amp_rows ? a.amp_rows[b] : b;
   const float* amp = a.amplitudes + (size_t)arow * N;
   const int e0 = blockIdx.y * kChunk + threadIdx.x;
-  float av[kPer];
-#pragma unroll
-  for (int i = 0; i < kPer; ++i) av[i] = __ldg(amp + e0 + i * kEwThreads);
   float err = 0.0f;
+  float2 f[kSingle ? 1 : 16];
 #pragma unroll
   for (int i = 0; i < kPer; ++i) {
     const int e = e0 + i * kEwThreads;
-    const size_t k = (size_t)b * N + e;
-    float2 f = W[k];
+    if (e >= N) break;
+    for (int m = 0; m < M; ++m) f[m] = W[((size_t)b * M + m) * N + e];
     const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
-    if (a.det_mask) f = c_scale(f, mk);
-    const float af = c_abs(f);
-    const float A = av[i];
-    const float d = A - af;
-    err += d * d;
-    if (!a.forward_only) {
-      const float q = af > 0.0f ? A / af : 0.0f;
-      float2 rr = af > 0.0f ? make_float2(fmaf(f.x, q, -f.x), fmaf(f.y, q, -f.y))
-                            : c_sub(make_float2(A, 0.0f), f);
-      if (a.det_mask) rr = c_scale(rr, mk);
-      W[k] = rr;
-    }
+    err += project_pixel<kSingle>(a, f, __ldg(amp + e), mk, a.det_mask != nullptr);
+    if (!a.forward_only)
+      for (int m = 0; m < M; ++m) W[((size_t)b * M + m) * N + e] = f[m];
   }
-  const float t = block_sum<kEwThreads>(err, red);
-  if (threadIdx.x == 0) err_part[(size_t)b * kChunks + blockIdx.y] = t;
+  store_partial(a, err, gridDim.y);
+}
+
+// Interpolation of output index k onto an input axis of n samples from an
+// output axis of n_out samples (end points aligned): lower index and weight of
+// the upper neighbour, formed in float64.
+struct Tap {
+  int i0, i1;
+  float t;
+};
+__device__ __forceinline__ Tap tap(int k, int n, int n_out) {
+  const double z = n_out > 1 ? (double)(n - 1) / (double)(n_out - 1) : 1.0;
+  const double cc = (double)k * z;
+  const double f = floor(cc);
+  int i0 = (int)f;
+  int i1 = i0 + 1;
+  if (i0 >= n) i0 -= n;  // grid-wrap (only the upper neighbour of the last sample)
+  if (i1 >= n) i1 -= n;
+  return Tap{i0, i1, (float)(cc - f)};
+}
+
+__device__ __forceinline__ float2 bilerp(const float2* g, int ny, Tap tx, Tap ty) {
+  const float ux = 1.0f - tx.t, uy = 1.0f - ty.t;
+  float2 v = c_scale(g[(size_t)tx.i0 * ny + ty.i0], ux * uy);
+  v = c_add(v, c_scale(g[(size_t)tx.i0 * ny + ty.i1], ux * ty.t));
+  v = c_add(v, c_scale(g[(size_t)tx.i1 * ny + ty.i0], tx.t * uy));
+  return c_add(v, c_scale(g[(size_t)tx.i1 * ny + ty.i1], tx.t * ty.t));
+}
+
+// Resampled projection: per detector pixel, F_m interpolated from the ROI grid
+// (divided by the pixel-count ratio), projected; G_m into det_f
+__global__ void __launch_bounds__(kEwThreads) staged_projection_resampled_kernel(
+    BatchArgs a, const float2* __restrict__ W) {
+  const int N = a.Sx * a.Sy;
+  const int Nd = a.Ax * a.Ay;
+  const int b = blockIdx.x;
+  const int arow = a.amp_rows ? a.amp_rows[b] : b;
+  const float* amp = a.amplitudes + (size_t)arow * Nd;
+  // far field sums are kept: divide by (Ax / Sx)(Ay / Sy)
+  const float ratio = (float)(((double)a.Ax / a.Sx) * ((double)a.Ay / a.Sy));
+  const int e0 = blockIdx.y * kChunk + threadIdx.x;
+  float err = 0.0f;
+  float2 f[16];
+#pragma unroll 1
+  for (int i = 0; i < kPer; ++i) {
+    const int e = e0 + i * kEwThreads;
+    if (e >= Nd) break;
+    const Tap tx = tap(e / a.Ay, a.Sx, a.Ax);
+    const Tap ty = tap(e % a.Ay, a.Sy, a.Ay);
+    for (int m = 0; m < a.M; ++m) {
+      const float2 v = bilerp(W + ((size_t)b * a.M + m) * N, a.Sy, tx, ty);
+      f[m] = make_float2(__fdiv_rn(v.x, ratio), __fdiv_rn(v.y, ratio));
+    }
+    const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
+    err += project_pixel<false>(a, f, __ldg(amp + e), mk, a.det_mask != nullptr);
+    if (!a.forward_only)
+      for (int m = 0; m < a.M; ++m) a.det_f[((size_t)b * a.M + m) * Nd + e] = f[m];
+  }
+  store_partial(a, err, gridDim.y);
+}
+
+// G_m from the detector grid back onto the ROI grid (grid: B M x chunks)
+__global__ void __launch_bounds__(kEwThreads) staged_resample_back_kernel(BatchArgs a,
+                                                                          float2* W) {
+  const int N = a.Sx * a.Sy;
+  const int Nd = a.Ax * a.Ay;
+  const float ratio = (float)(((double)a.Sx / a.Ax) * ((double)a.Sy / a.Ay));
+  const float2* g = a.det_f + (size_t)blockIdx.x * Nd;
+  const int e0 = blockIdx.y * kChunk + threadIdx.x;
+#pragma unroll 1
+  for (int i = 0; i < kPer; ++i) {
+    const int e = e0 + i * kEwThreads;
+    if (e >= N) break;
+    const float2 v = bilerp(g, a.Ay, tap(e / a.Sy, a.Ax, a.Sx), tap(e % a.Sy, a.Ay, a.Sy));
+    W[(size_t)blockIdx.x * N + e] = make_float2(__fdiv_rn(v.x, ratio), __fdiv_rn(v.y, ratio));
+  }
 }
 
 // err[b] = the position's chunk partials summed in order; NaN for a non-finite
 // position (reported as PTYCHO_ERR_NONFINITE).
-__global__ void staged_error_kernel(BatchArgs a, const float* err_part) {
+__global__ void staged_error_kernel(BatchArgs a, int chunks) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= a.B) return;
   float t = 0.0f;
-  for (int c = 0; c < kChunks; ++c) t += err_part[(size_t)b * kChunks + c];
+  for (int c = 0; c < chunks; ++c) t += a.err_part[(size_t)b * chunks + c];
   const int prow = a.pos_rows ? a.pos_rows[b] : b;
   const bool ok = isfinite(a.positions[2 * prow]) && isfinite(a.positions[2 * prow + 1]);
   a.err[b] = ok ? t : __int_as_float(0x7fc00000);
 }
 
-// chi = W / N: object terms and |P_s|^2, probe term conj(O) chi
-__global__ void __launch_bounds__(kEwThreads) staged_adjoint_kernel(BatchArgs a,
-                                                                    const float2* W) {
+// Adjoint at slice s: chi_m = W_m / N; object terms summed over the modes in
+// order; chi_m conj(O_s) back into W_m (s > 0) or into the probe term (s = 0)
+__global__ void __launch_bounds__(kEwThreads) staged_adjoint_kernel(BatchArgs a, float2* W,
+                                                                    int s) {
+  const int N = a.Sx * a.Sy;
   const int b = blockIdx.x;
   const int2 r = a.pos_round[b];
   const float invN = 1.0f / (float)N;
   const int e0 = blockIdx.y * kChunk + threadIdx.x;
-  float2 ov[kPer];
-#pragma unroll
+#pragma unroll 1
   for (int i = 0; i < kPer; ++i) {
     const int e = e0 + i * kEwThreads;
-    ov[i] = patch_value(a, r, e / S, e % S);
-  }
-#pragma unroll
-  for (int i = 0; i < kPer; ++i) {
-    const size_t k = (size_t)b * N + e0 + i * kEwThreads;
-    const float2 chi = c_scale(W[k], invN);
-    const float2 p = a.st_probe[k];
-    a.st_obj[k] = object_term(a.potential, ov[i], p, chi);
-    a.st_nobj[k] = c_abs2(p);
-    a.st_probe[k] = c_conj_mul(ov[i], chi);
+    if (e >= N) break;
+    const float2 o = patch_value(a, s, r, e / a.Sy, e % a.Sy);
+    float2 g = make_float2(0.0f, 0.0f);
+    float pn = 0.0f;
+    for (int m = 0; m < a.M; ++m) {
+      const size_t k = ((size_t)b * a.M + m) * N + e;
+      const float2 chi = c_scale(W[k], invN);
+      const float2 p = stash(a, s, b, m)[e];
+      const float2 gm = object_term(a.potential, o, p, chi);
+      g = m == 0 ? gm : c_add(g, gm);
+      pn = m == 0 ? c_abs2(p) : pn + c_abs2(p);
+      const float2 bt = c_conj_mul(o, chi);
+      if (s > 0) {
+        W[k] = bt;
+      } else {
+        a.st_probe[k] = bt;
+      }
+    }
+    a.st_obj[((size_t)s * a.B + b) * N + e] = g;
+    a.st_nobj[((size_t)s * a.B + b) * N + e] = pn;
+    if (s == 0 && !a.nprobe_from_object) a.st_nprobe[(size_t)b * N + e] = c_abs2(o);
   }
 }
 
 // |P_b|^2 = |W / N|^2, abs() then square as numpy forms it
 __global__ void __launch_bounds__(kEwThreads) staged_intensity_kernel(BatchArgs a,
                                                                       const float2* W) {
+  const int N = a.Sx * a.Sy;
   const int b = blockIdx.x;
   const float invN = 1.0f / (float)N;
   const int e0 = blockIdx.y * kChunk + threadIdx.x;
 #pragma unroll
   for (int i = 0; i < kPer; ++i) {
-    const size_t k = (size_t)b * N + e0 + i * kEwThreads;
+    const int e = e0 + i * kEwThreads;
+    if (e >= N) break;
+    const size_t k = (size_t)b * N + e;
     const float2 p = c_scale(W[k], invN);
     const float av = hypotf(p.x, p.y);
     a.st_nobj[k] = av * av;
@@ -267,12 +462,16 @@ __global__ void copy_waves_kernel(const float2* __restrict__ src, float2* dst, s
 // W[m] *= ramp(-CoM) for the probe centre-of-mass constraint, the CoM from
 // probe_com_kernel cast to float32 as the reference's shift does.
 __global__ void __launch_bounds__(kEwThreads) staged_com_ramp_kernel(BatchArgs a, float2* W) {
-  __shared__ float2 rx[S], ry[S];
+  __shared__ float2 rx[256], ry[256];
+  const int N = a.Sx * a.Sy;
   const float dx = (float)(-a.com[0]);
   const float dy = (float)(-a.com[1]);
-  for (int i = threadIdx.x; i < S; i += kEwThreads) {
-    const float k = (float)fint(i, S) / (float)S;
+  for (int i = threadIdx.x; i < a.Sx; i += kEwThreads) {
+    const float k = (float)fint(i, a.Sx) / (float)a.Sx;
     rx[i] = cis_rounded(__fmul_rn(__fmul_rn(-6.2831855f, k), dx));
+  }
+  for (int i = threadIdx.x; i < a.Sy; i += kEwThreads) {
+    const float k = (float)fint(i, a.Sy) / (float)a.Sy;
     ry[i] = cis_rounded(__fmul_rn(__fmul_rn(-6.2831855f, k), dy));
   }
   __syncthreads();
@@ -280,14 +479,15 @@ __global__ void __launch_bounds__(kEwThreads) staged_com_ramp_kernel(BatchArgs a
 #pragma unroll
   for (int i = 0; i < kPer; ++i) {
     const int e = e0 + i * kEwThreads;
+    if (e >= N) break;
     const size_t k = (size_t)blockIdx.x * N + e;
-    W[k] = c_mul(W[k], c_mul(rx[e / S], ry[e % S]));
+    W[k] = c_mul(W[k], c_mul(rx[e / a.Sy], ry[e % a.Sy]));
   }
 }
 
 // out[0] = sum |p|^2 over one wave (abs() then square), one 1024-thread block:
 // thread partials, then a fixed shuffle tree and warp order.
-__global__ void __launch_bounds__(1024) staged_power_kernel(const float2* p, float* out) {
+__global__ void __launch_bounds__(1024) staged_power_kernel(const float2* p, int N, float* out) {
   __shared__ float red[32];
   float part = 0.0f;
   for (int e = threadIdx.x; e < N; e += 1024) {
@@ -300,12 +500,13 @@ __global__ void __launch_bounds__(1024) staged_power_kernel(const float2* p, flo
 }
 
 // F <- aperture . exp(i angle F)
-__global__ void __launch_bounds__(kEwThreads) staged_aperture_kernel(float2* F,
+__global__ void __launch_bounds__(kEwThreads) staged_aperture_kernel(float2* F, int N,
                                                                      const float* aperture) {
   const int e0 = blockIdx.y * kChunk + threadIdx.x;
 #pragma unroll
   for (int i = 0; i < kPer; ++i) {
     const int e = e0 + i * kEwThreads;
+    if (e >= N) break;
     const float2 f = F[e];
     float sn, cs;
     sincosf(atan2f(f.y, f.x), &sn, &cs);
@@ -315,56 +516,90 @@ __global__ void __launch_bounds__(kEwThreads) staged_aperture_kernel(float2* F,
 }
 
 // p *= sqrt(pw[0] / pw[1])
-__global__ void __launch_bounds__(kEwThreads) staged_rescale_kernel(float2* p, const float* pw) {
+__global__ void __launch_bounds__(kEwThreads) staged_rescale_kernel(float2* p, int N,
+                                                                    const float* pw) {
   const float k = sqrtf(pw[0] / pw[1]);
   const int e0 = blockIdx.y * kChunk + threadIdx.x;
 #pragma unroll
-  for (int i = 0; i < kPer; ++i) p[e0 + i * kEwThreads] = c_scale(p[e0 + i * kEwThreads], k);
+  for (int i = 0; i < kPer; ++i) {
+    const int e = e0 + i * kEwThreads;
+    if (e < N) p[e] = c_scale(p[e], k);
+  }
 }
 
 }  // namespace
 
-bool staged_roi(int Sx, int Sy) { return Sx == S && Sy == S; }
+bool staged_roi(int Sx, int Sy) { return Sx == 256 && Sy == 256; }
+
+bool staged_batch(const BatchArgs& a) { return staged_roi(a.Sx, a.Sy) || a.resample; }
 
 bool staged_batch_supported(const BatchArgs& a) {
-  return a.T == 1 && a.M == 1 && !a.projection && !a.mixed_formula && !a.keep_farfield &&
-         !a.exact_probe_grad && !a.staging_t;
+  return a.M <= 16 && !a.projection && !a.keep_farfield && !a.exact_probe_grad && !a.staging_t;
 }
 
 cudaError_t launch_staged_spectrum(const BatchArgs& a, cudaStream_t s) {
-  const size_t n = (size_t)a.M * N;
+  const size_t n = (size_t)a.M * a.Sx * a.Sy;
   copy_waves_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a.probe, a.probe_spec, n);
-  return fft2_waves<-1>(a.probe_spec, a.M, 1.0f, s);
+  return fft2_waves<-1>(a.probe_spec, a.M, a.Sx, a.Sy, 1.0f, s);
 }
 
 cudaError_t launch_staged_positions(const BatchArgs& a, cudaStream_t s) {
   if (!staged_batch_supported(a)) return cudaErrorNotSupported;
+  const int N = a.Sx * a.Sy;
+  const int BM = a.B * a.M;
   float2* ramps = reinterpret_cast<float2*>(a.st_nobj);
-  float* err_part = a.st_nprobe;
   float2* W = a.scratch_f;
-  const dim3 ew(a.B, kChunks);
-  staged_ramps_kernel<<<a.B, S, 0, s>>>(a, ramps, 0);
-  staged_shift_kernel<<<ew, kEwThreads, 0, s>>>(a.probe_spec, ramps, W);
-  cudaError_t e = fft2_waves<+1>(W, a.B, 1.0f, s);
+  const dim3 per_pos(a.B, chunks_of(N));
+  const dim3 per_wave(BM, chunks_of(N));
+  staged_ramps_kernel<<<a.B, 256, 0, s>>>(a, ramps, 0);
+  staged_shift_kernel<<<per_wave, kEwThreads, 0, s>>>(a, ramps, W);
+  cudaError_t e = fft2_waves<+1>(W, BM, a.Sx, a.Sy, 1.0f, s);
+  for (int sl = 0; sl < a.T && e == cudaSuccess; ++sl) {
+    staged_overlap_kernel<<<per_pos, kEwThreads, 0, s>>>(a, W, sl);
+    if (sl + 1 < a.T) {
+      if ((e = fft2_waves<-1>(W, BM, a.Sx, a.Sy, 1.0f, s)) != cudaSuccess) break;
+      staged_propagate_kernel<<<per_wave, kEwThreads, 0, s>>>(a, W, sl, 0);
+      e = fft2_waves<+1>(W, BM, a.Sx, a.Sy, 1.0f, s);
+    }
+  }
   if (e != cudaSuccess) return e;
-  staged_overlap_kernel<<<ew, kEwThreads, 0, s>>>(a, W);
-  if ((e = fft2_waves<-1>(W, a.B, 1.0f, s)) != cudaSuccess) return e;
-  staged_projection_kernel<<<ew, kEwThreads, 0, s>>>(a, W, err_part);
-  staged_error_kernel<<<(a.B + 255) / 256, 256, 0, s>>>(a, err_part);
+  if ((e = fft2_waves<-1>(W, BM, a.Sx, a.Sy, 1.0f, s)) != cudaSuccess) return e;
+  int chunks;
+  if (a.resample) {
+    chunks = chunks_of(a.Ax * a.Ay);
+    staged_projection_resampled_kernel<<<dim3(a.B, chunks), kEwThreads, 0, s>>>(a, W);
+    if (!a.forward_only)
+      staged_resample_back_kernel<<<per_wave, kEwThreads, 0, s>>>(a, W);
+  } else {
+    chunks = chunks_of(N);
+    if (a.M == 1 && !a.mixed_formula)
+      staged_projection_kernel<true><<<per_pos, kEwThreads, 0, s>>>(a, W);
+    else
+      staged_projection_kernel<false><<<per_pos, kEwThreads, 0, s>>>(a, W);
+  }
+  staged_error_kernel<<<(a.B + 255) / 256, 256, 0, s>>>(a, chunks);
   if (a.forward_only) return cudaGetLastError();
-  if ((e = fft2_waves<+1>(W, a.B, 1.0f, s)) != cudaSuccess) return e;
-  staged_adjoint_kernel<<<ew, kEwThreads, 0, s>>>(a, W);
+  if ((e = fft2_waves<+1>(W, BM, a.Sx, a.Sy, 1.0f, s)) != cudaSuccess) return e;
+  for (int sl = a.T - 1; sl >= 0; --sl) {
+    staged_adjoint_kernel<<<per_pos, kEwThreads, 0, s>>>(a, W, sl);
+    if (sl > 0) {
+      if ((e = fft2_waves<-1>(W, BM, a.Sx, a.Sy, 1.0f, s)) != cudaSuccess) return e;
+      staged_propagate_kernel<<<per_wave, kEwThreads, 0, s>>>(a, W, sl - 1, 1);
+      if ((e = fft2_waves<+1>(W, BM, a.Sx, a.Sy, 1.0f, s)) != cudaSuccess) return e;
+    }
+  }
   return cudaGetLastError();
 }
 
 cudaError_t launch_staged_intensity(const BatchArgs& a, cudaStream_t s) {
-  // ramps in st_obj, waves in scratch_f, |P_b|^2 into st_nobj
+  // mode 0 only (a.M = 1); ramps in st_obj, waves in scratch_f, |P_b|^2 into st_nobj
+  const int N = a.Sx * a.Sy;
   float2* ramps = a.st_obj;
   float2* W = a.scratch_f;
-  const dim3 ew(a.B, kChunks);
-  staged_ramps_kernel<<<a.B, S, 0, s>>>(a, ramps, 1);
-  staged_shift_kernel<<<ew, kEwThreads, 0, s>>>(a.probe_spec, ramps, W);
-  cudaError_t e = fft2_waves<+1>(W, a.B, 1.0f, s);
+  const dim3 ew(a.B, chunks_of(N));
+  staged_ramps_kernel<<<a.B, 256, 0, s>>>(a, ramps, 1);
+  staged_shift_kernel<<<ew, kEwThreads, 0, s>>>(a, ramps, W);
+  cudaError_t e = fft2_waves<+1>(W, a.B, a.Sx, a.Sy, 1.0f, s);
   if (e != cudaSuccess) return e;
   staged_intensity_kernel<<<ew, kEwThreads, 0, s>>>(a, W);
   return cudaGetLastError();
@@ -372,10 +607,12 @@ cudaError_t launch_staged_intensity(const BatchArgs& a, cudaStream_t s) {
 
 cudaError_t launch_staged_probe_shift(const BatchArgs& a, cudaStream_t s) {
   // every mode through the probe spectrum buffer (free between batches)
+  const int N = a.Sx * a.Sy;
   cudaError_t e = launch_staged_spectrum(a, s);
   if (e != cudaSuccess) return e;
-  staged_com_ramp_kernel<<<dim3(a.M, kChunks), kEwThreads, 0, s>>>(a, a.probe_spec);
-  if ((e = fft2_waves<+1>(a.probe_spec, a.M, 1.0f / (float)N, s)) != cudaSuccess) return e;
+  staged_com_ramp_kernel<<<dim3(a.M, chunks_of(N)), kEwThreads, 0, s>>>(a, a.probe_spec);
+  if ((e = fft2_waves<+1>(a.probe_spec, a.M, a.Sx, a.Sy, 1.0f / (float)N, s)) != cudaSuccess)
+    return e;
   const size_t n = (size_t)a.M * N;
   copy_waves_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a.probe_spec, a.probe, n);
   return cudaGetLastError();
@@ -383,16 +620,18 @@ cudaError_t launch_staged_probe_shift(const BatchArgs& a, cudaStream_t s) {
 
 cudaError_t launch_staged_aperture(const BatchArgs& a, cudaStream_t s) {
   // mode 0 in place; its power before and after in two stream-ordered floats
+  const int N = a.Sx * a.Sy;
   float* pw = nullptr;
   cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&pw), 2 * sizeof(float), s);
   if (e != cudaSuccess) return e;
   float2* p = a.probe;
-  staged_power_kernel<<<1, 1024, 0, s>>>(p, pw);
-  if ((e = fft2_waves<-1>(p, 1, 1.0f, s)) == cudaSuccess) {
-    staged_aperture_kernel<<<dim3(1, kChunks), kEwThreads, 0, s>>>(p, a.aperture);
-    if ((e = fft2_waves<+1>(p, 1, 1.0f / (float)N, s)) == cudaSuccess) {
-      staged_power_kernel<<<1, 1024, 0, s>>>(p, pw + 1);
-      staged_rescale_kernel<<<dim3(1, kChunks), kEwThreads, 0, s>>>(p, pw);
+  const dim3 one(1, chunks_of(N));
+  staged_power_kernel<<<1, 1024, 0, s>>>(p, N, pw);
+  if ((e = fft2_waves<-1>(p, 1, a.Sx, a.Sy, 1.0f, s)) == cudaSuccess) {
+    staged_aperture_kernel<<<one, kEwThreads, 0, s>>>(p, N, a.aperture);
+    if ((e = fft2_waves<+1>(p, 1, a.Sx, a.Sy, 1.0f / (float)N, s)) == cudaSuccess) {
+      staged_power_kernel<<<1, 1024, 0, s>>>(p, N, pw + 1);
+      staged_rescale_kernel<<<one, kEwThreads, 0, s>>>(p, N, pw);
       e = cudaGetLastError();
     }
   }

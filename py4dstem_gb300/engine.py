@@ -76,8 +76,8 @@ class DeviceState:
 
 
 # The region of interest whose model runs as batch-wide staged kernels (a wave
-# does not fit one block's shared memory): single slice, single probe, gradient
-# descent only.
+# does not fit one block's shared memory): gradient descent only, as for a far
+# field resampled to a detector of another shape.
 STAGED_ROI = (256, 256)
 
 
@@ -86,11 +86,16 @@ def supported_roi(shape) -> bool:
 
 
 def make_geometry(roi_shape, object_shape, num_slices, num_probes, potential,
-                  mixed_state=False) -> _native.Geometry:
-    return _native.Geometry(int(roi_shape[0]), int(roi_shape[1]), int(object_shape[-2]),
-                            int(object_shape[-1]), int(num_slices), int(num_probes),
-                            1 if potential else 0,
-                            _native.FLAG_MIXED_STATE if mixed_state else 0)
+                  mixed_state=False, detector_shape=None) -> _native.Geometry:
+    """detector_shape: the amplitudes' shape when it differs from roi_shape (the
+    far field is then resampled between the two grids)."""
+    g = _native.Geometry(int(roi_shape[0]), int(roi_shape[1]), int(object_shape[-2]),
+                         int(object_shape[-1]), int(num_slices), int(num_probes),
+                         1 if potential else 0,
+                         _native.FLAG_MIXED_STATE if mixed_state else 0)
+    if detector_shape is not None and tuple(detector_shape) != tuple(roi_shape):
+        g.detector_x, g.detector_y = int(detector_shape[0]), int(detector_shape[1])
+    return g
 
 
 def create_state(*, roi_shape, object_array, probe_array, amplitudes, positions_px,
@@ -100,8 +105,10 @@ def create_state(*, roi_shape, object_array, probe_array, amplitudes, positions_
     if not np.all(np.isfinite(np.asarray(positions_px))):
         raise ValueError("scan positions contain NaN or infinite values")
     lib = _native.lib()
+    det_shape = tuple(int(v) for v in np.shape(amplitudes)[-2:])
     geom = make_geometry(roi_shape, object_array.shape, num_slices, num_probes, potential,
-                         mixed_state or num_probes > 1)
+                         mixed_state or num_probes > 1, det_shape)
+    resampled = det_shape != tuple(int(v) for v in roi_shape)
     if positions_initial is not None:
         geom.flags |= _native.FLAG_KEEP_FARFIELD
     if not lib.ptycho_roi_supported(geom.roi_x, geom.roi_y):
@@ -110,9 +117,10 @@ def create_state(*, roi_shape, object_array, probe_array, amplitudes, positions_
             "(supported: square 32, 48, 64, 96, 128, 256 and 96 x 128, 128 x 96)")
     if lib.ptycho_geometry_supported(ctypes.byref(geom)) != _native.PTYCHO_OK:
         raise NotImplementedError(lib.ptycho_last_error().decode())
-    if projection and (geom.roi_x, geom.roi_y) == STAGED_ROI:
+    if projection and ((geom.roi_x, geom.roi_y) == STAGED_ROI or resampled):
         raise NotImplementedError(
-            f"projection sets are not available for a {geom.roi_x}x{geom.roi_y} region of interest")
+            f"projection sets are not available for a {geom.roi_x}x{geom.roi_y} region of "
+            "interest or a far field resampled to the detector")
     torch = _torch()
     dev = torch.device("cuda", torch.cuda.current_device())
     ws_bytes = int(lib.ptycho_workspace_bytes(ctypes.byref(geom), int(max_batch)))
@@ -138,9 +146,9 @@ def create_state(*, roi_shape, object_array, probe_array, amplitudes, positions_
         amps_host = np.ascontiguousarray(amplitudes, dtype=np.float32)
         mapped = mapped_host_address(amps_host)
         if mapped is None:
-            amp_stage = torch.empty((max_batch,) + tuple(roi_shape), dtype=torch.float32,
+            amp_stage = torch.empty((max_batch,) + det_shape, dtype=torch.float32,
                                     device=dev)
-            amp_pinned = [torch.empty((max_batch,) + tuple(roi_shape), dtype=torch.float32,
+            amp_pinned = [torch.empty((max_batch,) + det_shape, dtype=torch.float32,
                                       pin_memory=True) for _ in range(2)]
     pos = torch.from_numpy(np.ascontiguousarray(positions_px, dtype=np.float32)).to(dev)
     order = torch.arange(pos.shape[0], dtype=torch.int32, device=dev)

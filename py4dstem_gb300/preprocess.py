@@ -35,6 +35,26 @@ from scipy.optimize import curve_fit
 
 from .optics import ComplexProbe, electron_wavelength_angstrom
 
+
+def bilinear_resample(array, output_size, conserve_array_sums=False):
+    """Resize the last two axes by linear interpolation on a periodic grid
+    (utils.py:2347-2428 with vectorized=True): scipy.ndimage.zoom with order 1,
+    mode "grid-wrap" and grid_mode=True, the leading axes kept; divided by the
+    ratio of pixel counts when conserve_array_sums. Host-side, once per
+    reconstruction (the vacuum probe); the reconstruction kernels resample the
+    far fields themselves."""
+    from scipy.ndimage import zoom
+
+    array = np.asarray(array)
+    input_size = np.array(array.shape[-2:])
+    output_size = np.array(output_size)
+    scale = tuple(output_size / input_size)
+    scale = (1,) * (array.ndim - 2) + scale
+    out = zoom(array, scale, order=1, mode="grid-wrap", grid_mode=True)
+    if conserve_array_sums:
+        out = out / np.array(scale).prod()
+    return out
+
 # ----------------------------------------------------------------- small helpers
 
 
@@ -630,9 +650,12 @@ class PreprocessMixin:
                 vpi = shift_bilinear(vpi, -x0, -y0)
                 if crop_patterns:
                     vpi = vpi[self._crop_mask].reshape(self._crop_mask_shape)
-                if vpi.shape != tuple(roi) and self._resample_exit_waves:
-                    raise NotImplementedError(
-                        "resampling the vacuum probe to region_of_interest_shape")
+                sx, sy = vpi.shape
+                tx, ty = (int(v) for v in roi)
+                # the reference's condition as written (ptychographic_methods.py:1056-1064:
+                # `or` binds the x test alone)
+                if sx != tx or sy != ty and self._resample_exit_waves is True:
+                    vpi = bilinear_resample(vpi, (tx, ty), conserve_array_sums=True)
                 vacuum_probe_intensity = vpi
             probe = ComplexProbe(
                 gpts=roi, sampling=self.sampling, energy=self._energy,

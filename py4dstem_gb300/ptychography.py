@@ -326,13 +326,15 @@ class _PtychographyBase(PreprocessMixin):
         amp_shape = tuple(self._amplitudes_for_state().shape)
         self._num_diffraction_patterns = amp_shape[0]
         self._amplitudes_shape = np.array(amp_shape[-2:])
-        if region_of_interest_shape is not None and tuple(region_of_interest_shape) != tuple(
-                self._amplitudes_shape):
-            raise NotImplementedError(
-                "region_of_interest_shape different from the detector shape "
-                "(exit-wave resampling) is not implemented")
-        self._resample_exit_waves = False
-        self._region_of_interest_shape = np.array(amp_shape[-2:])
+        # region_of_interest_shape (singleslice_ptychography.py:431-436): the probe
+        # and the object patches take that shape and every Fourier projection
+        # resamples the far field between it and the detector grid
+        if region_of_interest_shape is not None:
+            self._resample_exit_waves = True
+            self._region_of_interest_shape = np.array(region_of_interest_shape)
+        else:
+            self._resample_exit_waves = False
+            self._region_of_interest_shape = np.array(amp_shape[-2:])
 
         self._positions_px, self._object_padding_px = self._scan_positions_in_pixels(
             self._scan_positions, self._positions_mask, self._object_padding_px,

@@ -161,6 +161,30 @@ def positions_in_pixels(positions_ang, sampling, roi_shape, object_shape):
     return pos
 
 
+def _probe_float64(gpts, sampling, energy, semiangle_mrad, rolloff_mrad, defocus,
+                   astigmatism=0.0, astigmatism_angle=0.0):
+    """The same probe model as optics.ComplexProbe (soft aperture, defocus and
+    two-fold astigmatism), evaluated in float64 from end to end: the portable
+    generator's intensities must not depend on the platform's float32 math
+    library, whose last-bit differences move a Poisson draw now and then."""
+    lam = electron_wavelength_angstrom(energy)
+    kx = np.fft.fftfreq(int(gpts[0]), sampling)
+    ky = np.fft.fftfreq(int(gpts[1]), sampling)
+    x = kx * lam
+    y = ky * lam
+    alpha = np.sqrt(x[:, None] ** 2 + y[None, :] ** 2)
+    phi = np.arctan2(y[None, :], x[:, None])
+    c10 = -defocus
+    chi = 0.5 * alpha ** 2 * (c10 + astigmatism * np.cos(2 * (phi - astigmatism_angle)))
+    chi = 2 * np.pi / lam * chi
+    cutoff = semiangle_mrad / 1000.0
+    roll = rolloff_mrad / 1000.0
+    taper = 0.5 * (1 + np.cos(np.pi * (alpha - cutoff + roll) / roll))
+    aperture = np.where(alpha > cutoff - roll, np.where(alpha > cutoff, 0.0, taper), 1.0)
+    array = np.fft.ifft2(np.exp(-1.0j * chi) * aperture)
+    return array / np.sqrt((np.abs(array) ** 2).sum())
+
+
 def _fresnel(gpts, sampling, wavelength, dz):
     kx = np.fft.fftfreq(gpts[0], sampling)
     ky = np.fft.fftfreq(gpts[1], sampling)
@@ -288,21 +312,25 @@ def make_scan(
     pos_px = positions_in_pixels(pos_ang, sampling, roi, obj_shape)
     wavelength = electron_wavelength_angstrom(energy)
 
-    base = ComplexProbe(energy=energy, gpts=roi, sampling=(sampling, sampling),
-                        semiangle_cutoff=semiangle, rolloff=2.0,
-                        parameters={"defocus": defocus}).build()._array
+    if portable:
+        base = _probe_float64(roi, sampling, energy, semiangle, 2.0, defocus)
+    else:
+        base = ComplexProbe(energy=energy, gpts=roi, sampling=(sampling, sampling),
+                            semiangle_cutoff=semiangle, rolloff=2.0,
+                            parameters={"defocus": defocus}).build()._array
     probes = [base.astype(np.complex128)]
     for m in range(1, num_modes):
         if portable:
             z = portable_normal(rng, 2)
-            perturb = {"defocus": defocus + 20.0 * z[0], "astigmatism": abs(10.0 * z[1]),
-                       "astigmatism_angle": rng.uniform(0, np.pi)}
-        else:
-            perturb = {
-                "defocus": defocus + rng.normal(0.0, 20.0),
-                "astigmatism": abs(rng.normal(0.0, 10.0)),
-                "astigmatism_angle": rng.uniform(0, np.pi),
-            }
+            probes.append(_probe_float64(roi, sampling, energy, semiangle, 2.0,
+                                         defocus + 20.0 * z[0], abs(10.0 * z[1]),
+                                         rng.uniform(0, np.pi)))
+            continue
+        perturb = {
+            "defocus": defocus + rng.normal(0.0, 20.0),
+            "astigmatism": abs(rng.normal(0.0, 10.0)),
+            "astigmatism_angle": rng.uniform(0, np.pi),
+        }
         pm = ComplexProbe(energy=energy, gpts=roi, sampling=(sampling, sampling),
                           semiangle_cutoff=semiangle, rolloff=2.0,
                           parameters=perturb).build()._array

@@ -97,6 +97,38 @@ CASES = {
         cls="single", ctor=dict(object_fov_ang=(32.0, 32.0)), guess=(128, 128),
         mask_seed=5,
         rec=dict(num_iter=4, max_batch_size=16, step_size=0.5, seed_random=8)),
+    # region_of_interest_shape different from the detector: the far field is
+    # resampled onto the detector grid and back in every Fourier projection
+    "ss_gd_resample_up": dict(
+        gen=dict(name="rsu", seed=30, scan_shape=(12, 12), step_ang=0.5, jitter_ang=0.05,
+                 detector=48, object_px=96),
+        cls="single", ctor=dict(object_fov_ang=(24.0, 24.0)), guess=(96, 96),
+        pre_extra=dict(region_of_interest_shape=(64, 64)),
+        rec=dict(num_iter=4, max_batch_size=36, step_size=0.5, seed_random=11)),
+    "ss_gd_resample_down_mask": dict(
+        gen=dict(name="rsd", seed=31, scan_shape=(12, 12), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=96),
+        cls="single", ctor=dict(object_fov_ang=(24.0, 24.0)), guess=(96, 96), mask_seed=6,
+        pre_extra=dict(region_of_interest_shape=(48, 48)),
+        rec=dict(num_iter=4, max_batch_size=36, step_size=0.5, seed_random=12)),
+    "ss_gd_resample_nonsquare": dict(
+        gen=dict(name="rsn", seed=32, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=128),
+        cls="single", ctor=dict(object_fov_ang=(32.0, 32.0)), guess=(128, 128),
+        pre_extra=dict(region_of_interest_shape=(96, 128)),
+        rec=dict(num_iter=3, max_batch_size=25, step_size=0.5, seed_random=13)),
+    "mixed_gd_resample": dict(
+        gen=dict(name="rsm", seed=33, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=96, num_modes=2, mode_weights=(0.8, 0.2)),
+        cls="mixed", ctor=dict(object_fov_ang=(24.0, 24.0), num_probes=2), global_seed=14,
+        guess=(96, 96), pre_extra=dict(region_of_interest_shape=(48, 48)),
+        rec=dict(num_iter=4, max_batch_size=25, step_size=0.5, seed_random=14)),
+    "ms_gd_resample": dict(
+        gen=dict(name="rss", seed=34, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
+                 detector=48, object_px=96, num_slices=2, slice_thickness=20.0),
+        cls="multi", ctor=dict(object_fov_ang=(24.0, 24.0), num_slices=2, slice_thicknesses=20.0),
+        guess=(2, 96, 96), pre_extra=dict(region_of_interest_shape=(64, 64)),
+        rec=dict(num_iter=4, max_batch_size=25, step_size=0.5, seed_random=15)),
     # mixed-state multislice: two modes through three slices
     "mms_gd_T3M2": dict(
         gen=dict(name="mms", seed=24, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
@@ -342,7 +374,8 @@ def make_case(ref, name, spec):
         np.random.seed(spec["global_seed"])
     p = cls(datacube=dc, initial_scan_positions=positions, verbose=False,
             device="cpu", **ctor, **extra)
-    p.preprocess(**PRE)
+    pre_kwargs = dict(PRE, **spec.get("pre_extra", {}))
+    p.preprocess(**pre_kwargs)
     pre = dict(
         mean_intensity=np.float32(p._mean_diffraction_intensity),
         positions_px=p._positions_px.copy(),
@@ -372,7 +405,7 @@ def make_case(ref, name, spec):
         self_consistency_errors=p._return_self_consistency_errors(
             max_batch_size=spec["rec"].get("max_batch_size")),
     )
-    meta = dict(cls=spec["cls"], ctor=ctor, preprocess=PRE, reconstruct=spec["rec"],
+    meta = dict(cls=spec["cls"], ctor=ctor, preprocess=pre_kwargs, reconstruct=spec["rec"],
                 global_seed=spec.get("global_seed"), r_pixel_size=r, q_pixel_size=q,
                 generator=spec["gen"])
     path = os.path.join(HERE, f"{name}.npz")

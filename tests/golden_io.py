@@ -163,7 +163,9 @@ class Golden:
             mixed=m["cls"] in ("mixed", "mixed_multi"),
             propagators=(getattr(p, "_propagator_arrays", None)
                          if m["cls"] in ("multi", "mixed_multi") else None),
-            sampling=tuple(p.sampling))
+            sampling=tuple(p.sampling),
+            roi_shape=tuple(int(v) for v in p._region_of_interest_shape),
+            resample_exit_waves=bool(getattr(p, "_resample_exit_waves", False)))
 
     def oracle_kwargs(self):
         from oracle.ptycho_np import method_abc

@@ -115,7 +115,9 @@ def gpu_reconstruct(state, num_iter=1, method="GD", a=None, b=None, c=None, max_
         max_batch_size = J
     use_mask = bool(fix_potential_baseline and state.fov_mask_inverse.sum() > 0)
     st = engine.create_state(
-        roi_shape=state.amplitudes.shape[-2:], object_array=state.object, probe_array=state.probe,
+        roi_shape=(state.roi_shape if state.roi_shape is not None
+                   else state.amplitudes.shape[-2:]),
+        object_array=state.object, probe_array=state.probe,
         amplitudes=state.amplitudes, positions_px=state.positions_px,
         num_slices=state.num_slices, num_probes=state.num_probes,
         potential=state.object_type == "potential", max_batch=max_batch_size, storage=storage,

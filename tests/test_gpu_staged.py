@@ -1,8 +1,11 @@
-"""The 256 x 256 region of interest (batch-wide staged kernels) against the
-oracle: gradient descent with each option, the constraints over several
-iterations, the forward-only errors, the probe aperture constraint and the
-object gradient. Tolerances as for the fused kernels (the 256-point transforms
-round like the 128-point ones: two radix-16 passes)."""
+"""The staged batch-wide kernels against the oracle: the 256 x 256 region of
+interest (gradient descent of every model with each option, the constraints
+over several iterations, the forward-only errors, the probe aperture
+constraint and the object gradient) and far fields resampled to a detector of
+another shape at the fused sizes. Tolerances as for the fused kernels (the
+256-point transforms round like the 128-point ones: two radix-16 passes).
+The reference-run fixtures with region_of_interest_shape (ss_gd_resample_*,
+mixed_gd_resample, ms_gd_resample) go through tests/test_gpu_golden.py."""
 
 import ctypes
 
@@ -44,6 +47,44 @@ def test_gradient_descent_256_options(cuda, potential, masked, fix_probe):
         mask = (np.random.default_rng(5).uniform(size=(256, 256)) > 0.05).astype(np.float32)
     compare(st, 2e-5, 2e-5, 2e-5, num_iter=2, max_batch_size=5, seed_random=2,
             detector_fourier_mask=mask, fix_probe=fix_probe, **OFF)
+
+
+@pytest.mark.parametrize("modes,slices", [(2, 1), (1, 2), (2, 2)])
+def test_mixed_and_multislice_256(cuda, modes, slices):
+    st = make_state(S=256, J=9, modes=modes, slices=slices, seed=300 + 10 * modes + slices)
+    compare(st, 2e-5, 2e-5, 2e-5, num_iter=1, max_batch_size=5, seed_random=3, **OFF)
+
+
+def resampled_state(state, detector, seed):
+    """The state's model with the far field resampled onto a `detector` grid:
+    amplitudes from the oracle's float64 forward model of the true object are
+    replaced by the oracle's own resampled far field of a perturbed object, so
+    the data are consistent with the resampling model."""
+    import dataclasses
+
+    rng = np.random.default_rng(seed)
+    s = dataclasses.replace(state, roi_shape=tuple(state.amplitudes.shape[-2:]),
+                            resample_exit_waves=True)
+    o = Oracle(s, "float64")
+    o.amp_shape = np.array(detector)
+    truth = o.object * np.exp(1j * rng.uniform(-0.05, 0.05, o.object.shape))
+    o.object = truth
+    pos = o.positions_px
+    frac = pos - np.round(pos)
+    rows, cols = o.patch_indices(pos)
+    shifted = o.fft_shift(o.probe, frac)
+    _, _, ov = o.overlap(rows, cols, shifted)
+    amps = o.farfield(o.to_detector(o.fft2(ov))).astype(np.float32)
+    return dataclasses.replace(s, amplitudes=amps)
+
+
+@pytest.mark.parametrize("S,detector,modes", [(64, (48, 48), 1), (48, (64, 64), 1),
+                                              (64, (96, 80), 2), (96, (64, 64), 1)])
+def test_resampled_far_field(cuda, S, detector, modes):
+    """region_of_interest_shape: the far field is resampled to the detector grid
+    and back (staged path at a fused size), against the oracle."""
+    st = resampled_state(make_state(S=S, J=12, modes=modes, seed=400 + S), detector, S)
+    compare(st, 2e-5, 2e-5, 2e-5, num_iter=2, max_batch_size=5, seed_random=4, **OFF)
 
 
 def test_constraints_256(cuda):
@@ -105,14 +146,21 @@ def test_object_gradient_256(cuda):
     probe = torch.tensor(np.asarray(state.probe, np.complex64)[None], device="cuda")
     loss, g_obj, g_probe = model.loss_and_gradient(obj, probe, probe_gradient=False)
     assert g_probe is None
-    o = Oracle(state)
-    idx = np.arange(o.J)
-    shifted, patches, _, chi, err = o.forward_batch(idx)
-    term = o.scatter(o._obj_term(patches, shifted, chi), o.positions_px[idx])
+    def oracle_terms(o):
+        idx = np.arange(o.J)
+        shifted, patches, _, chi, err = o.forward_batch(idx)
+        return o.scatter(o._obj_term(patches, shifted, chi), o.positions_px[idx]), err
+
+    term, err = oracle_terms(Oracle(state))
+    # the reference algorithm's own rounding floor here: the same model with
+    # every FFT through complex128 (the dark field's phase is rounding-determined)
+    floor = rel(oracle_terms(Oracle(state, fft_round_trip=True))[0], term)
+    term64 = oracle_terms(Oracle(state, "float64"))[0]
     N = 256 * 256
     d_grad = rel(g_obj.cpu().numpy(), -2 * N * term)
     d_loss = abs(float(loss) - float(err)) / float(err)
-    print(f"grad {d_grad:.2e} loss {d_loss:.2e}")
-    assert d_grad < 1e-5 and d_loss < 1e-5
+    print(f"grad {d_grad:.2e} (floor {floor:.2e}, vs FP64 "
+          f"{rel(g_obj.cpu().numpy(), -2 * N * term64):.2e}) loss {d_loss:.2e}")
+    assert d_grad < max(1e-5, 3 * floor) and d_loss < 1e-5
     with pytest.raises(RuntimeError, match="probe gradient is not available"):
         model.loss_and_gradient(obj, probe, probe_gradient=True)

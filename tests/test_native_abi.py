@@ -33,7 +33,7 @@ def test_exports_every_declared_symbol(lib):
 
 
 def test_abi_version(lib):
-    assert lib.ptycho_abi_version() == 2
+    assert lib.ptycho_abi_version() == 3
 
 
 @pytest.mark.parametrize("n,ok", [(32, 1), (48, 1), (64, 1), (96, 1), (128, 1), (80, 0),
@@ -82,11 +82,11 @@ def test_rejects_unsupported_roi(lib):
 
 
 @pytest.mark.parametrize("T,M,flags,ok", [
-    (1, 1, 0, True), (2, 1, 0, False), (1, 2, 0, False), (1, 1, "FLAG_MIXED_STATE", False),
-    (1, 1, "FLAG_KEEP_FARFIELD", False)])
+    (1, 1, 0, True), (2, 1, 0, True), (1, 2, 0, True), (2, 2, 0, True),
+    (1, 1, "FLAG_MIXED_STATE", True), (1, 1, "FLAG_KEEP_FARFIELD", False)])
 def test_staged_roi_models(lib, T, M, flags, ok):
-    """256 x 256 runs the single-slice, single-probe model only: other
-    geometries are refused on the host with the reason."""
+    """256 x 256 runs every gradient-descent model on the staged kernels; kept far
+    fields (position correction) are refused on the host with the reason."""
     g = geometry(roi=256, obj=320, T=T, M=M)
     g.flags = getattr(_native, flags) if flags else 0
     status = lib.ptycho_geometry_supported(ctypes.byref(g))
@@ -95,8 +95,29 @@ def test_staged_roi_models(lib, T, M, flags, ok):
         assert _gd(lib, g) == 3  # the geometry passed; the null workspace did not
     else:
         assert status == 2
-        assert b"single-slice, single-probe" in lib.ptycho_last_error()
+        assert b"PTYCHO_FLAG_KEEP_FARFIELD" in lib.ptycho_last_error()
         assert _gd(lib, g) == 2
+
+
+@pytest.mark.parametrize("det,status", [((0, 0), 0), ((48, 48), 0), ((96, 128), 0),
+                                        ((0, 48), 1), ((1, 64), 1), ((-4, 64), 1),
+                                        ((8192, 64), 2)])
+def test_detector_shape_checks(lib, det, status):
+    """The detector shape (resampled far field) is validated on the host."""
+    g = geometry(roi=64, obj=128)
+    g.detector_x, g.detector_y = det
+    assert lib.ptycho_geometry_supported(ctypes.byref(g)) == status
+    assert (lib.ptycho_workspace_bytes(ctypes.byref(g), 4) > 0) == (status == 0)
+
+
+def test_resampled_workspace_holds_detector_far_fields(lib):
+    g = geometry(roi=64, obj=128, M=2)
+    base = lib.ptycho_workspace_bytes(ctypes.byref(g), 8)
+    g.detector_x, g.detector_y = 96, 96
+    # + B M Ax Ay c64 detector far fields and the error partials
+    assert lib.ptycho_workspace_bytes(ctypes.byref(g), 8) >= base + 8 * 2 * 96 * 96 * 8
+    g.flags = _native.FLAG_KEEP_FARFIELD
+    assert lib.ptycho_geometry_supported(ctypes.byref(g)) == 2
 
 
 def test_geometry_supported_matches_the_batch_checks(lib):
@@ -107,18 +128,25 @@ def test_geometry_supported_matches_the_batch_checks(lib):
 
 
 def test_staged_roi_refused_by_the_engine():
-    """The engine raises NotImplementedError for models the 256 x 256 kernels
+    """The engine raises NotImplementedError for options the 256 x 256 kernels
     do not run, before any device work."""
     import numpy as np
 
     from py4dstem_gb300 import engine
 
-    with pytest.raises(NotImplementedError, match="single-slice, single-probe"):
-        engine.create_state(roi_shape=(256, 256), object_array=np.ones((2, 320, 320), np.complex64),
+    with pytest.raises(NotImplementedError, match="PTYCHO_FLAG_KEEP_FARFIELD"):
+        engine.create_state(roi_shape=(256, 256), object_array=np.ones((320, 320), np.complex64),
                             probe_array=np.ones((256, 256), np.complex64),
                             amplitudes=np.ones((4, 256, 256), np.float32),
-                            positions_px=np.zeros((4, 2), np.float32), num_slices=2,
-                            num_probes=1, potential=False, max_batch=4)
+                            positions_px=np.zeros((4, 2), np.float32), num_slices=1,
+                            num_probes=1, potential=False, max_batch=4,
+                            positions_initial=np.zeros((4, 2), np.float32))
+    with pytest.raises(NotImplementedError, match="projection sets"):
+        engine.create_state(roi_shape=(256, 256), object_array=np.ones((320, 320), np.complex64),
+                            probe_array=np.ones((256, 256), np.complex64),
+                            amplitudes=np.ones((4, 256, 256), np.float32),
+                            positions_px=np.zeros((4, 2), np.float32), num_slices=1,
+                            num_probes=1, potential=False, max_batch=4, projection=True)
 
 
 def test_rejects_object_smaller_than_roi(lib):
