@@ -52,14 +52,18 @@ def _vp(t):
 class PtychoForwardModel:
     """Data, geometry and workspace of a forward model; `loss` is differentiable.
 
-    amplitudes   (J, Sx, Sy) float32, corner-centred (as preprocess() leaves them)
+    amplitudes   (J, Ax, Ay) float32, corner-centred (as preprocess() leaves them)
     positions_px (J, 2) float32 probe positions in object pixels
     object_shape (Px, Py) of one slice
+    roi_shape    (Sx, Sy) of the probe and the object patches when it differs from
+                 the detector (Ax, Ay): the far field is then resampled between
+                 the two grids (region_of_interest_shape); default the detector's
     """
 
     def __init__(self, amplitudes, positions_px, object_shape, *, num_slices: int = 1,
                  num_probes: int = 1, potential: bool = False, propagators=None,
-                 mixed_state: bool = False, max_batch: int = 1024, device=None):
+                 mixed_state: bool = False, max_batch: int = 1024, device=None,
+                 roi_shape=None):
         torch = _torch()
         self.torch = torch
         dev = torch.device(device) if device is not None else torch.device(
@@ -71,7 +75,8 @@ class PtychoForwardModel:
         pos = torch.as_tensor(np.ascontiguousarray(positions_px, dtype=np.float32)
                               if isinstance(positions_px, np.ndarray) else positions_px)
         self.positions = pos.to(dev, torch.float32).contiguous()
-        J, sx, sy = self.amplitudes.shape
+        J, ax, ay = self.amplitudes.shape
+        sx, sy = (ax, ay) if roi_shape is None else (int(roi_shape[0]), int(roi_shape[1]))
         self.num_positions = int(J)
         self.roi_shape = (int(sx), int(sy))
         self.num_slices = int(num_slices)
@@ -81,6 +86,8 @@ class PtychoForwardModel:
         self.geometry = _native.Geometry(int(sx), int(sy), int(object_shape[-2]),
                                          int(object_shape[-1]), self.num_slices,
                                          self.num_probes, 1 if potential else 0, flags)
+        if (ax, ay) != (sx, sy):
+            self.geometry.detector_x, self.geometry.detector_y = int(ax), int(ay)
         lib = _native.lib()
         if not lib.ptycho_roi_supported(int(sx), int(sy)):
             raise NotImplementedError(f"no GPU kernel for a {sx}x{sy} region of interest")
@@ -107,7 +114,8 @@ class PtychoForwardModel:
                    num_slices=p._num_slices, num_probes=p._num_probes,
                    potential=p._object_type == "potential",
                    propagators=getattr(p, "_propagator_arrays", None) if p._multislice else None,
-                   mixed_state=p._mixed, max_batch=max_batch)
+                   mixed_state=p._mixed, max_batch=max_batch,
+                   roi_shape=tuple(p._region_of_interest_shape))
 
     # ------------------------------------------------------------------ helpers
     def _ws(self):

