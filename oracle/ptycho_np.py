@@ -411,6 +411,62 @@ class Oracle:
         """ptychographic_constraints.py:1292-1311."""
         self.positions_px -= self.positions_px.mean(0) - self.positions_initial.mean(0)
 
+    # affine map x -> (x - o) @ M + t + o with M = scale @ shear @ rotation
+    # (utils.py:580-741); (scale0, scale1, shear1, angle, t0, t1)
+    @staticmethod
+    def _affine_apply(p, x, origin):
+        origin = np.asarray(origin, dtype=np.float32)
+        c, s = np.cos(p[3]), np.sin(p[3])
+        m = (np.array([[p[0], 0.0], [0.0, p[1]]], dtype="float32")
+             @ np.array([[1.0, 0.0], [p[2], 1.0]], dtype="float32")
+             @ np.array([[+c, -s], [+s, +c]], dtype="float32"))
+        return ((x - origin) @ np.asarray(m, dtype=np.float32)) + (np.array((p[4], p[5]))
+                                                                   + origin)
+
+    @classmethod
+    def _affine_fit(cls, x0, x1, origin):
+        """utils.py:743-770 (translation allowed) with AffineTransform.fromarray
+        (utils.py:640-671)."""
+        identity = (1.0, 1.0, 0.0, 0.0, 0.0, 0.0)
+        origin = np.asarray(origin, dtype=np.float32)
+        try:
+            a = np.pad(x0 - origin, ((0, 0), (0, 1)), constant_values=1)
+            aT = a.conj().swapaxes(-1, -2)
+            T = np.linalg.inv(aT @ a) @ aT @ (x1 - origin)
+            R = T[:2, :2].copy()
+            s0 = np.linalg.norm(R[0])
+            p = identity
+            if s0 > 0:
+                R[0] /= s0
+                sh = R[0] @ R[1]
+                R[1] -= sh * R[0]
+                s1 = np.linalg.norm(R[1])
+                if s1 > 0:
+                    R[1] /= s1
+                    sh /= s1
+                    p = (float(s0), float(s1), float(sh), float(np.arccos(R[0, 0])),
+                         T[2][0], T[2][1])
+        except np.linalg.LinAlgError:
+            p = identity
+        return p, np.linalg.norm(cls._affine_apply(p, x0, origin) - x1)
+
+    def positions_affine_constraint(self):
+        """ptychographic_constraints.py:1313-1350 with the RANSAC of utils.py:773-827
+        (20 subsets of J // 10 indices from the global generator, inliers within
+        16 px, consensus 0.75)."""
+        x0, x1 = self.positions_initial, self.positions_px
+        com = x0.mean(0)
+        best, params = np.inf, (1.0, 1.0, 0.0, 0.0, 0.0, 0.0)
+        for subset in np.random.choice(a=len(x0), size=(20, x0.shape[0] // 10), replace=True):
+            subset = np.unique(subset)
+            p, _ = self._affine_fit(x0[subset], x1[subset], com)
+            inl = np.linalg.norm(self._affine_apply(p, x0, com) - x1, axis=-1) <= 16
+            if np.sum(inl) / len(inl) >= 0.75:
+                p, fit = self._affine_fit(x0[inl], x1[inl], com)
+                if fit < best:
+                    best, params = fit, p
+        self.positions_px = self._affine_apply(params, x0, com)
+
     # ------------------------------------------------------- self-consistency A19
     def self_consistency_errors(self, max_batch_size=None):
         """ptychographic_methods.py:2227-2291: per-position sum (A - |F|)^2 of a
@@ -541,7 +597,8 @@ class Oracle:
                     fix_probe_aperture=False, constrain_probe_amplitude=False,
                     constrain_probe_amplitude_relative_radius=0.5,
                     constrain_probe_amplitude_relative_width=0.05, identical_slices=False,
-                    gaussian_filter_sigma=None, gaussian_filter=True):
+                    gaussian_filter_sigma=None, gaussian_filter=True,
+                    global_affine_transformation=False):
         """singleslice_ptychography.py:606-996 (and the multislice / mixed-state twins)."""
         projection = method != "GD"
         J = self.J
@@ -600,6 +657,8 @@ class Oracle:
             # phase_base_class.py:2179-2195 passes fix_positions_com and not fix_positions
             if not fix_positions and not (fix_positions_com and not fix_positions):
                 self.positions_com_constraint()
+            if not fix_positions and global_affine_transformation:
+                self.positions_affine_constraint()
             self.error_iterations.append(float(error))
         return self
 

@@ -300,6 +300,19 @@ def positions_com_constraint(st: DeviceState) -> None:
     st.positions -= st.positions.mean(0) - st.positions_initial.mean(0)
 
 
+def positions_affine_constraint(st: DeviceState, initial_positions: np.ndarray):
+    """positions <- the RANSAC affine map of the initial positions that best fits
+    them (ptychographic_constraints.py:1313-1350), fitted on the host from the
+    device positions (NumPy's global generator draws the subsets, between the
+    batch shuffles as in the reference); returns the transform."""
+    from .positions import affine_constraint
+
+    torch = _torch()
+    new, tf = affine_constraint(initial_positions, st.positions.cpu().numpy())
+    st.positions.copy_(torch.from_numpy(np.ascontiguousarray(new, dtype=np.float32)))
+    return tf
+
+
 def self_consistency_errors(st: DeviceState, max_batch: int) -> np.ndarray:
     """Per-position sum (A - |F|)^2 of a forward-only pass over the positions in
     natural order, batch by batch (ptychographic_methods.py:2227-2291); float32."""
@@ -492,6 +505,10 @@ class IterationDriver:
                              projection_abc=projection_abc,
                              position_correction=position_correction)
         self.positions_com = bool(position_correction and position_correction["center_of_mass"])
+        self.positions_affine = bool(position_correction and position_correction.get("affine"))
+        self.positions_initial_host = (st.positions_initial.cpu().numpy()
+                                       if self.positions_affine else None)
+        self.affine = None  # the last fitted AffineTransform
         self.shrinkage_rad = shrinkage_rad
         self.use_mask = use_mask
         self.pure_phase = pure_phase
@@ -579,6 +596,8 @@ class IterationDriver:
             probe_orthogonalization(st, on_device=self.device_orthogonalization)
         if self.positions_com:
             positions_com_constraint(st)
+        if self.positions_affine:
+            self.affine = positions_affine_constraint(st, self.positions_initial_host)
 
     def error(self) -> np.float32:
         """Normalised error of the last iteration: float32 sum over batches divided

@@ -462,7 +462,7 @@ class _PtychographyBase(PreprocessMixin):
                           constrain_probe_amplitude_relative_radius=0.5,
                           constrain_probe_amplitude_relative_width=0.05,
                           identical_slices=False, gaussian_filter_sigma=None,
-                          unsupported=None):
+                          global_affine_transformation=False, unsupported=None):
         self.set_device(device, clear_fft_cache)
         self._require_gpu()
         self._reset_reconstruction(store_iterations, reset)
@@ -506,7 +506,8 @@ class _PtychographyBase(PreprocessMixin):
                 max_total_px=self._distance_px(max_position_total_distance),
                 # the reference passes fix_positions_com and not fix_positions on
                 # (singleslice_ptychography.py:956, ptychographic_constraints.py:1355-1377)
-                center_of_mass=not fix_positions_com) if correct_positions else None))
+                center_of_mass=not fix_positions_com,
+                affine=global_affine_transformation) if correct_positions else None))
         # optional constraints: the initial probe's Fourier amplitude (mode 0) and the
         # soft top-hat of the amplitude constraint (ptychographic_constraints.py:920-957)
         aperture = amp_mask = None
@@ -605,6 +606,8 @@ class _PtychographyBase(PreprocessMixin):
         self._probe = st.probe.cpu().numpy().reshape(np.shape(self._probe))
         if correct_positions:
             self._positions_px = st.positions.cpu().numpy()
+            if driver.affine is not None:
+                self._tf = driver.affine
         self.object = self._object.copy()
         self.probe = self.probe_centered
         self.error = error.item()
@@ -815,8 +818,8 @@ class SingleslicePtychography(_PtychographyBase):
             constrain_probe_amplitude_relative_radius=constrain_probe_amplitude_relative_radius,
             constrain_probe_amplitude_relative_width=constrain_probe_amplitude_relative_width,
             gaussian_filter_sigma=gaussian_filter_sigma if gaussian_filter else None,
+            global_affine_transformation=global_affine_transformation and not fix_positions,
             unsupported=dict(
-                global_affine_transformation=global_affine_transformation and not fix_positions,
                 constrain_probe_fourier_amplitude=constrain_probe_fourier_amplitude
                 and not fix_probe,
                 fit_probe_aberrations=fit_probe_aberrations and not fix_probe,
@@ -952,8 +955,8 @@ class MixedstatePtychography(_PtychographyBase):
             constrain_probe_amplitude_relative_radius=constrain_probe_amplitude_relative_radius,
             constrain_probe_amplitude_relative_width=constrain_probe_amplitude_relative_width,
             gaussian_filter_sigma=gaussian_filter_sigma if gaussian_filter else None,
+            global_affine_transformation=global_affine_transformation and not fix_positions,
             unsupported=dict(
-                global_affine_transformation=global_affine_transformation and not fix_positions,
                 constrain_probe_fourier_amplitude=constrain_probe_fourier_amplitude
                 and not fix_probe,
                 fit_probe_aberrations=fit_probe_aberrations and not fix_probe,
@@ -1102,8 +1105,8 @@ class MultislicePtychography(_PtychographyBase):
             constrain_probe_amplitude_relative_width=constrain_probe_amplitude_relative_width,
             gaussian_filter_sigma=gaussian_filter_sigma if gaussian_filter else None,
             identical_slices=identical_slices,
+            global_affine_transformation=global_affine_transformation and not fix_positions,
             unsupported=dict(
-                global_affine_transformation=global_affine_transformation and not fix_positions,
                 constrain_probe_fourier_amplitude=constrain_probe_fourier_amplitude
                 and not fix_probe,
                 fit_probe_aberrations=fit_probe_aberrations and not fix_probe,
@@ -1274,8 +1277,8 @@ class MixedstateMultislicePtychography(_PtychographyBase):
             constrain_probe_amplitude_relative_width=constrain_probe_amplitude_relative_width,
             gaussian_filter_sigma=gaussian_filter_sigma if gaussian_filter else None,
             identical_slices=identical_slices,
+            global_affine_transformation=global_affine_transformation and not fix_positions,
             unsupported=dict(
-                global_affine_transformation=global_affine_transformation and not fix_positions,
                 constrain_probe_fourier_amplitude=constrain_probe_fourier_amplitude
                 and not fix_probe,
                 fit_probe_aberrations=fit_probe_aberrations and not fix_probe,

@@ -69,6 +69,16 @@ CASES = {
         rec=dict(num_iter=6, max_batch_size=36, step_size=0.5, seed_random=4,
                  fix_positions=False, fix_positions_com=False, positions_step_size=0.5,
                  max_position_update_distance=0.1, max_position_total_distance=0.3)),
+    # position correction with the global affine constraint (RANSAC on the global
+    # random generator, between the batch shuffles)
+    "ss_gd_poscorr_affine": dict(
+        gen=dict(name="ssf", seed=36, scan_shape=(12, 12), step_ang=0.5, jitter_ang=0.05,
+                 detector=64, object_px=96),
+        cls="single", ctor=dict(object_fov_ang=(24.0, 24.0)), guess=(96, 96),
+        perturb_ang=0.15,
+        rec=dict(num_iter=5, max_batch_size=36, step_size=0.5, seed_random=16,
+                 fix_positions=False, positions_step_size=0.5,
+                 global_affine_transformation=True)),
     "ms_gd_poscorr": dict(
         gen=dict(name="msc", seed=17, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
                  detector=64, object_px=96, num_slices=2, slice_thickness=20.0),
