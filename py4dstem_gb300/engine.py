@@ -570,8 +570,11 @@ class IterationDriver:
         # CUDA-graph replay of whole iterations: every kernel of an iteration in
         # one launch. Needs device-resident or page-locked amplitudes and, for
         # mixed states, the device eigen-decomposition (no host step inside).
+        # host steps inside an iteration (the eigh of the mode orthogonalisation,
+        # the affine fit of the positions) keep it out of a captured graph
         self.use_graph = bool(graph) and (st.amplitudes is not None or st.amp_mapped is not None) \
-            and (not self.orthogonalize or self.device_orthogonalization)
+            and (not self.orthogonalize or self.device_orthogonalization) \
+            and not self.positions_affine
 
     def _issue(self) -> None:
         st = self.st
