@@ -383,18 +383,6 @@ int ptycho_probe_overlap(const ptycho_geometry* geometry, const void* probe,
 int ptycho_mapped_host_pointer(const void* host, size_t bytes, void** device);
 
 /*
- * dst[k] = src[rows[k]] for k < num_rows: rows of row_bytes bytes (a non-zero
- * multiple of 16; src and dst 16-byte aligned), stream-ordered. With src the
- * device address of mapped host amplitudes (ptycho_mapped_host_pointer) and rows
- * a batch's slice of the position order, this is the per-batch copy_to_device
- * of the reference's storage="cpu" mode (singleslice_ptychography.py:873-875) as
- * one gather kernel; issued on a second stream one batch ahead, the transfer
- * overlaps the previous batch's computation.
- */
-int ptycho_gather_rows(const void* src, const int32_t* rows, int32_t num_rows, size_t row_bytes,
-                       void* dst, void* stream);
-
-/*
  * Creates, for batches issued on `stream`, the helper stream and events on which
  * the probe-side reductions of a batch run concurrently with the object side.
  * A batch call makes them on first use; call this for every stream before

@@ -81,7 +81,6 @@ _SIGNATURES = {
     "ptycho_probe_gram": ([ctypes.POINTER(Geometry), _vp, _vp, _vp], ctypes.c_int),
     "ptycho_probe_mix": ([ctypes.POINTER(Geometry), _vp, _vp, _vp, _vp], ctypes.c_int),
     "ptycho_probe_orthogonalize": ([ctypes.POINTER(Geometry), _vp, _vp, _sz, _vp], ctypes.c_int),
-    "ptycho_gather_rows": ([_vp, _vp, _i32, _sz, _vp, _vp], ctypes.c_int),
     "ptycho_prepare_stream": ([_vp], ctypes.c_int),
     "ptycho_mapped_host_pointer": ([_vp, _sz, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "ptycho_enable_kernel_timing": ([_i32], ctypes.c_int),

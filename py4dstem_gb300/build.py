@@ -24,7 +24,7 @@ SOURCES = ["ptycho_position_128.cu", "ptycho_position_96.cu", "ptycho_position_6
            "ptycho_position_96x128.cu", "ptycho_position_128x96.cu",
            "ptycho_position_48.cu", "ptycho_position_32.cu", "ptycho_gd128.cu",
            "ptycho_staged.cu", "ptycho_reduce.cu", "ptycho_preprocess.cu", "ptycho_volume.cu",
-           "ptycho_position.cu", "ptycho_gather.cu",
+           "ptycho_position.cu",
            "ptycho_capi.cu", "nn_conv.cu", "nn_unet.cu", "nn_data.cu"]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON_FLAGS = [

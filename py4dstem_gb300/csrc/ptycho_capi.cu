@@ -501,23 +501,6 @@ int ptycho_mapped_host_pointer(const void* host, size_t bytes, void** device) {
   return PTYCHO_OK;
 }
 
-int ptycho_gather_rows(const void* src, const int32_t* rows, int32_t num_rows, size_t row_bytes,
-                       void* dst, void* stream) {
-  if (num_rows < 0) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "num_rows must be >= 0");
-  if (num_rows == 0) return PTYCHO_OK;
-  if (!src || !rows || !dst)
-    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "src, rows and dst must be non-null");
-  if (row_bytes == 0 || row_bytes % 16 != 0 || reinterpret_cast<uintptr_t>(src) % 16 != 0 ||
-      reinterpret_cast<uintptr_t>(dst) % 16 != 0)
-    return fail(PTYCHO_ERR_INVALID_ARGUMENT,
-                "row_bytes (%zu) must be a non-zero multiple of 16 and src, dst 16-byte aligned",
-                row_bytes);
-  cudaError_t e = launch_gather_rows(src, rows, num_rows, row_bytes, dst,
-                                     static_cast<cudaStream_t>(stream));
-  if (e != cudaSuccess) return cuda_fail(e, "row gather kernel");
-  return PTYCHO_OK;
-}
-
 int ptycho_prepare_stream(void* stream) {
   cudaError_t e = prepare_stream(static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "helper stream");

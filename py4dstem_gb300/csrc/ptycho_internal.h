@@ -164,11 +164,6 @@ cudaError_t launch_staged_intensity(const BatchArgs& a, cudaStream_t s);
 cudaError_t launch_staged_probe_shift(const BatchArgs& a, cudaStream_t s);
 cudaError_t launch_staged_aperture(const BatchArgs& a, cudaStream_t s);
 
-// dst[k] = src[rows[k]] (rows of row_bytes, a multiple of 16, 16-byte aligned
-// bases): batch rows of host-mapped amplitudes into a device buffer (ptycho_gather.cu).
-cudaError_t launch_gather_rows(const void* src, const int32_t* rows, int num_rows,
-                               size_t row_bytes, void* dst, cudaStream_t s);
-
 // Preprocessing kernels (ptycho_preprocess.cu).
 cudaError_t launch_pattern_com(const float* in, int num, int Qx, int Qy, const void* mask,
                                int mask_mode, void* cx, void* cy, cudaStream_t s);

@@ -64,7 +64,6 @@ class DeviceState:
     amp_pinned: object = None     # two pinned host batch buffers (double-buffered)
     amp_events: object = None     # copy-done events of the pinned buffers
     amp_turn: int = 0
-    amp_prefetch: object = None   # mapped host amplitudes: device batch buffers, gather stream
     order_pinned: object = None   # two pinned host buffers for the per-iteration order
     order_events: object = None
     order_turn: int = 0
@@ -155,21 +154,10 @@ def create_state(*, roi_shape, object_array, probe_array, amplitudes, positions_
     order = torch.arange(pos.shape[0], dtype=torch.int32, device=dev)
     ws = torch.empty(ws_bytes + 256, dtype=torch.uint8, device=dev)
     err = torch.zeros(1, dtype=torch.float32, device=dev)
-    prefetch = None
-    if mapped is not None:
-        # page-locked host amplitudes: each batch's rows are gathered into one of
-        # two device buffers on a second stream, one batch ahead of the compute
-        prefetch = dict(
-            bufs=[torch.empty((max_batch,) + det_shape, dtype=torch.float32, device=dev)
-                  for _ in range(2)],
-            stream=torch.cuda.Stream(device=dev),
-            gathered=[torch.cuda.Event() for _ in range(2)],
-            released=[torch.cuda.Event() for _ in range(2)])
     st = DeviceState(geometry=geom, object=obj, probe=probe, amplitudes=amps_dev,
                      amplitudes_host=amps_host, positions=pos, order=order, workspace=ws,
                      workspace_bytes=ws_bytes, error_accum=err, max_batch=int(max_batch),
-                     amp_stage=amp_stage, amp_pinned=amp_pinned, amp_mapped=mapped,
-                     amp_prefetch=prefetch)
+                     amp_stage=amp_stage, amp_pinned=amp_pinned, amp_mapped=mapped)
     if propagators is not None:
         st.propagators = torch.from_numpy(
             np.ascontiguousarray(propagators, dtype=np.complex64)).to(dev)
@@ -269,30 +257,13 @@ def _batch_amplitudes(st: DeviceState, start: int, end: int, host_order: np.ndar
         return _ptr(st.amp_stage), None
 
 
-def _gather_batch(st: DeviceState, start: int, end: int, k: int) -> None:
-    """Rows order[start:end] of the mapped host amplitudes into prefetch buffer k
-    on the gather stream."""
-    pf = st.amp_prefetch
-    buf = pf["bufs"][k]
-    row_bytes = buf[0].numel() * 4
-    _native.check(_native.lib().ptycho_gather_rows(
-        ctypes.c_void_p(st.amp_mapped), ctypes.c_void_p(st.order.data_ptr() + 4 * start),
-        end - start, ctypes.c_size_t(row_bytes), _ptr(buf),
-        ctypes.c_void_p(pf["stream"].cuda_stream)))
-    st.launches += 1
-
-
 def run_batch(st: DeviceState, start: int, end: int, host_order: np.ndarray, *,
               projection=False, step_size=0.5, normalization_min=1.0, fix_probe=False,
-              projection_abc=(0.0, 0.0, 0.0), position_correction=None, amplitudes_ptr=None):
-    """amplitudes_ptr: this batch's amplitudes, already gathered in order (rows None)."""
+              projection_abc=(0.0, 0.0, 0.0), position_correction=None):
     lib = _native.lib()
     n = end - start
     rows_ptr = ctypes.c_void_p(st.order.data_ptr() + 4 * start)
-    if amplitudes_ptr is not None:
-        amps_ptr, amp_rows = amplitudes_ptr, None
-    else:
-        amps_ptr, amp_rows = _batch_amplitudes(st, start, end, host_order)
+    amps_ptr, amp_rows = _batch_amplitudes(st, start, end, host_order)
     g = ctypes.byref(st.geometry)
     props = _ptr(st.propagators)
     if projection:
@@ -410,15 +381,6 @@ def run_iteration(st: DeviceState, host_order: Optional[np.ndarray], max_batch: 
     fixed = bool(kw.get("fix_probe"))
     chain = not fixed and kw.get("position_correction") is None
     base = st.geometry.flags & ~(_native.FLAG_SPECTRUM_READY | _native.FLAG_PREPARE_SPECTRUM)
-    pf = st.amp_prefetch
-    if pf is not None:
-        # the gather stream starts after the order upload; it then runs one batch
-        # ahead, each buffer refilled once the batch that read it is done (events
-        # recorded in this iteration only, so a captured graph holds them all)
-        main = torch.cuda.current_stream()
-        pf["stream"].wait_stream(main)
-        _gather_batch(st, *batches[0], 0)
-        pf["gathered"][0].record(pf["stream"])
     try:
         for i, (start, end) in enumerate(batches):
             flags = base
@@ -427,18 +389,7 @@ def run_iteration(st: DeviceState, host_order: Optional[np.ndarray], max_batch: 
             if chain and i + 1 < len(batches):
                 flags |= _native.FLAG_PREPARE_SPECTRUM
             st.geometry.flags = flags
-            if pf is None:
-                run_batch(st, start, end, host_order, **kw)
-                continue
-            k = i % 2
-            main.wait_event(pf["gathered"][k])
-            run_batch(st, start, end, host_order, amplitudes_ptr=_ptr(pf["bufs"][k]), **kw)
-            pf["released"][k].record(main)
-            if i + 1 < len(batches):
-                if i >= 1:
-                    pf["stream"].wait_event(pf["released"][1 - k])
-                _gather_batch(st, *batches[i + 1], 1 - k)
-                pf["gathered"][1 - k].record(pf["stream"])
+            run_batch(st, start, end, host_order, **kw)
     finally:
         st.geometry.flags = base
     if kw.get("projection"):

@@ -112,8 +112,7 @@ def test_storage_cpu_matches_gpu(cuda):
 
 
 def test_storage_cpu_page_locked_matches_gpu(cuda):
-    """Host amplitudes in page-locked memory, gathered one batch ahead on a second
-    stream (ptycho_gather_rows), give the device-resident run's bits."""
+    """Host amplitudes in page-locked memory are read in place by the kernels."""
     torch = cuda
     from py4dstem_gb300 import engine
 
