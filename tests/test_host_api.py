@@ -73,7 +73,7 @@ def test_unsupported_options_raise_before_gpu():
     p = g.build(device="cpu")
     kw = dict(num_iter=1, device="gpu")
     with pytest.raises(NotImplementedError):
-        p.reconstruct(fix_positions=False, global_affine_transformation=True, **kw)
+        p.reconstruct(fit_probe_aberrations=True, **kw)
     with pytest.raises(NotImplementedError):
         p.reconstruct(q_lowpass=0.5, **kw)
 
