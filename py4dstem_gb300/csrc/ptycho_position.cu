@@ -9,7 +9,6 @@
 namespace pty {
 
 #define PTY_DECLARE_SIZE(S)                                                         \
-  cudaError_t launch_probe_spectrum_##S(const BatchArgs& a, cudaStream_t s);        \
   cudaError_t launch_position_kernel_##S(const BatchArgs& a, cudaStream_t s);       \
   cudaError_t launch_position_correction_##S(const BatchArgs& a, cudaStream_t s);   \
   cudaError_t launch_probe_inverse_##S(const BatchArgs& a, cudaStream_t s);         \
@@ -58,9 +57,12 @@ bool roi_supported(int Sx, int Sy) {
 
 // (the staged path has no position correction and no exact probe gradient:
 // the C ABI refuses both for 256 x 256 and resampled batches)
+// The probe spectrum of every ROI shape: two passes of line transforms over all
+// modes, many blocks each (ptycho_staged.cu), which also publish the twiddle
+// tables the fused kernels read. Same passes and twiddles as the fused kernels'
+// 2D transform, so the spectrum has the same bits as one block's would.
 cudaError_t launch_probe_spectrum(const BatchArgs& a, cudaStream_t s) {
-  if (staged_roi(a.Sx, a.Sy)) return launch_staged_spectrum(a, s);
-  PTY_DISPATCH(launch_probe_spectrum, a, s)
+  return launch_staged_spectrum(a, s);
 }
 
 cudaError_t launch_position_kernel(const BatchArgs& a, cudaStream_t s) {

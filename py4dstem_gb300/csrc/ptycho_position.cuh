@@ -85,26 +85,6 @@ __device__ __forceinline__ float block_sum(float v, float* red) {
   return t;  // valid in thread 0
 }
 
-template <int SX, int SY, int NT>
-__global__ void __launch_bounds__(NT, 1) probe_spectrum_kernel(BatchArgs a) {
-  using L = Layout<SX, SY>;
-  extern __shared__ float4 smem4[];
-  float2* buf = reinterpret_cast<float2*>(smem4);
-  float2* twx = buf + SX * L::LD;
-  float2* twy = twx + SX;
-  fill_twiddles<SX, NT>(twx);
-  fill_twiddles<SY, NT>(twy);
-  const float2* src = a.probe + (size_t)blockIdx.x * L::N;
-  for (int e = threadIdx.x; e < L::N; e += NT) buf[(e / SY) * L::LD + e % SY] = src[e];
-  __syncthreads();
-  if (blockIdx.x == 0) {  // publish the tables for the position kernel of this batch
-    for (int i = threadIdx.x; i < SX; i += NT) a.tw[i] = twx[i];
-    for (int i = threadIdx.x; i < SY; i += NT) a.tw[SX + i] = twy[i];
-  }
-  fft2d<SX, SY, NT, -1>(buf, twx, twy);
-  float2* dst = a.probe_spec + (size_t)blockIdx.x * L::N;
-  for (int e = threadIdx.x; e < L::N; e += NT) dst[e] = buf[(e / SY) * L::LD + e % SY];
-}
 
 // Everything of one scan position b (see the file header); the block's shared
 // memory holds the wave, the tables and the ramps. `red` is the block-sum scratch.
@@ -1072,18 +1052,6 @@ cudaError_t launch_probe_inverse_t(const BatchArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-template <int SX, int SY, int NT>
-cudaError_t launch_spectrum_t(const BatchArgs& a, cudaStream_t s) {
-  const size_t smem = Layout<SX, SY>::smem_bytes(false);
-  {
-    const cudaError_t e0 =
-        ensure_smem_limit(reinterpret_cast<const void*>(probe_spectrum_kernel<SX, SY, NT>),
-                          (int)Layout<SX, SY>::smem_bytes(true));
-    if (e0 != cudaSuccess) return e0;
-  }
-  probe_spectrum_kernel<SX, SY, NT><<<a.M, NT, smem, s>>>(a);
-  return cudaGetLastError();
-}
 
 template <int SX, int SY, int NT>
 cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
@@ -1130,9 +1098,6 @@ cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
 // translation unit per size).
 #define PTY_POSITION_INSTANCES_XY(SX, SY, NAME, NT)                                      \
   namespace pty {                                                                        \
-  cudaError_t launch_probe_spectrum_##NAME(const BatchArgs& a, cudaStream_t s) {         \
-    return launch_spectrum_t<SX, SY, NT>(a, s);                                          \
-  }                                                                                      \
   cudaError_t launch_position_kernel_##NAME(const BatchArgs& a, cudaStream_t s) {        \
     return launch_position_t<SX, SY, NT>(a, s);                                          \
   }                                                                                      \

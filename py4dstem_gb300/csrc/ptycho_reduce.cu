@@ -5,8 +5,8 @@
 // and the update lines of _gradient_descent_adjoint / _projection_sets_adjoint):
 //   object_reduce_kernel   one block per 16x16 object tile and slice. It lists, in
 //                          batch order, the positions whose patch touches the
-//                          tile; each warp sums every eighth list entry, a lane
-//                          an 8-sample row segment per entry, and the warp
+//                          tile; each warp sums every eighth list entry (a warp
+//                          load reads two whole staged tile rows), and the warp
 //                          partials are added in warp order (fixed, so the result
 //                          is deterministic); then the tile maximum of the
 //                          normaliser sums. Every staged value is read once.
@@ -91,26 +91,26 @@ __device__ __forceinline__ void mark_nonfinite(const BatchArgs& a, float2 v) {
 
 // ------------------------------------------------------------------ object side
 constexpr int kListChunk = 2048;
-constexpr int kSeg = 8;  // staged samples per lane and list entry (one row segment)
+constexpr int kRowsPerLane = 8;  // tile rows one lane visits per list entry (every other row)
 
 // One block (8 warps) per 16x16 object tile and slice. The block lists, in batch
 // order, the positions whose patch touches the tile (with the tile origin in
 // patch coordinates); warp w sums list entries w, w + 8, w + 16, ... For an
-// entry a lane reads one 8-sample segment of one staged row (lane pairs cover a
-// 16-sample row of the tile, the 16 pairs its 16 rows), so the index arithmetic
-// is paid once per segment and the reads of a warp are 128-byte rows. The eight
-// warp partials are then added in warp order for each pixel (a fixed order:
-// the result is deterministic), written as the object gradient and normaliser
-// sums, and the tile maximum of the normaliser is taken. Every staged value is
-// read once.
-__global__ void __launch_bounds__(NT) object_reduce_kernel(BatchArgs a) {
+// entry, lane l covers tile column l % 16 of rows l / 16, l / 16 + 2, ..., so
+// each warp load reads two whole 16-sample staged rows (two 128-byte lines of
+// the object term, two 64-byte ones of |P|^2) and the column arithmetic is paid
+// once per entry. The eight warp partials are then added in warp order for
+// each pixel (a fixed order: the result is deterministic), written as the
+// object gradient and normaliser sums, and the tile maximum of the normaliser
+// is taken. Every staged value is read once.
+__global__ void __launch_bounds__(NT, 4) object_reduce_kernel(BatchArgs a) {
   __shared__ int list[kListChunk];
   __shared__ int list_d[kListChunk];  // (dx << 16) | dy: tile origin in patch coordinates
   __shared__ int warp_count[NT / 32];
   __shared__ int warp_base[NT / 32 + 1];
   __shared__ float part[NT / 32][3][NT];  // per-warp partials (g.x, g.y, n) per tile pixel
   __shared__ float red[NT / 32];
-  static_assert(kTile * kTile == NT && kTile == 2 * kSeg, "tile layout");
+  static_assert(kTile * kTile == NT && kTile == 2 * kRowsPerLane, "tile layout");
   const int s = blockIdx.y;
   const int nty = (a.Py + kTile - 1) / kTile;
   const int tile = blockIdx.x;
@@ -128,12 +128,12 @@ __global__ void __launch_bounds__(NT) object_reduce_kernel(BatchArgs a) {
   const int Su = tr ? a.Sy : a.Sx, Sv = tr ? a.Sx : a.Sy;
   const int tu = tr ? th : tw, tv = tr ? tw : th;
   const int hu = Su / 2, hv = Sv / 2;  // fftfreq origin: patch sample k sits at (k + S/2) mod S
-  const int iu = lane >> 1;             // this lane's tile row (u)
-  const int iv0 = (lane & 1) * kSeg;    // and segment start (v)
+  const int iv = lane & (kTile - 1);   // this lane's tile column (v)
+  const int iu0 = lane >> 4;           // and first row (u); rows iu0, iu0 + 2, ...
 
-  float gx[kSeg], gy[kSeg], gn[kSeg];
+  float gx[kRowsPerLane], gy[kRowsPerLane], gn[kRowsPerLane];
 #pragma unroll
-  for (int k = 0; k < kSeg; ++k) gx[k] = gy[k] = gn[k] = 0.f;
+  for (int k = 0; k < kRowsPerLane; ++k) gx[k] = gy[k] = gn[k] = 0.f;
   const float2* __restrict__ st = a.st_obj + (size_t)s * a.B * N;
   const float* __restrict__ sn = a.st_nobj + (size_t)s * a.B * N;
   const int fminx = -(a.Sx / 2), fminy = -(a.Sy / 2);
@@ -173,47 +173,33 @@ __global__ void __launch_bounds__(NT) object_reduce_kernel(BatchArgs a) {
       const int d = list_d[l];
       const int du = tr ? (d & 0xffff) : (d >> 16);
       const int dv = tr ? (d >> 16) : (d & 0xffff);
-      // this lane's row: patch coordinate su (one object wrap at most)
-      int su = du + iu;
-      if (su >= Pu) su -= Pu;
-      if (iu >= tu || su >= Su) continue;
-      const int lu = su >= hu ? su - hu : su + hu;
-      const size_t row = (size_t)b * N + (size_t)lu * Sv;
-      const int raw = dv + iv0;
-      const int sv = raw >= Pv ? raw - Pv : raw;
-      const bool fast = iv0 + kSeg <= tv && (raw >= Pv || raw + kSeg - 1 < Pv) &&
-                        sv + kSeg <= Sv && !(sv < hv && sv + kSeg > hv);
-      if (fast) {
-        // 8 consecutive staged samples
-        const int lv = sv >= hv ? sv - hv : sv + hv;
-        float2 v[kSeg];
-        float w[kSeg];
+      // this lane's column: patch coordinate sv (one object wrap at most)
+      int sv = dv + iv;
+      if (sv >= Pv) sv -= Pv;
+      const bool vok = iv < tv && sv < Sv;
+      const int lv = sv >= hv ? sv - hv : sv + hv;
+      const size_t col = (size_t)b * N + lv;
+      float2 v[kRowsPerLane];
+      float w[kRowsPerLane];
 #pragma unroll
-        for (int k = 0; k < kSeg; ++k) {
-          v[k] = a.nobj_only ? make_float2(0.f, 0.f) : st[row + lv + k];
-          w[k] = sn[row + lv + k];
+      for (int k = 0; k < kRowsPerLane; ++k) {
+        const int iu = iu0 + 2 * k;
+        int su = du + iu;
+        if (su >= Pu) su -= Pu;
+        v[k] = make_float2(0.f, 0.f);
+        w[k] = 0.f;
+        if (vok && iu < tu && su < Su) {
+          const int lu = su >= hu ? su - hu : su + hu;
+          const size_t e = col + (size_t)lu * Sv;
+          if (!a.nobj_only) v[k] = st[e];
+          w[k] = sn[e];
         }
+      }
 #pragma unroll
-        for (int k = 0; k < kSeg; ++k) {
-          gx[k] += v[k].x;
-          gy[k] += v[k].y;
-          gn[k] += w[k];
-        }
-      } else {
-#pragma unroll
-        for (int k = 0; k < kSeg; ++k) {
-          int t = dv + iv0 + k;
-          if (t >= Pv) t -= Pv;
-          if (iv0 + k < tv && t < Sv) {
-            const int lv = t >= hv ? t - hv : t + hv;
-            if (!a.nobj_only) {
-              const float2 v = st[row + lv];
-              gx[k] += v.x;
-              gy[k] += v.y;
-            }
-            gn[k] += sn[row + lv];
-          }
-        }
+      for (int k = 0; k < kRowsPerLane; ++k) {
+        gx[k] += v[k].x;
+        gy[k] += v[k].y;
+        gn[k] += w[k];
       }
     }
     __syncthreads();  // the list is rewritten by the next chunk
@@ -221,8 +207,8 @@ __global__ void __launch_bounds__(NT) object_reduce_kernel(BatchArgs a) {
 
   // warp partials in warp order, per tile pixel (u-major index iu * 16 + iv)
 #pragma unroll
-  for (int k = 0; k < kSeg; ++k) {
-    const int t = iu * kTile + iv0 + k;
+  for (int k = 0; k < kRowsPerLane; ++k) {
+    const int t = (iu0 + 2 * k) * kTile + iv;
     part[warp][0][t] = gx[k];
     part[warp][1][t] = gy[k];
     part[warp][2][t] = gn[k];
@@ -320,13 +306,26 @@ __global__ void __launch_bounds__(NT) overlap_accumulate_kernel(BatchArgs a, flo
 }
 
 // ------------------------------------------------------------------- probe side
+constexpr int kProbeChunkMax = 1024;  // positions per chunk whose patch origins are staged
+
 __global__ void __launch_bounds__(NT) probe_reduce_kernel(BatchArgs a) {
+  __shared__ int2 origin[kProbeChunkMax];  // patch origins (pmod'ed) of this chunk's positions
   const int N = a.Sx * a.Sy;
   const int e = blockIdx.x * NT + threadIdx.x;
   const int c = blockIdx.y;
   const int per = (a.B + kProbeChunks - 1) / kProbeChunks;
   const int lo = c * per;
   const int hi = min(a.B, lo + per);
+  const bool staged_origins = a.nprobe_from_object && hi - lo <= kProbeChunkMax;
+  if (staged_origins) {
+    // the integer modulo of each position's patch origin once per block, not
+    // once per pixel and position
+    for (int i = threadIdx.x; i < hi - lo; i += NT) {
+      const int2 r = a.pos_round[lo + i];
+      origin[i] = make_int2(pmod(r.x - a.Sx / 2, a.Px), pmod(r.y - a.Sy / 2, a.Py));
+    }
+    __syncthreads();
+  }
   if (e >= N) return;
   const float2* __restrict__ sp = a.st_probe;
   const float* __restrict__ snp = a.st_nprobe;
@@ -345,11 +344,18 @@ __global__ void __launch_bounds__(NT) probe_reduce_kernel(BatchArgs a) {
     // |O|^2 of each position's patch at this probe pixel, gathered from the
     // object (the plain GD position kernel stages none)
     const int x = e / a.Sy, y = e % a.Sy;
+    const int xo = (x + a.Sx / 2) % a.Sx, yo = (y + a.Sy / 2) % a.Sy;
 #pragma unroll 4
     for (int b = lo; b < hi; ++b) {
-      const int2 r = a.pos_round[b];
-      int ox = pmod(r.x - a.Sx / 2, a.Px) + (x + a.Sx / 2) % a.Sx;
-      int oy = pmod(r.y - a.Sy / 2, a.Py) + (y + a.Sy / 2) % a.Sy;
+      int2 base;
+      if (staged_origins) {
+        base = origin[b - lo];
+      } else {
+        const int2 r = a.pos_round[b];
+        base = make_int2(pmod(r.x - a.Sx / 2, a.Px), pmod(r.y - a.Sy / 2, a.Py));
+      }
+      int ox = base.x + xo;
+      int oy = base.y + yo;
       if (ox >= a.Px) ox -= a.Px;
       if (oy >= a.Py) oy -= a.Py;
       const size_t idx = (size_t)ox * a.Py + oy;

@@ -139,25 +139,31 @@ __global__ void __launch_bounds__(kEwThreads) staged_shift_kernel(BatchArgs a,
 
 // One pass of 1D transforms of length L over 16 lines of wave blockIdx.x: rows
 // (ROWS, line l is elements l Sy .. l Sy + Sy - 1, L = Sy) or columns (line l is
-// elements l, l + Sy, ..., L = Sx); the results times `scale`.
+// elements l, l + Sy, ..., L = Sx), read from `src` and written, times `scale`,
+// to W (src may be W). Block (0, 0) also publishes its twiddle table to
+// tw_out when that is not null.
 template <int DIR, int L, bool ROWS>
-__global__ void __launch_bounds__(kLineThreads) staged_lines_kernel(float2* W, int N, int Sy,
-                                                                    float scale) {
+__global__ void __launch_bounds__(kLineThreads) staged_lines_kernel(const float2* src, float2* W,
+                                                                    int N, int Sy, float scale,
+                                                                    float2* tw_out) {
   constexpr int LD = L + 1;
   __shared__ float2 buf[kLines * LD];
   __shared__ float2 tw[L];
+  const float2* r = src + (size_t)blockIdx.x * N;
   float2* w = W + (size_t)blockIdx.x * N;
   const int l0 = blockIdx.y * kLines;
   fill_twiddles<L, kLineThreads>(tw);
+  if (tw_out && blockIdx.x == 0 && blockIdx.y == 0)
+    for (int i = threadIdx.x; i < L; i += kLineThreads) tw_out[i] = tw[i];
   if (ROWS) {
     for (int e = threadIdx.x; e < kLines * L; e += kLineThreads) {
       const int l = e / L, j = e % L;
-      buf[l * LD + j] = w[(size_t)(l0 + l) * Sy + j];
+      buf[l * LD + j] = r[(size_t)(l0 + l) * Sy + j];
     }
   } else {
     for (int e = threadIdx.x; e < kLines * L; e += kLineThreads) {
       const int j = e / kLines, l = e % kLines;
-      buf[l * LD + j] = w[(size_t)j * Sy + l0 + l];
+      buf[l * LD + j] = r[(size_t)j * Sy + l0 + l];
     }
   }
   __syncthreads();
@@ -176,33 +182,43 @@ __global__ void __launch_bounds__(kLineThreads) staged_lines_kernel(float2* W, i
 }
 
 template <int DIR, int L, bool ROWS>
-void lines_t(float2* W, int count, int Sx, int Sy, float scale, cudaStream_t s) {
+void lines_t(const float2* src, float2* W, int count, int Sx, int Sy, float scale,
+             float2* tw_out, cudaStream_t s) {
   const int nlines = ROWS ? Sx : Sy;
   staged_lines_kernel<DIR, L, ROWS><<<dim3(count, nlines / kLines), kLineThreads, 0, s>>>(
-      W, Sx * Sy, Sy, scale);
+      src, W, Sx * Sy, Sy, scale, tw_out);
 }
 
 template <int DIR, bool ROWS>
-cudaError_t lines(float2* W, int count, int L, int Sx, int Sy, float scale, cudaStream_t s) {
+cudaError_t lines(const float2* src, float2* W, int count, int L, int Sx, int Sy, float scale,
+                  float2* tw_out, cudaStream_t s) {
   switch (L) {
-    case 32: lines_t<DIR, 32, ROWS>(W, count, Sx, Sy, scale, s); break;
-    case 48: lines_t<DIR, 48, ROWS>(W, count, Sx, Sy, scale, s); break;
-    case 64: lines_t<DIR, 64, ROWS>(W, count, Sx, Sy, scale, s); break;
-    case 96: lines_t<DIR, 96, ROWS>(W, count, Sx, Sy, scale, s); break;
-    case 128: lines_t<DIR, 128, ROWS>(W, count, Sx, Sy, scale, s); break;
-    case 256: lines_t<DIR, 256, ROWS>(W, count, Sx, Sy, scale, s); break;
+    case 32: lines_t<DIR, 32, ROWS>(src, W, count, Sx, Sy, scale, tw_out, s); break;
+    case 48: lines_t<DIR, 48, ROWS>(src, W, count, Sx, Sy, scale, tw_out, s); break;
+    case 64: lines_t<DIR, 64, ROWS>(src, W, count, Sx, Sy, scale, tw_out, s); break;
+    case 96: lines_t<DIR, 96, ROWS>(src, W, count, Sx, Sy, scale, tw_out, s); break;
+    case 128: lines_t<DIR, 128, ROWS>(src, W, count, Sx, Sy, scale, tw_out, s); break;
+    case 256: lines_t<DIR, 256, ROWS>(src, W, count, Sx, Sy, scale, tw_out, s); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
 }
 
-// FFT2 (DIR -1) or unnormalised inverse (DIR +1) of `count` Sx x Sy waves in
-// place, times `scale`.
+// FFT2 (DIR -1) or unnormalised inverse (DIR +1) of `count` Sx x Sy waves, from
+// src (rows first, along y) into W, times `scale`; tw_out (or null) receives the
+// x table then the y table.
+template <int DIR>
+cudaError_t fft2_waves(const float2* src, float2* W, int count, int Sx, int Sy, float scale,
+                       float2* tw_out, cudaStream_t s) {
+  cudaError_t e = lines<DIR, true>(src, W, count, Sy, Sx, Sy, 1.0f,
+                                   tw_out ? tw_out + Sx : nullptr, s);
+  if (e != cudaSuccess) return e;
+  return lines<DIR, false>(W, W, count, Sx, Sx, Sy, scale, tw_out, s);
+}
+
 template <int DIR>
 cudaError_t fft2_waves(float2* W, int count, int Sx, int Sy, float scale, cudaStream_t s) {
-  cudaError_t e = lines<DIR, true>(W, count, Sy, Sx, Sy, 1.0f, s);
-  if (e != cudaSuccess) return e;
-  return lines<DIR, false>(W, count, Sx, Sx, Sy, scale, s);
+  return fft2_waves<DIR>(W, W, count, Sx, Sy, scale, nullptr, s);
 }
 
 // Slice s of the forward model: P_{s,m} = W_m / N (stashed), W_m = P_{s,m} O_s
@@ -538,9 +554,9 @@ bool staged_batch_supported(const BatchArgs& a) {
 }
 
 cudaError_t launch_staged_spectrum(const BatchArgs& a, cudaStream_t s) {
-  const size_t n = (size_t)a.M * a.Sx * a.Sy;
-  copy_waves_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a.probe, a.probe_spec, n);
-  return fft2_waves<-1>(a.probe_spec, a.M, a.Sx, a.Sy, 1.0f, s);
+  // FFT2 of every probe mode into the spectrum buffer, the x and y twiddle
+  // tables published for the fused position kernels
+  return fft2_waves<-1>(a.probe, a.probe_spec, a.M, a.Sx, a.Sy, 1.0f, a.tw, s);
 }
 
 cudaError_t launch_staged_positions(const BatchArgs& a, cudaStream_t s) {
