@@ -499,26 +499,29 @@ __global__ void __launch_bounds__(NT) masked_mean_partial_kernel(BatchArgs a, co
   }
 }
 
+// The masked mean's block partials summed in block order, once (one thread),
+// into red[2 kConstraintBlocks] and [2 kConstraintBlocks + 1].
+__global__ void masked_mean_final_kernel(BatchArgs a) {
+  double s = 0.0, c = 0.0;
+  const double* part = reinterpret_cast<const double*>(a.red);
+  for (int b = 0; b < kConstraintBlocks; ++b) {
+    s += part[2 * b];
+    c += part[2 * b + 1];
+  }
+  reinterpret_cast<double*>(a.red)[2 * kConstraintBlocks] = s;
+  reinterpret_cast<double*>(a.red)[2 * kConstraintBlocks + 1] = c;
+}
+
 __global__ void __launch_bounds__(NT) object_constraint_kernel(BatchArgs a, int use_mask,
                                                                  float shrinkage,
                                                                  int apply_shrinkage,
                                                                  int pure_phase,
                                                                  int positivity) {
-  __shared__ double ms[2];
-  if (threadIdx.x == 0) {
-    double s = 0.0, c = 0.0;
-    if (use_mask) {
-      for (int b = 0; b < kConstraintBlocks; ++b) {
-        s += reinterpret_cast<const double*>(a.red)[2 * b];
-        c += reinterpret_cast<const double*>(a.red)[2 * b + 1];
-      }
-    }
-    ms[0] = s;
-    ms[1] = c;
-  }
-  __syncthreads();
   float shrink = shrinkage;
-  if (use_mask) shrink = shrink + (float)(ms[0] / ms[1]);
+  if (use_mask) {
+    const double* ms = reinterpret_cast<const double*>(a.red) + 2 * kConstraintBlocks;
+    shrink = shrink + (float)(ms[0] / ms[1]);
+  }
   const size_t P = (size_t)a.Px * a.Py * a.T;
   const size_t i = (size_t)blockIdx.x * NT + threadIdx.x;
   if (i >= P) return;
@@ -546,12 +549,18 @@ __global__ void __launch_bounds__(NT) object_constraint_kernel(BatchArgs a, int 
   }
 }
 
-// Probe CoM of |P_0|^2 with corner-centred (fftfreq) coordinates; one block.
-__global__ void __launch_bounds__(NT) probe_com_kernel(BatchArgs a) {
+// Probe CoM of |P_0|^2 with corner-centred (fftfreq) coordinates, in float64:
+// kComBlocks blocks each sum a contiguous slice of the pixels (partials in
+// a.red), then one thread adds the partials in block order.
+constexpr int kComBlocks = 16;
+
+__global__ void __launch_bounds__(NT) probe_com_partial_kernel(BatchArgs a) {
   __shared__ double redd[NT / 32];
   const int N = a.Sx * a.Sy;
+  const int per = (N + kComBlocks - 1) / kComBlocks;
+  const int lo = blockIdx.x * per, hi = min(N, lo + per);
   double t = 0.0, sx = 0.0, sy = 0.0;
-  for (int e = threadIdx.x; e < N; e += NT) {
+  for (int e = lo + threadIdx.x; e < hi; e += NT) {
     const float2 p = a.probe[e];
     const float h = hypotf(p.x, p.y);
     const float v = h * h;
@@ -566,10 +575,24 @@ __global__ void __launch_bounds__(NT) probe_com_kernel(BatchArgs a) {
   const double tx = block_sum_all(sx, redd);
   const double ty = block_sum_all(sy, redd);
   if (threadIdx.x == 0) {
-    const double tf = (double)(float)tt;  // total intensity is a float32 sum
-    a.com[0] = tx / tf;
-    a.com[1] = ty / tf;
+    double* part = reinterpret_cast<double*>(a.red) + 3 * blockIdx.x;
+    part[0] = tt;
+    part[1] = tx;
+    part[2] = ty;
   }
+}
+
+__global__ void probe_com_final_kernel(BatchArgs a) {
+  const double* part = reinterpret_cast<const double*>(a.red);
+  double tt = 0.0, tx = 0.0, ty = 0.0;
+  for (int b = 0; b < kComBlocks; ++b) {
+    tt += part[3 * b];
+    tx += part[3 * b + 1];
+    ty += part[3 * b + 2];
+  }
+  const double tf = (double)(float)tt;  // total intensity is a float32 sum
+  a.com[0] = tx / tf;
+  a.com[1] = ty / tf;
 }
 
 template <int SX, int SY, int NTF>
@@ -1033,7 +1056,10 @@ cudaError_t launch_object_constraints(const BatchArgs& a, const uint8_t* mask, f
                                       int apply_shrinkage, int pure_phase, int positivity,
                                       cudaStream_t s) {
   const int use_mask = (apply_shrinkage && mask != nullptr) ? 1 : 0;
-  if (use_mask) masked_mean_partial_kernel<<<kConstraintBlocks, NT, 0, s>>>(a, mask);
+  if (use_mask) {
+    masked_mean_partial_kernel<<<kConstraintBlocks, NT, 0, s>>>(a, mask);
+    masked_mean_final_kernel<<<1, 1, 0, s>>>(a);
+  }
   const size_t P = (size_t)a.Px * a.Py * a.T;
   object_constraint_kernel<<<(unsigned)((P + NT - 1) / NT), NT, 0, s>>>(
       a, use_mask, shrinkage, apply_shrinkage, pure_phase, positivity);
@@ -1041,7 +1067,8 @@ cudaError_t launch_object_constraints(const BatchArgs& a, const uint8_t* mask, f
 }
 
 cudaError_t launch_probe_com(const BatchArgs& a, cudaStream_t s) {
-  probe_com_kernel<<<1, NT, 0, s>>>(a);
+  probe_com_partial_kernel<<<kComBlocks, NT, 0, s>>>(a);
+  probe_com_final_kernel<<<1, 1, 0, s>>>(a);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   switch (a.Sx * 4096 + a.Sy) {

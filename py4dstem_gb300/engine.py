@@ -405,14 +405,14 @@ def object_constraints(st: DeviceState, *, shrinkage_rad: float, use_mask: bool,
         ctypes.byref(st.geometry), _ptr(st.object), mask, float(shrinkage_rad),
         1 if apply_shrinkage else 0, 1 if pure_phase else 0, 1 if positivity else 0,
         _ws_ptr(st), st.workspace_bytes, _stream()))
-    st.launches += 2 if use_mask else 1
+    st.launches += 3 if use_mask else 1
 
 
 def probe_com_constraint(st: DeviceState) -> None:
     lib = _native.lib()
     _native.check(lib.ptycho_probe_com_constraint(
         ctypes.byref(st.geometry), _ptr(st.probe), _ws_ptr(st), st.workspace_bytes, _stream()))
-    st.launches += 2
+    st.launches += 3
 
 
 def probe_orthogonalization(st: DeviceState, on_device: bool = False) -> None:
