@@ -81,7 +81,7 @@ def parse_args(argv=None):
                          "16 mixed-state scans of uneven sizes in one graph-captured launch")
     ap.add_argument("--scans", type=int, default=16, help="multiscan: number of scans")
     ap.add_argument("--ms-batch", type=int, default=256, help="multiscan: max_batch_size")
-    ap.add_argument("--staged-batch", type=int, default=256, help="gd256: max_batch_size")
+    ap.add_argument("--staged-batch", type=int, default=128, help="gd256: max_batch_size")
     ap.add_argument("--li-scans", type=int, default=20000,
                     help="learned-init: training scans (128x128 positions each)")
     ap.add_argument("--li-epochs", type=int, default=8, help="learned-init: training epochs")
@@ -796,7 +796,7 @@ def run_variant(args):
                         both distance limits and the positions CoM constraint;
       mixed-multislice  a 64x64 scan through 4 slices with 2 probe modes, batch 256;
       gd256             gradient descent on a 256^2 detector (the staged batch-wide
-                        kernels): a 64x64 scan at 0.75 A, 512^2 object, batch 256
+                        kernels): a 64x64 scan at 0.75 A, 512^2 object, batch 128
                         (--staged-batch).
     value = position updates/s over K full iterations (device-resident amplitudes)."""
     rank, world, local = dist_env()

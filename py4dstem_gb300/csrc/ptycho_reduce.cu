@@ -499,17 +499,19 @@ __global__ void __launch_bounds__(NT) masked_mean_partial_kernel(BatchArgs a, co
   }
 }
 
-// The masked mean's block partials summed in block order, once (one thread),
-// into red[2 kConstraintBlocks] and [2 kConstraintBlocks + 1].
-__global__ void masked_mean_final_kernel(BatchArgs a) {
-  double s = 0.0, c = 0.0;
+// The masked mean's block partials added once, by one block in a fixed order
+// (thread b holds partial b; then the block's shuffle tree and warp order), into
+// red[2 kConstraintBlocks] and [2 kConstraintBlocks + 1].
+__global__ void __launch_bounds__(NT) masked_mean_final_kernel(BatchArgs a) {
+  static_assert(kConstraintBlocks == NT, "one partial per thread");
+  __shared__ double redd[NT / 32];
   const double* part = reinterpret_cast<const double*>(a.red);
-  for (int b = 0; b < kConstraintBlocks; ++b) {
-    s += part[2 * b];
-    c += part[2 * b + 1];
+  const double s = block_sum_all(part[2 * threadIdx.x], redd);
+  const double c = block_sum_all(part[2 * threadIdx.x + 1], redd);
+  if (threadIdx.x == 0) {
+    reinterpret_cast<double*>(a.red)[2 * kConstraintBlocks] = s;
+    reinterpret_cast<double*>(a.red)[2 * kConstraintBlocks + 1] = c;
   }
-  reinterpret_cast<double*>(a.red)[2 * kConstraintBlocks] = s;
-  reinterpret_cast<double*>(a.red)[2 * kConstraintBlocks + 1] = c;
 }
 
 __global__ void __launch_bounds__(NT) object_constraint_kernel(BatchArgs a, int use_mask,
@@ -1058,7 +1060,7 @@ cudaError_t launch_object_constraints(const BatchArgs& a, const uint8_t* mask, f
   const int use_mask = (apply_shrinkage && mask != nullptr) ? 1 : 0;
   if (use_mask) {
     masked_mean_partial_kernel<<<kConstraintBlocks, NT, 0, s>>>(a, mask);
-    masked_mean_final_kernel<<<1, 1, 0, s>>>(a);
+    masked_mean_final_kernel<<<1, NT, 0, s>>>(a);
   }
   const size_t P = (size_t)a.Px * a.Py * a.T;
   object_constraint_kernel<<<(unsigned)((P + NT - 1) / NT), NT, 0, s>>>(
