@@ -10,14 +10,11 @@ outside the probe aperture, so A*exp(i*angle(F)) takes a rounding-determined
 phase there; projection-set methods (RAAR here) are chaotic on small scans. We
 measure that floor by re-running the oracle with every FFT evaluated in
 complex128 and rounded back to complex64 (a different, correct float32 FFT).
-Gradient-descent fixtures must meet the benchmark spec's tolerance (error per
-iteration 1e-5 relative, object and probe 1e-4 relative L2) or 3x the measured
-floor, whichever is larger; projection-set fixtures 5x the floor. Fixtures
-with region_of_interest_shape take 10x the floor: linear interpolation of the
-complex far field onto a coarser detector grid makes near-zeros between samples
-of differing phase, where the projection follows the rounding of F, so a third
-float32 FFT (the GPU's) lands several floors from the reference. Each result's
-distance to the float64 evaluation of the same model is printed.
+Gradient-descent fixtures must meet the benchmark spec's tolerance outright (error
+per iteration 1e-5 relative, object and probe 1e-4 relative L2); the one whose
+measured floor is at that bar already (FLOOR_BOUND) takes 3x the floor.
+Projection-set fixtures take 5x the floor. Each result's distance to the
+float64 evaluation of the same model is printed.
 """
 
 import numpy as np
@@ -28,7 +25,14 @@ from oracle.ptycho_np import Oracle
 
 pytestmark = pytest.mark.gpu
 
-STRICT = {"ss_gd_32x32_det64"}
+# Gradient-descent fixtures meet the spec bar outright (error 1e-5 per
+# iteration, object and probe 1e-4), except where the reference's own rounding
+# floor is at that bar already: there 3x the floor.
+FLOOR_BOUND = {
+    # mixed state with position correction: the probe floor is 1.3e-4 (the
+    # reference moves by that much under another float32 FFT)
+    "mixed_gd_poscorr",
+}
 
 
 @pytest.mark.parametrize("name", names())
@@ -56,12 +60,10 @@ def test_reconstruction_matches_reference(cuda, name):
           f"probe {rel_l2(p._probe, o64.probe):.2e} | "
           f"ref-vs-fp64 obj {rel_l2(g.out['object'], o64.object):.2e}")
     k = 5.0 if g.projection else 3.0
-    if "region_of_interest_shape" in g.meta["preprocess"]:
-        k = 10.0
     tol_err = max(1e-5, k * f_err)
     tol_obj = max(1e-4, k * f_obj)
     tol_probe = max(1e-4, k * f_probe)
-    if name in STRICT:  # the CPU-runnable benchmark workload: spec numbers as stated
+    if not g.projection and name not in FLOOR_BOUND:  # the spec numbers as stated
         tol_err, tol_obj, tol_probe = 1e-5, 1e-4, 1e-4
     assert d_err <= tol_err
     if g.projection:
