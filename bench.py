@@ -371,6 +371,55 @@ def _run_oracle_batch(o, idx):
     o.adjoint(patches, shifted, pos, ew, 0.5, 1.0, False, False)
 
 
+def _ms_ref_batch(state):
+    """One gradient-descent batch of the mixed-state reference algorithm (float32
+    NumPy restatement) on one core: (positions, seconds)."""
+    for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[var] = "1"
+    from oracle.ptycho_np import Oracle, State
+
+    o = Oracle(State(**state))
+    idx = np.arange(o.J)
+    t0 = time.perf_counter()
+    _run_oracle_batch(o, idx)
+    return o.J, time.perf_counter() - t0
+
+
+def multiscan_cpu_baseline(scans, batch):
+    """The reference algorithm on the multi-scan workload: one batch of each scan
+    (its first `batch` positions in a seeded order), the scans in parallel in
+    single-threaded worker processes, one per host core as the scans allow;
+    positions/s = sampled positions / the slowest worker's time."""
+    import multiprocessing as mp
+
+    states = []
+    rng = np.random.default_rng(0)
+    for p in scans:
+        J = p._num_diffraction_patterns
+        idx = np.sort(rng.permutation(J)[:min(batch, J)])
+        amps = p._amplitudes_for_state()
+        amps = amps[idx].cpu().numpy() if hasattr(amps, "cpu") else np.asarray(amps)[idx]
+        states.append(dict(
+            amplitudes=np.ascontiguousarray(amps, dtype=np.float32),
+            positions_px=np.asarray(p._positions_px)[idx].astype(np.float32),
+            probe=np.array(p._probe), object=np.array(p._object),
+            mean_intensity=p._mean_diffraction_intensity,
+            fov_mask_inverse=p._object_fov_mask_inverse, num_probes=p._num_probes, mixed=True))
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    workers = max(1, min(cores, len(states)))
+    with mp.get_context("spawn").Pool(workers) as pool:
+        res = pool.map(_ms_ref_batch, states, chunksize=1)
+    n = sum(r[0] for r in res)
+    # a worker runs its scans one after another: the slowest worker's sum of times
+    per_worker = [0.0] * workers
+    for k, r in enumerate(res):
+        per_worker[k % workers] += r[1]
+    return {"value": n / max(per_worker), "unit": UNIT, "cores": workers, "kind": "port",
+            "sample": f"one batch of up to {batch} positions of each of the {len(states)} "
+                      f"scans (float32 NumPy restatement of the reference's mixed-state "
+                      f"gradient descent), {workers} single-threaded processes"}
+
+
 def bench_config(scan, batch, object_shape, world):
     return {"workload": WORKLOAD, "positions": scan * scan, "batch": min(batch, scan * scan),
             "detector": 128, "object": object_shape, "iterations_per_step": 1,
@@ -707,6 +756,8 @@ def run_multiscan(args):
              int(p._region_of_interest_shape[0])] for p in scans],
             "positions": J, "batch": args.ms_batch, "modes": 4, "iterations_per_step": 1},
         "sequential_value": J * args.steps / (ms_seq * 1e-3),
+        "cpu_baseline": None if args.no_cpu_baseline else multiscan_cpu_baseline(
+            scans, args.ms_batch),
         "tuning": {"choice": graph_run.tuning["choice"],
                    "timings_ms": [[c["concurrent"], t] for c, t in
                                   graph_run.tuning["timings_ms"]]},
