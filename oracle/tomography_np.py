@@ -178,7 +178,11 @@ class TomographyOracle:
     def reconstruct(self, num_iter=8, max_batch_size=None, seed_random=None, step_size=0.5,
                     normalization_min=1.0, fix_probe=False, object_positivity=True,
                     shrinkage_rad=0.0, collective_measurement_updates=True,
-                    detector_fourier_mask=None):
+                    detector_fourier_mask=None, gaussian_filter_sigma=None,
+                    gaussian_filter=True, sampling=None):
+        """gaussian_filter_sigma (A, with the real-space `sampling`): the volume's
+        3D Gaussian blur (ptychographic_constraints.py:119-151 inside the 3D
+        object constraints, :836-887), before shrinkage and positivity."""
         n_meas = len(self.tilt_matrices)
         total = int(self.cum[-1])
         if max_batch_size is not None:
@@ -187,6 +191,10 @@ class TomographyOracle:
             max_batch_size = total
 
         def constraints(vol):
+            if gaussian_filter and gaussian_filter_sigma is not None:
+                from scipy.ndimage import gaussian_filter as blur
+
+                vol = blur(vol, gaussian_filter_sigma / sampling[0])
             if shrinkage_rad > 0.0:
                 vol -= shrinkage_rad
             if object_positivity:

@@ -23,8 +23,15 @@ Per iteration, for each tilt in a shuffled order (ptychographic_tomography.py:
 What the reference computes and throws away is not computed: its per-tilt probe
 constraints return a new probe into a local name that is never stored
 (ptychographic_tomography.py:1139-1161), so the per-tilt probes carry the
-gradient updates only, here as there. Not implemented (they raise): projection
-sets, position correction, and the 3D Gaussian, Butterworth and TV filters.
+gradient updates only, here as there. The volume's 3D Gaussian blur runs among
+the object constraints (the object Gaussian kernels over the volume's Z
+slices). Not implemented (they raise): projection sets and position correction,
+which the reference's own tomography loop cannot run either (with projection
+sets its _forward call fails, "can't multiply sequence by non-int of type
+'float'", ptychographic_tomography.py:1065; position correction passes the
+forward's per-slice probe stack where the slice-0 probe is expected and fails
+to broadcast, :1097 into ptychographic_methods.py:2342), the 3D Butterworth
+filter (an FFT of the whole volume) and TV denoising (pylops).
 """
 
 from __future__ import annotations
@@ -100,6 +107,26 @@ class VolumeOps:
             _ptr(volume), _ptr(addend), ctypes.c_int64(volume.numel()), int(divisor),
             self._stream()))
         self.launches += 1
+
+    def gaussian(self, volume, sigma_px, roi):
+        """scipy.ndimage.gaussian_filter of the whole (Z, Px, Py) volume, every axis
+        (ptychographic_constraints.py:119-151 as the 3D object constraints call it,
+        :836-887): the object Gaussian kernels of the reconstruction over the
+        volume taken as Z slices."""
+        torch = engine._torch()
+        radius = int(4.0 * sigma_px + 0.5)
+        x = np.arange(-radius, radius + 1)
+        phi = np.exp(-0.5 / (sigma_px * sigma_px) * x ** 2)
+        w = torch.from_numpy(np.ascontiguousarray(phi / phi.sum())).to(volume.device)
+        if getattr(self, "gauss_scratch", None) is None:
+            self.gauss_scratch = torch.empty(4 * volume.numel(), dtype=torch.float32,
+                                             device=volume.device)
+        n0, n1, n2 = self.shape
+        g = _native.Geometry(int(roi[0]), int(roi[1]), n1, n2, n0, 1, 1, 0)
+        _native.check(self.lib.ptycho_object_gaussian_constraint(
+            ctypes.byref(g), _ptr(volume), _ptr(w), radius, 0, _ptr(self.gauss_scratch),
+            self._stream()))
+        self.launches += 3 if n0 > 1 else 2
 
     def constraints(self, volume, shrinkage_rad, positivity):
         shrink = shrinkage_rad > 0.0
@@ -486,7 +513,6 @@ class PtychographicTomography(_PtychographyBase):
             reconstruction_parameter_b, reconstruction_parameter_c, step_size)
         self._unsupported(
             projection_sets=use_projection, position_correction=not fix_positions,
-            gaussian_filter=gaussian_filter and gaussian_filter_sigma is not None,
             butterworth_filter=butterworth_filter and (q_lowpass is not None
                                                         or q_highpass is not None),
             tv_denoise=tv_denoise and tv_denoise_weights is not None,
@@ -553,6 +579,14 @@ class PtychographicTomography(_PtychographyBase):
                 mean_intensity=self._mean_diffraction_intensity[index], graph=False))
         sliced = base.object
         sliced_old = torch.empty_like(sliced)
+        blur_px = (gaussian_filter_sigma / self.sampling[0]
+                   if gaussian_filter and gaussian_filter_sigma is not None else None)
+
+        def volume_constraints():
+            # gaussian, then shrinkage and positivity (the 3D object constraints)
+            if blur_px is not None:
+                ops.gaussian(vol, blur_px, roi)
+            ops.constraints(vol, shrinkage_rad, object_positivity)
         collective = torch.empty_like(vol) if collective_measurement_updates else None
         self._device_states = states
 
@@ -578,12 +612,12 @@ class PtychographicTomography(_PtychographyBase):
                     ops.rotate(ops.update, collective, np.asarray(rot).T, 2)
                 else:
                     ops.expand(sliced, sliced_old, vol, 2)
-                    ops.constraints(vol, shrinkage_rad, object_positivity)
+                    volume_constraints()
                 old = rot
             ops.rotate(vol, vol, np.asarray(old).T, 0)
             if collective is not None:
                 ops.add_scaled(vol, collective, n_meas)
-                ops.constraints(vol, shrinkage_rad, object_positivity)
+                volume_constraints()
             # every tilt keeps its own error sum: one read-back per iteration.
             # float64 error as the reference forms it: float32 mean intensity
             # times the tilt's pattern count (an int64) is a float64

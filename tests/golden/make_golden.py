@@ -453,6 +453,14 @@ TOMO_CASES = {
         ctor=dict(num_slices=3, object_padding_px=(8, 8)),
         rec=dict(num_iter=3, max_batch_size=20, seed_random=5, step_size=0.5,
                  collective_measurement_updates=False, shrinkage_rad=1e-3)),
+    # the volume's 3D Gaussian blur among the object constraints
+    "tomo_gd_gaussian": dict(
+        seeds=(40, 41, 42), tilts_deg=(-10.0, 0.0, 12.0), guess_peak=0.03,
+        gen=dict(scan_shape=(8, 8), step_ang=0.5, jitter_ang=0.05, detector=48,
+                 object_px=64, num_slices=2, slice_thickness=10.0),
+        ctor=dict(num_slices=4, object_padding_px=(8, 8)),
+        rec=dict(num_iter=3, max_batch_size=16, seed_random=1, step_size=0.5,
+                 gaussian_filter_sigma=0.4)),
     "tomo_gd_zero_start": dict(
         seeds=(40, 41, 42), tilts_deg=(-10.0, 0.0, 12.0),
         gen=dict(scan_shape=(8, 8), step_ang=0.5, jitter_ang=0.05, detector=48,

@@ -131,7 +131,8 @@ def _distances(p_object, p_probes, p_errors, f):
     return np.array([d_err, d_obj, d_pr])
 
 
-@pytest.mark.parametrize("name", ["tomo_gd_collective", "tomo_gd_sequential"])
+@pytest.mark.parametrize("name", ["tomo_gd_collective", "tomo_gd_sequential",
+                                  "tomo_gd_gaussian"])
 def test_reconstruction_matches_reference(cuda, name):
     """From a smooth initial volume (well conditioned: a change of the float32
     FFT alone moves the reference's result by about 3e-7) the float32 kernels
