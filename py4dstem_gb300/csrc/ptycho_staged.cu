@@ -501,46 +501,81 @@ __global__ void __launch_bounds__(kEwThreads) staged_com_ramp_kernel(BatchArgs a
   }
 }
 
-// out[0] = sum |p|^2 over one wave (abs() then square), one 1024-thread block:
-// thread partials, then a fixed shuffle tree and warp order.
-__global__ void __launch_bounds__(1024) staged_power_kernel(const float2* p, int N, float* out) {
-  __shared__ float red[32];
+// The probe aperture constraint of mode 0 at 256 x 256 in one 512-thread block
+// (ptychographic_constraints.py:1004-1040): P <- IFFT2(A exp(i angle FFT2(P))),
+// rescaled to the power sum |P|^2 it had before. The transforms walk the wave in
+// global memory 16 lines at a time; the two power sums stay in the block, so
+// the call allocates nothing and concurrent calls do not share state.
+constexpr int kBlockThreads = 512;
+
+template <int DIR, bool ROWS>
+__device__ void block_lines_256(float2* w, float scale, float2* buf, const float2* tw) {
+  constexpr int L = 256, LD = L + 1;
+  for (int l0 = 0; l0 < L; l0 += kLines) {
+    for (int e = threadIdx.x; e < kLines * L; e += kBlockThreads) {
+      if (ROWS) {
+        const int l = e / L, j = e % L;
+        buf[l * LD + j] = w[(size_t)(l0 + l) * L + j];
+      } else {
+        const int j = e / kLines, l = e % kLines;
+        buf[l * LD + j] = w[(size_t)j * L + l0 + l];
+      }
+    }
+    __syncthreads();
+    Schedule<L>::template run<kLines, kBlockThreads, DIR>(buf, LD, 1, tw);
+    for (int e = threadIdx.x; e < kLines * L; e += kBlockThreads) {
+      if (ROWS) {
+        const int l = e / L, j = e % L;
+        w[(size_t)(l0 + l) * L + j] = c_scale(buf[l * LD + j], scale);
+      } else {
+        const int j = e / kLines, l = e % kLines;
+        w[(size_t)j * L + l0 + l] = c_scale(buf[l * LD + j], scale);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// sum |p|^2 (abs() then square): thread partials, a fixed shuffle tree, warp order
+__device__ float block_power_256(const float2* p, float* red) {
   float part = 0.0f;
-  for (int e = threadIdx.x; e < N; e += 1024) {
+  for (int e = threadIdx.x; e < 256 * 256; e += kBlockThreads) {
     const float2 v = p[e];
     const float av = hypotf(v.x, v.y);
     part += av * av;
   }
-  const float t = block_sum<1024>(part, red);
-  if (threadIdx.x == 0) *out = t;
+  const float t = block_sum<kBlockThreads>(part, red);
+  __syncthreads();
+  if (threadIdx.x == 0) red[0] = t;
+  __syncthreads();
+  const float r = red[0];
+  __syncthreads();
+  return r;
 }
 
-// F <- aperture . exp(i angle F)
-__global__ void __launch_bounds__(kEwThreads) staged_aperture_kernel(float2* F, int N,
-                                                                     const float* aperture) {
-  const int e0 = blockIdx.y * kChunk + threadIdx.x;
-#pragma unroll
-  for (int i = 0; i < kPer; ++i) {
-    const int e = e0 + i * kEwThreads;
-    if (e >= N) break;
-    const float2 f = F[e];
+__global__ void __launch_bounds__(kBlockThreads) staged_aperture_block_kernel(
+    float2* p, const float* __restrict__ aperture) {
+  constexpr int N = 256 * 256;
+  __shared__ float2 buf[kLines * 257];
+  __shared__ float2 tw[256];
+  __shared__ float red[kBlockThreads / 32];
+  fill_twiddles<256, kBlockThreads>(tw);
+  const float s0 = block_power_256(p, red);  // (its barriers also cover the tables)
+  block_lines_256<-1, true>(p, 1.0f, buf, tw);
+  block_lines_256<-1, false>(p, 1.0f, buf, tw);
+  for (int e = threadIdx.x; e < N; e += kBlockThreads) {
+    const float2 f = p[e];
     float sn, cs;
     sincosf(atan2f(f.y, f.x), &sn, &cs);
     const float ap = aperture[e];
-    F[e] = make_float2(cs * ap, sn * ap);
+    p[e] = make_float2(cs * ap, sn * ap);
   }
-}
-
-// p *= sqrt(pw[0] / pw[1])
-__global__ void __launch_bounds__(kEwThreads) staged_rescale_kernel(float2* p, int N,
-                                                                    const float* pw) {
-  const float k = sqrtf(pw[0] / pw[1]);
-  const int e0 = blockIdx.y * kChunk + threadIdx.x;
-#pragma unroll
-  for (int i = 0; i < kPer; ++i) {
-    const int e = e0 + i * kEwThreads;
-    if (e < N) p[e] = c_scale(p[e], k);
-  }
+  __syncthreads();
+  block_lines_256<+1, true>(p, 1.0f, buf, tw);
+  block_lines_256<+1, false>(p, 1.0f / (float)N, buf, tw);
+  const float s1 = block_power_256(p, red);
+  const float k = sqrtf(s0 / s1);
+  for (int e = threadIdx.x; e < N; e += kBlockThreads) p[e] = c_scale(p[e], k);
 }
 
 }  // namespace
@@ -635,24 +670,9 @@ cudaError_t launch_staged_probe_shift(const BatchArgs& a, cudaStream_t s) {
 }
 
 cudaError_t launch_staged_aperture(const BatchArgs& a, cudaStream_t s) {
-  // mode 0 in place; its power before and after in two stream-ordered floats
-  const int N = a.Sx * a.Sy;
-  float* pw = nullptr;
-  cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&pw), 2 * sizeof(float), s);
-  if (e != cudaSuccess) return e;
-  float2* p = a.probe;
-  const dim3 one(1, chunks_of(N));
-  staged_power_kernel<<<1, 1024, 0, s>>>(p, N, pw);
-  if ((e = fft2_waves<-1>(p, 1, a.Sx, a.Sy, 1.0f, s)) == cudaSuccess) {
-    staged_aperture_kernel<<<one, kEwThreads, 0, s>>>(p, N, a.aperture);
-    if ((e = fft2_waves<+1>(p, 1, a.Sx, a.Sy, 1.0f / (float)N, s)) == cudaSuccess) {
-      staged_power_kernel<<<1, 1024, 0, s>>>(p, N, pw + 1);
-      staged_rescale_kernel<<<one, kEwThreads, 0, s>>>(p, N, pw);
-      e = cudaGetLastError();
-    }
-  }
-  const cudaError_t f = cudaFreeAsync(pw, s);
-  return e != cudaSuccess ? e : f;
+  if (a.Sx != 256 || a.Sy != 256) return cudaErrorInvalidValue;
+  staged_aperture_block_kernel<<<1, kBlockThreads, 0, s>>>(a.probe, a.aperture);
+  return cudaGetLastError();
 }
 
 }  // namespace pty
