@@ -112,9 +112,16 @@ __global__ void __launch_bounds__(NT, 4) object_reduce_kernel(BatchArgs a) {
   __shared__ float red[NT / 32];
   static_assert(kTile * kTile == NT && kTile == 2 * kRowsPerLane, "tile layout");
   const int s = blockIdx.y;
+  const int ntx = (a.Px + kTile - 1) / kTile;
   const int nty = (a.Py + kTile - 1) / kTile;
-  const int tile = blockIdx.x;
-  const int tx0 = (tile / nty) * kTile;
+  // tile rows from the middle outwards (16, 15, 17, 14, ...): the scan sits in
+  // the middle of the object, so the tiles with the longest lists start first
+  // and the short ones at the edges fill the end of the launch
+  const int k = blockIdx.x / nty;
+  const int mid = ntx / 2;
+  const int trow = (k & 1) ? mid - ((k + 1) >> 1) : mid + (k >> 1);
+  const int tile = trow * nty + blockIdx.x % nty;
+  const int tx0 = trow * kTile;
   const int ty0 = (tile % nty) * kTile;
   const int tw = min(kTile, a.Px - tx0);
   const int th = min(kTile, a.Py - ty0);
