@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define PTYCHO_ABI_VERSION 3
+#define PTYCHO_ABI_VERSION 4
 
 enum ptycho_status {
   PTYCHO_OK = 0,
@@ -381,6 +381,22 @@ int ptycho_probe_overlap(const ptycho_geometry* geometry, const void* probe,
  * singleslice_ptychography.py:873-875).
  */
 int ptycho_mapped_host_pointer(const void* host, size_t bytes, void** device);
+
+/*
+ * out[i, :] = patterns[rows[i], :] for i < num_out (rows NULL: row i), each
+ * pattern pattern_size float32 values; rows is a device array. The per-batch
+ * copy of host-resident amplitudes to the device (copy_to_device(
+ * self._amplitudes[batch_indices]) in reconstruct,
+ * singleslice_ptychography.py:873-875) as one device gather: `patterns` is
+ * device memory or the device address of page-locked host memory
+ * (ptycho_mapped_host_pointer), read over the CPU-GPU link. The kernel runs at
+ * the device's greatest stream priority, so that a gather issued on a second
+ * stream for the next batch overlaps the running batch. A row index outside
+ * [0, num_patterns) yields a pattern of NaN (the batch error is then
+ * non-finite), never an access outside `patterns`.
+ */
+int ptycho_gather_patterns(const float* patterns, int32_t num_patterns, int64_t pattern_size,
+                           const int32_t* rows, int32_t num_out, float* out, void* stream);
 
 /*
  * Creates, for batches issued on `stream`, the helper stream and events on which

@@ -83,6 +83,7 @@ _SIGNATURES = {
     "ptycho_probe_orthogonalize": ([ctypes.POINTER(Geometry), _vp, _vp, _sz, _vp], ctypes.c_int),
     "ptycho_prepare_stream": ([_vp], ctypes.c_int),
     "ptycho_mapped_host_pointer": ([_vp, _sz, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "ptycho_gather_patterns": ([_vp, _i32, ctypes.c_int64, _vp, _i32, _vp, _vp], ctypes.c_int),
     "ptycho_enable_kernel_timing": ([_i32], ctypes.c_int),
     "ptycho_kernel_timing": ([ctypes.POINTER(_f32), ctypes.POINTER(_i32)], ctypes.c_int),
     "ptycho_fp32_fma_probe": ([_i32, _i32, _vp, _vp], ctypes.c_int),

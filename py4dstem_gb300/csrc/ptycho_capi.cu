@@ -757,6 +757,22 @@ int ptycho_normalize_patterns(const float* intensities, int32_t qx, int32_t qy,
   return PTYCHO_OK;
 }
 
+int ptycho_gather_patterns(const float* patterns, int32_t num_patterns, int64_t pattern_size,
+                           const int32_t* rows, int32_t num_out, float* out, void* stream) {
+  if (num_out < 0 || num_patterns < 0 || pattern_size < 1 || pattern_size > (int64_t)1 << 28)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "bad counts (%d of %d patterns of %lld values)",
+                num_out, num_patterns, (long long)pattern_size);
+  if (num_out == 0) return PTYCHO_OK;
+  if (!patterns || !out) return fail(PTYCHO_ERR_INVALID_ARGUMENT, "null pointer argument");
+  if (!rows && num_out > num_patterns)
+    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "%d rows requested of %d patterns", num_out,
+                num_patterns);
+  cudaError_t e = launch_gather_patterns(patterns, rows, num_out, num_patterns,
+                                         (int)pattern_size, out, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "pattern gather kernel");
+  return PTYCHO_OK;
+}
+
 int ptycho_probe_overlap(const ptycho_geometry* g, const void* probe, const float* positions_px,
                          int32_t num_positions, int32_t max_batch, float* overlap,
                          void* workspace, size_t workspace_bytes, void* stream) {

@@ -173,6 +173,9 @@ cudaError_t launch_rotation_search(const void* nx, const void* ny, int R0, int R
 cudaError_t launch_pattern_normalize(const float* in, int Qx, int Qy, const int32_t* rows,
                                      int num_out, const float* cfx, const float* cfy,
                                      int crop_w, float* amps, float* sums, cudaStream_t s);
+// out[i] = src[rows[i]] (pattern_size floats each), at the greatest stream priority
+cudaError_t launch_gather_patterns(const float* src, const int32_t* rows, int n, int num_patterns,
+                                   int pattern_size, float* dst, cudaStream_t s);
 
 // ---- ptycho_volume.cu (tomography)
 cudaError_t launch_volume_rotate(const void* in, int in_is_double, void* out, int out_mode,

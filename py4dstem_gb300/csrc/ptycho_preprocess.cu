@@ -660,4 +660,99 @@ cudaError_t launch_pattern_normalize(const float* in, int Qx, int Qy, const int3
   return cudaGetLastError();
 }
 
+// ---- batch pattern gather
+//
+// out[i, :] = patterns[rows[i], :] for i < n (rows = null: row i). Serves the
+// host-resident amplitudes of a reconstruction: the source is page-locked host
+// memory mapped into the device address space, read at the CPU-GPU link's rate,
+// and the gather of batch k + 1 runs on a second stream while batch k computes.
+// A few blocks with 8 loads of 16 bytes in flight per thread keep the link busy;
+// they are launched at the device's greatest stream priority, so that they take
+// the SM slots that blocks of the running batch free instead of waiting behind
+// all of them. A row index outside [0, num_patterns) yields a row of NaN (the
+// batch error then reads non-finite) instead of an access outside the source.
+namespace {
+constexpr int kGatherThreads = 1024;
+constexpr int kGatherBlocks = 4;
+constexpr int kGatherRows = 2;  // rows per block step
+constexpr int kGatherCols = 4;  // vectors per row and thread in one step
+
+template <typename V>
+__device__ __forceinline__ V nan_value();
+template <>
+__device__ __forceinline__ float nan_value<float>() { return __int_as_float(0x7fc00000); }
+template <>
+__device__ __forceinline__ float4 nan_value<float4>() {
+  const float q = __int_as_float(0x7fc00000);
+  return make_float4(q, q, q, q);
+}
+
+template <typename V>
+__global__ void __launch_bounds__(kGatherThreads)
+    gather_rows_kernel(const V* __restrict__ src, const int32_t* __restrict__ rows, int n,
+                       int num_patterns, int row_len, V* __restrict__ dst) {
+  for (int r0 = blockIdx.x * kGatherRows; r0 < n; r0 += gridDim.x * kGatherRows) {
+    const V* sp[kGatherRows];
+#pragma unroll
+    for (int q = 0; q < kGatherRows; ++q) {
+      const int r = r0 + q;
+      const int sr = r < n ? (rows ? rows[r] : r) : -1;
+      sp[q] = (sr >= 0 && sr < num_patterns) ? src + (size_t)sr * row_len : nullptr;
+    }
+    for (int c0 = threadIdx.x; c0 < row_len; c0 += kGatherThreads * kGatherCols) {
+      V v[kGatherRows][kGatherCols];
+#pragma unroll
+      for (int q = 0; q < kGatherRows; ++q) {
+#pragma unroll
+        for (int k = 0; k < kGatherCols; ++k) {
+          const int c = c0 + k * kGatherThreads;
+          v[q][k] = (sp[q] && c < row_len) ? __ldg(sp[q] + c) : nan_value<V>();
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < kGatherRows; ++q) {
+        const int r = r0 + q;
+        if (r >= n) continue;
+        V* d = dst + (size_t)r * row_len;
+#pragma unroll
+        for (int k = 0; k < kGatherCols; ++k) {
+          const int c = c0 + k * kGatherThreads;
+          if (c < row_len) d[c] = v[q][k];
+        }
+      }
+    }
+  }
+}
+
+template <typename V>
+cudaError_t launch_gather(const V* src, const int32_t* rows, int n, int num_patterns, int row_len,
+                          V* dst, cudaStream_t s) {
+  int least = 0, greatest = 0;
+  cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  const int blocks = (n + kGatherRows - 1) / kGatherRows;
+  cfg.gridDim = dim3(blocks < kGatherBlocks ? blocks : kGatherBlocks);
+  cfg.blockDim = dim3(kGatherThreads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributePriority;
+  attr[0].val.priority = greatest;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, gather_rows_kernel<V>, src, rows, n, num_patterns, row_len, dst);
+}
+}  // namespace
+
+cudaError_t launch_gather_patterns(const float* src, const int32_t* rows, int n, int num_patterns,
+                                   int pattern_size, float* dst, cudaStream_t s) {
+  const bool vec = pattern_size % 4 == 0 && reinterpret_cast<uintptr_t>(src) % 16 == 0 &&
+                   reinterpret_cast<uintptr_t>(dst) % 16 == 0;
+  if (vec)
+    return launch_gather(reinterpret_cast<const float4*>(src), rows, n, num_patterns,
+                         pattern_size / 4, reinterpret_cast<float4*>(dst), s);
+  return launch_gather(src, rows, n, num_patterns, pattern_size, dst, s);
+}
+
 }  // namespace pty

@@ -60,6 +60,11 @@ class DeviceState:
     exit_waves: object = None
     exit_waves_valid: bool = False
     amp_mapped: Optional[int] = None  # device address of page-locked host amplitudes
+    amp_ring: object = None       # (2, max_batch, det) device batch buffers, filled one
+                                  # batch ahead from amp_mapped on the prefetch stream
+    ring_ready: object = None     # gather-done events of the two ring slots
+    ring_free: object = None      # last-reader-done events of the two ring slots
+    prefetch_stream: object = None
     amp_stage: object = None      # device batch buffer when streaming from the host
     amp_pinned: object = None     # two pinned host batch buffers (double-buffered)
     amp_events: object = None     # copy-done events of the pinned buffers
@@ -158,6 +163,16 @@ def create_state(*, roi_shape, object_array, probe_array, amplitudes, positions_
                      amplitudes_host=amps_host, positions=pos, order=order, workspace=ws,
                      workspace_bytes=ws_bytes, error_accum=err, max_batch=int(max_batch),
                      amp_stage=amp_stage, amp_pinned=amp_pinned, amp_mapped=mapped)
+    if mapped is not None:
+        # page-locked host amplitudes: each batch's patterns are gathered into a
+        # device slot one batch ahead, on a second stream, while the batch before
+        # it computes (the link's transfer hidden behind the batch instead of
+        # stalling the position kernels that would read the rows in place)
+        st.amp_ring = torch.empty((2, int(max_batch)) + det_shape, dtype=torch.float32,
+                                  device=dev)
+        st.ring_ready = [torch.cuda.Event(), torch.cuda.Event()]
+        st.ring_free = [torch.cuda.Event(), torch.cuda.Event()]
+        st.prefetch_stream = torch.cuda.Stream(device=dev)
     if propagators is not None:
         st.propagators = torch.from_numpy(
             np.ascontiguousarray(propagators, dtype=np.complex64)).to(dev)
@@ -257,13 +272,34 @@ def _batch_amplitudes(st: DeviceState, start: int, end: int, host_order: np.ndar
         return _ptr(st.amp_stage), None
 
 
+def _gather_batch(st: DeviceState, slot: int, start: int, end: int) -> None:
+    """On the prefetch stream, once ring slot `slot` is free: gather the patterns
+    of order[start:end] from the page-locked host amplitudes into the slot."""
+    lib = _native.lib()
+    ps = st.prefetch_stream
+    ps.wait_event(st.ring_free[slot])
+    J = int(st.amplitudes_host.shape[0])
+    size = int(np.prod(st.amplitudes_host.shape[1:]))
+    _native.check(lib.ptycho_gather_patterns(
+        ctypes.c_void_p(st.amp_mapped), J, size,
+        ctypes.c_void_p(st.order.data_ptr() + 4 * start), end - start,
+        ctypes.c_void_p(st.amp_ring[slot].data_ptr()), ctypes.c_void_p(ps.cuda_stream)))
+    st.ring_ready[slot].record(ps)
+    st.launches += 1
+
+
 def run_batch(st: DeviceState, start: int, end: int, host_order: np.ndarray, *,
               projection=False, step_size=0.5, normalization_min=1.0, fix_probe=False,
-              projection_abc=(0.0, 0.0, 0.0), position_correction=None):
+              projection_abc=(0.0, 0.0, 0.0), position_correction=None, amplitudes=None):
+    """amplitudes: (pointer, rows pointer) of the batch's patterns when the caller
+    staged them; else taken from the state."""
     lib = _native.lib()
     n = end - start
     rows_ptr = ctypes.c_void_p(st.order.data_ptr() + 4 * start)
-    amps_ptr, amp_rows = _batch_amplitudes(st, start, end, host_order)
+    if amplitudes is not None:
+        amps_ptr, amp_rows = amplitudes
+    else:
+        amps_ptr, amp_rows = _batch_amplitudes(st, start, end, host_order)
     g = ctypes.byref(st.geometry)
     props = _ptr(st.propagators)
     if projection:
@@ -357,12 +393,28 @@ def upload_order(st: DeviceState, host_order: np.ndarray) -> None:
     st.order_events[k] = ev
 
 
+def stage_first_batch(st: DeviceState, max_batch: int) -> None:
+    """Gather the first batch's patterns of the order in st.order into ring slot 0
+    on the prefetch stream, after everything issued so far on the current stream
+    (page-locked host amplitudes only). The transfer then runs while the host
+    prepares the iteration; the current stream waits for it (ring_ready[0])
+    before the iteration, which runs with first_staged=True."""
+    torch = _torch()
+    n = int(st.positions.shape[0])
+    start, end = next(iter(generate_batches(n, max_batch)))
+    st.prefetch_stream.wait_stream(torch.cuda.current_stream())
+    st.ring_free[0].record(st.prefetch_stream)
+    _gather_batch(st, 0, start, end)
+
+
 def run_iteration(st: DeviceState, host_order: Optional[np.ndarray], max_batch: int,
-                  **kw) -> None:
+                  first_staged: bool = False, **kw) -> None:
     """One pass over all positions in `host_order` (already shuffled), batch by batch.
     The batch errors accumulate into st.error_accum (float32 on the device).
     host_order=None uses the order already in st.order (no host transfer: the
-    form that a CUDA graph can capture; device-resident amplitudes only)."""
+    form that a CUDA graph can capture; device-resident or page-locked amplitudes).
+    first_staged: the first batch's patterns are already in ring slot 0
+    (stage_first_batch) and the current stream has waited for them."""
     torch = _torch()
     if host_order is None:
         if st.amplitudes is None and st.amp_mapped is None:
@@ -381,6 +433,15 @@ def run_iteration(st: DeviceState, host_order: Optional[np.ndarray], max_batch: 
     fixed = bool(kw.get("fix_probe"))
     chain = not fixed and kw.get("position_correction") is None
     base = st.geometry.flags & ~(_native.FLAG_SPECTRUM_READY | _native.FLAG_PREPARE_SPECTRUM)
+    ring = st.amp_ring is not None
+    if ring:
+        # both slots are free once everything issued so far on this stream is done
+        # (this also orders the gathers after the order upload)
+        cur = torch.cuda.current_stream()
+        for ev in st.ring_free:
+            ev.record(cur)
+        if not first_staged:
+            _gather_batch(st, 0, *batches[0])
     try:
         for i, (start, end) in enumerate(batches):
             flags = base
@@ -389,7 +450,17 @@ def run_iteration(st: DeviceState, host_order: Optional[np.ndarray], max_batch: 
             if chain and i + 1 < len(batches):
                 flags |= _native.FLAG_PREPARE_SPECTRUM
             st.geometry.flags = flags
-            run_batch(st, start, end, host_order, **kw)
+            amps = None
+            if ring:
+                slot = i & 1
+                if i + 1 < len(batches):
+                    _gather_batch(st, slot ^ 1, *batches[i + 1])
+                if i > 0 or not first_staged:
+                    cur.wait_event(st.ring_ready[slot])
+                amps = (ctypes.c_void_p(st.amp_ring[slot].data_ptr()), None)
+            run_batch(st, start, end, host_order, amplitudes=amps, **kw)
+            if ring:
+                st.ring_free[slot].record(cur)
     finally:
         st.geometry.flags = base
     if kw.get("projection"):
@@ -497,6 +568,7 @@ class IterationDriver:
         self.device_orthogonalization = bool(device_orthogonalization)
         self.graph = None
         self.calls = 0
+        self._prefetched = None  # the order whose first batch prefetch() staged
         self.max_batch = int(max_batch)
         if position_correction is not None and st.positions_initial is None:
             raise ValueError("position correction needs a state created with positions_initial")
@@ -527,18 +599,42 @@ class IterationDriver:
             and (not self.orthogonalize or self.device_orthogonalization) \
             and not self.positions_affine
 
-    def _issue(self) -> None:
+    def _issue(self, first_staged: bool = False) -> None:
         st = self.st
-        run_iteration(st, None, self.max_batch, **self.batch_kw)
+        run_iteration(st, None, self.max_batch, first_staged=first_staged, **self.batch_kw)
         self._constraints()
+
+    def prefetch(self, order: np.ndarray) -> None:
+        """Start the next iteration's transfers for `order`: the order upload and,
+        with page-locked host amplitudes, the first batch's pattern gather, so
+        that they overlap the host work before iterate(order)."""
+        st = self.st
+        if st.amp_ring is None or order is None:
+            return
+        upload_order(st, order)
+        stage_first_batch(st, self.max_batch)
+        self._prefetched = np.array(order, copy=True)
 
     def iterate(self, order: Optional[np.ndarray]) -> None:
         """One iteration; order=None takes the order already in st.order."""
         st = self.st
         self.calls += 1
+        ring = st.amp_ring is not None
+        staged = self._prefetched is not None and order is not None and \
+            np.array_equal(self._prefetched, order)
+        self._prefetched = None
+        if ring and order is not None and not staged:
+            # page-locked host amplitudes: the first batch is gathered ahead of
+            # the iteration, the others inside it one batch ahead
+            upload_order(st, order)
+            stage_first_batch(st, self.max_batch)
+            staged = True
+        if staged:
+            _torch().cuda.current_stream().wait_event(st.ring_ready[0])
         if self.use_graph and order is not None:
             torch = _torch()
-            upload_order(st, order)
+            if not ring:
+                upload_order(st, order)
             if self.graph is None and self.calls >= 2:
                 # the first iteration ran eagerly (library set-up for the stream);
                 # capture the second on a side stream, then replay it from now on
@@ -549,7 +645,7 @@ class IterationDriver:
                 g = torch.cuda.CUDAGraph()
                 before = st.launches
                 with torch.cuda.graph(g, stream=side):
-                    self._issue()
+                    self._issue(first_staged=ring)
                 torch.cuda.current_stream().wait_stream(side)
                 self.graph = g
                 self.graph_launches = st.launches - before
@@ -558,11 +654,14 @@ class IterationDriver:
                 self.graph.replay()
                 st.launches += self.graph_launches
             else:
-                self._issue()
+                self._issue(first_staged=ring)
             if self.batch_kw.get("projection"):
                 st.exit_waves_valid = True
             return
-        run_iteration(st, order, self.max_batch, **self.batch_kw)
+        if staged:
+            run_iteration(st, None, self.max_batch, first_staged=True, **self.batch_kw)
+        else:
+            run_iteration(st, order, self.max_batch, **self.batch_kw)
         self._constraints()
 
     def _constraints(self) -> None:

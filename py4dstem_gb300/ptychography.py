@@ -153,8 +153,9 @@ class _PtychographyBase(PreprocessMixin):
 
     def _set_device_amplitudes(self, amps):
         if self._storage == "cpu":
-            # host storage: one copy into page-locked memory, which the batch
-            # kernels read in place; the device copy is released
+            # host storage: one copy into page-locked memory, from which each
+            # batch's patterns are gathered to the device one batch ahead; the
+            # device copy is released
             import torch
 
             host = torch.empty(tuple(amps.shape), dtype=amps.dtype, pin_memory=True)
@@ -169,8 +170,9 @@ class _PtychographyBase(PreprocessMixin):
         """The amplitudes as create_state takes them: the device tensor when the
         preprocessing left one and storage is "gpu", else the host array. With
         storage "cpu" a pageable host array is moved once into page-locked memory
-        (kept for later calls), so the batch kernels read it in place instead of
-        staging every batch through a host-side gather."""
+        (kept for later calls), so that each batch's patterns are gathered to the
+        device over the CPU-GPU link, one batch ahead on a second stream, instead
+        of staging every batch through a host-side gather and copy."""
         dev = self.__dict__.get("_amplitudes_device")
         if dev is not None and self._storage == "gpu":
             return dev
@@ -487,7 +489,8 @@ class _PtychographyBase(PreprocessMixin):
 
         potential = self._object_type == "potential"
         obj = np.asarray(self._object, dtype=np.float32 if potential else np.complex64)
-        use_mask = bool(fix_potential_baseline and self._object_fov_mask_inverse.sum() > 0)
+        # (the reference's mask.sum() > 0, as a test for any set pixel)
+        use_mask = bool(fix_potential_baseline and self._object_fov_mask_inverse.any())
         amplitudes = self._amplitudes_for_state()
         if amplitudes is None:
             raise ValueError("no diffraction amplitudes: call preprocess() with a datacube first "
@@ -549,13 +552,9 @@ class _PtychographyBase(PreprocessMixin):
                detector_fourier_mask is not None, constraint_key,
                repr(sorted((k, repr(v)) for k, v in driver_kw.items())))
         cached = self.__dict__.get("_state_cache")
-        if cached is not None and cached[0] == key and cached[1] is amplitudes:
+        refresh = cached is not None and cached[0] == key and cached[1] is amplitudes
+        if refresh:
             st, driver = cached[2], cached[3]
-            engine.refresh_state(
-                st, object_array=obj, probe_array=self._probe, positions_px=self._positions_px,
-                detector_mask=detector_fourier_mask,
-                fov_mask_inverse=self._object_fov_mask_inverse if use_mask else None,
-                positions_initial=self._positions_px_initial if correct_positions else None)
         else:
             self.__dict__["_state_cache"] = None  # release the previous buffers first
             st = engine.create_state(
@@ -575,6 +574,18 @@ class _PtychographyBase(PreprocessMixin):
                                             probe_amplitude_mask=amp_mask, gaussian=gaussian,
                                             **driver_kw)
             self.__dict__["_state_cache"] = (key, amplitudes, st, driver)
+        if num_iter > 0 and not use_projection:
+            np.random.shuffle(shuffled)
+        if num_iter > 0:
+            # with host-resident amplitudes the first batch's patterns start
+            # crossing the CPU-GPU link now, while the host copies the arrays in
+            driver.prefetch(shuffled)
+        if refresh:
+            engine.refresh_state(
+                st, object_array=obj, probe_array=self._probe, positions_px=self._positions_px,
+                detector_mask=detector_fourier_mask,
+                fov_mask_inverse=self._object_fov_mask_inverse if use_mask else None,
+                positions_initial=self._positions_px_initial if correct_positions else None)
         if use_projection:
             if self._exit_waves is not None:
                 import torch
@@ -586,8 +597,6 @@ class _PtychographyBase(PreprocessMixin):
                 st.exit_waves_valid = False
         self._device_state = st
         error = np.float32(0.0)
-        if num_iter > 0 and not use_projection:
-            np.random.shuffle(shuffled)
         for it in range(num_iter):
             driver.iterate(shuffled)
             # the next iteration's shuffle (same global-RNG sequence as the
@@ -603,12 +612,12 @@ class _PtychographyBase(PreprocessMixin):
                                     axes=(-2, -1)))
 
         self._object = st.object.cpu().numpy()
+        self.object = st.object.cpu().numpy()  # a second transfer, not a host copy
         self._probe = st.probe.cpu().numpy().reshape(np.shape(self._probe))
         if correct_positions:
             self._positions_px = st.positions.cpu().numpy()
             if driver.affine is not None:
                 self._tf = driver.affine
-        self.object = self._object.copy()
         self.probe = self.probe_centered
         self.error = error.item()
         if use_projection:

@@ -114,7 +114,8 @@ def test_storage_cpu_matches_gpu(cuda):
 
 
 def test_storage_cpu_page_locked_matches_gpu(cuda):
-    """Host amplitudes in page-locked memory are read in place by the kernels."""
+    """Host amplitudes in page-locked memory, gathered to the device one batch
+    ahead: the same result bit for bit."""
     torch = cuda
     from py4dstem_gb300 import engine
 

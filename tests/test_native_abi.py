@@ -33,7 +33,7 @@ def test_exports_every_declared_symbol(lib):
 
 
 def test_abi_version(lib):
-    assert lib.ptycho_abi_version() == 3
+    assert lib.ptycho_abi_version() == 4
 
 
 @pytest.mark.parametrize("n,ok", [(32, 1), (48, 1), (64, 1), (96, 1), (128, 1), (80, 0),
@@ -267,3 +267,18 @@ def test_nonfinite_positions_rejected_on_the_host():
                             probe_array=np.ones((64, 64), np.complex64),
                             amplitudes=np.ones((4, 64, 64), np.float32), positions_px=pos,
                             num_slices=1, num_probes=1, potential=False, max_batch=4)
+
+
+def test_gather_patterns_argument_checks(lib):
+    """The batch gather refuses bad counts and null pointers before any device
+    work; an empty gather is a no-op."""
+    p = ctypes.c_void_p(0x1000)
+    assert lib.ptycho_gather_patterns(p, 4, 16, None, 0, p, None) == 0
+    assert lib.ptycho_gather_patterns(p, 4, 16, None, -1, p, None) == 1
+    assert lib.ptycho_gather_patterns(p, 4, 0, None, 2, p, None) == 1
+    assert lib.ptycho_gather_patterns(None, 4, 16, None, 2, p, None) == 1
+    assert b"null pointer" in lib.ptycho_last_error()
+    assert lib.ptycho_gather_patterns(p, 4, 16, None, 2, None, None) == 1
+    # without a row list the first num_out patterns are taken: there must be as many
+    assert lib.ptycho_gather_patterns(p, 4, 16, None, 5, p, None) == 1
+    assert b"5 rows requested of 4 patterns" in lib.ptycho_last_error()
