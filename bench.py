@@ -90,7 +90,9 @@ def parse_args(argv=None):
     ap.add_argument("--li-iterations", type=int, default=200,
                     help="learned-init: iterations of the plain run")
     ap.add_argument("--schedule", type=int, default=0,
-                    help="128^2 kernel schedule: 0 default, 1 shared-memory, 2 register")
+                    help="128^2 kernel schedule: 0 default (3), 1 shared-memory passes by "
+                         "the whole block, 2 register-resident, 3 shared-memory passes by "
+                         "groups of warps")
     return ap.parse_args(argv)
 
 
@@ -628,7 +630,8 @@ def run_ours(args):
     from py4dstem_gb300 import roofline as _rl
 
     bound_name, _ = _rl.bound(flops_pos, bytes_pos, fp32_peak or 77.0, hbm_peak)
-    kernel_name = ("gd128_kernel" if args.schedule == 2 else "position_kernel<128,128,1024,1>")
+    kernel_name = {1: "position_kernel<128,128,1024,1>", 2: "gd128_kernel"}.get(
+        args.schedule, "position_grouped_kernel<1024>")
     if bound_name == "hbm":
         roof = {"bound": "hbm", "achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": hbm_achieved / hbm_peak, "peak_source": hbm_source + ", of measured"}

@@ -507,8 +507,12 @@ int ptycho_gd_batch_noalloc(const ptycho_geometry* geometry, void* object, void*
  * Kernel schedule for the fused per-position kernel of a given ROI edge length:
  * 0 = library default, 1 = shared-memory Stockham passes (every ROI and
  * variant), 2 = register-resident four-step transform (128 x 128 single-slice
- * gradient descent only; other cases fall back to 1). Process-wide; results
- * agree between schedules to float32 rounding. Returns the previous setting.
+ * gradient descent only; other cases fall back to 1), 3 = shared-memory passes
+ * by groups of warps that each own 16 rows / columns, with block-wide barriers
+ * only between the axes of a transform (128 x 128 plain single-slice gradient
+ * descent; other cases fall back to 1). The default is 3 where it applies, else
+ * 1. Process-wide; results agree between schedules to float32 rounding.
+ * Returns the previous setting.
  * No reference counterpart (tuning knob of this library's autotuner).
  */
 int ptycho_set_kernel_schedule(int32_t roi, int32_t schedule);

@@ -271,19 +271,32 @@ __device__ __forceinline__ float2 cis_rounded(float phi) {
   return make_float2(__fadd_rn(c.hi, c.lo), __fadd_rn(s.hi, s.lo));
 }
 
+// Barriers a pass synchronises its threads with: the whole block, or a named
+// barrier of one group of warps that owns its lines alone (bar.sync id, n;
+// ids 1..15, id 0 being the block barrier).
+struct BlockSync {
+  __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+struct GroupSync {
+  int id, threads;
+  __device__ __forceinline__ void operator()() const {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+  }
+};
+
 // One Stockham pass over NLINES lines of length L with radix R; NS is the length
 // of the sub-transforms already completed. Lanes of a warp take consecutive
 // lines, so with a pitch of SY+1 rows (row pass) or unit-stride columns (column
-// pass) the 32 lanes touch 32 distinct banks pairs.
-template <int L, int R, int NS, int NLINES, int NT, int DIR>
+// pass) the 32 lanes touch 32 distinct banks pairs. The NT threads that own the
+// lines (thread index tid < NT among them) synchronise through `sync`.
+template <int L, int R, int NS, int NLINES, int NT, int DIR, typename Sync>
 __device__ __forceinline__ void line_pass(float2* buf, int line_stride, int elem_stride,
-                                          const float2* __restrict__ tw) {
+                                          const float2* __restrict__ tw, int tid, Sync sync) {
   constexpr int BF = L / R;            // butterflies per line
   constexpr int WORK = NLINES * BF;    // butterflies per pass
   constexpr int ITEMS = (WORK + NT - 1) / NT;
   static_assert(L % (NS * R) == 0, "invalid Stockham schedule");
   float2 v[ITEMS][R];
-  const int tid = threadIdx.x;
 #pragma unroll
   for (int it = 0; it < ITEMS; ++it) {
     const int w = tid + it * NT;
@@ -306,7 +319,7 @@ __device__ __forceinline__ void line_pass(float2* buf, int line_stride, int elem
       dft<R, DIR>(row);
     }
   }
-  __syncthreads();
+  sync();
 #pragma unroll
   for (int it = 0; it < ITEMS; ++it) {
     const int w = tid + it * NT;
@@ -320,68 +333,66 @@ __device__ __forceinline__ void line_pass(float2* buf, int line_stride, int elem
       for (int k = 0; k < R; ++k) p[(base + k * NS) * elem_stride] = v[it][k];
     }
   }
-  __syncthreads();
+  sync();
 }
 
 // Radix schedule per transform length: a compile-time list of passes.
+#define PTY_PASS(L, R, NS) line_pass<L, R, NS, NLINES, NT, DIR>(b, ls, es, tw, tid, sync)
+#define PTY_SCHEDULE_RUN                                                                  \
+  template <int NLINES, int NT, int DIR, typename Sync = BlockSync>                       \
+  __device__ static void run(float2* b, int ls, int es, const float2* tw, int tid,        \
+                             Sync sync = Sync())
 template <int L>
 struct Schedule;
 template <>
 struct Schedule<16> {
-  template <int NLINES, int NT, int DIR>
-  __device__ static void run(float2* b, int ls, int es, const float2* tw) {
-    line_pass<16, 16, 1, NLINES, NT, DIR>(b, ls, es, tw);
-  }
+  PTY_SCHEDULE_RUN { PTY_PASS(16, 16, 1); }
 };
 template <>
 struct Schedule<32> {
-  template <int NLINES, int NT, int DIR>
-  __device__ static void run(float2* b, int ls, int es, const float2* tw) {
-    line_pass<32, 8, 1, NLINES, NT, DIR>(b, ls, es, tw);
-    line_pass<32, 4, 8, NLINES, NT, DIR>(b, ls, es, tw);
+  PTY_SCHEDULE_RUN {
+    PTY_PASS(32, 8, 1);
+    PTY_PASS(32, 4, 8);
   }
 };
 template <>
 struct Schedule<48> {
-  template <int NLINES, int NT, int DIR>
-  __device__ static void run(float2* b, int ls, int es, const float2* tw) {
-    line_pass<48, 16, 1, NLINES, NT, DIR>(b, ls, es, tw);
-    line_pass<48, 3, 16, NLINES, NT, DIR>(b, ls, es, tw);
+  PTY_SCHEDULE_RUN {
+    PTY_PASS(48, 16, 1);
+    PTY_PASS(48, 3, 16);
   }
 };
 template <>
 struct Schedule<64> {
-  template <int NLINES, int NT, int DIR>
-  __device__ static void run(float2* b, int ls, int es, const float2* tw) {
-    line_pass<64, 8, 1, NLINES, NT, DIR>(b, ls, es, tw);
-    line_pass<64, 8, 8, NLINES, NT, DIR>(b, ls, es, tw);
+  PTY_SCHEDULE_RUN {
+    PTY_PASS(64, 8, 1);
+    PTY_PASS(64, 8, 8);
   }
 };
 template <>
 struct Schedule<96> {
-  template <int NLINES, int NT, int DIR>
-  __device__ static void run(float2* b, int ls, int es, const float2* tw) {
-    line_pass<96, 8, 1, NLINES, NT, DIR>(b, ls, es, tw);
-    line_pass<96, 4, 8, NLINES, NT, DIR>(b, ls, es, tw);
-    line_pass<96, 3, 32, NLINES, NT, DIR>(b, ls, es, tw);
+  PTY_SCHEDULE_RUN {
+    PTY_PASS(96, 8, 1);
+    PTY_PASS(96, 4, 8);
+    PTY_PASS(96, 3, 32);
   }
 };
 template <>
 struct Schedule<128> {
-  template <int NLINES, int NT, int DIR>
-  __device__ static void run(float2* b, int ls, int es, const float2* tw) {
-    line_pass<128, 16, 1, NLINES, NT, DIR>(b, ls, es, tw);
-    line_pass<128, 8, 16, NLINES, NT, DIR>(b, ls, es, tw);
+  PTY_SCHEDULE_RUN {
+    PTY_PASS(128, 16, 1);
+    PTY_PASS(128, 8, 16);
   }
 };
 template <>
 struct Schedule<256> {
-  template <int NLINES, int NT, int DIR>
-  __device__ static void run(float2* b, int ls, int es, const float2* tw) {
-    line_pass<256, 16, 1, NLINES, NT, DIR>(b, ls, es, tw);
-    line_pass<256, 16, 16, NLINES, NT, DIR>(b, ls, es, tw);
+  PTY_SCHEDULE_RUN {
+    PTY_PASS(256, 16, 1);
+    PTY_PASS(256, 16, 16);
   }
 };
+#undef PTY_SCHEDULE_RUN
+#undef PTY_PASS
 
 // Full 2D transform of the SX x SY block in shared memory (pitch SY + 1).
 // twx: table for length SX, twy: table for length SY.
@@ -389,9 +400,9 @@ template <int SX, int SY, int NT, int DIR>
 __device__ __forceinline__ void fft2d(float2* buf, const float2* twx, const float2* twy) {
   constexpr int LD = SY + 1;
   // rows: SX lines of length SY, contiguous
-  Schedule<SY>::template run<SX, NT, DIR>(buf, LD, 1, twy);
+  Schedule<SY>::template run<SX, NT, DIR>(buf, LD, 1, twy, threadIdx.x);
   // columns: SY lines of length SX, stride LD
-  Schedule<SX>::template run<SY, NT, DIR>(buf, 1, LD, twx);
+  Schedule<SX>::template run<SY, NT, DIR>(buf, 1, LD, twx, threadIdx.x);
 }
 
 }  // namespace pty

@@ -441,6 +441,8 @@ int set_schedule(int roi, int schedule) {
   return prev;
 }
 
+int get_schedule(int roi) { return roi == S ? g_schedule_128 : 0; }
+
 bool position_v2_eligible(const BatchArgs& a) {
   if (g_schedule_128 != 2) return false;
   return a.Sx == S && a.Sy == S && a.T == 1 && a.M == 1 && !a.projection && !a.mixed_formula &&

@@ -127,8 +127,10 @@ cudaError_t launch_object_gaussian(const BatchArgs& a, const double* w, int R, i
 cudaError_t launch_overlap_accumulate(const BatchArgs& a, float* overlap, cudaStream_t s);
 // Register-resident 128 x 128 single-slice GD kernel (ptycho_gd128.cu).
 // set_schedule stores the preferred schedule for a ROI edge (0 default,
-// 1 shared-memory passes, 2 register-resident) and returns the previous one.
+// 1 shared-memory passes, 2 register-resident, 3 shared-memory passes by groups
+// of warps) and returns the previous one; get_schedule reads it.
 int set_schedule(int roi, int schedule);
+int get_schedule(int roi);
 bool position_v2_eligible(const BatchArgs& a);
 cudaError_t launch_position_v2(const BatchArgs& a, cudaStream_t s);
 // Creates the helper stream and events that batches issued on s use (idempotent).

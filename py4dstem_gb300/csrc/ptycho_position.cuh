@@ -663,6 +663,194 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
   position_one<SX, SY, NT, kMode>(a, blockIdx.x, red);
 }
 
+// Plain single-slice gradient descent at 128 x 128 (the model of kMode 1) with
+// the block split into 8 groups of 4 warps. A group owns 16 rows in the
+// real-space phases and 16 columns in the Fourier-space phases; its elementwise
+// work and its share of each 2D transform (the same Stockham passes and
+// twiddles as fft2d, on its own lines) synchronise through a named barrier of
+// its 128 threads. A block-wide barrier is needed only where a transform turns
+// from one axis to the other: 4 per position instead of the 24 of the
+// block-wide schedule, and between them the groups drift apart in phase (one
+// loading from memory while another runs its passes). To need no extra turn,
+// the inverse transforms run columns then rows and the forward ones rows then
+// columns (fft2d: rows then columns both ways), so results agree with the
+// block-wide schedule to rounding, not bit for bit.
+//   real space (row group g):      x = 16 g + i,          y = t        (i < 16)
+//   Fourier space (column group g): x = t / 16 + 8 i,     y = 16 g + t % 16
+// for thread t < 128 of the group; both walks are bank-conflict free on the
+// pitch-129 wave and coalesced in global memory.
+template <int NT>
+__device__ __forceinline__ void position_grouped_128(const BatchArgs& a, const int b,
+                                                     float* red) {
+  constexpr int S = 128;
+  using L = Layout<S, S>;
+  constexpr int N = L::N;
+  constexpr int LD = L::LD;
+  constexpr int GT = 128;                // threads per group
+  constexpr int G = NT / GT;             // groups
+  constexpr int LINES = S / G;           // rows (columns) a group owns
+  constexpr int PER = LINES * S / GT;    // samples per thread
+  constexpr int CH = 8;                  // global loads in flight per thread
+  static_assert(NT == 1024 && LINES == 16 && PER == 16, "grouped 128 x 128 layout");
+  extern __shared__ float4 smem4[];
+  float2* buf = reinterpret_cast<float2*>(smem4);
+  float2* twx = buf + S * LD;
+  float2* twy = twx + S;
+  float2* rpx = twy + S;
+  float2* rpy = rpx + S;
+
+  const int tid = threadIdx.x;
+  const int g = tid / GT;
+  const int tg = tid % GT;
+  const GroupSync gsync{1 + g, GT};
+  const int prow = a.pos_rows ? a.pos_rows[b] : b;
+  const int arow = a.amp_rows ? a.amp_rows[b] : b;
+  const bool pos_ok = isfinite(a.positions[2 * prow]) && isfinite(a.positions[2 * prow + 1]);
+  const float posx = finite_or_zero(a.positions[2 * prow]);
+  const float posy = finite_or_zero(a.positions[2 * prow + 1]);
+  const float rx = rintf(posx);  // numpy.round: half to even
+  const float ry = rintf(posy);
+  const float dx = posx - rx;
+  const float dy = posy - ry;
+  const int x0 = (int)rx;
+  const int y0 = (int)ry;
+  const float invN = 1.0f / (float)N;
+  const float* amp = a.amplitudes + (size_t)arow * N;
+
+  for (int i = tid; i < S; i += NT) {
+    twx[i] = a.tw[i];
+    twy[i] = a.tw[S + i];
+    const float k = (float)fint(i, S) / (float)S;
+    rpx[i] = cis_rounded(__fmul_rn(__fmul_rn(-6.2831855f, k), dx));
+  }
+  for (int i = tid - S; i >= 0 && i < S; i += NT) {
+    const float k = (float)fint(i, S) / (float)S;
+    rpy[i] = cis_rounded(__fmul_rn(__fmul_rn(-6.2831855f, k), dy));
+  }
+  if (tid == 0) a.pos_round[b] = make_int2(x0, y0);
+  __syncthreads();
+
+  const int bx = pmod(x0 - S / 2, a.Px);
+  const int by = pmod(y0 - S / 2, a.Py);
+  auto obj_x = [&](int x) {
+    const int t = bx + (x + S / 2) % S;
+    return t >= a.Px ? t - a.Px : t;
+  };
+  auto obj_y = [&](int y) {
+    const int t = by + (y + S / 2) % S;
+    return t >= a.Py ? t - a.Py : t;
+  };
+  // sample i of this thread in either walk
+  const int ry0 = LINES * g;                // real space: rows ry0 + i, column tg
+  const int fx0 = tg / LINES;               // Fourier space: rows fx0 + 8 i,
+  const int fy = LINES * g + tg % LINES;    //   column fy
+  constexpr int FXS = GT / LINES;
+  float2* const rows_g = buf + ry0 * LD;    // the group's rows
+  float2* const cols_g = buf + LINES * g;   // the group's columns
+
+  // shifted probe: spectrum x ramps, inverse transform (columns, then rows)
+#pragma unroll 1  // (unrolled, the chunks' live values spill)
+  for (int c0 = 0; c0 < PER; c0 += CH) {
+    float2 sv[CH];
+#pragma unroll
+    for (int i = 0; i < CH; ++i) sv[i] = __ldg(a.probe_spec + (fx0 + FXS * (c0 + i)) * S + fy);
+#pragma unroll
+    for (int i = 0; i < CH; ++i) {
+      const int x = fx0 + FXS * (c0 + i);
+      buf[x * LD + fy] = c_mul(sv[i], c_mul(rpx[x], rpy[fy]));
+    }
+  }
+  gsync();
+  Schedule<S>::template run<LINES, GT, +1>(cols_g, 1, LD, twx, tg, gsync);
+  __syncthreads();
+  Schedule<S>::template run<LINES, GT, +1>(rows_g, LD, 1, twy, tg, gsync);
+
+  // psi = P O; P stashed for the adjoint
+  float2* pst = a.st_probe + (size_t)b * N;
+#pragma unroll 1  // (unrolled, the chunks' live values spill)
+  for (int c0 = 0; c0 < PER; c0 += CH) {
+    float2 ov[CH];
+#pragma unroll
+    for (int i = 0; i < CH; ++i) ov[i] = load_object(a, 0, obj_x(ry0 + c0 + i), obj_y(tg));
+#pragma unroll
+    for (int i = 0; i < CH; ++i) {
+      const int x = ry0 + c0 + i;
+      const float2 p = c_scale(buf[x * LD + tg], invN);
+      pst[x * S + tg] = p;
+      buf[x * LD + tg] = c_mul(p, ov[i]);
+    }
+  }
+  gsync();
+  // forward transform: rows, then columns
+  Schedule<S>::template run<LINES, GT, -1>(rows_g, LD, 1, twy, tg, gsync);
+  __syncthreads();
+  Schedule<S>::template run<LINES, GT, -1>(cols_g, 1, LD, twx, tg, gsync);
+
+  // A exp(i angle F) - F, one division per pixel
+  float err = 0.0f;
+#pragma unroll 1  // (unrolled, the chunks' live values spill)
+  for (int c0 = 0; c0 < PER; c0 += CH) {
+    float av[CH];
+#pragma unroll
+    for (int i = 0; i < CH; ++i) av[i] = __ldg(amp + (fx0 + FXS * (c0 + i)) * S + fy);
+#pragma unroll
+    for (int i = 0; i < CH; ++i) {
+      const int x = fx0 + FXS * (c0 + i);
+      const int e = x * S + fy;
+      const int idx = x * LD + fy;
+      float2 f = buf[idx];
+      const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
+      if (a.det_mask) f = c_scale(f, mk);
+      const float af = c_abs(f);
+      const float A = av[i];
+      const float d = A - af;
+      err += d * d;
+      const float q = af > 0.0f ? A / af : 0.0f;
+      float2 r = af > 0.0f ? make_float2(fmaf(f.x, q, -f.x), fmaf(f.y, q, -f.y))
+                           : c_sub(make_float2(A, 0.0f), f);
+      if (a.det_mask) r = c_scale(r, mk);
+      buf[idx] = r;
+    }
+  }
+  gsync();
+  // inverse transform: columns, then rows
+  Schedule<S>::template run<LINES, GT, +1>(cols_g, 1, LD, twx, tg, gsync);
+  __syncthreads();
+  Schedule<S>::template run<LINES, GT, +1>(rows_g, LD, 1, twy, tg, gsync);
+
+  // adjoint terms: conj(P) chi (or the potential's), |P|^2, conj(O) chi
+  float2* gobj = a.st_obj + (size_t)b * N;
+  float* nobj = a.st_nobj + (size_t)b * N;
+#pragma unroll 1  // (unrolled, the chunks' live values spill)
+  for (int c0 = 0; c0 < PER; c0 += CH) {
+    float2 ov[CH], pv[CH];
+#pragma unroll
+    for (int i = 0; i < CH; ++i) {
+      const int x = ry0 + c0 + i;
+      ov[i] = load_object(a, 0, obj_x(x), obj_y(tg));
+      pv[i] = pst[x * S + tg];
+    }
+#pragma unroll
+    for (int i = 0; i < CH; ++i) {
+      const int x = ry0 + c0 + i;
+      const int e = x * S + tg;
+      const float2 chi = c_scale(buf[x * LD + tg], invN);
+      gobj[e] = object_term(a.potential, ov[i], pv[i], chi);
+      nobj[e] = c_abs2(pv[i]);
+      pst[e] = c_conj_mul(ov[i], chi);
+    }
+  }
+  const float tot = block_sum<NT>(err, red);
+  if (tid == 0) a.err[b] = pos_ok ? tot : __int_as_float(0x7fc00000);
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT, 1) position_grouped_kernel(BatchArgs a) {
+  __shared__ float red[NT / 32];
+  position_grouped_128<NT>(a, blockIdx.x, red);
+}
+
+
 // Position correction of one batch (ptychographic_methods.py:2071-2225), run
 // after the batch's object update. One block per position:
 //   F0_m = FFT2(P_m O_old)        kept by the forward pass in scratch_f
@@ -1077,6 +1265,20 @@ cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
                    : !plain ? 0
                    : a.T == 1 ? (a.M == 1 && !a.mixed_formula ? 1 : 2)
                    : 3;
+  if constexpr (SX == 128 && SY == 128 && NT == 1024) {
+    // the default (0) and schedule 3: passes by groups of warps
+    const int schedule = get_schedule(128);
+    if (mode == 1 && (schedule == 0 || schedule == 3)) {
+      const void* fn = reinterpret_cast<const void*>(position_grouped_kernel<NT>);
+      const cudaError_t e0 = ensure_smem_limit(fn, (int)smem);
+      if (e0 != cudaSuccess) return e0;
+      timing_before(s);
+      position_grouped_kernel<NT><<<a.B, NT, smem, s>>>(a);
+      const cudaError_t e1 = cudaGetLastError();
+      timing_after(s);
+      return e1;
+    }
+  }
   timing_before(s);
   switch (mode) {
     case 1: position_kernel<SX, SY, NT, 1><<<a.B, NT, smem, s>>>(a); break;

@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(kLineThreads) staged_lines_kernel(const float2
     }
   }
   __syncthreads();
-  Schedule<L>::template run<kLines, kLineThreads, DIR>(buf, LD, 1, tw);
+  Schedule<L>::template run<kLines, kLineThreads, DIR>(buf, LD, 1, tw, threadIdx.x);
   if (ROWS) {
     for (int e = threadIdx.x; e < kLines * L; e += kLineThreads) {
       const int l = e / L, j = e % L;
@@ -522,7 +522,7 @@ __device__ void block_lines_256(float2* w, float scale, float2* buf, const float
       }
     }
     __syncthreads();
-    Schedule<L>::template run<kLines, kBlockThreads, DIR>(buf, LD, 1, tw);
+    Schedule<L>::template run<kLines, kBlockThreads, DIR>(buf, LD, 1, tw, threadIdx.x);
     for (int e = threadIdx.x; e < kLines * L; e += kBlockThreads) {
       if (ROWS) {
         const int l = e / L, j = e % L;

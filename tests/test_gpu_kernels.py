@@ -54,14 +54,40 @@ def test_register_resident_128_variants(cuda, potential, masked, fix_probe):
         lib.ptycho_set_kernel_schedule(128, 0)
 
 
+@pytest.mark.parametrize("potential,masked,fix_probe", [
+    (False, False, False), (True, False, False), (False, True, False), (False, False, True)])
+def test_grouped_128_variants(cuda, potential, masked, fix_probe):
+    """The 128^2 single-slice kernel with passes by groups of warps (schedule 3)
+    with each option, against the oracle and against the block-wide schedule."""
+    from py4dstem_gb300 import _native
+
+    lib = _native.lib()
+    st = make_state(S=128, J=20, potential=potential, seed=27)
+    mask = None
+    if masked:
+        mask = (np.random.default_rng(3).uniform(size=(128, 128)) > 0.05).astype(np.float32)
+    kw = dict(num_iter=2, max_batch_size=7, seed_random=5, detector_fourier_mask=mask,
+              fix_probe=fix_probe, **OFF)
+    try:
+        lib.ptycho_set_kernel_schedule(128, 3)
+        g = compare(st, 2e-5, 2e-5, 2e-5, **kw)
+        lib.ptycho_set_kernel_schedule(128, 1)
+        b = gpu_reconstruct(st, **kw)
+    finally:
+        lib.ptycho_set_kernel_schedule(128, 0)
+    assert rel(g[0], b[0]) < 2e-6
+    assert rel(g[1], b[1]) < 2e-6
+
+
 def test_both_128_schedules_agree_with_oracle(cuda):
-    """Shared-memory passes and the register-resident schedule at 128^2."""
+    """Shared-memory passes (block-wide and by groups of warps) and the
+    register-resident schedule at 128^2."""
     from py4dstem_gb300 import _native
 
     lib = _native.lib()
     st = make_state(S=128, J=16, seed=23)
     try:
-        for schedule in (1, 2):
+        for schedule in (1, 2, 3):
             lib.ptycho_set_kernel_schedule(128, schedule)
             compare(st, 2e-5, 2e-5, 2e-5, num_iter=1, max_batch_size=8, seed_random=4, **OFF)
     finally:

@@ -116,3 +116,33 @@ def test_prefetched_host_amplitudes_mixed_multislice_projection(cuda):
     np.testing.assert_array_equal(a[0], b[0])
     np.testing.assert_array_equal(a[1], b[1])
     assert a[2] == b[2]
+
+
+def test_grouped_kernel_amplitude_sources_agree(cuda):
+    """The 128^2 grouped schedule on device amplitudes and on page-locked host
+    rows that the kernel reads in place (the C ABI takes either): the same bits."""
+    from py4dstem_gb300 import _native, engine
+
+    lib = _native.lib()
+    state = make_state(S=128, J=12, seed=93)
+    pinned = _pinned(state.amplitudes)
+    try:
+        lib.ptycho_set_kernel_schedule(128, 3)
+        a = _run(state, state.amplitudes, "gpu", graph=False, iters=2, batch=5)
+        st = engine.create_state(
+            roi_shape=(128, 128), object_array=state.object, probe_array=state.probe,
+            amplitudes=pinned.numpy(), positions_px=state.positions_px, num_slices=1,
+            num_probes=1, potential=False, max_batch=5, storage="cpu")
+        st.amp_ring = None  # in-place reads of the mapped host rows
+        drv = engine.IterationDriver(st, max_batch=5, step_size=0.5, fix_probe_com=True,
+                                     mean_intensity=state.mean_intensity)
+        rng = np.random.default_rng(5)
+        errors = []
+        for _ in range(2):
+            drv.iterate(rng.permutation(12))
+            errors.append(float(drv.error()))
+    finally:
+        lib.ptycho_set_kernel_schedule(128, 0)
+    np.testing.assert_array_equal(a[0], st.object.cpu().numpy())
+    np.testing.assert_array_equal(a[1], st.probe.cpu().numpy())
+    assert a[2] == errors
