@@ -812,6 +812,7 @@ struct ForkJoin {
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr;
   cudaEvent_t join = nullptr;
+  cudaEvent_t gathered = nullptr;  // the probe side has read the object
 };
 std::mutex g_fork_mu;
 std::map<std::pair<int, cudaStream_t>, ForkJoin> g_fork;
@@ -830,6 +831,8 @@ cudaError_t fork_join_for(cudaStream_t s, ForkJoin& out) {
       return e;
     if ((e = cudaEventCreateWithFlags(&n.fork, cudaEventDisableTiming)) != cudaSuccess) return e;
     if ((e = cudaEventCreateWithFlags(&n.join, cudaEventDisableTiming)) != cudaSuccess) return e;
+    if ((e = cudaEventCreateWithFlags(&n.gathered, cudaEventDisableTiming)) != cudaSuccess)
+      return e;
     fj = n;
   }
   out = fj;
@@ -857,6 +860,10 @@ cudaError_t launch_reduce_and_update(const BatchArgs& a, cudaStream_t s) {
     const int N = a.Sx * a.Sy;
     const int nb = (N + NT - 1) / NT;
     probe_reduce_kernel<<<dim3(nb, kProbeChunks), NT, 0, fj.side>>>(a);
+    // gathering |O|^2 the probe reduction reads the object, which the object
+    // update below rewrites: the update waits for it
+    if (a.nprobe_from_object && (e = cudaEventRecord(fj.gathered, fj.side)) != cudaSuccess)
+      return e;
     probe_finalize_kernel<<<nb, NT, 0, fj.side>>>(a);
     probe_update_kernel<<<nb, NT, 0, fj.side>>>(a, nb);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -865,6 +872,9 @@ cudaError_t launch_reduce_and_update(const BatchArgs& a, cudaStream_t s) {
     if ((e = cudaEventRecord(fj.join, fj.side)) != cudaSuccess) return e;
   }
   object_reduce_kernel<<<dim3(ntiles, a.T), NT, 0, s>>>(a);
+  if (!a.fix_probe && a.nprobe_from_object &&
+      (e = cudaStreamWaitEvent(s, fj.gathered, 0)) != cudaSuccess)
+    return e;
   const size_t P = (size_t)a.Px * a.Py;
   object_update_kernel<<<dim3((unsigned)((P + NT - 1) / NT), a.T), NT, 0, s>>>(a, ntiles);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
