@@ -785,7 +785,9 @@ def run_multislice(args):
     import torch
 
     torch.cuda.set_device(local)
-    from py4dstem_gb300 import MultislicePtychography, engine, roofline, synthetic
+    from py4dstem_gb300 import MultislicePtychography, _native, engine, roofline, synthetic
+
+    _native.lib().ptycho_set_kernel_schedule(128, args.schedule)
 
     c = synthetic.multislice_case(seed=3, num_slices=8, scan=64, backend="torch",
                                   device=f"cuda:{local}", object_px=256)

@@ -679,7 +679,7 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
 //   Fourier space (column group g): x = t / 16 + 8 i,     y = 16 g + t % 16
 // for thread t < 128 of the group; both walks are bank-conflict free on the
 // pitch-129 wave and coalesced in global memory.
-template <int NT>
+template <int NT, bool kMultislice>
 __device__ __forceinline__ void position_grouped_128(const BatchArgs& a, const int b,
                                                      float* red) {
   constexpr int S = 128;
@@ -765,89 +765,187 @@ __device__ __forceinline__ void position_grouped_128(const BatchArgs& a, const i
   __syncthreads();
   Schedule<S>::template run<LINES, GT, +1>(rows_g, LD, 1, twy, tg, gsync);
 
-  // psi = P O; P stashed for the adjoint
-  float2* pst = a.st_probe + (size_t)b * N;
+  // the transforms of the group's lines: forward = rows then columns (real
+  // space in, Fourier space out), inverse = columns then rows
+  auto forward = [&]() {
+    Schedule<S>::template run<LINES, GT, -1>(rows_g, LD, 1, twy, tg, gsync);
+    __syncthreads();
+    Schedule<S>::template run<LINES, GT, -1>(cols_g, 1, LD, twx, tg, gsync);
+  };
+  auto inverse = [&]() {
+    Schedule<S>::template run<LINES, GT, +1>(cols_g, 1, LD, twx, tg, gsync);
+    __syncthreads();
+    Schedule<S>::template run<LINES, GT, +1>(rows_g, LD, 1, twy, tg, gsync);
+  };
+  // A exp(i angle F) - F on the group's columns, one division per pixel;
+  // returns this thread's share of sum (A - |F|)^2
+  auto project = [&]() {
+    float err = 0.0f;
 #pragma unroll 1  // (unrolled, the chunks' live values spill)
-  for (int c0 = 0; c0 < PER; c0 += CH) {
-    float2 ov[CH];
+    for (int c0 = 0; c0 < PER; c0 += CH) {
+      float av[CH];
 #pragma unroll
-    for (int i = 0; i < CH; ++i) ov[i] = load_object(a, 0, obj_x(ry0 + c0 + i), obj_y(tg));
+      for (int i = 0; i < CH; ++i) av[i] = __ldg(amp + (fx0 + FXS * (c0 + i)) * S + fy);
 #pragma unroll
-    for (int i = 0; i < CH; ++i) {
-      const int x = ry0 + c0 + i;
-      const float2 p = c_scale(buf[x * LD + tg], invN);
-      pst[x * S + tg] = p;
-      buf[x * LD + tg] = c_mul(p, ov[i]);
+      for (int i = 0; i < CH; ++i) {
+        const int x = fx0 + FXS * (c0 + i);
+        const int e = x * S + fy;
+        const int idx = x * LD + fy;
+        float2 f = buf[idx];
+        const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
+        if (a.det_mask) f = c_scale(f, mk);
+        const float af = c_abs(f);
+        const float A = av[i];
+        const float d = A - af;
+        err += d * d;
+        const float q = af > 0.0f ? A / af : 0.0f;
+        float2 r = af > 0.0f ? make_float2(fmaf(f.x, q, -f.x), fmaf(f.y, q, -f.y))
+                             : c_sub(make_float2(A, 0.0f), f);
+        if (a.det_mask) r = c_scale(r, mk);
+        buf[idx] = r;
+      }
     }
-  }
-  gsync();
-  // forward transform: rows, then columns
-  Schedule<S>::template run<LINES, GT, -1>(rows_g, LD, 1, twy, tg, gsync);
-  __syncthreads();
-  Schedule<S>::template run<LINES, GT, -1>(cols_g, 1, LD, twx, tg, gsync);
-
-  // A exp(i angle F) - F, one division per pixel
+    return err;
+  };
   float err = 0.0f;
-#pragma unroll 1  // (unrolled, the chunks' live values spill)
-  for (int c0 = 0; c0 < PER; c0 += CH) {
-    float av[CH];
-#pragma unroll
-    for (int i = 0; i < CH; ++i) av[i] = __ldg(amp + (fx0 + FXS * (c0 + i)) * S + fy);
-#pragma unroll
-    for (int i = 0; i < CH; ++i) {
-      const int x = fx0 + FXS * (c0 + i);
-      const int e = x * S + fy;
-      const int idx = x * LD + fy;
-      float2 f = buf[idx];
-      const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
-      if (a.det_mask) f = c_scale(f, mk);
-      const float af = c_abs(f);
-      const float A = av[i];
-      const float d = A - af;
-      err += d * d;
-      const float q = af > 0.0f ? A / af : 0.0f;
-      float2 r = af > 0.0f ? make_float2(fmaf(f.x, q, -f.x), fmaf(f.y, q, -f.y))
-                           : c_sub(make_float2(A, 0.0f), f);
-      if (a.det_mask) r = c_scale(r, mk);
-      buf[idx] = r;
-    }
-  }
-  gsync();
-  // inverse transform: columns, then rows
-  Schedule<S>::template run<LINES, GT, +1>(cols_g, 1, LD, twx, tg, gsync);
-  __syncthreads();
-  Schedule<S>::template run<LINES, GT, +1>(rows_g, LD, 1, twy, tg, gsync);
 
-  // adjoint terms: conj(P) chi (or the potential's), |P|^2, conj(O) chi
-  float2* gobj = a.st_obj + (size_t)b * N;
-  float* nobj = a.st_nobj + (size_t)b * N;
+  if constexpr (!kMultislice) {
+    // psi = P O; P stashed for the adjoint
+    float2* pst = a.st_probe + (size_t)b * N;
 #pragma unroll 1  // (unrolled, the chunks' live values spill)
-  for (int c0 = 0; c0 < PER; c0 += CH) {
-    float2 ov[CH], pv[CH];
+    for (int c0 = 0; c0 < PER; c0 += CH) {
+      float2 ov[CH];
 #pragma unroll
-    for (int i = 0; i < CH; ++i) {
-      const int x = ry0 + c0 + i;
-      ov[i] = load_object(a, 0, obj_x(x), obj_y(tg));
-      pv[i] = pst[x * S + tg];
+      for (int i = 0; i < CH; ++i) ov[i] = load_object(a, 0, obj_x(ry0 + c0 + i), obj_y(tg));
+#pragma unroll
+      for (int i = 0; i < CH; ++i) {
+        const int x = ry0 + c0 + i;
+        const float2 p = c_scale(buf[x * LD + tg], invN);
+        pst[x * S + tg] = p;
+        buf[x * LD + tg] = c_mul(p, ov[i]);
+      }
     }
+    gsync();
+    forward();
+    err = project();
+    gsync();
+    inverse();
+
+    // adjoint terms: conj(P) chi (or the potential's), |P|^2, conj(O) chi
+    float2* gobj = a.st_obj + (size_t)b * N;
+    float* nobj = a.st_nobj + (size_t)b * N;
+#pragma unroll 1  // (unrolled, the chunks' live values spill)
+    for (int c0 = 0; c0 < PER; c0 += CH) {
+      float2 ov[CH], pv[CH];
 #pragma unroll
-    for (int i = 0; i < CH; ++i) {
-      const int x = ry0 + c0 + i;
-      const int e = x * S + tg;
-      const float2 chi = c_scale(buf[x * LD + tg], invN);
-      gobj[e] = object_term(a.potential, ov[i], pv[i], chi);
-      nobj[e] = c_abs2(pv[i]);
-      pst[e] = c_conj_mul(ov[i], chi);
+      for (int i = 0; i < CH; ++i) {
+        const int x = ry0 + c0 + i;
+        ov[i] = load_object(a, 0, obj_x(x), obj_y(tg));
+        pv[i] = pst[x * S + tg];
+      }
+#pragma unroll
+      for (int i = 0; i < CH; ++i) {
+        const int x = ry0 + c0 + i;
+        const int e = x * S + tg;
+        const float2 chi = c_scale(buf[x * LD + tg], invN);
+        gobj[e] = object_term(a.potential, ov[i], pv[i], chi);
+        nobj[e] = c_abs2(pv[i]);
+        pst[e] = c_conj_mul(ov[i], chi);
+      }
+    }
+  } else {
+    // multislice: P_{s+1} = IFFT2(FFT2(O_s P_s) H_s), each P_s stashed in its
+    // slice's object-term row (the adjoint overwrites it with the term)
+    const int T = a.T;
+    // buf (Fourier space, the group's columns) times H or conj(H)
+    auto propagate = [&](const float2* __restrict__ h, bool conjugate) {
+#pragma unroll 1
+      for (int c0 = 0; c0 < PER; c0 += CH) {
+        float2 hv[CH];
+#pragma unroll
+        for (int i = 0; i < CH; ++i) hv[i] = __ldg(h + (fx0 + FXS * (c0 + i)) * S + fy);
+#pragma unroll
+        for (int i = 0; i < CH; ++i) {
+          const int idx = (fx0 + FXS * (c0 + i)) * LD + fy;
+          buf[idx] = c_mul(buf[idx], conjugate ? make_float2(hv[i].x, -hv[i].y) : hv[i]);
+        }
+      }
+    };
+    for (int s = 0; s < T; ++s) {
+      float2* pst = a.st_obj + ((size_t)s * a.B + b) * N;
+#pragma unroll 1  // (unrolled, the chunks' live values spill)
+      for (int c0 = 0; c0 < PER; c0 += CH) {
+        float2 ov[CH];
+#pragma unroll
+        for (int i = 0; i < CH; ++i) ov[i] = load_object(a, s, obj_x(ry0 + c0 + i), obj_y(tg));
+#pragma unroll
+        for (int i = 0; i < CH; ++i) {
+          const int x = ry0 + c0 + i;
+          const float2 p = c_scale(buf[x * LD + tg], invN);
+          pst[x * S + tg] = p;
+          buf[x * LD + tg] = c_mul(ov[i], p);
+        }
+      }
+      gsync();
+      if (s + 1 < T) {
+        forward();
+        propagate(a.props + (size_t)s * N, false);
+        gsync();
+        inverse();
+      }
+    }
+    forward();  // far field of the last slice's exit wave
+    err = project();
+    gsync();
+    inverse();
+    // adjoint, slice by slice backwards; chi conj(O_s) goes back through the
+    // propagator into the slice before, at slice 0 it is the probe term
+    for (int s = T - 1; s >= 0; --s) {
+      float2* pst = a.st_obj + ((size_t)s * a.B + b) * N;
+      float* nst = a.st_nobj + ((size_t)s * a.B + b) * N;
+#pragma unroll 1  // (unrolled, the chunks' live values spill)
+      for (int c0 = 0; c0 < PER; c0 += CH) {
+        float2 ov[CH], pv[CH];
+#pragma unroll
+        for (int i = 0; i < CH; ++i) {
+          const int x = ry0 + c0 + i;
+          ov[i] = load_object(a, s, obj_x(x), obj_y(tg));
+          pv[i] = pst[x * S + tg];
+        }
+#pragma unroll
+        for (int i = 0; i < CH; ++i) {
+          const int x = ry0 + c0 + i;
+          const int e = x * S + tg;
+          const int idx = x * LD + tg;
+          const float2 chi = c_scale(buf[idx], invN);
+          pst[e] = object_term(a.potential, ov[i], pv[i], chi);
+          nst[e] = c_abs2(pv[i]);
+          const float2 bt = c_mul(chi, make_float2(ov[i].x, -ov[i].y));  // chi conj(O_s)
+          if (s > 0) {
+            buf[idx] = bt;
+          } else {
+            a.st_probe[(size_t)b * N + e] = bt;
+            a.st_nprobe[(size_t)b * N + e] = c_abs2(ov[i]);
+          }
+        }
+      }
+      if (s > 0) {
+        gsync();
+        forward();
+        propagate(a.props + (size_t)(s - 1) * N, true);
+        gsync();
+        inverse();
+      }
     }
   }
   const float tot = block_sum<NT>(err, red);
   if (tid == 0) a.err[b] = pos_ok ? tot : __int_as_float(0x7fc00000);
 }
 
-template <int NT>
+template <int NT, bool kMultislice>
 __global__ void __launch_bounds__(NT, 1) position_grouped_kernel(BatchArgs a) {
   __shared__ float red[NT / 32];
-  position_grouped_128<NT>(a, blockIdx.x, red);
+  position_grouped_128<NT, kMultislice>(a, blockIdx.x, red);
 }
 
 
@@ -1268,12 +1366,17 @@ cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
   if constexpr (SX == 128 && SY == 128 && NT == 1024) {
     // the default (0) and schedule 3: passes by groups of warps
     const int schedule = get_schedule(128);
-    if (mode == 1 && (schedule == 0 || schedule == 3)) {
-      const void* fn = reinterpret_cast<const void*>(position_grouped_kernel<NT>);
+    if ((mode == 1 || mode == 3) && (schedule == 0 || schedule == 3)) {
+      const void* fn =
+          mode == 1 ? reinterpret_cast<const void*>(position_grouped_kernel<NT, false>)
+                    : reinterpret_cast<const void*>(position_grouped_kernel<NT, true>);
       const cudaError_t e0 = ensure_smem_limit(fn, (int)smem);
       if (e0 != cudaSuccess) return e0;
       timing_before(s);
-      position_grouped_kernel<NT><<<a.B, NT, smem, s>>>(a);
+      if (mode == 1)
+        position_grouped_kernel<NT, false><<<a.B, NT, smem, s>>>(a);
+      else
+        position_grouped_kernel<NT, true><<<a.B, NT, smem, s>>>(a);
       const cudaError_t e1 = cudaGetLastError();
       timing_after(s);
       return e1;

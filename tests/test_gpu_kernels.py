@@ -79,6 +79,30 @@ def test_grouped_128_variants(cuda, potential, masked, fix_probe):
     assert rel(g[1], b[1]) < 2e-6
 
 
+@pytest.mark.parametrize("slices,potential,masked", [(3, False, False), (2, True, False),
+                                                      (4, False, True)])
+def test_grouped_128_multislice(cuda, slices, potential, masked):
+    """Multislice gradient descent at 128^2 with passes by groups of warps (the
+    default schedule), against the oracle and the block-wide schedule."""
+    from py4dstem_gb300 import _native
+
+    lib = _native.lib()
+    st = make_state(S=128, J=12, slices=slices, potential=potential, seed=81 + slices)
+    mask = None
+    if masked:
+        mask = (np.random.default_rng(9).uniform(size=(128, 128)) > 0.05).astype(np.float32)
+    kw = dict(num_iter=2, max_batch_size=5, seed_random=7, detector_fourier_mask=mask, **OFF)
+    try:
+        lib.ptycho_set_kernel_schedule(128, 3)
+        g = compare(st, 2e-5, 2e-5, 2e-5, **kw)
+        lib.ptycho_set_kernel_schedule(128, 1)
+        b = gpu_reconstruct(st, **kw)
+    finally:
+        lib.ptycho_set_kernel_schedule(128, 0)
+    assert rel(g[0], b[0]) < 2e-6
+    assert rel(g[1], b[1]) < 2e-6
+
+
 def test_both_128_schedules_agree_with_oracle(cuda):
     """Shared-memory passes (block-wide and by groups of warps) and the
     register-resident schedule at 128^2."""
