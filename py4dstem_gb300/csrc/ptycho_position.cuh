@@ -679,7 +679,7 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
 //   Fourier space (column group g): x = t / 16 + 8 i,     y = 16 g + t % 16
 // for thread t < 128 of the group; both walks are bank-conflict free on the
 // pitch-129 wave and coalesced in global memory.
-template <int NT, bool kMultislice>
+template <int NT, int kKind>
 __device__ __forceinline__ void position_grouped_128(const BatchArgs& a, const int b,
                                                      float* red) {
   constexpr int S = 128;
@@ -748,23 +748,6 @@ __device__ __forceinline__ void position_grouped_128(const BatchArgs& a, const i
   float2* const rows_g = buf + ry0 * LD;    // the group's rows
   float2* const cols_g = buf + LINES * g;   // the group's columns
 
-  // shifted probe: spectrum x ramps, inverse transform (columns, then rows)
-#pragma unroll 1  // (unrolled, the chunks' live values spill)
-  for (int c0 = 0; c0 < PER; c0 += CH) {
-    float2 sv[CH];
-#pragma unroll
-    for (int i = 0; i < CH; ++i) sv[i] = __ldg(a.probe_spec + (fx0 + FXS * (c0 + i)) * S + fy);
-#pragma unroll
-    for (int i = 0; i < CH; ++i) {
-      const int x = fx0 + FXS * (c0 + i);
-      buf[x * LD + fy] = c_mul(sv[i], c_mul(rpx[x], rpy[fy]));
-    }
-  }
-  gsync();
-  Schedule<S>::template run<LINES, GT, +1>(cols_g, 1, LD, twx, tg, gsync);
-  __syncthreads();
-  Schedule<S>::template run<LINES, GT, +1>(rows_g, LD, 1, twy, tg, gsync);
-
   // the transforms of the group's lines: forward = rows then columns (real
   // space in, Fourier space out), inverse = columns then rows
   auto forward = [&]() {
@@ -777,6 +760,26 @@ __device__ __forceinline__ void position_grouped_128(const BatchArgs& a, const i
     __syncthreads();
     Schedule<S>::template run<LINES, GT, +1>(rows_g, LD, 1, twy, tg, gsync);
   };
+  // shifted probe of mode m: spectrum x ramps, inverse transform (columns,
+  // then rows)
+  auto shifted_probe = [&](int m) {
+    const float2* __restrict__ spec = a.probe_spec + (size_t)m * N;
+#pragma unroll 1  // (unrolled, the chunks' live values spill)
+    for (int c0 = 0; c0 < PER; c0 += CH) {
+      float2 sv[CH];
+#pragma unroll
+      for (int i = 0; i < CH; ++i) sv[i] = __ldg(spec + (fx0 + FXS * (c0 + i)) * S + fy);
+#pragma unroll
+      for (int i = 0; i < CH; ++i) {
+        const int x = fx0 + FXS * (c0 + i);
+        buf[x * LD + fy] = c_mul(sv[i], c_mul(rpx[x], rpy[fy]));
+      }
+    }
+    gsync();
+    inverse();
+  };
+  shifted_probe(0);
+
   // A exp(i angle F) - F on the group's columns, one division per pixel;
   // returns this thread's share of sum (A - |F|)^2
   auto project = [&]() {
@@ -809,7 +812,7 @@ __device__ __forceinline__ void position_grouped_128(const BatchArgs& a, const i
   };
   float err = 0.0f;
 
-  if constexpr (!kMultislice) {
+  if constexpr (kKind == 0) {
     // psi = P O; P stashed for the adjoint
     float2* pst = a.st_probe + (size_t)b * N;
 #pragma unroll 1  // (unrolled, the chunks' live values spill)
@@ -853,7 +856,7 @@ __device__ __forceinline__ void position_grouped_128(const BatchArgs& a, const i
         pst[e] = c_conj_mul(ov[i], chi);
       }
     }
-  } else {
+  } else if constexpr (kKind == 1) {
     // multislice: P_{s+1} = IFFT2(FFT2(O_s P_s) H_s), each P_s stashed in its
     // slice's object-term row (the adjoint overwrites it with the term)
     const int T = a.T;
@@ -937,15 +940,114 @@ __device__ __forceinline__ void position_grouped_128(const BatchArgs& a, const i
         inverse();
       }
     }
+  } else {
+    // mixed state: the far fields F_m of every mode share the ratio
+    // A / sqrt(sum_m |F_m|^2) (0 where the model is 0); F_m wait in scratch_f
+    const int M = a.M;
+    float* itot = reinterpret_cast<float*>(rpy + S);  // N, indexed by Fourier pixel
+    for (int m = 0; m < M; ++m) {
+      if (m > 0) shifted_probe(m);
+      float2* pst = a.st_probe + ((size_t)b * M + m) * N;
+#pragma unroll 1  // (unrolled, the chunks' live values spill)
+      for (int c0 = 0; c0 < PER; c0 += CH) {
+        float2 ov[CH];
+#pragma unroll
+        for (int i = 0; i < CH; ++i) ov[i] = load_object(a, 0, obj_x(ry0 + c0 + i), obj_y(tg));
+#pragma unroll
+        for (int i = 0; i < CH; ++i) {
+          const int x = ry0 + c0 + i;
+          const float2 p = c_scale(buf[x * LD + tg], invN);
+          pst[x * S + tg] = p;
+          buf[x * LD + tg] = c_mul(p, ov[i]);
+        }
+      }
+      gsync();
+      forward();
+      float2* f = a.scratch_f + ((size_t)b * M + m) * N;
+      for (int i = 0; i < PER; ++i) {
+        const int x = fx0 + FXS * i;
+        const int e = x * S + fy;
+        const float2 v = buf[x * LD + fy];
+        f[e] = v;
+        const float av = hypotf(v.x, v.y);  // |F_m|^2 as numpy forms it
+        itot[e] = (m == 0 ? 0.0f : itot[e]) + av * av;
+      }
+    }
+#pragma unroll 1  // (unrolled, the chunks' live values spill)
+    for (int c0 = 0; c0 < PER; c0 += CH) {
+      float av[CH];
+#pragma unroll
+      for (int i = 0; i < CH; ++i) av[i] = __ldg(amp + (fx0 + FXS * (c0 + i)) * S + fy);
+#pragma unroll
+      for (int i = 0; i < CH; ++i) {
+        const int e = (fx0 + FXS * (c0 + i)) * S + fy;
+        const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
+        float tot = sqrtf(itot[e]);
+        if (a.det_mask) tot = sqrtf(itot[e] * mk * mk);
+        const float A = av[i];
+        const float d = A - tot;
+        err += d * d;
+        itot[e] = tot == 0.0f ? 0.0f : A / tot;
+      }
+    }
+    float2* gobj = a.st_obj + (size_t)b * N;
+    float* nobj = a.st_nobj + (size_t)b * N;
+    for (int m = 0; m < M; ++m) {
+      // (the previous mode's adjoint read the wave by rows)
+      if (m > 0) __syncthreads();
+      const float2* f = a.scratch_f + ((size_t)b * M + m) * N;
+      for (int i = 0; i < PER; ++i) {
+        const int x = fx0 + FXS * i;
+        const int e = x * S + fy;
+        const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
+        float2 fv = f[e];
+        if (a.det_mask) fv = c_scale(fv, mk);
+        float2 r = c_sub(c_scale(fv, itot[e]), fv);
+        if (a.det_mask) r = c_scale(r, mk);
+        buf[x * LD + fy] = r;
+      }
+      gsync();
+      inverse();
+      float2* pst = a.st_probe + ((size_t)b * M + m) * N;
+#pragma unroll 1  // (unrolled, the chunks' live values spill)
+      for (int c0 = 0; c0 < PER; c0 += CH) {
+        float2 ov[CH], pv[CH];
+#pragma unroll
+        for (int i = 0; i < CH; ++i) {
+          const int x = ry0 + c0 + i;
+          ov[i] = load_object(a, 0, obj_x(x), obj_y(tg));
+          pv[i] = pst[x * S + tg];
+        }
+#pragma unroll
+        for (int i = 0; i < CH; ++i) {
+          const int x = ry0 + c0 + i;
+          const int e = x * S + tg;
+          const float2 chi = c_scale(buf[x * LD + tg], invN);
+          const float2 g = object_term(a.potential, ov[i], pv[i], chi);
+          const float pn = c_abs2(pv[i]);
+          if (m == 0) {
+            gobj[e] = g;
+            nobj[e] = pn;
+            a.st_nprobe[(size_t)b * N + e] = c_abs2(ov[i]);
+          } else {
+            gobj[e] = c_add(gobj[e], g);
+            nobj[e] = nobj[e] + pn;
+          }
+          pst[e] = c_conj_mul(ov[i], chi);
+        }
+      }
+    }
   }
   const float tot = block_sum<NT>(err, red);
   if (tid == 0) a.err[b] = pos_ok ? tot : __int_as_float(0x7fc00000);
 }
 
-template <int NT, bool kMultislice>
+// kKind: 0 single slice, 1 multislice, 2 mixed state (single slice); plain
+// gradient descent
+template <int NT, int kKind>
 __global__ void __launch_bounds__(NT, 1) position_grouped_kernel(BatchArgs a) {
   __shared__ float red[NT / 32];
-  position_grouped_128<NT, kMultislice>(a, blockIdx.x, red);
+  position_grouped_128<NT, kKind>(a, blockIdx.x, red);
 }
 
 
@@ -1366,17 +1468,20 @@ cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
   if constexpr (SX == 128 && SY == 128 && NT == 1024) {
     // the default (0) and schedule 3: passes by groups of warps
     const int schedule = get_schedule(128);
-    if ((mode == 1 || mode == 3) && (schedule == 0 || schedule == 3)) {
+    if ((mode == 1 || mode == 2 || mode == 3) && (schedule == 0 || schedule == 3)) {
       const void* fn =
-          mode == 1 ? reinterpret_cast<const void*>(position_grouped_kernel<NT, false>)
-                    : reinterpret_cast<const void*>(position_grouped_kernel<NT, true>);
+          mode == 1   ? reinterpret_cast<const void*>(position_grouped_kernel<NT, 0>)
+          : mode == 3 ? reinterpret_cast<const void*>(position_grouped_kernel<NT, 1>)
+                      : reinterpret_cast<const void*>(position_grouped_kernel<NT, 2>);
       const cudaError_t e0 = ensure_smem_limit(fn, (int)smem);
       if (e0 != cudaSuccess) return e0;
       timing_before(s);
       if (mode == 1)
-        position_grouped_kernel<NT, false><<<a.B, NT, smem, s>>>(a);
+        position_grouped_kernel<NT, 0><<<a.B, NT, smem, s>>>(a);
+      else if (mode == 3)
+        position_grouped_kernel<NT, 1><<<a.B, NT, smem, s>>>(a);
       else
-        position_grouped_kernel<NT, true><<<a.B, NT, smem, s>>>(a);
+        position_grouped_kernel<NT, 2><<<a.B, NT, smem, s>>>(a);
       const cudaError_t e1 = cudaGetLastError();
       timing_after(s);
       return e1;

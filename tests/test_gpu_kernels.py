@@ -103,6 +103,33 @@ def test_grouped_128_multislice(cuda, slices, potential, masked):
     assert rel(g[1], b[1]) < 2e-6
 
 
+@pytest.mark.parametrize("modes,masked", [(3, False), (2, True), (1, False)])
+def test_grouped_128_mixed_state(cuda, modes, masked):
+    """Mixed-state single-slice gradient descent at 128^2 with passes by groups
+    of warps (one mode: the mixed-state formula on a single probe), against the
+    oracle and the block-wide schedule."""
+    from py4dstem_gb300 import _native
+
+    lib = _native.lib()
+    st = make_state(S=128, J=12, modes=modes, seed=85 + modes)
+    if modes == 1:
+        st.mixed = True
+        st.probe = st.probe[None]
+    mask = None
+    if masked:
+        mask = (np.random.default_rng(11).uniform(size=(128, 128)) > 0.05).astype(np.float32)
+    kw = dict(num_iter=2, max_batch_size=5, seed_random=8, detector_fourier_mask=mask, **OFF)
+    try:
+        lib.ptycho_set_kernel_schedule(128, 3)
+        g = compare(st, 2e-5, 2e-5, 2e-5, **kw)
+        lib.ptycho_set_kernel_schedule(128, 1)
+        b = gpu_reconstruct(st, **kw)
+    finally:
+        lib.ptycho_set_kernel_schedule(128, 0)
+    assert rel(g[0], b[0]) < 2e-6
+    assert rel(g[1], b[1]) < 2e-6
+
+
 def test_both_128_schedules_agree_with_oracle(cuda):
     """Shared-memory passes (block-wide and by groups of warps) and the
     register-resident schedule at 128^2."""
