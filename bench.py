@@ -865,9 +865,10 @@ def run_variant(args):
     import torch
 
     torch.cuda.set_device(local)
-    from py4dstem_gb300 import engine, roofline, synthetic
+    from py4dstem_gb300 import _native, engine, roofline, synthetic
     from py4dstem_gb300.ptychography import method_parameters
 
+    _native.lib().ptycho_set_kernel_schedule(128, args.schedule)
     w = args.workload
     det = 256 if w == "gd256" else 128
     n = det * det

@@ -940,6 +940,81 @@ __device__ __forceinline__ void position_grouped_128(const BatchArgs& a, const i
         inverse();
       }
     }
+  } else if constexpr (kKind == 3) {
+    // projection sets, single slice and probe: the factor c psi + (1 - c) w of
+    // the exit wave w is projected, A exp(i angle F); the new exit wave
+    // x w + a psi + b projected is kept and is chi of the adjoint
+    const float px_ = 1.0f - a.pa - a.pb;
+    const float py_ = 1.0f - a.pc;
+    float2* pst = a.st_probe + (size_t)b * N;
+    float2* ew = a.exit_waves + (size_t)prow * N;
+#pragma unroll 1  // (unrolled, the chunks' live values spill)
+    for (int c0 = 0; c0 < PER; c0 += CH) {
+      float2 ov[CH];
+#pragma unroll
+      for (int i = 0; i < CH; ++i) ov[i] = load_object(a, 0, obj_x(ry0 + c0 + i), obj_y(tg));
+#pragma unroll
+      for (int i = 0; i < CH; ++i) {
+        const int x = ry0 + c0 + i;
+        const int e = x * S + tg;
+        const float2 p = c_scale(buf[x * LD + tg], invN);
+        pst[e] = p;
+        const float2 psi = c_mul(p, ov[i]);
+        const float2 w = a.ew_valid ? ew[e] : psi;
+        buf[x * LD + tg] = c_add(c_scale(psi, a.pc), c_scale(w, py_));
+      }
+    }
+    gsync();
+    forward();
+#pragma unroll 1  // (unrolled, the chunks' live values spill)
+    for (int c0 = 0; c0 < PER; c0 += CH) {
+      float av[CH];
+#pragma unroll
+      for (int i = 0; i < CH; ++i) av[i] = __ldg(amp + (fx0 + FXS * (c0 + i)) * S + fy);
+#pragma unroll
+      for (int i = 0; i < CH; ++i) {
+        const int x = fx0 + FXS * (c0 + i);
+        const int e = x * S + fy;
+        const int idx = x * LD + fy;
+        float2 f = buf[idx];
+        if (a.det_mask) f = c_scale(f, a.det_mask[e]);
+        const float af = c_abs(f);
+        const float A = av[i];
+        const float d = A - af;
+        err += d * d;
+        const float q = af > 0.0f ? A / af : 0.0f;
+        buf[idx] = af > 0.0f ? c_scale(f, q) : make_float2(A, 0.0f);
+      }
+    }
+    gsync();
+    inverse();
+    float2* gobj = a.st_obj + (size_t)b * N;
+    float* nobj = a.st_nobj + (size_t)b * N;
+#pragma unroll 1  // (unrolled, the chunks' live values spill)
+    for (int c0 = 0; c0 < PER; c0 += CH) {
+      float2 ov[CH], pv[CH];
+#pragma unroll
+      for (int i = 0; i < CH; ++i) {
+        const int x = ry0 + c0 + i;
+        ov[i] = load_object(a, 0, obj_x(x), obj_y(tg));
+        pv[i] = pst[x * S + tg];
+      }
+#pragma unroll
+      for (int i = 0; i < CH; ++i) {
+        const int x = ry0 + c0 + i;
+        const int e = x * S + tg;
+        const float2 proj = c_scale(buf[x * LD + tg], invN);
+        const float2 psi = c_mul(pv[i], ov[i]);
+        const float2 w = a.ew_valid ? ew[e] : psi;
+        const float2 chi =
+            c_add(c_add(c_scale(w, px_), c_scale(psi, a.pa)), c_scale(proj, a.pb));
+        ew[e] = chi;
+        gobj[e] = object_term(a.potential, ov[i], pv[i], chi);
+        nobj[e] = c_abs2(pv[i]);
+        pst[e] = c_conj_mul(ov[i], chi);
+        a.st_nprobe[(size_t)b * N + e] = c_abs2(ov[i]);
+      }
+    }
   } else {
     // mixed state: the far fields F_m of every mode share the ratio
     // A / sqrt(sum_m |F_m|^2) (0 where the model is 0); F_m wait in scratch_f
@@ -1042,8 +1117,8 @@ __device__ __forceinline__ void position_grouped_128(const BatchArgs& a, const i
   if (tid == 0) a.err[b] = pos_ok ? tot : __int_as_float(0x7fc00000);
 }
 
-// kKind: 0 single slice, 1 multislice, 2 mixed state (single slice); plain
-// gradient descent
+// kKind: gradient descent 0 single slice, 1 multislice, 2 mixed state (single
+// slice); 3 projection sets (single slice and probe)
 template <int NT, int kKind>
 __global__ void __launch_bounds__(NT, 1) position_grouped_kernel(BatchArgs a) {
   __shared__ float red[NT / 32];
@@ -1468,11 +1543,15 @@ cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
   if constexpr (SX == 128 && SY == 128 && NT == 1024) {
     // the default (0) and schedule 3: passes by groups of warps
     const int schedule = get_schedule(128);
-    if ((mode == 1 || mode == 2 || mode == 3) && (schedule == 0 || schedule == 3)) {
+    // projection sets of one slice and probe without kept far fields
+    const bool ps1 = mode == 0 && a.projection && a.T == 1 && a.M == 1 && !a.mixed_formula &&
+                     !a.forward_only && !a.keep_farfield && !a.exact_probe_grad;
+    if ((mode == 1 || mode == 2 || mode == 3 || ps1) && (schedule == 0 || schedule == 3)) {
       const void* fn =
           mode == 1   ? reinterpret_cast<const void*>(position_grouped_kernel<NT, 0>)
           : mode == 3 ? reinterpret_cast<const void*>(position_grouped_kernel<NT, 1>)
-                      : reinterpret_cast<const void*>(position_grouped_kernel<NT, 2>);
+          : mode == 2 ? reinterpret_cast<const void*>(position_grouped_kernel<NT, 2>)
+                      : reinterpret_cast<const void*>(position_grouped_kernel<NT, 3>);
       const cudaError_t e0 = ensure_smem_limit(fn, (int)smem);
       if (e0 != cudaSuccess) return e0;
       timing_before(s);
@@ -1480,8 +1559,10 @@ cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
         position_grouped_kernel<NT, 0><<<a.B, NT, smem, s>>>(a);
       else if (mode == 3)
         position_grouped_kernel<NT, 1><<<a.B, NT, smem, s>>>(a);
-      else
+      else if (mode == 2)
         position_grouped_kernel<NT, 2><<<a.B, NT, smem, s>>>(a);
+      else
+        position_grouped_kernel<NT, 3><<<a.B, NT, smem, s>>>(a);
       const cudaError_t e1 = cudaGetLastError();
       timing_after(s);
       return e1;

@@ -225,6 +225,28 @@ def test_projection_sets(cuda, method, abc):
     compare(st, 5e-5, 5e-5, 5e-5, num_iter=2, method="PS", a=a, b=b, c=c, **OFF)
 
 
+@pytest.mark.parametrize("abc,potential", [((-1.0, 1.0, 2.0), False), ((0.0, 0.5, 2.0), True),
+                                           ((0.3, 0.6, 1.4), False)])
+def test_grouped_128_projection_sets(cuda, abc, potential):
+    """Projection sets (DM, RAAR, generalized) at 128^2 with passes by groups of
+    warps, against the oracle and the block-wide schedule."""
+    from py4dstem_gb300 import _native
+
+    lib = _native.lib()
+    st = make_state(S=128, J=12, potential=potential, seed=95 + int(10 * abc[1]))
+    a, b, c = abc
+    kw = dict(num_iter=3, method="PS", a=a, b=b, c=c, **OFF)
+    try:
+        lib.ptycho_set_kernel_schedule(128, 3)
+        g = compare(st, 5e-5, 5e-5, 5e-5, **kw)
+        lib.ptycho_set_kernel_schedule(128, 1)
+        bw = gpu_reconstruct(st, **kw)
+    finally:
+        lib.ptycho_set_kernel_schedule(128, 0)
+    assert rel(g[0], bw[0]) < 1e-5
+    assert rel(g[1], bw[1]) < 1e-5
+
+
 def test_projection_mixed_and_multislice(cuda):
     st = make_state(S=32, J=16, modes=2, seed=8)
     compare(st, 5e-5, 5e-5, 5e-5, num_iter=2, method="PS", a=0.0, b=0.5, c=2.0, **OFF)
