@@ -940,6 +940,135 @@ __device__ __forceinline__ void position_grouped_128(const BatchArgs& a, const i
         inverse();
       }
     }
+  } else if constexpr (kKind == 4) {
+    // mixed-state multislice gradient descent: every mode through every slice,
+    // P_{s+1,m} = IFFT2(FFT2(O_s P_{s,m}) H_s) with each P_{s,m} stashed; the far
+    // fields F_m share the ratio A / sqrt(sum_m |F_m|^2); each mode's adjoint
+    // walks back through the slices, summing its terms into slice s's rows
+    const int T = a.T, M = a.M;
+    float* itot = reinterpret_cast<float*>(rpy + S);  // N, indexed by Fourier pixel
+    auto propagate = [&](const float2* __restrict__ h, bool conjugate) {
+#pragma unroll 1
+      for (int c0 = 0; c0 < PER; c0 += CH) {
+        float2 hv[CH];
+#pragma unroll
+        for (int i = 0; i < CH; ++i) hv[i] = __ldg(h + (fx0 + FXS * (c0 + i)) * S + fy);
+#pragma unroll
+        for (int i = 0; i < CH; ++i) {
+          const int idx = (fx0 + FXS * (c0 + i)) * LD + fy;
+          buf[idx] = c_mul(buf[idx], conjugate ? make_float2(hv[i].x, -hv[i].y) : hv[i]);
+        }
+      }
+    };
+    for (int m = 0; m < M; ++m) {
+      if (m > 0) shifted_probe(m);
+      for (int s = 0; s < T; ++s) {
+        float2* pst = a.st_pm + (((size_t)s * a.B + b) * M + m) * N;
+#pragma unroll 1  // (unrolled, the chunks' live values spill)
+        for (int c0 = 0; c0 < PER; c0 += CH) {
+          float2 ov[CH];
+#pragma unroll
+          for (int i = 0; i < CH; ++i)
+            ov[i] = load_object(a, s, obj_x(ry0 + c0 + i), obj_y(tg));
+#pragma unroll
+          for (int i = 0; i < CH; ++i) {
+            const int x = ry0 + c0 + i;
+            const float2 p = c_scale(buf[x * LD + tg], invN);
+            pst[x * S + tg] = p;
+            buf[x * LD + tg] = c_mul(ov[i], p);
+          }
+        }
+        gsync();
+        if (s + 1 < T) {
+          forward();
+          propagate(a.props + (size_t)s * N, false);
+          gsync();
+          inverse();
+        }
+      }
+      forward();
+      float2* f = a.scratch_f + ((size_t)b * M + m) * N;
+      for (int i = 0; i < PER; ++i) {
+        const int x = fx0 + FXS * i;
+        const int e = x * S + fy;
+        const float2 v = buf[x * LD + fy];
+        f[e] = v;
+        const float av = hypotf(v.x, v.y);  // |F_m|^2 as numpy forms it
+        itot[e] = (m == 0 ? 0.0f : itot[e]) + av * av;
+      }
+    }
+    for (int i = 0; i < PER; ++i) {
+      const int e = (fx0 + FXS * i) * S + fy;
+      const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
+      float tot = sqrtf(itot[e]);
+      if (a.det_mask) tot = sqrtf(itot[e] * mk * mk);
+      const float A = __ldg(amp + e);
+      const float d = A - tot;
+      err += d * d;
+      itot[e] = tot == 0.0f ? 0.0f : A / tot;
+    }
+    for (int m = 0; m < M; ++m) {
+      // (the previous mode's adjoint read the wave by rows)
+      if (m > 0) __syncthreads();
+      const float2* f = a.scratch_f + ((size_t)b * M + m) * N;
+      for (int i = 0; i < PER; ++i) {
+        const int x = fx0 + FXS * i;
+        const int e = x * S + fy;
+        const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
+        float2 fv = f[e];
+        if (a.det_mask) fv = c_scale(fv, mk);
+        float2 r = c_sub(c_scale(fv, itot[e]), fv);
+        if (a.det_mask) r = c_scale(r, mk);
+        buf[x * LD + fy] = r;
+      }
+      gsync();
+      inverse();
+      for (int s = T - 1; s >= 0; --s) {
+        const float2* pst = a.st_pm + (((size_t)s * a.B + b) * M + m) * N;
+        float2* gobj = a.st_obj + ((size_t)s * a.B + b) * N;
+        float* nobj = a.st_nobj + ((size_t)s * a.B + b) * N;
+#pragma unroll 1  // (unrolled, the chunks' live values spill)
+        for (int c0 = 0; c0 < PER; c0 += CH) {
+          float2 ov[CH], pv[CH];
+#pragma unroll
+          for (int i = 0; i < CH; ++i) {
+            const int x = ry0 + c0 + i;
+            ov[i] = load_object(a, s, obj_x(x), obj_y(tg));
+            pv[i] = pst[x * S + tg];
+          }
+#pragma unroll
+          for (int i = 0; i < CH; ++i) {
+            const int x = ry0 + c0 + i;
+            const int e = x * S + tg;
+            const int idx = x * LD + tg;
+            const float2 chi = c_scale(buf[idx], invN);
+            const float2 g = object_term(a.potential, ov[i], pv[i], chi);
+            const float pn = c_abs2(pv[i]);
+            if (m == 0) {
+              gobj[e] = g;
+              nobj[e] = pn;
+            } else {
+              gobj[e] = c_add(gobj[e], g);
+              nobj[e] = nobj[e] + pn;
+            }
+            const float2 bt = c_mul(chi, make_float2(ov[i].x, -ov[i].y));  // chi conj(O_s)
+            if (s > 0) {
+              buf[idx] = bt;
+            } else {
+              a.st_probe[((size_t)b * M + m) * N + e] = bt;
+              if (m == 0) a.st_nprobe[(size_t)b * N + e] = c_abs2(ov[i]);
+            }
+          }
+        }
+        if (s > 0) {
+          gsync();
+          forward();
+          propagate(a.props + (size_t)(s - 1) * N, true);
+          gsync();
+          inverse();
+        }
+      }
+    }
   } else if constexpr (kKind == 3) {
     // projection sets, single slice and probe: the factor c psi + (1 - c) w of
     // the exit wave w is projected, A exp(i angle F); the new exit wave
@@ -1118,7 +1247,7 @@ __device__ __forceinline__ void position_grouped_128(const BatchArgs& a, const i
 }
 
 // kKind: gradient descent 0 single slice, 1 multislice, 2 mixed state (single
-// slice); 3 projection sets (single slice and probe)
+// slice), 4 mixed-state multislice; 3 projection sets (single slice and probe)
 template <int NT, int kKind>
 __global__ void __launch_bounds__(NT, 1) position_grouped_kernel(BatchArgs a) {
   __shared__ float red[NT / 32];
@@ -1546,11 +1675,15 @@ cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
     // projection sets of one slice and probe without kept far fields
     const bool ps1 = mode == 0 && a.projection && a.T == 1 && a.M == 1 && !a.mixed_formula &&
                      !a.forward_only && !a.keep_farfield && !a.exact_probe_grad;
-    if ((mode == 1 || mode == 2 || mode == 3 || ps1) && (schedule == 0 || schedule == 3)) {
+    // mixed-state multislice gradient descent (its far fields are kept anyway)
+    const bool mms_gd = mode == 4 && !a.projection && !a.forward_only && !a.exact_probe_grad;
+    if ((mode == 1 || mode == 2 || mode == 3 || ps1 || mms_gd) &&
+        (schedule == 0 || schedule == 3)) {
       const void* fn =
           mode == 1   ? reinterpret_cast<const void*>(position_grouped_kernel<NT, 0>)
           : mode == 3 ? reinterpret_cast<const void*>(position_grouped_kernel<NT, 1>)
           : mode == 2 ? reinterpret_cast<const void*>(position_grouped_kernel<NT, 2>)
+          : mms_gd    ? reinterpret_cast<const void*>(position_grouped_kernel<NT, 4>)
                       : reinterpret_cast<const void*>(position_grouped_kernel<NT, 3>);
       const cudaError_t e0 = ensure_smem_limit(fn, (int)smem);
       if (e0 != cudaSuccess) return e0;
@@ -1561,6 +1694,8 @@ cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
         position_grouped_kernel<NT, 1><<<a.B, NT, smem, s>>>(a);
       else if (mode == 2)
         position_grouped_kernel<NT, 2><<<a.B, NT, smem, s>>>(a);
+      else if (mms_gd)
+        position_grouped_kernel<NT, 4><<<a.B, NT, smem, s>>>(a);
       else
         position_grouped_kernel<NT, 3><<<a.B, NT, smem, s>>>(a);
       const cudaError_t e1 = cudaGetLastError();

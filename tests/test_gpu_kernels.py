@@ -130,6 +130,27 @@ def test_grouped_128_mixed_state(cuda, modes, masked):
     assert rel(g[1], b[1]) < 2e-6
 
 
+@pytest.mark.parametrize("slices,modes,potential", [(2, 2, False), (3, 3, True)])
+def test_grouped_128_mixed_state_multislice(cuda, slices, modes, potential):
+    """Mixed-state multislice gradient descent at 128^2 with passes by groups of
+    warps, against the oracle and the block-wide schedule."""
+    from py4dstem_gb300 import _native
+
+    lib = _native.lib()
+    st = make_state(S=128, J=10, slices=slices, modes=modes, potential=potential,
+                    seed=70 + slices + modes)
+    kw = dict(num_iter=2, max_batch_size=4, seed_random=6, **OFF)
+    try:
+        lib.ptycho_set_kernel_schedule(128, 3)
+        g = compare(st, 2e-5, 2e-5, 2e-5, **kw)
+        lib.ptycho_set_kernel_schedule(128, 1)
+        b = gpu_reconstruct(st, **kw)
+    finally:
+        lib.ptycho_set_kernel_schedule(128, 0)
+    assert rel(g[0], b[0]) < 2e-6
+    assert rel(g[1], b[1]) < 2e-6
+
+
 def test_both_128_schedules_agree_with_oracle(cuda):
     """Shared-memory passes (block-wide and by groups of warps) and the
     register-resident schedule at 128^2."""
