@@ -189,10 +189,8 @@ class MultiScanReconstruction:
         # the 128 x 128 kernel schedule (1: shared-memory transforms by the whole
         # block, 2: register-resident four-step transforms for single-slice
         # single-probe scans, 3: shared-memory transforms by groups of warps)
-        # matters for gradient-descent scans at a 128^2 detector other than
-        # mixed-state multislice ones
-        eligible = any(tuple(p._region_of_interest_shape) == (128, 128)
-                       and not (p._num_slices > 1 and p._num_probes > 1) for p in self.scans)
+        # matters for scans at a 128^2 detector
+        eligible = any(tuple(p._region_of_interest_shape) == (128, 128) for p in self.scans)
         scheds = [1, 2, 3] if eligible else [0]
         cands = [{"concurrent": c, "schedule": sc} for c in concs for sc in scheds]
         key = key + (tuple((c["concurrent"], c["schedule"]) for c in cands),)
