@@ -510,7 +510,8 @@ int ptycho_gd_batch_noalloc(const ptycho_geometry* geometry, void* object, void*
  * gradient descent only; other cases fall back to 1), 3 = shared-memory passes
  * by groups of warps that each own 16 rows / columns, with block-wide barriers
  * only between the axes of a transform (128 x 128: gradient descent of every
- * model, projection sets of one slice and probe; other cases fall back to 1). The default is 3 where it applies, else
+ * model, projection sets of one slice and probe, the position correction of
+ * single-slice batches; other cases fall back to 1). The default is 3 where it applies, else
  * 1. Process-wide; results agree between schedules to float32 rounding.
  * Returns the previous setting.
  * No reference counterpart (tuning knob of this library's autotuner).

@@ -781,8 +781,9 @@ __device__ __forceinline__ void position_grouped_128(const BatchArgs& a, const i
   shifted_probe(0);
 
   // A exp(i angle F) - F on the group's columns, one division per pixel;
-  // returns this thread's share of sum (A - |F|)^2
-  auto project = [&]() {
+  // returns this thread's share of sum (A - |F|)^2. keep (or null) receives F
+  // unmasked, for the position correction after the batch update.
+  auto project = [&](float2* keep) {
     float err = 0.0f;
 #pragma unroll 1  // (unrolled, the chunks' live values spill)
     for (int c0 = 0; c0 < PER; c0 += CH) {
@@ -795,6 +796,7 @@ __device__ __forceinline__ void position_grouped_128(const BatchArgs& a, const i
         const int e = x * S + fy;
         const int idx = x * LD + fy;
         float2 f = buf[idx];
+        if (keep) keep[e] = f;
         const float mk = a.det_mask ? a.det_mask[e] : 1.0f;
         if (a.det_mask) f = c_scale(f, mk);
         const float af = c_abs(f);
@@ -812,7 +814,7 @@ __device__ __forceinline__ void position_grouped_128(const BatchArgs& a, const i
   };
   float err = 0.0f;
 
-  if constexpr (kKind == 0) {
+  if constexpr (kKind == 0 || kKind == 5) {
     // psi = P O; P stashed for the adjoint
     float2* pst = a.st_probe + (size_t)b * N;
 #pragma unroll 1  // (unrolled, the chunks' live values spill)
@@ -830,7 +832,7 @@ __device__ __forceinline__ void position_grouped_128(const BatchArgs& a, const i
     }
     gsync();
     forward();
-    err = project();
+    err = project(kKind == 5 ? a.scratch_f + (size_t)b * N : nullptr);
     gsync();
     inverse();
 
@@ -854,6 +856,9 @@ __device__ __forceinline__ void position_grouped_128(const BatchArgs& a, const i
         gobj[e] = object_term(a.potential, ov[i], pv[i], chi);
         nobj[e] = c_abs2(pv[i]);
         pst[e] = c_conj_mul(ov[i], chi);
+        // (plain gradient descent leaves |O|^2 to the probe side's gather from
+        // the object; with kept far fields the probe side reads it staged)
+        if constexpr (kKind == 5) a.st_nprobe[(size_t)b * N + e] = c_abs2(ov[i]);
       }
     }
   } else if constexpr (kKind == 1) {
@@ -898,7 +903,7 @@ __device__ __forceinline__ void position_grouped_128(const BatchArgs& a, const i
       }
     }
     forward();  // far field of the last slice's exit wave
-    err = project();
+    err = project(nullptr);
     gsync();
     inverse();
     // adjoint, slice by slice backwards; chi conj(O_s) goes back through the
@@ -1247,7 +1252,8 @@ __device__ __forceinline__ void position_grouped_128(const BatchArgs& a, const i
 }
 
 // kKind: gradient descent 0 single slice, 1 multislice, 2 mixed state (single
-// slice), 4 mixed-state multislice; 3 projection sets (single slice and probe)
+// slice), 4 mixed-state multislice, 5 single slice keeping the far fields for
+// the position correction; 3 projection sets (single slice and probe)
 template <int NT, int kKind>
 __global__ void __launch_bounds__(NT, 1) position_grouped_kernel(BatchArgs a) {
   __shared__ float red[NT / 32];
@@ -1284,6 +1290,36 @@ __device__ __forceinline__ void block_sum5(double (&v)[5], double (*red)[NT / 32
       for (int w = 0; w < NT / 32; ++w) t += red[k][w];
       v[k] = t;
     }
+  }
+}
+
+// The position update from the summed normal equations s5 = (xx, xy, yy, xd,
+// yd): the 2 x 2 solve, both distance limits, positions -= u (thread 0).
+__device__ __forceinline__ void correction_update(const BatchArgs& a, int prow, float posx,
+                                                  float posy, bool pos_ok, const double* s5) {
+  const double det = s5[0] * s5[2] - s5[1] * s5[1];
+  float ux = 0.0f, uy = 0.0f;
+  if (det != 0.0 && isfinite(det)) {  // the reference's inverse fails on a singular system
+    ux = __fmul_rn((float)((s5[2] * s5[3] - s5[1] * s5[4]) / det), a.pc_step);
+    uy = __fmul_rn((float)((s5[0] * s5[4] - s5[1] * s5[3]) / det), a.pc_step);
+  }
+  if (a.pc_max_update >= 0.0) {
+    const float n = sqrtf(__fadd_rn(__fmul_rn(ux, ux), __fmul_rn(uy, uy)));
+    if ((double)n > a.pc_max_update) {
+      const double r = (double)n / a.pc_max_update;
+      ux = (float)((double)ux / r);
+      uy = (float)((double)uy / r);
+    }
+  }
+  if (a.pc_max_total >= 0.0) {
+    const float ddx = __fsub_rn(__fsub_rn(posx, a.positions_initial[2 * prow]), ux);
+    const float ddy = __fsub_rn(__fsub_rn(posy, a.positions_initial[2 * prow + 1]), uy);
+    const float dist = sqrtf(__fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(ddy, ddy)));
+    if ((double)dist > a.pc_max_total) ux = uy = 0.0f;
+  }
+  if (pos_ok) {  // a non-finite position stays as it is (its error is already NaN)
+    a.positions_rw[2 * prow] = __fsub_rn(posx, ux);
+    a.positions_rw[2 * prow + 1] = __fsub_rn(posy, uy);
   }
 }
 
@@ -1435,37 +1471,195 @@ __global__ void __launch_bounds__(NT, 1) position_correction_kernel(BatchArgs a)
   }
   double s5[5] = {sxx, sxy, syy, sxd, syd};
   block_sum5<NT>(s5, red);
-  if (tid == 0) {
-    const double det = s5[0] * s5[2] - s5[1] * s5[1];
-    float ux = 0.0f, uy = 0.0f;
-    if (det != 0.0 && isfinite(det)) {  // the reference's inverse fails on a singular system
-      ux = __fmul_rn((float)((s5[2] * s5[3] - s5[1] * s5[4]) / det), a.pc_step);
-      uy = __fmul_rn((float)((s5[0] * s5[4] - s5[1] * s5[3]) / det), a.pc_step);
-    }
-    if (a.pc_max_update >= 0.0) {
-      const float n = sqrtf(__fadd_rn(__fmul_rn(ux, ux), __fmul_rn(uy, uy)));
-      if ((double)n > a.pc_max_update) {
-        const double r = (double)n / a.pc_max_update;
-        ux = (float)((double)ux / r);
-        uy = (float)((double)uy / r);
+  if (tid == 0) correction_update(a, prow, posx, posy, pos_ok, s5);
+}
+
+// Position correction of a single-slice batch at 128 x 128 with the passes and
+// walks of position_grouped_kernel: per mode and direction the shifted probe
+// (Fourier space by columns, inverse transform), times the moved object patch
+// (real space by rows), forward transform, and the gradient term against the
+// kept far field (Fourier space by columns); the normal-equation sums walk the
+// same columns. Same expressions as position_correction_kernel.
+template <int NT>
+__global__ void __launch_bounds__(NT, 1) position_correction_grouped_kernel(BatchArgs a) {
+  constexpr int S = 128;
+  using L = Layout<S, S>;
+  constexpr int N = L::N;
+  constexpr int LD = L::LD;
+  constexpr int GT = 128;
+  constexpr int G = NT / GT;
+  constexpr int LINES = S / G;
+  constexpr int PER = LINES * S / GT;
+  constexpr int CH = 8;
+  constexpr int FXS = GT / LINES;
+  static_assert(NT == 1024 && LINES == 16 && PER == 16, "grouped 128 x 128 layout");
+  extern __shared__ float4 smem4[];
+  float2* buf = reinterpret_cast<float2*>(smem4);
+  float2* twx = buf + S * LD;
+  float2* twy = twx + S;
+  float2* rpx = twy + S;
+  float2* rpy = rpx + S;
+  __shared__ double red[5][NT / 32];
+
+  const int b = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int g = tid / GT;
+  const int tg = tid % GT;
+  const GroupSync gsync{1 + g, GT};
+  const int M = a.M;
+  const int prow = a.pos_rows ? a.pos_rows[b] : b;
+  const int arow = a.amp_rows ? a.amp_rows[b] : b;
+  const bool pos_ok = isfinite(a.positions_rw[2 * prow]) && isfinite(a.positions_rw[2 * prow + 1]);
+  const float posx = finite_or_zero(a.positions_rw[2 * prow]);
+  const float posy = finite_or_zero(a.positions_rw[2 * prow + 1]);
+  const float rx = rintf(posx);
+  const float ry = rintf(posy);
+  const float dx = posx - rx;
+  const float dy = posy - ry;
+  const int x0 = (int)rx;
+  const int y0 = (int)ry;
+  const float invN = 1.0f / (float)N;
+
+  for (int i = tid; i < S; i += NT) {
+    twx[i] = a.tw[i];
+    twy[i] = a.tw[S + i];
+    const float k = (float)fint(i, S) / (float)S;
+    rpx[i] = cis_rounded(__fmul_rn(__fmul_rn(-6.2831855f, k), dx));
+  }
+  for (int i = tid - S; i >= 0 && i < S; i += NT) {
+    const float k = (float)fint(i, S) / (float)S;
+    rpy[i] = cis_rounded(__fmul_rn(__fmul_rn(-6.2831855f, k), dy));
+  }
+  __syncthreads();
+
+  const int bx = pmod(x0 - S / 2, a.Px);
+  const int by = pmod(y0 - S / 2, a.Py);
+  const int ry0 = LINES * g;
+  const int fx0 = tg / LINES;
+  const int fy = LINES * g + tg % LINES;
+  float2* const rows_g = buf + ry0 * LD;
+  float2* const cols_g = buf + LINES * g;
+  auto forward = [&]() {
+    Schedule<S>::template run<LINES, GT, -1>(rows_g, LD, 1, twy, tg, gsync);
+    __syncthreads();
+    Schedule<S>::template run<LINES, GT, -1>(cols_g, 1, LD, twx, tg, gsync);
+  };
+  auto inverse = [&]() {
+    Schedule<S>::template run<LINES, GT, +1>(cols_g, 1, LD, twx, tg, gsync);
+    __syncthreads();
+    Schedule<S>::template run<LINES, GT, +1>(rows_g, LD, 1, twy, tg, gsync);
+  };
+  // object column of this thread's real-space samples, and the object row of
+  // sample i, with the patch moved one pixel along x (dir 0) or y (dir 1)
+  auto obj_col = [&](int dir) {
+    int t2 = by + (tg + S / 2) % S;
+    if (t2 >= a.Py) t2 -= a.Py;
+    if (dir == 1) t2 = t2 + 1 == a.Py ? 0 : t2 + 1;
+    return t2;
+  };
+  auto obj_row = [&](int dir, int x) {
+    int t2 = bx + (x + S / 2) % S;
+    if (t2 >= a.Px) t2 -= a.Px;
+    if (dir == 0) t2 = t2 + 1 == a.Px ? 0 : t2 + 1;
+    return t2;
+  };
+
+  float* gx = a.st_nobj + (size_t)b * N;
+  float* gy = a.st_nprobe + (size_t)b * N;
+  const float2* f0 = a.scratch_f + (size_t)b * M * N;
+  for (int m = 0; m < M; ++m) {
+    const float2* __restrict__ spec = a.probe_spec + (size_t)m * N;
+    for (int dir = 0; dir < 2; ++dir) {
+      // P_m shifted as in the forward pass
+#pragma unroll 1
+      for (int c0 = 0; c0 < PER; c0 += CH) {
+        float2 sv[CH];
+#pragma unroll
+        for (int i = 0; i < CH; ++i) sv[i] = __ldg(spec + (fx0 + FXS * (c0 + i)) * S + fy);
+#pragma unroll
+        for (int i = 0; i < CH; ++i) {
+          const int x = fx0 + FXS * (c0 + i);
+          buf[x * LD + fy] = c_mul(sv[i], c_mul(rpx[x], rpy[fy]));
+        }
+      }
+      gsync();
+      inverse();
+      // times the moved object patch
+      const int oy = obj_col(dir);
+#pragma unroll 1
+      for (int c0 = 0; c0 < PER; c0 += CH) {
+        float2 ov[CH];
+#pragma unroll
+        for (int i = 0; i < CH; ++i) ov[i] = load_object(a, 0, obj_row(dir, ry0 + c0 + i), oy);
+#pragma unroll
+        for (int i = 0; i < CH; ++i) {
+          const int idx = (ry0 + c0 + i) * LD + tg;
+          const float2 p = c_scale(buf[idx], invN);
+          buf[idx] = c_mul(p, ov[i]);
+        }
+      }
+      gsync();
+      forward();
+      float* gd = dir == 0 ? gx : gy;
+      for (int i = 0; i < PER; ++i) {
+        const int x = fx0 + FXS * i;
+        const int e = x * S + fy;
+        const float2 f = buf[x * LD + fy];
+        const float2 r = f0[(size_t)m * N + e];
+        const float2 d = c_sub(r, f);
+        const float v = 2.0f * __fadd_rn(__fmul_rn(d.x, r.x), __fmul_rn(d.y, r.y));
+        gd[e] = m == 0 ? v : gd[e] + v;
       }
     }
-    if (a.pc_max_total >= 0.0) {
-      const float ddx = __fsub_rn(__fsub_rn(posx, a.positions_initial[2 * prow]), ux);
-      const float ddy = __fsub_rn(__fsub_rn(posy, a.positions_initial[2 * prow + 1]), uy);
-      const float dist = sqrtf(__fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(ddy, ddy)));
-      if ((double)dist > a.pc_max_total) ux = uy = 0.0f;
-    }
-    if (pos_ok) {  // a non-finite position stays as it is (its error is already NaN)
-      a.positions_rw[2 * prow] = __fsub_rn(posx, ux);
-      a.positions_rw[2 * prow + 1] = __fsub_rn(posy, uy);
-    }
   }
+
+  const float* amp = a.amplitudes + (size_t)arow * N;
+  const bool mixed = M > 1 || a.mixed_formula;
+  float sxx = 0.f, sxy = 0.f, syy = 0.f, sxd = 0.f, syd = 0.f;
+  for (int i = 0; i < PER; ++i) {
+    const int e = (fx0 + FXS * i) * S + fy;
+    float est;
+    if (mixed) {
+      float tt = 0.0f;
+      for (int m = 0; m < M; ++m) {
+        const float2 r = f0[(size_t)m * N + e];
+        const float av = hypotf(r.x, r.y);
+        tt += av * av;
+      }
+      const float amp_tot = sqrtf(tt);
+      est = amp_tot * amp_tot;
+    } else {
+      const float2 r = f0[e];
+      const float af = hypotf(r.x, r.y);
+      est = af * af;
+    }
+    const float A = amp[e];
+    const float d = __fsub_rn(__fmul_rn(A, A), est);
+    const float px = gx[e], py = gy[e];
+    sxx = fmaf(px, px, sxx);
+    sxy = fmaf(px, py, sxy);
+    syy = fmaf(py, py, syy);
+    sxd = fmaf(px, d, sxd);
+    syd = fmaf(py, d, syd);
+  }
+  double s5[5] = {sxx, sxy, syy, sxd, syd};
+  block_sum5<NT>(s5, red);
+  if (tid == 0) correction_update(a, prow, posx, posy, pos_ok, s5);
 }
 
 template <int SX, int SY, int NT>
 cudaError_t launch_correction_t(const BatchArgs& a, cudaStream_t s) {
   const size_t smem = Layout<SX, SY>::smem_bytes(false);
+  if constexpr (SX == 128 && SY == 128 && NT == 1024) {
+    const int schedule = get_schedule(128);
+    if (a.T == 1 && (schedule == 0 || schedule == 3)) {
+      const void* fn = reinterpret_cast<const void*>(position_correction_grouped_kernel<NT>);
+      const cudaError_t e0 = ensure_smem_limit(fn, (int)smem);
+      if (e0 != cudaSuccess) return e0;
+      position_correction_grouped_kernel<NT><<<a.B, NT, smem, s>>>(a);
+      return cudaGetLastError();
+    }
+  }
   {
     const cudaError_t e0 =
         ensure_smem_limit(reinterpret_cast<const void*>(position_correction_kernel<SX, SY, NT>),
@@ -1677,13 +1871,17 @@ cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
                      !a.forward_only && !a.keep_farfield && !a.exact_probe_grad;
     // mixed-state multislice gradient descent (its far fields are kept anyway)
     const bool mms_gd = mode == 4 && !a.projection && !a.forward_only && !a.exact_probe_grad;
-    if ((mode == 1 || mode == 2 || mode == 3 || ps1 || mms_gd) &&
+    // single-slice single-probe gradient descent keeping its far fields
+    const bool keep1 = mode == 0 && !a.projection && a.keep_farfield && a.T == 1 && a.M == 1 &&
+                       !a.mixed_formula && !a.forward_only && !a.exact_probe_grad;
+    if ((mode == 1 || mode == 2 || mode == 3 || ps1 || mms_gd || keep1) &&
         (schedule == 0 || schedule == 3)) {
       const void* fn =
           mode == 1   ? reinterpret_cast<const void*>(position_grouped_kernel<NT, 0>)
           : mode == 3 ? reinterpret_cast<const void*>(position_grouped_kernel<NT, 1>)
           : mode == 2 ? reinterpret_cast<const void*>(position_grouped_kernel<NT, 2>)
           : mms_gd    ? reinterpret_cast<const void*>(position_grouped_kernel<NT, 4>)
+          : keep1     ? reinterpret_cast<const void*>(position_grouped_kernel<NT, 5>)
                       : reinterpret_cast<const void*>(position_grouped_kernel<NT, 3>);
       const cudaError_t e0 = ensure_smem_limit(fn, (int)smem);
       if (e0 != cudaSuccess) return e0;
@@ -1696,6 +1894,8 @@ cudaError_t launch_position_t(const BatchArgs& a, cudaStream_t s) {
         position_grouped_kernel<NT, 2><<<a.B, NT, smem, s>>>(a);
       else if (mms_gd)
         position_grouped_kernel<NT, 4><<<a.B, NT, smem, s>>>(a);
+      else if (keep1)
+        position_grouped_kernel<NT, 5><<<a.B, NT, smem, s>>>(a);
       else
         position_grouped_kernel<NT, 3><<<a.B, NT, smem, s>>>(a);
       const cudaError_t e1 = cudaGetLastError();

@@ -209,3 +209,45 @@ def test_repeated_calls_reuse_state_and_match(cuda):
     st = b._device_state
     b.reconstruct(num_iter=1, **dict(kw, step_size=0.25))
     assert b._device_state is not st
+
+
+@pytest.mark.parametrize("cls_modes", [1, 2])
+def test_position_correction_128_grouped_and_block_wide(cuda, cls_modes):
+    """Gradient descent with position correction at a 128^2 detector (the
+    grouped kernels keep the far fields and correct the positions), against the
+    oracle on the same preprocessed state and against the block-wide schedule."""
+    from oracle.ptycho_np import Oracle
+    from py4dstem_gb300 import _native
+
+    lib = _native.lib()
+    g = Golden("ss_gd_det128")
+    extra = dict(fix_positions=False, fix_positions_com=False, positions_step_size=0.5,
+                 max_position_update_distance=0.1, max_position_total_distance=0.3)
+    if cls_modes > 1:
+        g.meta = dict(g.meta, cls="mixed", ctor=dict(g.meta["ctor"], num_probes=cls_modes))
+    kw = dict(g.rec_kwargs(), **extra)
+    out = {}
+    try:
+        for schedule in (0, 1):
+            lib.ptycho_set_kernel_schedule(128, schedule)
+            p = g.build()
+            if schedule == 0:
+                state = g.state(p)
+            p.reconstruct(progress_bar=False, **kw)
+            out[schedule] = (np.asarray(p._object), np.asarray(p._probe),
+                             np.asarray(p.error_iterations), np.array(p._positions_px))
+    finally:
+        lib.ptycho_set_kernel_schedule(128, 0)
+    okw = dict(g.oracle_kwargs(), **extra)
+    o = Oracle(state).reconstruct(**okw)
+    obj, probe, err, pos = out[0]
+    d_err = float(np.max(np.abs(err - o.error_iterations) / np.abs(o.error_iterations)))
+    print(f"\ngrouped vs oracle: err {d_err:.2e} obj {rel_l2(obj, o.object):.2e} "
+          f"probe {rel_l2(probe, o.probe):.2e} "
+          f"pos {float(np.max(np.abs(pos - o.positions_px))):.2e} px")
+    assert d_err < 2e-5
+    assert rel_l2(obj, o.object) < 1e-4
+    assert rel_l2(probe, o.probe) < 1e-4
+    assert float(np.max(np.abs(pos - o.positions_px))) < 1e-3
+    assert rel_l2(obj, out[1][0]) < 1e-5
+    assert float(np.max(np.abs(pos - out[1][3]))) < 1e-3
