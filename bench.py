@@ -202,6 +202,14 @@ def measured_hbm_gbs():
         return 6800.0, "fallback 6.8 TB/s"
 
 
+def set_schedule(schedule):
+    """The 128^2 kernel schedule for this process (refused values raise)."""
+    from py4dstem_gb300 import _native
+
+    if _native.lib().ptycho_set_kernel_schedule(128, int(schedule)) < 0:
+        raise SystemExit(_native.lib().ptycho_last_error().decode())
+
+
 def read_profile_traffic():
     """DRAM bytes per launch of the position kernel from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "position_kernel_128_gd.md")
@@ -537,7 +545,7 @@ def run_ours(args):
     from py4dstem_gb300 import _native, engine
 
     lib = _native.lib()
-    lib.ptycho_set_kernel_schedule(128, args.schedule)
+    set_schedule(args.schedule)
     seed = 1234 + rank
     t_setup = time.time()
     case = build_case(args.scan, seed, f"cuda:{local}")
@@ -785,9 +793,9 @@ def run_multislice(args):
     import torch
 
     torch.cuda.set_device(local)
-    from py4dstem_gb300 import MultislicePtychography, _native, engine, roofline, synthetic
+    from py4dstem_gb300 import MultislicePtychography, engine, roofline, synthetic
 
-    _native.lib().ptycho_set_kernel_schedule(128, args.schedule)
+    set_schedule(args.schedule)
 
     c = synthetic.multislice_case(seed=3, num_slices=8, scan=64, backend="torch",
                                   device=f"cuda:{local}", object_px=256)
@@ -865,10 +873,10 @@ def run_variant(args):
     import torch
 
     torch.cuda.set_device(local)
-    from py4dstem_gb300 import _native, engine, roofline, synthetic
+    from py4dstem_gb300 import engine, roofline, synthetic
     from py4dstem_gb300.ptychography import method_parameters
 
-    _native.lib().ptycho_set_kernel_schedule(128, args.schedule)
+    set_schedule(args.schedule)
     w = args.workload
     det = 256 if w == "gd256" else 128
     n = det * det

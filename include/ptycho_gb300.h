@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define PTYCHO_ABI_VERSION 4
+#define PTYCHO_ABI_VERSION 5
 
 enum ptycho_status {
   PTYCHO_OK = 0,
@@ -511,9 +511,10 @@ int ptycho_gd_batch_noalloc(const ptycho_geometry* geometry, void* object, void*
  * by groups of warps that each own 16 rows / columns, with block-wide barriers
  * only between the axes of a transform (128 x 128: gradient descent of every
  * model, projection sets of one slice and probe, the position correction of
- * single-slice batches; other cases fall back to 1). The default is 3 where it applies, else
- * 1. Process-wide; results agree between schedules to float32 rounding.
- * Returns the previous setting.
+ * single-slice batches; other cases fall back to 1). The default is 3 where it
+ * applies, else 1. Process-wide; results agree between schedules to float32
+ * rounding. Returns the previous setting (0-3), or -PTYCHO_ERR_INVALID_ARGUMENT
+ * for a schedule outside 0-3 (the setting is then unchanged).
  * No reference counterpart (tuning knob of this library's autotuner).
  */
 int ptycho_set_kernel_schedule(int32_t roi, int32_t schedule);

@@ -508,8 +508,11 @@ int ptycho_prepare_stream(void* stream) {
 }
 
 int ptycho_set_kernel_schedule(int32_t roi, int32_t schedule) {
-  if (schedule < 0 || schedule > 3)
-    return fail(PTYCHO_ERR_INVALID_ARGUMENT, "schedule must be 0, 1, 2 or 3 (got %d)", schedule);
+  if (schedule < 0 || schedule > 3) {
+    // (negative: a previous setting is never negative, a status could be one)
+    fail(PTYCHO_ERR_INVALID_ARGUMENT, "schedule must be 0, 1, 2 or 3 (got %d)", schedule);
+    return -PTYCHO_ERR_INVALID_ARGUMENT;
+  }
   return set_schedule(roi, schedule);
 }
 

@@ -33,7 +33,7 @@ def test_exports_every_declared_symbol(lib):
 
 
 def test_abi_version(lib):
-    assert lib.ptycho_abi_version() == 4
+    assert lib.ptycho_abi_version() == 5
 
 
 @pytest.mark.parametrize("n,ok", [(32, 1), (48, 1), (64, 1), (96, 1), (128, 1), (80, 0),
@@ -282,3 +282,18 @@ def test_gather_patterns_argument_checks(lib):
     # without a row list the first num_out patterns are taken: there must be as many
     assert lib.ptycho_gather_patterns(p, 4, 16, None, 5, p, None) == 1
     assert b"5 rows requested of 4 patterns" in lib.ptycho_last_error()
+
+
+def test_kernel_schedule_argument_checks(lib):
+    """Schedules 0-3 are taken (the previous one returned), others refused; the
+    setting is process-wide and is put back."""
+    prev = lib.ptycho_set_kernel_schedule(128, 3)
+    try:
+        assert lib.ptycho_set_kernel_schedule(128, 1) == 3
+        assert lib.ptycho_set_kernel_schedule(128, 0) == 1
+        assert lib.ptycho_set_kernel_schedule(128, 4) == -1  # -PTYCHO_ERR_INVALID_ARGUMENT
+        assert b"schedule must be 0, 1, 2 or 3" in lib.ptycho_last_error()
+        assert lib.ptycho_set_kernel_schedule(128, -1) == -1
+        assert lib.ptycho_set_kernel_schedule(128, 2) == 0  # unchanged by the refusals
+    finally:
+        lib.ptycho_set_kernel_schedule(128, prev)
