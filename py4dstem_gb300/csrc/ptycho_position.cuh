@@ -16,7 +16,10 @@
 //                   multislice back-transmits and back-propagates chi
 //                                  (ptychographic_methods.py:1818-1908, 2353-2565, 2906-3093)
 // The adjoint terms go to position-major staging buffers; ptycho_reduce.cu sums
-// them over positions in a fixed order.
+// them over positions in a fixed order. position_one runs every phase with the
+// whole block; position_grouped_128 (the default at 128 x 128) runs the same
+// model with 8 groups of warps that synchronise among themselves between the
+// turns of its transforms.
 //
 // This header holds the kernel templates; ptycho_position_<S>.cu instantiates
 // them for one region-of-interest edge S each (the translation units compile in
@@ -663,14 +666,15 @@ __global__ void __launch_bounds__(NT, 1) position_kernel(BatchArgs a) {
   position_one<SX, SY, NT, kMode>(a, blockIdx.x, red);
 }
 
-// Plain single-slice gradient descent at 128 x 128 (the model of kMode 1) with
+// The per-position model at 128 x 128 (kKind, see position_grouped_kernel) with
 // the block split into 8 groups of 4 warps. A group owns 16 rows in the
 // real-space phases and 16 columns in the Fourier-space phases; its elementwise
 // work and its share of each 2D transform (the same Stockham passes and
 // twiddles as fft2d, on its own lines) synchronise through a named barrier of
 // its 128 threads. A block-wide barrier is needed only where a transform turns
-// from one axis to the other: 4 per position instead of the 24 of the
-// block-wide schedule, and between them the groups drift apart in phase (one
+// from one axis to the other (one per transform: 4 per position of single-slice
+// gradient descent instead of the 24 of the block-wide schedule), and between
+// them the groups drift apart in phase (one
 // loading from memory while another runs its passes). To need no extra turn,
 // the inverse transforms run columns then rows and the forward ones rows then
 // columns (fft2d: rows then columns both ways), so results agree with the
