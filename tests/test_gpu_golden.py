@@ -10,8 +10,8 @@ outside the probe aperture, so A*exp(i*angle(F)) takes a rounding-determined
 phase there; projection-set methods (RAAR here) are chaotic on small scans. We
 measure that floor by re-running the oracle with every FFT evaluated in
 complex128 and rounded back to complex64 (a different, correct float32 FFT).
-Gradient-descent fixtures must meet the benchmark spec's tolerance outright (error
-per iteration 1e-5 relative, object and probe 1e-4 relative L2); the one whose
+Gradient-descent fixtures must meet the parity tolerance outright (error per
+iteration 1e-5 relative, object and probe 1e-4 relative L2); the one whose
 measured floor is at that bar already (FLOOR_BOUND) takes 3x the floor.
 Projection-set fixtures take 5x the floor. Each result's distance to the
 float64 evaluation of the same model is printed.
@@ -25,7 +25,7 @@ from oracle.ptycho_np import Oracle
 
 pytestmark = pytest.mark.gpu
 
-# Gradient-descent fixtures meet the spec bar outright (error 1e-5 per
+# Gradient-descent fixtures meet the parity bar outright (error 1e-5 per
 # iteration, object and probe 1e-4), except where the reference's own rounding
 # floor is at that bar already: there 3x the floor.
 FLOOR_BOUND = {
@@ -63,7 +63,7 @@ def test_reconstruction_matches_reference(cuda, name):
     tol_err = max(1e-5, k * f_err)
     tol_obj = max(1e-4, k * f_obj)
     tol_probe = max(1e-4, k * f_probe)
-    if not g.projection and name not in FLOOR_BOUND:  # the spec numbers as stated
+    if not g.projection and name not in FLOOR_BOUND:  # the parity bar as stated
         tol_err, tol_obj, tol_probe = 1e-5, 1e-4, 1e-4
     assert d_err <= tol_err
     if g.projection:
