@@ -146,3 +146,23 @@ def test_grouped_kernel_amplitude_sources_agree(cuda):
     np.testing.assert_array_equal(a[0], st.object.cpu().numpy())
     np.testing.assert_array_equal(a[1], st.probe.cpu().numpy())
     assert a[2] == errors
+
+
+def test_prefetched_host_amplitudes_with_position_correction(cuda):
+    """Gradient descent with position correction through the public API: the
+    correction reads the batch's gathered rows from the same device slot."""
+    from golden_io import Golden
+
+    g = Golden("ss_gd_poscorr")
+    out = []
+    for storage in ("gpu", "cpu"):
+        p = g.build(storage=storage)
+        if storage == "cpu":
+            p._amplitudes = _pinned(np.ascontiguousarray(p._amplitudes)).numpy()
+        p.reconstruct(progress_bar=False, **g.rec_kwargs())
+        out.append((np.asarray(p._object), np.asarray(p._probe), list(p.error_iterations),
+                    np.array(p._positions_px)))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2]
+    np.testing.assert_array_equal(out[0][3], out[1][3])
