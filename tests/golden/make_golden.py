@@ -100,6 +100,16 @@ CASES = {
                  detector=128, object_px=192),
         cls="single", ctor=dict(object_fov_ang=(48.0, 48.0)), guess=(192, 192),
         rec=dict(num_iter=4, max_batch_size=18, step_size=0.5, seed_random=7)),
+    # position correction at a 128^2 detector (the grouped kernels' far-field
+    # keeping form and the grouped correction)
+    "ss_gd_poscorr_det128": dict(
+        gen=dict(name="scp", seed=37, scan_shape=(8, 8), step_ang=0.5, jitter_ang=0.05,
+                 detector=128, object_px=192),
+        cls="single", ctor=dict(object_fov_ang=(48.0, 48.0)), guess=(192, 192),
+        perturb_ang=0.15,
+        rec=dict(num_iter=4, max_batch_size=32, step_size=0.5, seed_random=9,
+                 fix_positions=False, fix_positions_com=False, positions_step_size=0.5,
+                 max_position_update_distance=0.1, max_position_total_distance=0.3)),
     # a 96^2 detector (radix-8/4/3 transforms) with a detector Fourier mask
     "ss_gd_det96_mask": dict(
         gen=dict(name="s96", seed=19, scan_shape=(8, 8), step_ang=0.5, jitter_ang=0.05,
