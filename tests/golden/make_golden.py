@@ -53,6 +53,12 @@ CASES = {
                  detector=64, object_px=96),
         cls="single", ctor=dict(object_fov_ang=(24.0, 24.0)), guess=(96, 96),
         rec=dict(num_iter=6, reconstruction_method="DM_AP", reconstruction_parameter=0.0)),
+    # projection sets (RAAR) at a 128^2 detector: the grouped kernels' form
+    "ss_ap_det128": dict(
+        gen=dict(name="sra", seed=38, scan_shape=(6, 6), step_ang=0.5, jitter_ang=0.05,
+                 detector=128, object_px=192),
+        cls="single", ctor=dict(object_fov_ang=(48.0, 48.0)), guess=(192, 192),
+        rec=dict(num_iter=4, reconstruction_method="RAAR", reconstruction_parameter=0.8)),
     "ms_gd_T3": dict(
         gen=dict(name="ms", seed=13, scan_shape=(10, 10), step_ang=0.5, jitter_ang=0.05,
                  detector=64, object_px=96, num_slices=3, slice_thickness=20.0),
