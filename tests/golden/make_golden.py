@@ -164,6 +164,15 @@ CASES = {
                                      slice_thicknesses=20.0, num_probes=2),
         global_seed=9, guess=(3, 96, 96),
         rec=dict(num_iter=5, max_batch_size=25, step_size=0.5, seed_random=10)),
+    # mixed-state multislice at a 128^2 detector: the grouped kernels' form
+    "mms_gd_det128": dict(
+        gen=dict(name="mmd", seed=39, scan_shape=(6, 6), step_ang=0.5, jitter_ang=0.05,
+                 detector=128, object_px=192, num_slices=2, slice_thickness=20.0,
+                 num_modes=2, mode_weights=(0.8, 0.2)),
+        cls="mixed_multi", ctor=dict(object_fov_ang=(48.0, 48.0), num_slices=2,
+                                     slice_thicknesses=20.0, num_probes=2),
+        global_seed=11, guess=(2, 192, 192),
+        rec=dict(num_iter=3, max_batch_size=18, step_size=0.5, seed_random=12)),
     "mms_ap": dict(
         gen=dict(name="msa", seed=25, scan_shape=(8, 8), step_ang=0.5, jitter_ang=0.05,
                  detector=64, object_px=96, num_slices=2, slice_thickness=20.0, num_modes=2,
